@@ -1,0 +1,239 @@
+/*
+ * fmftsaxs-gb300: GB300 (sm_103a) implementation of libfmftsaxs's
+ * FFT-correlation dimer scoring path.
+ *
+ * Two layers, both plain C ABI (no C++ or torch types):
+ *
+ *  1. Drop-in: the reference's own functions, names, argument meanings,
+ *     struct layouts and error behaviour (print + exit(EXIT_FAILURE)), so a
+ *     program written against libfmftsaxs links against this library
+ *     instead.  Each declaration cites the reference header line it
+ *     replaces (paths relative to the reference project).
+ *
+ *  2. sxsg_*: status-returning extensions (0 = success, negative = error,
+ *     message from sxsg_last_error()) that the reference has no equivalent
+ *     for: flat-array inputs, 64-bit pose indices, grid fit over (c1, c2),
+ *     cross-term output, reusable device plans.
+ *
+ * Everything numerical runs on the GPU; the CUDA extension must be present,
+ * there is no CPU path for the scoring.
+ */
+#ifndef FMFTSAXS_GB300_H
+#define FMFTSAXS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- types */
+
+/* src/pdb2spf.h:30-35: coefficients A_lm for one q, lm = l(l+1)+m. */
+struct sxs_spf_sing {
+	int L;
+	double *re;
+	double *im;
+};
+
+/* src/pdb2spf.h:41-53: vacuum (V), excluded-volume (D) and hydration (W)
+ * coefficients for every q. */
+struct sxs_spf_full {
+	int L;
+	int qnum;
+	double rm;
+	struct sxs_spf_sing **V;
+	struct sxs_spf_sing **D;
+	struct sxs_spf_sing **W;
+};
+
+/* src/profile.h:23-49 */
+struct sxs_profile {
+	int qnum;
+	double rerr;
+	double *in;
+	double *err;
+	double *qvals;
+	double *VV, *VD, *VW, *DD, *DW, *WW;
+	double score;
+	double scale;
+	double c1;
+	double c2;
+	double b1, g1, a2, b2, g2;
+};
+
+/* src/min_saxs.h:32-46 (the L-BFGS-B workspace is kept for layout
+ * compatibility; `integer` and `logical` there are `long int`). */
+struct sxs_opt_params {
+	double rm;
+	double mult;
+	double peak;
+	double *a;
+	double wa[43251];
+	long iwa[3072];
+	double dsave[29];
+	long isave[44];
+	long lsave[4];
+};
+
+/* src/index.h:25-43 */
+struct sxs_euler { double z, b1, g1, a2, b2, g2; };
+struct sxs_index { int z, b1, g1, a2, b2, g2; };
+
+#ifndef SXS_HAVE_MOL2_TYPES
+/* libmol2's 3-vector and 3x3 matrix, as used by src/index.h and
+ * src/saxs_utils.h (define SXS_HAVE_MOL2_TYPES when libmol2's headers are
+ * already included). */
+struct mol_vector3 { double X, Y, Z; };
+struct mol_matrix3 { double m11, m12, m13, m21, m22, m23, m31, m32, m33; };
+#endif
+
+/* -------------------------------------------------- drop-in: scoring path */
+
+/* src/fftsaxs.h:95-105.  Scores every grid pose in index_list; outputs are
+ * caller-allocated, length nout.  Index packing (src/index.c:3-7):
+ * ((((z (L+1) + b1)(L+1) + b2)(2L+1) + a2)(2L+1) + g1)(2L+1) + g2.
+ * The fit is the reference's L-BFGS-B over (c1, c2), run on the GPU. */
+void sxs_compute_saxs_scores(double *scores_list, double *c1_list, double *c2_list,
+                             int *index_list, int nout,
+                             struct sxs_spf_full *A, struct sxs_spf_full *B,
+                             struct sxs_opt_params *params,
+                             double *qvals, int qnum, double *zvals, int znum, int L, int skip);
+
+/* ------------------------------------------------ drop-in: containers, I/O */
+
+struct sxs_spf_sing *sxs_spf_sing_create(int L);          /* src/pdb2spf.h:98 */
+void sxs_spf_sing_init(struct sxs_spf_sing *s, int L);    /* src/pdb2spf.h:105 */
+void sxs_spf_sing_destroy(struct sxs_spf_sing *s);        /* src/pdb2spf.h:111 */
+void sxs_spf_sing_free(struct sxs_spf_sing *s);           /* src/pdb2spf.h:117 */
+struct sxs_spf_full *sxs_spf_full_create(int L, int qnum);                /* src/pdb2spf.h:125 */
+void sxs_spf_full_init(struct sxs_spf_full *s, int L, int qnum);          /* src/pdb2spf.h:133 */
+void sxs_spf_full_free(struct sxs_spf_full *s);                           /* src/pdb2spf.h:139 */
+void sxs_spf_full_destroy(struct sxs_spf_full *s);                        /* src/pdb2spf.h:145 */
+void sxs_spf_full_reset(struct sxs_spf_full *s);                          /* src/pdb2spf.h:151 */
+void sxs_spf_full_write(char *path, struct sxs_spf_full *s);              /* src/pdb2spf.h:158 */
+struct sxs_spf_full *sxs_spf_full_read(char *path);                       /* src/pdb2spf.h:165 */
+struct sxs_spf_full *sxs_spf_full_fread(FILE *f);                         /* src/pdb2spf.h:172 */
+
+struct sxs_profile *sxs_profile_create(double *qvals, int qnum, int cross_terms_flag);        /* src/profile.h:59 */
+void sxs_profile_init(struct sxs_profile *p, double *qvals, int qnum, int cross_terms_flag);  /* src/profile.h:69 */
+void sxs_profile_alloc_cross_terms(struct sxs_profile *p, int qnum);                         /* src/profile.h:76 */
+void sxs_profile_destroy(struct sxs_profile *p);                                             /* src/profile.h:84 */
+void sxs_profile_free(struct sxs_profile *p);                                                /* src/profile.h:91 */
+void sxs_profile_write(char *path, struct sxs_profile *p);                                   /* src/profile.h:98 */
+struct sxs_profile *sxs_profile_read(char *path);                                            /* src/profile.h:104 */
+struct sxs_profile *sxs_profile_fread(FILE *f);                                              /* src/profile.h:110 */
+void sxs_profile_from_spf(struct sxs_profile *p, struct sxs_spf_full *spf, double c1, double c2); /* src/profile.h:120 */
+
+/* ---------------------------------------------------- drop-in: fitting */
+
+struct sxs_opt_params *sxs_opt_params_create(struct sxs_profile *exp, double *qvals, int qnum, double rm); /* src/min_saxs.h:57 */
+void sxs_opt_params_init(struct sxs_opt_params *p, struct sxs_profile *exp, double *qvals, int qnum, double rm); /* :68 */
+void sxs_opt_params_destroy(struct sxs_opt_params *p);     /* src/min_saxs.h:75 */
+void sxs_opt_params_free(struct sxs_opt_params *p);        /* src/min_saxs.h:81 */
+/* src/min_saxs.h:94.  Peak rescale + L-BFGS-B of every masked profile (GPU). */
+void sxs_fit_params(struct sxs_profile **profiles, struct sxs_opt_params *params, int *mask, int n);
+/* src/min_saxs.h:104.  L-BFGS-B of one profile (GPU). */
+void sxs_lbfgs_fitting(struct sxs_profile *profile, struct sxs_opt_params *params);
+double *scoring_helper(struct sxs_profile *exp, int qnum, double *qvals);                          /* src/min_saxs.h:114 */
+void sxs_compile_intensity(struct sxs_profile *p, double rm, double c1, double c2);                /* src/min_saxs.h:136 */
+double sxs_best_scale(struct sxs_profile *p, struct sxs_opt_params *params, double c1, double c2);  /* src/min_saxs.h:148 */
+/* src/min_saxs.h:161 declares sxs_point_score; the reference defines it as
+ * point_score (src/min_saxs.c:391).  Both names are exported here. */
+double sxs_point_score(struct sxs_profile *p, struct sxs_opt_params *params, double c1, double c2);
+double point_score(struct sxs_profile *p, struct sxs_opt_params *params, double c1, double c2);
+void sxs_spf2cross_terms(struct sxs_profile *p, struct sxs_spf_full *s);                           /* src/min_saxs.h:169 */
+void sxs_spf2fitted_profile(struct sxs_profile *p, struct sxs_spf_full *s, struct sxs_opt_params *params); /* :179 */
+
+/* ----------------------------------------------- drop-in: grids, indices */
+
+double *sxs_mkarray(double begin, double end, int qnum);                                        /* src/saxs_utils.h:30 */
+void sxs_fill_active_rotation_matrix(struct mol_matrix3 *rm, double alpha, double beta, double gamma); /* :39 */
+void sxs_mult_rot_mats(struct mol_matrix3 *c, struct mol_matrix3 *a, struct mol_matrix3 *b);    /* src/saxs_utils.h:44 */
+size_t sxs_assemble_index(struct sxs_index *id, int nbeta, int L);                              /* src/index.h:45 */
+void sxs_disassemble_index(struct sxs_index *id, size_t index, int nbeta, int L);               /* src/index.h:47 */
+void sxs_ft2euler(struct sxs_euler *euler, struct mol_vector3 *tv, struct mol_matrix3 *rm, struct mol_vector3 *ref_lig); /* :59 */
+double sxs_sbessel(int order, double x);                                                        /* src/sfbessel.h:19 */
+
+/* ======================================================== extensions */
+
+const char *sxsg_last_error(void);
+/* Initialise the library on a CUDA device (called implicitly with device 0). */
+int sxsg_init(int device);
+/* Number of kernel launches issued by this library since load. */
+long long sxsg_launch_count(void);
+
+/* Form-factor constants of one type name of the reference's mapping file
+ * ("C", "N", "O", "S", "CH2", ...; src/form_factor_table.c:8-49, 76-107):
+ * vacuum and excluded-volume zero-angle form factors.  Returns -1 for an
+ * unknown name. */
+int sxsg_ff_type(const char *name, double *vacuum_ff, double *dummy_ff);
+/* zero-angle form factor of water, the hydration-shell weight (s_OH2) */
+double sxsg_ff_water(void);
+/* Load a (residue, atom) -> type mapping file in the reference's format
+ * (prms/pdb_formfactor_mapping_clean.prm) and resolve n atoms (names in
+ * 8-byte slots) to (vacuum_ff, dummy_ff).  Returns the number of atoms that
+ * had no mapping (their factors are set to NaN), or < 0 on error. */
+int sxsg_ff_lookup(const char *mapping_path, const char *res8, const char *atom8, int n,
+                   double *vacuum_ff, double *dummy_ff);
+
+/* A_lm(q) of one molecule on the GPU (atom_grp2spf_inplace, src/pdb2spf.c:24-152)
+ * from arrays: coordinates xyz[3n] (already centred), per-atom vacuum and
+ * excluded-volume form factors, per-atom accessible fraction sasa (NULL:
+ * no hydration shell, W = 0), water form factor.  spf_out is the flat
+ * layout [3 (V,D,W)][qnum][(L+1)^2][re,im].  rm (mean vdW radius) is not
+ * computed here. */
+int sxsg_expand(const double *xyz, const double *vacuum_ff, const double *dummy_ff, const double *sasa,
+                double water_ff, int natoms, const double *qvals, int qnum, int L, double *spf_out);
+
+/* Binned experiment for the fit from flat arrays: a[6 qnum], mult and peak
+ * exactly as sxs_opt_params_create computes them (min_saxs.c:116-124,
+ * 353-389; the bin loop stops at the last experimental point). */
+int sxsg_bin_experiment(const double *exp_q, const double *exp_i, const double *exp_err, int nexp,
+                        const double *qvals, int qnum, double rm, double *a, double *mult, double *peak);
+
+/* Flat-array view of an sxs_spf_full ([3][qnum][(L+1)^2][2]). */
+int sxsg_spf_to_flat(const struct sxs_spf_full *s, double *flat);
+int sxsg_spf_from_flat(struct sxs_spf_full *s, const double *flat);
+
+/* Reusable scoring plan: receptor/ligand coefficients, grids and the
+ * experiment stay resident on the device between runs. */
+typedef struct sxsg_plan sxsg_plan;
+
+enum { SXSG_FIT_NONE = 0, SXSG_FIT_GRID = 1, SXSG_FIT_LBFGSB = 2 };
+enum { SXSG_FP64 = 0 };
+
+/* A, B: flat [3][qnum][(L+1)^2][2]; a[6 qnum], mult, peak: the binned
+ * experiment of scoring_helper / sxs_opt_params (min_saxs.c:116-124,
+ * 353-389); c1grid/c2grid: fit grid (may be NULL with n = 0 when no grid fit
+ * is run). */
+int sxsg_plan_create(sxsg_plan **plan, const double *A, const double *B, const double *qvals, int qnum,
+                     const double *zvals, int znum, int L, const double *a, double mult, double peak,
+                     const double *c1grid, int n1, const double *c2grid, int n2, int precision);
+/* Pose list (64-bit packed indices as above).  skip = 1 scores the listed
+ * poses the way the reference's skip = 1 does (simple_ft twiddles);
+ * skip = 0 as its FFTW branch. */
+int sxsg_plan_set_poses(sxsg_plan *plan, const int64_t *index, int64_t n, int skip);
+/* Run the GPU work for the current pose list (asynchronous until results). */
+int sxsg_plan_run(sxsg_plan *plan, int fit_mode);
+/* Copy results to the host.  Any pointer may be NULL.  chi/c1/c2/cell: [n];
+ * cross: raw cross terms [n][6][qnum] (VV,VD,VW,DD,DW,WW before the peak
+ * rescale); grid: chi^2 [n][n1][n2] (grid fit only). */
+int sxsg_plan_results(sxsg_plan *plan, double *chi, double *c1, double *c2, int32_t *cell,
+                      double *cross, double *grid);
+/* Stage timings of the last run in ms (CUDA events on the plan stream):
+ * [0] tables, [1] translate, [2] per-pose, [3] fit, [4] total. */
+int sxsg_plan_timings(sxsg_plan *plan, double *ms5);
+void sxsg_plan_destroy(sxsg_plan *plan);
+
+/* Pose ingestion helpers (tools/correlate.c:202-240): grid index of one
+ * Euler 6-tuple (z, b1, g1, a2, b2, g2 as written by sxs_ft2euler) at
+ * translation slot z_idx. */
+int64_t sxsg_assemble_index(const double *euler6, int z_idx, int L);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

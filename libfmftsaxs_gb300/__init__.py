@@ -1,0 +1,223 @@
+"""Python mirror of the fmftsaxs-gb300 C API (ctypes over the in-tree
+libfmftsaxs_gb300.so).  The library is the product: every call below runs
+the sm_103a kernels through the C ABI declared in include/fmftsaxs_gb300.h.
+There is no fallback: if the shared library is missing or cannot find a
+GPU, calls raise.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfmftsaxs_gb300.so")
+
+FIT_NONE, FIT_GRID, FIT_LBFGSB = 0, 1, 2
+FP64 = 0
+
+_lib = None
+
+
+class SxsError(RuntimeError):
+    pass
+
+
+def _p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def load():
+    """Load the shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise SxsError("libfmftsaxs_gb300.so not built (run __graft_entry__.build())")
+    lib = C.CDLL(LIB_PATH)
+    lib.sxsg_last_error.restype = C.c_char_p
+    lib.sxsg_launch_count.restype = C.c_longlong
+    lib.sxsg_ff_water.restype = C.c_double
+    lib.sxsg_assemble_index.restype = C.c_int64
+    lib.sxsg_assemble_index.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_int]
+    lib.sxs_sbessel.restype = C.c_double
+    lib.sxs_sbessel.argtypes = [C.c_int, C.c_double]
+    lib.sxs_mkarray.restype = C.POINTER(C.c_double)
+    lib.sxs_mkarray.argtypes = [C.c_double, C.c_double, C.c_int]
+    lib.sxsg_plan_create.argtypes = [C.POINTER(C.c_void_p)] + [C.c_void_p] * 3 + [C.c_int, C.c_void_p, C.c_int, C.c_int,
+                                     C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                                     C.c_int]
+    lib.sxsg_plan_set_poses.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int]
+    lib.sxsg_plan_run.argtypes = [C.c_void_p, C.c_int]
+    lib.sxsg_plan_results.argtypes = [C.c_void_p] + [C.c_void_p] * 6
+    lib.sxsg_plan_timings.argtypes = [C.c_void_p, C.c_void_p]
+    lib.sxsg_plan_destroy.argtypes = [C.c_void_p]
+    lib.sxsg_plan_destroy.restype = None
+    _lib = lib
+    return lib
+
+
+def _check(rc):
+    if rc != 0:
+        raise SxsError(load().sxsg_last_error().decode(errors="replace"))
+    return rc
+
+
+def last_error():
+    return load().sxsg_last_error().decode(errors="replace")
+
+
+def launch_count():
+    return int(load().sxsg_launch_count())
+
+
+def init(device=0):
+    _check(load().sxsg_init(int(device)))
+
+
+def f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def ff_type(name):
+    """(vacuum_ff, dummy_ff) of a form-factor type name of the mapping file."""
+    v, d = C.c_double(), C.c_double()
+    if load().sxsg_ff_type(name.encode(), C.byref(v), C.byref(d)) != 0:
+        raise KeyError(name)
+    return v.value, d.value
+
+
+def ff_water():
+    return load().sxsg_ff_water()
+
+
+def ff_lookup(mapping_path, res, atom):
+    """(vacuum_ff[n], dummy_ff[n], n_missing) for (residue, atom) names."""
+    n = len(res)
+    rb = np.zeros((n, 8), dtype=np.uint8)
+    ab = np.zeros((n, 8), dtype=np.uint8)
+    for i in range(n):
+        r, a = res[i].encode()[:8], atom[i].encode()[:8]
+        rb[i, :len(r)] = np.frombuffer(r, dtype=np.uint8)
+        ab[i, :len(a)] = np.frombuffer(a, dtype=np.uint8)
+    vac, dum = np.zeros(n), np.zeros(n)
+    rc = load().sxsg_ff_lookup(mapping_path.encode(), rb.ctypes.data_as(C.c_char_p), ab.ctypes.data_as(C.c_char_p),
+                               C.c_int(n), _p(vac), _p(dum))
+    if rc < 0:
+        raise SxsError(last_error())
+    return vac, dum, rc
+
+
+def sbessel(l, x):
+    return load().sxs_sbessel(int(l), float(x))
+
+
+def mkarray(begin, end, n):
+    lib = load()
+    ptr = lib.sxs_mkarray(float(begin), float(end), int(n))
+    out = np.array([ptr[i] for i in range(n)])
+    C.CDLL(None).free(C.cast(ptr, C.c_void_p))
+    return out
+
+
+def expand(xyz, vacuum_ff, dummy_ff, sasa, water_ff, qvals, L):
+    """A_lm(q) of one molecule on the GPU: flat [3][Q][(L+1)^2][2]."""
+    xyz, vac, dum, q = f64(xyz), f64(vacuum_ff), f64(dummy_ff), f64(qvals)
+    n = len(vac)
+    out = np.zeros(3 * len(q) * (L + 1) ** 2 * 2)
+    sp = None
+    if sasa is not None:
+        sasa = f64(sasa)
+        sp = _p(sasa)
+    _check(load().sxsg_expand(_p(xyz), _p(vac), _p(dum), sp, C.c_double(water_ff), C.c_int(n), _p(q),
+                              C.c_int(len(q)), C.c_int(L), _p(out)))
+    return out
+
+
+def bin_experiment(exp_q, exp_i, exp_err, qvals, rm):
+    """(a[6Q], mult, peak): the binned experiment of sxs_opt_params_create."""
+    eq, ei, ee, q = f64(exp_q), f64(exp_i), f64(exp_err), f64(qvals)
+    a = np.zeros(6 * len(q))
+    mult, peak = C.c_double(), C.c_double()
+    _check(load().sxsg_bin_experiment(_p(eq), _p(ei), _p(ee), C.c_int(len(eq)), _p(q), C.c_int(len(q)),
+                                      C.c_double(rm), _p(a), C.byref(mult), C.byref(peak)))
+    return a, mult.value, peak.value
+
+
+def ft2euler(tv, rm9, ref_lig):
+    """sxs_ft2euler on plain arrays -> (z, b1, g1, a2, b2, g2)."""
+    class V3(C.Structure):
+        _fields_ = [("X", C.c_double), ("Y", C.c_double), ("Z", C.c_double)]
+
+    class M3(C.Structure):
+        _fields_ = [(n, C.c_double) for n in ("m11", "m12", "m13", "m21", "m22", "m23", "m31", "m32", "m33")]
+
+    class EU(C.Structure):
+        _fields_ = [(n, C.c_double) for n in ("z", "b1", "g1", "a2", "b2", "g2")]
+
+    t = V3(*map(float, tv))
+    r = V3(*map(float, ref_lig))
+    m = M3(*map(float, np.asarray(rm9).reshape(9)))
+    e = EU()
+    load().sxs_ft2euler(C.byref(e), C.byref(t), C.byref(m), C.byref(r))
+    return np.array([e.z, e.b1, e.g1, e.a2, e.b2, e.g2])
+
+
+def assemble_index(eu6, z_idx, L):
+    e = f64(eu6)
+    return int(load().sxsg_assemble_index(_p(e), int(z_idx), int(L)))
+
+
+class Plan:
+    """A device-resident scoring plan (sxsg_plan_*)."""
+
+    def __init__(self, A, B, qvals, zvals, L, a, mult, peak, c1grid=None, c2grid=None, precision=FP64):
+        lib = load()
+        self.A, self.B, self.q, self.z, self.a = f64(A), f64(B), f64(qvals), f64(zvals), f64(a)
+        self.c1g = f64(c1grid if c1grid is not None else np.zeros(0))
+        self.c2g = f64(c2grid if c2grid is not None else np.zeros(0))
+        self.L, self.Q = L, len(self.q)
+        self.h = C.c_void_p()
+        _check(lib.sxsg_plan_create(C.byref(self.h), self.A.ctypes.data, self.B.ctypes.data, self.q.ctypes.data,
+                                    self.Q, self.z.ctypes.data, len(self.z), L, self.a.ctypes.data, mult, peak,
+                                    self.c1g.ctypes.data if len(self.c1g) else None, len(self.c1g),
+                                    self.c2g.ctypes.data if len(self.c2g) else None, len(self.c2g), precision))
+        self.n = 0
+
+    def set_poses(self, index, skip=1):
+        idx = np.ascontiguousarray(index, dtype=np.int64)
+        self.n = len(idx)
+        _check(load().sxsg_plan_set_poses(self.h, idx.ctypes.data, self.n, int(skip)))
+
+    def run(self, fit=FIT_GRID):
+        _check(load().sxsg_plan_run(self.h, int(fit)))
+
+    def results(self, cross=False, grid=False):
+        n = self.n
+        chi, c1, c2 = np.zeros(n), np.zeros(n), np.zeros(n)
+        cell = np.zeros(n, dtype=np.int32)
+        cr = np.zeros((n, 6, self.Q)) if cross else None
+        gr = np.zeros((n, len(self.c1g), len(self.c2g))) if grid else None
+        _check(load().sxsg_plan_results(self.h, chi.ctypes.data, c1.ctypes.data, c2.ctypes.data, cell.ctypes.data,
+                                        cr.ctypes.data if cross else None, gr.ctypes.data if grid else None))
+        out = dict(chi=chi, c1=c1, c2=c2, cell=cell)
+        if cross:
+            out["cross"] = cr
+        if grid:
+            out["grid"] = gr
+        return out
+
+    def timings(self):
+        ms = np.zeros(5)
+        _check(load().sxsg_plan_timings(self.h, ms.ctypes.data))
+        return dict(tables=ms[0], translate=ms[1], pose=ms[2], fit=ms[3], total=ms[4])
+
+    def close(self):
+        if self.h:
+            load().sxsg_plan_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

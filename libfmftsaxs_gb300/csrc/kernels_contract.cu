@@ -1,0 +1,332 @@
+/*
+ * FP64 contraction kernels of the factorized correlation (multiply-add
+ * fusion allowed; each output is a short fixed-order sum).
+ *
+ * The reference evaluates, per touched (z, beta1, beta2) triple, the 6-channel
+ * sums X[m,m1,m2] (src/fftsaxs.c:416-524) and then an angular DFT at each
+ * listed cell (529-606 or FFTW).  Writing the DFT phase as a product of the
+ * per-angle phases and moving each sum next to the angle it depends on gives,
+ * for one listed pose (z, b1, b2, a2, g1, g2) and one q,
+ *
+ *   P^a[m,l](b1,g1) = sum_{m1} w^{m1' g1} d^l_{m m1}(beta_b1) A^a_{l m1}
+ *   U^b[m,l1](b2,g2)= sum_{m2} w^{m2' g2} d^l1_{m m2}(beta_b2) conj(B^b_{l1 m2})
+ *   R^b[m,l]        = sum_{l1>=|m|} conj(T^{|m|}_{l l1}(q z)) U^b[m,l1]
+ *   F^{ab}          = sum_m w^{m' a2} sum_{l>=|m|} P^a[m,l] R^b[m,l]
+ *
+ * (w = the twiddle table, x' = x mod N), which is the reference's F with the
+ * same terms regrouped.  P depends on (b1, g1) only and U on (b2, g2) only, so
+ * they are tabulated once per call; R is tabulated for each touched
+ * (z, b2, g2); the per-pose work is the final K^2-term contraction.
+ */
+#include "kernels.h"
+
+namespace {
+
+__device__ __forceinline__ int lm_index(int l, int m) { return l * (l + 1) + m; }
+
+/* index of the first (m, l) pair of row m, pairs ordered m = -L..L, l = |m|..L */
+__device__ __forceinline__ int pair_off(int m, int L)
+{
+	int K = L + 1;
+	if (m <= 0) {
+		int t = L + m; /* rows before: m' = -L .. m-1, sizes 1 .. L+m */
+		return t * (t + 1) / 2;
+	}
+	return L * (L + 1) / 2 + K + (m - 1) * K - (m - 1) * m / 2;
+}
+
+__device__ __forceinline__ void cfma(double2 &acc, double2 a, double2 b)
+{
+	acc.x = fma(a.x, b.x, acc.x);
+	acc.x = fma(-a.y, b.y, acc.x);
+	acc.y = fma(a.x, b.y, acc.y);
+	acc.y = fma(a.y, b.x, acc.y);
+}
+
+/* [3][Q][K2][2] -> [3][K2][Q] complex */
+__global__ void k_spf_transpose(const double *__restrict__ flat, double2 *__restrict__ t, int Q, int K2)
+{
+	long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= 3L * Q * K2) return;
+	int iq = (int)(i % Q);
+	long r = i / Q;
+	int lm = (int)(r % K2), ch = (int)(r / K2);
+	const double *s = flat + (((size_t)ch * Q + iq) * K2 + lm) * 2;
+	t[i] = make_double2(s[0], s[1]);
+}
+
+/* block = (b*N+g, m+L); threads over q */
+__global__ void k_rotate(const double2 *__restrict__ spf_t, const double *__restrict__ dtab,
+                         const double2 *__restrict__ tw, int Q, int L, int conj, double2 *__restrict__ out)
+{
+	int K = L + 1, N = 2 * L + 1, K2 = K * K;
+	int bg = blockIdx.x, mi = blockIdx.y, m = mi - L, am = m < 0 ? -m : m;
+	int b = bg / N, g = bg % N;
+	int iq = threadIdx.x;
+	if (iq >= Q) return;
+	const double *db = dtab + (size_t)b * K * N * N;
+	double sg = conj ? -1.0 : 1.0;
+	int po = pair_off(m, L);
+	for (int l = am; l <= L; l++) {
+		double2 acc0 = make_double2(0, 0), acc1 = acc0, acc2 = acc0;
+		const double *drow = db + ((size_t)l * N + mi) * N;
+		for (int m1 = -l; m1 <= l; m1++) {
+			int e = ((m1 < 0 ? m1 + N : m1) * g) % N;
+			double dv = drow[m1 + L];
+			double2 f = make_double2(tw[e].x * dv, tw[e].y * dv);
+			int lm = lm_index(l, m1);
+			double2 c0 = spf_t[((size_t)0 * K2 + lm) * Q + iq];
+			double2 c1 = spf_t[((size_t)1 * K2 + lm) * Q + iq];
+			double2 c2 = spf_t[((size_t)2 * K2 + lm) * Q + iq];
+			c0.y *= sg; c1.y *= sg; c2.y *= sg;
+			cfma(acc0, f, c0);
+			cfma(acc1, f, c1);
+			cfma(acc2, f, c2);
+		}
+		double2 *o = out + (((size_t)bg * K2 + po + (l - am)) * 3) * Q + iq;
+		o[0] = acc0;
+		o[Q] = acc1;
+		o[2 * Q] = acc2;
+	}
+}
+
+/* block = (combo, m+L); threads over q; l blocked by LB for register reuse of U */
+template <int LB>
+__global__ void k_translate(const double2 *__restrict__ U, const double2 *__restrict__ tmat,
+                            const int32_t *__restrict__ combo_zbg, int Q, int L, double2 *__restrict__ out)
+{
+	int K = L + 1, N = 2 * L + 1, K2 = K * K;
+	int c = blockIdx.x, mi = blockIdx.y, m = mi - L, am = m < 0 ? -m : m;
+	int iq = threadIdx.x;
+	if (iq >= Q) return;
+	int zi = combo_zbg[3 * c], b2 = combo_zbg[3 * c + 1], g2 = combo_zbg[3 * c + 2];
+	const double2 *Ub = U + (size_t)(b2 * N + g2) * K2 * 3 * Q;
+	const double2 *Tm = tmat + ((size_t)zi * K + am) * K * K * Q;
+	int po = pair_off(m, L);
+	double2 *Ob = out + (size_t)c * K2 * 3 * Q;
+	for (int l0 = am; l0 <= L; l0 += LB) {
+		double2 acc[LB][3];
+#pragma unroll
+		for (int j = 0; j < LB; j++) acc[j][0] = acc[j][1] = acc[j][2] = make_double2(0, 0);
+		for (int l1 = am; l1 <= L; l1++) {
+			const double2 *u = Ub + ((size_t)(po + l1 - am) * 3) * Q + iq;
+			double2 u0 = u[0], u1 = u[Q], u2 = u[2 * Q];
+#pragma unroll
+			for (int j = 0; j < LB; j++) {
+				int l = l0 + j;
+				if (l > L) break;
+				double2 t = Tm[((size_t)l * K + l1) * Q + iq];
+				t.y = -t.y;
+				cfma(acc[j][0], t, u0);
+				cfma(acc[j][1], t, u1);
+				cfma(acc[j][2], t, u2);
+			}
+		}
+#pragma unroll
+		for (int j = 0; j < LB; j++) {
+			int l = l0 + j;
+			if (l > L) break;
+			double2 *o = Ob + ((size_t)(po + l - am) * 3) * Q + iq;
+			o[0] = acc[j][0];
+			o[Q] = acc[j][1];
+			o[2 * Q] = acc[j][2];
+		}
+	}
+}
+
+/* block = one pose; threads over q.  Writes cross[src][c][q]. */
+__global__ void k_pose_cross(const sxsk_pose *__restrict__ poses, int combo_base, const double2 *__restrict__ P,
+                             const double2 *__restrict__ R, const double2 *__restrict__ tw,
+                             const double *__restrict__ cst, int Q, int L, double *__restrict__ cross)
+{
+	int K = L + 1, N = 2 * L + 1, K2 = K * K;
+	sxsk_pose ps = poses[blockIdx.x];
+	int iq = threadIdx.x;
+	if (iq >= Q) return;
+	const double2 *Pb = P + (size_t)(ps.b1 * N + ps.g1) * K2 * 3 * Q + iq;
+	const double2 *Rb = R + (size_t)(ps.combo - combo_base) * K2 * 3 * Q + iq;
+	double f[6] = {0, 0, 0, 0, 0, 0};
+	int p = 0;
+	for (int m = -L; m <= L; m++) {
+		int am = m < 0 ? -m : m;
+		double2 g[6];
+#pragma unroll
+		for (int c = 0; c < 6; c++) g[c] = make_double2(0, 0);
+		for (int l = am; l <= L; l++, p++) {
+			const double2 *pp = Pb + (size_t)p * 3 * Q;
+			const double2 *rr = Rb + (size_t)p * 3 * Q;
+			double2 pv = pp[0], pd = pp[Q], pw = pp[2 * Q];
+			double2 rv = rr[0], rd = rr[Q], rw = rr[2 * Q];
+			cfma(g[0], pv, rv);
+			cfma(g[1], pv, rd); cfma(g[1], pd, rv);
+			cfma(g[2], pv, rw); cfma(g[2], pw, rv);
+			cfma(g[3], pd, rd);
+			cfma(g[4], pd, rw); cfma(g[4], pw, rd);
+			cfma(g[5], pw, rw);
+		}
+		double2 w = tw[((m < 0 ? m + N : m) * ps.a2) % N];
+#pragma unroll
+		for (int c = 0; c < 6; c++) f[c] += w.x * g[c].x - w.y * g[c].y;
+	}
+	double *o = cross + (size_t)ps.src * 6 * Q + iq;
+#pragma unroll
+	for (int c = 0; c < 6; c++) {
+		double v = cst[c * Q + iq];
+		v += 2.0 * f[c];
+		o[c * Q] = v;
+	}
+}
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+	return v;
+}
+
+/* One warp per pose: peak rescale (src/min_saxs.c:170-188), then for each c1
+ * the scale-optimal chi^2 of point_score (391-448) as a function of c2.  With
+ * I_i(c2) = al_i + be_i c2 + ga_i c2^2 (al = VV - G VD + G^2 DD,
+ * be = VW - G DW, ga = WW) the piecewise-linear model's tan_i and buf_i are
+ * quadratics in c2, so best_scale's up(c2) (quadratic) and down(c2)
+ * (quartic) are accumulated once per c1 as coefficients; each cell is then
+ * chi^2 = sum a0 + k (-2 up + k down), k = up/down. */
+#define FIT_WARPS 4
+__global__ void k_fit_grid(const double *__restrict__ cross, int npose, int Q, const double *__restrict__ q,
+                           const double *__restrict__ a, double a0sum, double peak, const double *__restrict__ gtab,
+                           const double *__restrict__ c1g, int n1, const double *__restrict__ c2g, int n2,
+                           double *__restrict__ chi, double *__restrict__ c1o, double *__restrict__ c2o,
+                           int32_t *__restrict__ cello, double *__restrict__ grid, double *__restrict__ scaled)
+{
+	extern __shared__ double sm[];
+	int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	int pid = blockIdx.x * FIT_WARPS + w;
+	if (pid >= npose) return;
+	double *sc = sm + (size_t)w * 6 * Q;
+	const double *src = cross + (size_t)pid * 6 * Q;
+	for (int i = lane; i < 6 * Q; i += 32) sc[i] = src[i];
+	__syncwarp();
+	double s = sc[0] + sc[3 * Q] + sc[5 * Q] + sc[2 * Q] - sc[Q] - sc[4 * Q];
+	s = peak / s;
+	__syncwarp();
+	for (int i = lane; i < 6 * Q; i += 32) sc[i] *= s;
+	__syncwarp();
+	if (scaled)
+		for (int i = lane; i < 6 * Q; i += 32) scaled[(size_t)pid * 6 * Q + i] = sc[i];
+	const double *VV = sc, *VD = sc + Q, *VW = sc + 2 * Q, *DD = sc + 3 * Q, *DW = sc + 4 * Q, *WW = sc + 5 * Q;
+	double best = __longlong_as_double(0x7ff0000000000000LL);
+	int bcell = -1;
+	for (int i1 = 0; i1 < n1; i1++) {
+		const double *G = gtab + (size_t)i1 * Q;
+		double U0 = 0, U1 = 0, U2 = 0, D0 = 0, D1 = 0, D2 = 0, D3 = 0, D4 = 0;
+		for (int i = lane; i < Q; i += 32) {
+			int ip = i > 0 ? i - 1 : 0;
+			double gi = G[i], gp = G[ip];
+			double al = VV[i] - gi * VD[i] + gi * gi * DD[i];
+			double be = VW[i] - gi * DW[i];
+			double ga = WW[i];
+			double alp = VV[ip] - gp * VD[ip] + gp * gp * DD[ip];
+			double bep = VW[ip] - gp * DW[ip];
+			double gap = WW[ip];
+			double qc = q[i], qp = i > 0 ? q[i - 1] : -1.0;
+			double h = qc - qp;
+			double t0 = (al - alp) / h, t1 = (be - bep) / h, t2 = (ga - gap) / h;
+			double b0 = al - t0 * qc, b1 = be - t1 * qc, b2 = ga - t2 * qc;
+			double a1 = a[6 * i + 1], a2 = a[6 * i + 2], a3 = a[6 * i + 3], a4 = a[6 * i + 4], a5 = a[6 * i + 5];
+			U0 += b0 * a1 + t0 * a2;
+			U1 += b1 * a1 + t1 * a2;
+			U2 += b2 * a1 + t2 * a2;
+			D0 += b0 * b0 * a3 + 2.0 * t0 * b0 * a4 + t0 * t0 * a5;
+			D1 += 2.0 * b0 * b1 * a3 + 2.0 * (t0 * b1 + t1 * b0) * a4 + 2.0 * t0 * t1 * a5;
+			D2 += (b1 * b1 + 2.0 * b0 * b2) * a3 + 2.0 * (t0 * b2 + t1 * b1 + t2 * b0) * a4 + (t1 * t1 + 2.0 * t0 * t2) * a5;
+			D3 += 2.0 * b1 * b2 * a3 + 2.0 * (t1 * b2 + t2 * b1) * a4 + 2.0 * t1 * t2 * a5;
+			D4 += b2 * b2 * a3 + 2.0 * t2 * b2 * a4 + t2 * t2 * a5;
+		}
+		U0 = warp_sum(U0); U1 = warp_sum(U1); U2 = warp_sum(U2);
+		D0 = warp_sum(D0); D1 = warp_sum(D1); D2 = warp_sum(D2); D3 = warp_sum(D3); D4 = warp_sum(D4);
+		for (int i2 = lane; i2 < n2; i2 += 32) {
+			double c2 = c2g[i2];
+			double up = U0 + c2 * (U1 + c2 * U2);
+			double down = D0 + c2 * (D1 + c2 * (D2 + c2 * (D3 + c2 * D4)));
+			double k = up / down;
+			double score = a0sum + k * (-2.0 * up + k * down);
+			if (grid) grid[((size_t)pid * n1 + i1) * n2 + i2] = score;
+			int cell = i1 * n2 + i2;
+			if (score < best || (score == best && cell < bcell)) { best = score; bcell = cell; }
+		}
+	}
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) {
+		double ob = __shfl_xor_sync(0xffffffffu, best, o);
+		int oc = __shfl_xor_sync(0xffffffffu, bcell, o);
+		bool take = (oc >= 0) && (bcell < 0 || ob < best || (ob == best && oc < bcell));
+		if (take) { best = ob; bcell = oc; }
+	}
+	if (lane == 0) {
+		if (bcell >= 0) {
+			chi[pid] = sqrt(best);
+			c1o[pid] = c1g[bcell / n2];
+			c2o[pid] = c2g[bcell % n2];
+		} else {
+			chi[pid] = __longlong_as_double(0x7ff8000000000000LL);
+			c1o[pid] = __longlong_as_double(0x7ff8000000000000LL);
+			c2o[pid] = __longlong_as_double(0x7ff8000000000000LL);
+		}
+		if (cello) cello[pid] = bcell;
+	}
+}
+
+inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
+inline int qthreads(int Q) { return ((Q + 31) / 32) * 32; }
+
+} // namespace
+
+extern "C" {
+
+int sxsk_spf_transpose(const double *flat, double2 *spf_t, int Q, int L, cudaStream_t s)
+{
+	int K2 = (L + 1) * (L + 1);
+	k_spf_transpose<<<nblk(3L * Q * K2, 256), 256, 0, s>>>(flat, spf_t, Q, K2);
+	return cudaGetLastError();
+}
+
+int sxsk_rotate(const double2 *spf_t, const double *dtab, const double2 *tw, int Q, int L, int conj,
+                double2 *out, cudaStream_t s)
+{
+	int K = L + 1, N = 2 * L + 1;
+	dim3 grid(K * N, N);
+	k_rotate<<<grid, qthreads(Q), 0, s>>>(spf_t, dtab, tw, Q, L, conj, out);
+	return cudaGetLastError();
+}
+
+int sxsk_translate(const double2 *U, const double2 *tmat, const int32_t *combo_zbg, int ncombo,
+                   int Q, int L, double2 *out, cudaStream_t s)
+{
+	if (ncombo <= 0) return 0;
+	dim3 grid(ncombo, 2 * L + 1);
+	k_translate<4><<<grid, qthreads(Q), 0, s>>>(U, tmat, combo_zbg, Q, L, out);
+	return cudaGetLastError();
+}
+
+int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, const double2 *P, const double2 *R,
+                    const double2 *tw, const double *cst, int Q, int L, double *cross, cudaStream_t s)
+{
+	if (npose <= 0) return 0;
+	k_pose_cross<<<npose, qthreads(Q), 0, s>>>(poses, combo_base, P, R, tw, cst, Q, L, cross);
+	return cudaGetLastError();
+}
+
+int sxsk_fit_grid(const double *cross, int npose, int Q, const double *q, const double *a, double a0sum,
+                  double peak, const double *gtab, const double *c1g, int n1, const double *c2g, int n2,
+                  double *chi, double *c1, double *c2, int32_t *cell, double *grid, double *scaled,
+                  cudaStream_t s)
+{
+	if (npose <= 0) return 0;
+	size_t smem = (size_t)FIT_WARPS * 6 * Q * sizeof(double);
+	if (smem > 48 * 1024) cudaFuncSetAttribute(k_fit_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	k_fit_grid<<<nblk(npose, FIT_WARPS), FIT_WARPS * 32, smem, s>>>(cross, npose, Q, q, a, a0sum, peak, gtab, c1g,
+	                                                               n1, c2g, n2, chi, c1, c2, cell, grid, scaled);
+	return cudaGetLastError();
+}
+
+} // extern "C"

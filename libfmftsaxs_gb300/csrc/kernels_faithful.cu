@@ -1,0 +1,262 @@
+/*
+ * FP64 kernels whose rounding must follow the reference operation by
+ * operation: the spherical-Bessel power series (its cancellation at large
+ * q*r amplifies any reordering), the associated-Legendre recurrence, the
+ * translation-matrix p-sum, the A_lm accumulation and the self terms.
+ *
+ * This translation unit is compiled with -fmad=false so that no multiply-add
+ * is contracted: every expression below is evaluated in the reference's
+ * order with one rounding per operation, as gcc -std=c11 does on the host.
+ */
+#include "kernels.h"
+
+#include <math.h>
+
+#define SXS_PI 3.14159265358 /* the reference's pi (src/define.h:14-16 under -std=c11) */
+
+namespace {
+
+__device__ __forceinline__ int lm_index(int l, int m) { return l * (l + 1) + m; }
+
+/* (2l+1)!! as the reference's doublefact (src/sfbessel.c:21-37). */
+__device__ double odd_factorial(int n)
+{
+	double r = 1.0;
+	for (int i = 1; i <= n; i += 2) r *= (double)i;
+	return r;
+}
+
+/* j_l(x) by the reference's truncated power series (src/sfbessel.c:40-60). */
+__device__ double sbessel(int l, double x)
+{
+	if (x > 0.0) {
+		double tl1 = 2.0 * (double)l + 1.0;
+		double term = 1.0 / odd_factorial((int)tl1);
+		double sum = term;
+		/* the reference has no iteration bound; terms decay factorially, so
+		 * the cap (far above any count the series reaches) only guards
+		 * against non-finite input */
+		for (int k = 1; fabs(term / sum) > 0.00001 && k < 100000; k++) {
+			double ratio = ((-1.0) * x * x) / ((2.0 * (double)k) * (2.0 * (double)k + tl1));
+			term = term * ratio;
+			sum = sum + term;
+		}
+		return sum * pow(x, (double)l);
+	}
+	return l == 0 ? 1.0 : 0.0;
+}
+
+/* Per atom and m >= 0: P_l^m(cos theta) by the recurrence of
+ * src/borrowed.c:40-65 (N = L+1), times the Y norm, times e^{-i m phi}
+ * (src/pdb2spf.c:76-84), written for +m and -m. */
+__global__ void k_ylm(const double *__restrict__ xyz, int natoms, int L, const double *__restrict__ ynorm,
+                      double2 *__restrict__ ylm)
+{
+	int K = L + 1, K2 = K * K;
+	long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= (long)natoms * K) return;
+	int a = (int)(t / K), m = (int)(t % K);
+	double x = xyz[3 * a], y = xyz[3 * a + 1], z = xyz[3 * a + 2];
+	double r = sqrt(x * x + y * y + z * z);
+	double th = acos(z / r);
+	double ph;
+	if (y > 0.0) ph = acos(x / sqrt(x * x + y * y));
+	else ph = -acos(x / sqrt(x * x + y * y)) + 2.0 * SXS_PI;
+	double c = cos(th);
+	double s = sqrt(1. - c * c);
+	int N = K;
+	/* P_m^m: the reference's diagonal chain (lines 54 and 63 agree on the
+	 * formula), then P_{m+1}^m and the upward recurrence in l. */
+	double pmm = 1;
+	for (int j = 1; j <= m; j++) pmm = -1. * (2. * j - 1.) * s * pmm;
+	double p_lm2 = 0.0, p_lm1 = pmm;
+	double2 *out = ylm + (size_t)a * K2;
+	for (int l = m; l < N; l++) {
+		double p;
+		if (l == m) {
+			p = pmm;
+		} else if (l == m + 1) {
+			if (m == 0) p = c;                          /* P_1^0 = x */
+			else p = (2. * m + 1.) * c * pmm;           /* P_{m+1}^m */
+		} else {
+			if (m == 0) p = (2. * l - 1.) / l * c * p_lm1 - (l - 1.) / l * p_lm2;
+			else p = (2. * l - 1.) / (l - m) * c * p_lm1 - (l + m - 1.) / (l - m) * p_lm2;
+		}
+		p_lm2 = p_lm1;
+		p_lm1 = p;
+		if (l == m) { p_lm2 = 0.0; p_lm1 = p; }
+		double hp = ynorm[l * (2 * L + 1) + (m + L)] * p;
+		out[lm_index(l, m)] = make_double2(hp * cos(ph * m), hp * sin(-ph * m));
+		if (m > 0) {
+			double hn = ynorm[l * (2 * L + 1) + (-m + L)] * p;
+			out[lm_index(l, -m)] = make_double2(hn * cos(ph * (-m)), hn * sin(-ph * (-m)));
+		}
+	}
+}
+
+/* j_l(q r_a): jl[a][q][l]. */
+__global__ void k_jl(const double *__restrict__ xyz, int natoms, const double *__restrict__ q, int Q, int L,
+                     double *__restrict__ jl)
+{
+	int K = L + 1;
+	long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= (long)natoms * Q * K) return;
+	int l = (int)(t % K);
+	long r2 = t / K;
+	int iq = (int)(r2 % Q), a = (int)(r2 / Q);
+	double x = xyz[3 * a], y = xyz[3 * a + 1], z = xyz[3 * a + 2];
+	double r = sqrt(x * x + y * y + z * z);
+	jl[t] = sbessel(l, q[iq] * r);
+}
+
+/* A[ch][q][lm] = 4 pi i^l sum_a f_ch(a) (j_l(q r_a) Y*_lm(a)), atoms in
+ * order, each term f*(j*Y) as src/pdb2spf.c:104-112, then the phase of
+ * lines 118-147.  Output in the host flat layout [3][Q][K2][2]. */
+__global__ void k_accum(const double2 *__restrict__ ylm, const double *__restrict__ jl,
+                        const double *__restrict__ vac, const double *__restrict__ dum, const double *__restrict__ wfac,
+                        int natoms, int Q, int L, double *__restrict__ spf)
+{
+	int K = L + 1, K2 = K * K;
+	long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= (long)Q * K2) return;
+	int lm = (int)(t % K2), iq = (int)(t / K2);
+	int l = 0;
+	while ((l + 1) * (l + 1) <= lm) l++;
+	double vr = 0.0, vi = 0.0, dr = 0.0, di = 0.0, wr = 0.0, wi = 0.0;
+	for (int a = 0; a < natoms; a++) {
+		double b = jl[((size_t)a * Q + iq) * K + l];
+		double2 h = ylm[(size_t)a * K2 + lm];
+		double xr = b * h.x, xi = b * h.y;
+		double fv = vac[a], fd = dum[a], fw = wfac[a];
+		vr += fv * xr; vi += fv * xi;
+		dr += fd * xr; di += fd * xi;
+		wr += fw * xr; wi += fw * xi;
+	}
+	const double fp = 4.0 * SXS_PI;
+	double cre[4] = {fp, 0.0, -fp, 0.0}, cim[4] = {0.0, fp, 0.0, -fp};
+	double c_r = cre[l % 4], c_i = cim[l % 4];
+	size_t chs = (size_t)Q * K2 * 2;
+	double *o = spf + ((size_t)iq * K2 + lm) * 2;
+	o[0] = c_r * vr - c_i * vi;           o[1] = c_r * vi + c_i * vr;
+	o[chs] = c_r * dr - c_i * di;         o[chs + 1] = c_r * di + c_i * dr;
+	o[2 * chs] = c_r * wr - c_i * wi;     o[2 * chs + 1] = c_r * wi + c_i * wr;
+}
+
+/* bes[iz][q][p] = j_p(z q) (src/fftsaxs.c:110-121). */
+__global__ void k_bessel_z(const double *__restrict__ z, int nz, const double *__restrict__ q, int Q, int L,
+                           double *__restrict__ bes)
+{
+	int N = 2 * L + 1;
+	long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= (long)nz * Q * N) return;
+	int p = (int)(t % N);
+	long r2 = t / N;
+	int iq = (int)(r2 % Q), iz = (int)(r2 / Q);
+	bes[t] = sbessel(p, z[iz] * q[iq]);
+}
+
+/* T^{|m|}_{l l1}(q z) = sum_p (-1)^m i^p j_p d_lm(l1,p) for l <= l1, mirrored
+ * (src/fftsaxs.c:182-243).  Thread = (iz, m, l, l1 >= l, q), q fastest. */
+__global__ void k_tmatrix(const double *__restrict__ bes, const double *__restrict__ ds, int nz, int Q, int L,
+                          const int2 *__restrict__ ll1, int nll1, double2 *__restrict__ tmat)
+{
+	const double ipr[4] = {1.0, 0.0, -1.0, 0.0};
+	const double ipi[4] = {0.0, 1.0, 0.0, -1.0};
+	int K = L + 1, N = 2 * L + 1;
+	long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= (long)nz * (K) * nll1 * Q) return;
+	int iq = (int)(t % Q);
+	long r2 = t / Q;
+	int j = (int)(r2 % nll1);
+	r2 /= nll1;
+	int m = (int)(r2 % K), iz = (int)(r2 / K);
+	int l = ll1[j].x, l1 = ll1[j].y;
+	if (l < m) return;
+	double sgn = (m % 2 == 0) ? 1.0 : -1.0;
+	const double *dp = ds + ((size_t)lm_index(l, m) * K + l1) * N;
+	const double *bp = bes + ((size_t)iz * Q + iq) * N;
+	double re = 0.0, im = 0.0;
+	int p0 = l1 - l;  /* |l - l1| with l <= l1 */
+	for (int p = p0; p <= l + l1; p++) {
+		double v = sgn * dp[p] * bp[p];
+		re += ipr[p % 4] * v;
+		im += ipi[p % 4] * v;
+	}
+	size_t base = ((size_t)iz * K + m) * K;
+	tmat[((base + l) * K + l1) * Q + iq] = make_double2(re, im);
+	tmat[((base + l1) * K + l) * Q + iq] = make_double2(re, im);
+}
+
+/* Self terms of fill_const (src/fftsaxs.c:27-50, 52-85): per channel pair
+ * and q, sum over lm of Re(A1 conj A2) then Re(B1 conj B2), interleaved as in
+ * comp_const_int, times {1,2,2,1,2,1}.  spf in the host flat layout. */
+__global__ void k_const_int(const double *__restrict__ A, const double *__restrict__ B, int Q, int L,
+                            double *__restrict__ cst)
+{
+	int K2 = (L + 1) * (L + 1);
+	int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= 6 * Q) return;
+	int c = t / Q, iq = t % Q;
+	const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {0, 1, 2, 1, 2, 2};
+	const double mul[6] = {1.0, 2.0, 2.0, 1.0, 2.0, 1.0};
+	size_t chs = (size_t)Q * K2 * 2;
+	const double *a1 = A + pa[c] * chs + (size_t)iq * K2 * 2, *a2 = A + pb[c] * chs + (size_t)iq * K2 * 2;
+	const double *b1 = B + pa[c] * chs + (size_t)iq * K2 * 2, *b2 = B + pb[c] * chs + (size_t)iq * K2 * 2;
+	double s = 0.0;
+	for (int i = 0; i < K2; i++) {
+		s += a1[2 * i] * a2[2 * i] + a1[2 * i + 1] * a2[2 * i + 1];
+		s += b1[2 * i] * b2[2 * i] + b1[2 * i + 1] * b2[2 * i + 1];
+	}
+	cst[t] = s * mul[c];
+}
+
+inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
+
+} // namespace
+
+extern "C" {
+
+size_t sxsk_expand_ws_ylm(int natoms, int L) { return (size_t)natoms * (L + 1) * (L + 1) * sizeof(double2); }
+size_t sxsk_expand_ws_jl(int natoms, int Q, int L) { return (size_t)natoms * Q * (L + 1) * sizeof(double); }
+
+int sxsk_expand(const double *xyz, const double *vac, const double *dum, const double *wfac, int natoms,
+                 const double *q, int Q, int L, const double *ynorm, double2 *ylm_ws, double *jl_ws,
+                 double *spf_out, cudaStream_t s)
+{
+	int K = L + 1;
+	if (natoms <= 0) {
+		cudaMemsetAsync(spf_out, 0, (size_t)3 * Q * K * K * 2 * sizeof(double), s);
+		return cudaGetLastError();
+	}
+	k_ylm<<<nblk((long)natoms * K, 128), 128, 0, s>>>(xyz, natoms, L, ynorm, ylm_ws);
+	k_jl<<<nblk((long)natoms * Q * K, 128), 128, 0, s>>>(xyz, natoms, q, Q, L, jl_ws);
+	k_accum<<<nblk((long)Q * K * K, 128), 128, 0, s>>>(ylm_ws, jl_ws, vac, dum, wfac, natoms, Q, L, spf_out);
+	return cudaGetLastError();
+}
+
+int sxsk_bessel_z(const double *z, int nz, const double *q, int Q, int L, double *bes, cudaStream_t s)
+{
+	long n = (long)nz * Q * (2 * L + 1);
+	if (n == 0) return 0;
+	k_bessel_z<<<nblk(n, 128), 128, 0, s>>>(z, nz, q, Q, L, bes);
+	return cudaGetLastError();
+}
+
+int sxsk_tmatrix(const double *bes, const double *dsymb, int nz, int Q, int L, const int2 *ll1, int nll1,
+                  double2 *tmat, cudaStream_t s)
+{
+	int K = L + 1;
+	long n = (long)nz * K * nll1 * Q;
+	if (n == 0) return 0;
+	cudaMemsetAsync(tmat, 0, (size_t)nz * K * K * K * Q * sizeof(double2), s);
+	k_tmatrix<<<nblk(n, 128), 128, 0, s>>>(bes, dsymb, nz, Q, L, ll1, nll1, tmat);
+	return cudaGetLastError();
+}
+
+int sxsk_const_int(const double *A, const double *B, int Q, int L, double *cst, cudaStream_t s)
+{
+	k_const_int<<<nblk(6 * Q, 64), 64, 0, s>>>(A, B, Q, L, cst);
+	return cudaGetLastError();
+}
+
+} // extern "C"

@@ -1,0 +1,555 @@
+/*
+ * Host orchestration of the GPU scoring path: device context, reusable
+ * plans, the expansion entry point and the drop-in sxs_compute_saxs_scores
+ * (src/fftsaxs.c:608-986 of the reference).
+ *
+ * The device computes, per call:
+ *   tables   twiddles; self terms (fill_const); receptor rotation table
+ *            P(b1,g1) and ligand rotation table U(b2,g2); j_p(qz) and the
+ *            translation matrices T for every touched z
+ *   per chunk of touched (z, b2, g2) combos: the translated ligand table R,
+ *            then the per-pose cross terms of every pose in those combos
+ *   fit      grid chi^2 over (c1, c2) or L-BFGS-B, per pose
+ * Poses are grouped by (z, b2, g2) with a counting sort on the host.
+ */
+#define _XOPEN_SOURCE 700
+#include <math.h>
+#include <pthread.h>
+#include <stdarg.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "sxs_internal.h"
+
+/* ------------------------------------------------------------- errors */
+static _Thread_local char g_err[512];
+
+const char *sxsg_last_error(void) { return g_err; }
+
+int sxs_fail(int code, const char *fmt, ...)
+{
+	va_list ap;
+	va_start(ap, fmt);
+	vsnprintf(g_err, sizeof(g_err), fmt, ap);
+	va_end(ap);
+	return code;
+}
+
+int sxs_cuda_fail(cudaError_t e, const char *what)
+{
+	return sxs_fail(-100 - (int)e, "%s: %s", what, cudaGetErrorString(e));
+}
+
+void sxs_die(const char *func, const char *msg)
+{
+	fprintf(stderr, "[Error] fmftsaxs-gb300, function %s: %s\n", func, msg);
+	exit(EXIT_FAILURE);
+}
+
+/* ------------------------------------------------------------ context */
+static pthread_mutex_t g_init_lock = PTHREAD_MUTEX_INITIALIZER;
+static int g_inited = 0;
+static int g_device = 0;
+static cudaStream_t g_stream;
+static long long g_launches = 0;
+
+void sxs_count_launches(int n) { __atomic_add_fetch(&g_launches, n, __ATOMIC_RELAXED); }
+long long sxsg_launch_count(void) { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
+
+int sxsg_init(int device)
+{
+	pthread_mutex_lock(&g_init_lock);
+	if (g_inited) {
+		pthread_mutex_unlock(&g_init_lock);
+		return 0;
+	}
+	int n = 0;
+	cudaError_t e = cudaGetDeviceCount(&n);
+	if (e != cudaSuccess || n == 0) {
+		pthread_mutex_unlock(&g_init_lock);
+		return sxs_fail(-1, "no CUDA device available (%s)", cudaGetErrorString(e));
+	}
+	if (device < 0 || device >= n) {
+		pthread_mutex_unlock(&g_init_lock);
+		return sxs_fail(-1, "device %d out of range (%d devices)", device, n);
+	}
+	e = cudaSetDevice(device);
+	if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking);
+	if (e != cudaSuccess) {
+		pthread_mutex_unlock(&g_init_lock);
+		return sxs_cuda_fail(e, "device init");
+	}
+	g_device = device;
+	g_inited = 1;
+	pthread_mutex_unlock(&g_init_lock);
+	return 0;
+}
+
+int sxs_ensure_init(void)
+{
+	if (g_inited) {
+		cudaSetDevice(g_device);
+		return 0;
+	}
+	return sxsg_init(0);
+}
+
+cudaStream_t sxs_default_stream(void) { return g_stream; }
+
+/* --------------------------------------------------------- expansion */
+int sxsg_expand(const double *xyz, const double *vac, const double *dum, const double *sasa, double water_ff,
+                int natoms, const double *q, int Q, int L, double *spf_out)
+{
+	if (natoms < 0 || Q <= 0 || !q || !spf_out || (natoms > 0 && (!xyz || !vac || !dum)))
+		return sxs_fail(-2, "sxsg_expand: bad arguments");
+	const sxs_ltables *lt;
+	int rc = sxs_ltables_get(L, &lt);
+	if (rc) return rc;
+	cudaStream_t s = g_stream;
+	int K = L + 1;
+	size_t spf_n = (size_t)3 * Q * K * K * 2;
+	double *wf = malloc(sizeof(double) * (natoms > 0 ? natoms : 1));
+	for (int i = 0; i < natoms; i++) wf[i] = sasa ? water_ff * sasa[i] : 0.0;
+	double *d_xyz = NULL, *d_vac = NULL, *d_dum = NULL, *d_wf = NULL, *d_q = NULL, *d_jl = NULL, *d_out = NULL;
+	double2 *d_ylm = NULL;
+	int na = natoms > 0 ? natoms : 1;
+	cudaError_t e = cudaSuccess;
+	if (!e) e = cudaMalloc((void **)&d_xyz, sizeof(double) * 3 * na);
+	if (!e) e = cudaMalloc((void **)&d_vac, sizeof(double) * na);
+	if (!e) e = cudaMalloc((void **)&d_dum, sizeof(double) * na);
+	if (!e) e = cudaMalloc((void **)&d_wf, sizeof(double) * na);
+	if (!e) e = cudaMalloc((void **)&d_q, sizeof(double) * Q);
+	if (!e) e = cudaMalloc((void **)&d_jl, sxsk_expand_ws_jl(na, Q, L));
+	if (!e) e = cudaMalloc((void **)&d_ylm, sxsk_expand_ws_ylm(na, L));
+	if (!e) e = cudaMalloc((void **)&d_out, sizeof(double) * spf_n);
+	if (!e && natoms > 0) {
+		e = cudaMemcpyAsync(d_xyz, xyz, sizeof(double) * 3 * natoms, cudaMemcpyHostToDevice, s);
+		if (!e) e = cudaMemcpyAsync(d_vac, vac, sizeof(double) * natoms, cudaMemcpyHostToDevice, s);
+		if (!e) e = cudaMemcpyAsync(d_dum, dum, sizeof(double) * natoms, cudaMemcpyHostToDevice, s);
+		if (!e) e = cudaMemcpyAsync(d_wf, wf, sizeof(double) * natoms, cudaMemcpyHostToDevice, s);
+	}
+	if (!e) e = cudaMemcpyAsync(d_q, q, sizeof(double) * Q, cudaMemcpyHostToDevice, s);
+	if (!e) {
+		e = (cudaError_t)sxsk_expand(d_xyz, d_vac, d_dum, d_wf, natoms, d_q, Q, L, lt->d_ynorm, d_ylm, d_jl, d_out, s);
+		sxs_count_launches(natoms > 0 ? 3 : 0);
+	}
+	if (!e) e = cudaMemcpyAsync(spf_out, d_out, sizeof(double) * spf_n, cudaMemcpyDeviceToHost, s);
+	if (!e) e = cudaStreamSynchronize(s);
+	cudaFree(d_xyz); cudaFree(d_vac); cudaFree(d_dum); cudaFree(d_wf); cudaFree(d_q);
+	cudaFree(d_jl); cudaFree(d_ylm); cudaFree(d_out);
+	free(wf);
+	if (e) return sxs_cuda_fail(e, "sxsg_expand");
+	return 0;
+}
+
+/* --------------------------------------------------------------- plan */
+struct sxsg_plan {
+	int L, K, N, K2, Q, nz, n1, n2, precision;
+	const sxs_ltables *lt;
+	cudaStream_t s;
+	double mult, peak, a0sum;
+	/* resident inputs */
+	double *d_A, *d_B, *d_q, *d_a, *d_gtab, *d_c1g, *d_c2g, *d_cst;
+	double2 *d_At, *d_Bt, *d_tw;
+	double *h_z;
+	/* rotation tables (depend on the twiddle variant) */
+	double2 *d_P, *d_U;
+	int tw_variant; /* -1 none, 0 simple_ft, 1 exact */
+	/* poses */
+	int64_t npose;
+	int skip;
+	sxsk_pose *h_poses, *d_poses;
+	int ncombo;
+	int32_t *h_combo, *d_combo; /* [ncombo][3]: tslot, b2, g2 */
+	int64_t *h_cstart;          /* [ncombo+1] first sorted pose of each combo */
+	int nzt;                    /* touched z count */
+	double *h_zt, *d_zt;        /* touched z values */
+	double *d_bes;
+	double2 *d_tmat;
+	size_t pose_cap, combo_cap, zt_cap;
+	/* per-chunk translated table */
+	double2 *d_R;
+	int64_t R_combos;
+	size_t r_budget;
+	/* outputs */
+	double *d_cross, *d_chi, *d_c1, *d_c2, *d_grid, *d_scaled, *d_scale;
+	int32_t *d_cell;
+	int *d_iters;
+	size_t out_cap;
+	int last_fit;
+	int grid_valid;
+	cudaEvent_t ev[6];
+	double ms[5];
+};
+
+static void plan_free_poses(sxsg_plan *p)
+{
+	free(p->h_poses); free(p->h_combo); free(p->h_cstart); free(p->h_zt);
+	cudaFree(p->d_poses); cudaFree(p->d_combo); cudaFree(p->d_zt); cudaFree(p->d_bes); cudaFree(p->d_tmat);
+	p->h_poses = NULL; p->h_combo = NULL; p->h_cstart = NULL; p->h_zt = NULL;
+	p->d_poses = NULL; p->d_combo = NULL; p->d_zt = NULL; p->d_bes = NULL; p->d_tmat = NULL;
+	p->pose_cap = p->combo_cap = p->zt_cap = 0;
+}
+
+void sxsg_plan_destroy(sxsg_plan *p)
+{
+	if (!p) return;
+	cudaStreamSynchronize(p->s);
+	plan_free_poses(p);
+	cudaFree(p->d_A); cudaFree(p->d_B); cudaFree(p->d_q); cudaFree(p->d_a); cudaFree(p->d_gtab);
+	cudaFree(p->d_c1g); cudaFree(p->d_c2g); cudaFree(p->d_cst); cudaFree(p->d_At); cudaFree(p->d_Bt);
+	cudaFree(p->d_tw); cudaFree(p->d_P); cudaFree(p->d_U); cudaFree(p->d_R);
+	cudaFree(p->d_cross); cudaFree(p->d_chi); cudaFree(p->d_c1); cudaFree(p->d_c2); cudaFree(p->d_grid);
+	cudaFree(p->d_scaled); cudaFree(p->d_scale); cudaFree(p->d_cell); cudaFree(p->d_iters);
+	for (int i = 0; i < 6; i++) if (p->ev[i]) cudaEventDestroy(p->ev[i]);
+	free(p->h_z);
+	free(p);
+}
+
+int sxsg_plan_create(sxsg_plan **out, const double *A, const double *B, const double *q, int Q, const double *z,
+                     int nz, int L, const double *a, double mult, double peak, const double *c1g, int n1,
+                     const double *c2g, int n2, int precision)
+{
+	if (!out || !A || !B || !q || Q <= 0 || Q > 1024 || !z || nz <= 0 || !a)
+		return sxs_fail(-2, "sxsg_plan_create: bad arguments (Q must be in [1, 1024])");
+	if ((n1 > 0 && !c1g) || (n2 > 0 && !c2g) || n1 < 0 || n2 < 0)
+		return sxs_fail(-2, "sxsg_plan_create: bad fit grid");
+	if (precision != SXSG_FP64) return sxs_fail(-2, "sxsg_plan_create: unknown precision %d", precision);
+	const sxs_ltables *lt;
+	int rc = sxs_ltables_get(L, &lt);
+	if (rc) return rc;
+	sxsg_plan *p = calloc(1, sizeof(*p));
+	p->L = L; p->K = L + 1; p->N = 2 * L + 1; p->K2 = p->K * p->K; p->Q = Q; p->nz = nz;
+	p->n1 = n1; p->n2 = n2; p->precision = precision; p->lt = lt; p->s = g_stream;
+	p->mult = mult; p->peak = peak; p->tw_variant = -1;
+	double s0 = 0.0;
+	for (int i = 0; i < Q; i++) s0 += a[6 * i];
+	p->a0sum = s0;
+	p->h_z = malloc(sizeof(double) * nz);
+	memcpy(p->h_z, z, sizeof(double) * nz);
+	size_t spf_n = (size_t)3 * Q * p->K2 * 2;
+	cudaError_t e = cudaSuccess;
+	for (int i = 0; i < 6 && !e; i++) e = cudaEventCreate(&p->ev[i]);
+	if (!e) e = cudaMalloc((void **)&p->d_A, sizeof(double) * spf_n);
+	if (!e) e = cudaMalloc((void **)&p->d_B, sizeof(double) * spf_n);
+	if (!e) e = cudaMalloc((void **)&p->d_At, sizeof(double) * spf_n);
+	if (!e) e = cudaMalloc((void **)&p->d_Bt, sizeof(double) * spf_n);
+	if (!e) e = cudaMalloc((void **)&p->d_q, sizeof(double) * Q);
+	if (!e) e = cudaMalloc((void **)&p->d_a, sizeof(double) * 6 * Q);
+	if (!e) e = cudaMalloc((void **)&p->d_cst, sizeof(double) * 6 * Q);
+	if (!e) e = cudaMalloc((void **)&p->d_tw, sizeof(double2) * p->N);
+	if (!e && n1 > 0) e = cudaMalloc((void **)&p->d_gtab, sizeof(double) * n1 * Q);
+	if (!e && n1 > 0) e = cudaMalloc((void **)&p->d_c1g, sizeof(double) * n1);
+	if (!e && n2 > 0) e = cudaMalloc((void **)&p->d_c2g, sizeof(double) * n2);
+	size_t rot_n = (size_t)p->K * p->N * p->K2 * 3 * Q;
+	if (!e) e = cudaMalloc((void **)&p->d_P, sizeof(double2) * rot_n);
+	if (!e) e = cudaMalloc((void **)&p->d_U, sizeof(double2) * rot_n);
+	if (e) {
+		sxsg_plan_destroy(p);
+		return sxs_cuda_fail(e, "sxsg_plan_create allocation");
+	}
+	cudaStream_t s = p->s;
+	e = cudaMemcpyAsync(p->d_A, A, sizeof(double) * spf_n, cudaMemcpyHostToDevice, s);
+	if (!e) e = cudaMemcpyAsync(p->d_B, B, sizeof(double) * spf_n, cudaMemcpyHostToDevice, s);
+	if (!e) e = cudaMemcpyAsync(p->d_q, q, sizeof(double) * Q, cudaMemcpyHostToDevice, s);
+	if (!e) e = cudaMemcpyAsync(p->d_a, a, sizeof(double) * 6 * Q, cudaMemcpyHostToDevice, s);
+	if (!e && n1 > 0) {
+		/* G(c1, q) = c1^3 exp(-mult (c1^2 - 1) q^2) exactly as point_score
+		 * evaluates it (src/min_saxs.c:404-423) */
+		double *g = malloc(sizeof(double) * n1 * Q);
+		for (int i = 0; i < n1; i++) {
+			double c1 = c1g[i];
+			double corr = -mult * (c1 * c1 - 1.0);
+			double c1c = c1 * c1 * c1;
+			for (int k = 0; k < Q; k++) g[(size_t)i * Q + k] = c1c * exp(corr * q[k] * q[k]);
+		}
+		e = cudaMemcpy(p->d_gtab, g, sizeof(double) * n1 * Q, cudaMemcpyHostToDevice);
+		free(g);
+		if (!e) e = cudaMemcpyAsync(p->d_c1g, c1g, sizeof(double) * n1, cudaMemcpyHostToDevice, s);
+	}
+	if (!e && n2 > 0) e = cudaMemcpyAsync(p->d_c2g, c2g, sizeof(double) * n2, cudaMemcpyHostToDevice, s);
+	if (!e) {
+		e = (cudaError_t)sxsk_spf_transpose(p->d_A, p->d_At, Q, L, s);
+		if (!e) e = (cudaError_t)sxsk_spf_transpose(p->d_B, p->d_Bt, Q, L, s);
+		if (!e) e = (cudaError_t)sxsk_const_int(p->d_A, p->d_B, Q, L, p->d_cst, s);
+		sxs_count_launches(3);
+	}
+	if (!e) e = cudaStreamSynchronize(s);
+	if (e) {
+		sxsg_plan_destroy(p);
+		return sxs_cuda_fail(e, "sxsg_plan_create upload");
+	}
+	size_t fr = 0, tot = 0;
+	cudaMemGetInfo(&fr, &tot);
+	p->r_budget = fr / 2;
+	*out = p;
+	return 0;
+}
+
+static int grow(void **ptr, size_t *cap, size_t need, size_t elem)
+{
+	if (*cap >= need && *ptr) return 0;
+	cudaFree(*ptr);
+	*ptr = NULL;
+	size_t n = need > 0 ? need : 1;
+	cudaError_t e = cudaMalloc(ptr, n * elem);
+	if (e) {
+		*cap = 0;
+		return sxs_cuda_fail(e, "device allocation");
+	}
+	*cap = n;
+	return 0;
+}
+
+int sxsg_plan_set_poses(sxsg_plan *p, const int64_t *index, int64_t n, int skip)
+{
+	if (!p || n < 0 || (n > 0 && !index)) return sxs_fail(-2, "sxsg_plan_set_poses: bad arguments");
+	if (n > INT32_MAX) return sxs_fail(-2, "sxsg_plan_set_poses: at most 2^31-1 poses per plan");
+	int L = p->L, N = p->N, nb = p->K, nz = p->nz;
+	plan_free_poses(p);
+	p->npose = n;
+	p->skip = skip;
+	p->grid_valid = 0;
+	int64_t nkey = (int64_t)nz * nb * N;
+	int64_t *cnt = calloc(nkey + 1, sizeof(int64_t));
+	int32_t *key = malloc(sizeof(int32_t) * (n > 0 ? n : 1));
+	sxsk_pose *tmp = malloc(sizeof(sxsk_pose) * (n > 0 ? n : 1));
+	char *zused = calloc(nz, 1);
+	for (int64_t i = 0; i < n; i++) {
+		int64_t v = index[i];
+		if (v < 0) {
+			free(cnt); free(key); free(tmp); free(zused);
+			return sxs_fail(-3, "pose %lld: negative grid index %lld", (long long)i, (long long)v);
+		}
+		sxsk_pose ps;
+		ps.g2 = (int32_t)(v % N); v /= N;
+		ps.g1 = (int32_t)(v % N); v /= N;
+		ps.a2 = (int32_t)(v % N); v /= N;
+		ps.b2 = (int32_t)(v % nb); v /= nb;
+		ps.b1 = (int32_t)(v % nb); v /= nb;
+		if (v >= nz) {
+			free(cnt); free(key); free(tmp); free(zused);
+			return sxs_fail(-3, "pose %lld: translation slot %lld >= znum %d", (long long)i, (long long)v, nz);
+		}
+		ps.zi = (int32_t)v;
+		ps.src = (int32_t)i;
+		ps.combo = 0;
+		tmp[i] = ps;
+		key[i] = (int32_t)(((int64_t)ps.zi * nb + ps.b2) * N + ps.g2);
+		cnt[key[i] + 1]++;
+		zused[ps.zi] = 1;
+	}
+	/* touched z -> slot */
+	int *zslot = malloc(sizeof(int) * nz);
+	int nzt = 0;
+	for (int i = 0; i < nz; i++) zslot[i] = zused[i] ? nzt++ : -1;
+	p->nzt = nzt;
+	p->h_zt = malloc(sizeof(double) * (nzt > 0 ? nzt : 1));
+	for (int i = 0; i < nz; i++) if (zslot[i] >= 0) p->h_zt[zslot[i]] = p->h_z[i];
+	/* combos and counting sort */
+	int ncombo = 0;
+	for (int64_t k = 0; k < nkey; k++) if (cnt[k + 1]) ncombo++;
+	p->ncombo = ncombo;
+	p->h_combo = malloc(sizeof(int32_t) * 3 * (ncombo > 0 ? ncombo : 1));
+	p->h_cstart = malloc(sizeof(int64_t) * (ncombo + 1));
+	int32_t *cid = malloc(sizeof(int32_t) * nkey);
+	int c = 0;
+	for (int64_t k = 0; k < nkey; k++) {
+		if (cnt[k + 1]) {
+			cid[k] = c;
+			int g2 = (int)(k % N), b2 = (int)((k / N) % nb), zi = (int)(k / N / nb);
+			p->h_combo[3 * c] = zslot[zi];
+			p->h_combo[3 * c + 1] = b2;
+			p->h_combo[3 * c + 2] = g2;
+			c++;
+		} else {
+			cid[k] = -1;
+		}
+	}
+	for (int64_t k = 0; k < nkey; k++) cnt[k + 1] += cnt[k];
+	int64_t *pos = cnt; /* cnt[k] = first slot of key k */
+	p->h_poses = malloc(sizeof(sxsk_pose) * (n > 0 ? n : 1));
+	c = 0;
+	for (int64_t k = 0; k < nkey; k++)
+		if (cid[k] >= 0) p->h_cstart[c++] = pos[k];
+	p->h_cstart[ncombo] = n;
+	for (int64_t i = 0; i < n; i++) {
+		int64_t dst = pos[key[i]]++;
+		sxsk_pose ps = tmp[i];
+		ps.combo = cid[key[i]];
+		p->h_poses[dst] = ps;
+	}
+	free(cnt); free(key); free(tmp); free(zused); free(zslot); free(cid);
+
+	/* upload */
+	size_t nn = (size_t)(n > 0 ? n : 1);
+	int rc = 0;
+	cudaError_t e = cudaMalloc((void **)&p->d_poses, sizeof(sxsk_pose) * nn);
+	if (!e) e = cudaMalloc((void **)&p->d_combo, sizeof(int32_t) * 3 * (ncombo > 0 ? ncombo : 1));
+	if (!e) e = cudaMalloc((void **)&p->d_zt, sizeof(double) * (nzt > 0 ? nzt : 1));
+	if (!e && nzt > 0) e = cudaMalloc((void **)&p->d_bes, sizeof(double) * (size_t)nzt * p->Q * N);
+	if (!e && nzt > 0) e = cudaMalloc((void **)&p->d_tmat, sizeof(double2) * (size_t)nzt * p->K * p->K * p->K * p->Q);
+	if (!e && n > 0) e = cudaMemcpyAsync(p->d_poses, p->h_poses, sizeof(sxsk_pose) * n, cudaMemcpyHostToDevice, p->s);
+	if (!e && ncombo > 0) e = cudaMemcpyAsync(p->d_combo, p->h_combo, sizeof(int32_t) * 3 * ncombo, cudaMemcpyHostToDevice, p->s);
+	if (!e && nzt > 0) e = cudaMemcpyAsync(p->d_zt, p->h_zt, sizeof(double) * nzt, cudaMemcpyHostToDevice, p->s);
+	if (e) return sxs_cuda_fail(e, "sxsg_plan_set_poses upload");
+	size_t need = (size_t)nn;
+	if ((rc = grow((void **)&p->d_cross, &p->out_cap, need * 6 * p->Q, sizeof(double)))) return rc;
+	/* out_cap tracks d_cross in doubles; the per-pose vectors follow it */
+	cudaFree(p->d_chi); cudaFree(p->d_c1); cudaFree(p->d_c2); cudaFree(p->d_cell); cudaFree(p->d_scaled);
+	cudaFree(p->d_scale); cudaFree(p->d_iters); cudaFree(p->d_grid);
+	p->d_chi = p->d_c1 = p->d_c2 = p->d_scaled = p->d_scale = p->d_grid = NULL;
+	p->d_cell = NULL; p->d_iters = NULL;
+	e = cudaMalloc((void **)&p->d_chi, sizeof(double) * nn);
+	if (!e) e = cudaMalloc((void **)&p->d_c1, sizeof(double) * nn);
+	if (!e) e = cudaMalloc((void **)&p->d_c2, sizeof(double) * nn);
+	if (!e) e = cudaMalloc((void **)&p->d_cell, sizeof(int32_t) * nn);
+	if (!e) e = cudaMalloc((void **)&p->d_scale, sizeof(double) * nn);
+	if (!e) e = cudaMalloc((void **)&p->d_iters, sizeof(int) * nn);
+	if (!e) e = cudaMalloc((void **)&p->d_scaled, sizeof(double) * nn * 6 * p->Q);
+	if (e) return sxs_cuda_fail(e, "sxsg_plan_set_poses outputs");
+	(void)L;
+	return 0;
+}
+
+static int plan_tables(sxsg_plan *p)
+{
+	int L = p->L, Q = p->Q, N = p->N;
+	cudaStream_t s = p->s;
+	int variant = p->skip == 1 ? 0 : 1;
+	if (p->tw_variant != variant) {
+		double *tw = malloc(sizeof(double) * 2 * N);
+		sxs_twiddles_host(N, variant, tw);
+		cudaError_t e = cudaMemcpy(p->d_tw, tw, sizeof(double2) * N, cudaMemcpyHostToDevice);
+		free(tw);
+		if (e) return sxs_cuda_fail(e, "twiddle upload");
+		SXS_K(sxsk_rotate(p->d_At, p->lt->d_dtab, p->d_tw, Q, L, 0, p->d_P, s));
+		SXS_K(sxsk_rotate(p->d_Bt, p->lt->d_dtab, p->d_tw, Q, L, 1, p->d_U, s));
+		sxs_count_launches(2);
+		p->tw_variant = variant;
+	}
+	if (p->nzt > 0) {
+		SXS_K(sxsk_bessel_z(p->d_zt, p->nzt, p->d_q, Q, L, p->d_bes, s));
+		SXS_K(sxsk_tmatrix(p->d_bes, p->lt->d_dsymb, p->nzt, Q, L, p->lt->d_ll1, p->lt->nll1, p->d_tmat, s));
+		sxs_count_launches(2);
+	}
+	return 0;
+}
+
+int sxsg_plan_run(sxsg_plan *p, int fit_mode)
+{
+	if (!p) return sxs_fail(-2, "sxsg_plan_run: null plan");
+	if (fit_mode == SXSG_FIT_GRID && (p->n1 <= 0 || p->n2 <= 0))
+		return sxs_fail(-2, "sxsg_plan_run: grid fit needs a (c1, c2) grid");
+	if (fit_mode < 0 || fit_mode > 2) return sxs_fail(-2, "sxsg_plan_run: unknown fit mode %d", fit_mode);
+	int rc;
+	cudaStream_t s = p->s;
+	int Q = p->Q, L = p->L;
+	SXS_CU(cudaEventRecord(p->ev[0], s));
+	if ((rc = plan_tables(p))) return rc;
+	SXS_CU(cudaEventRecord(p->ev[1], s));
+	/* translated table in chunks of combos that fit the budget */
+	size_t per_combo = (size_t)p->K2 * 3 * Q * sizeof(double2);
+	int64_t chunk = (int64_t)(p->r_budget / per_combo);
+	if (chunk < 1) chunk = 1;
+	if (chunk > p->ncombo) chunk = p->ncombo;
+	if (chunk > 0 && p->R_combos < chunk) {
+		cudaFree(p->d_R);
+		p->d_R = NULL;
+		SXS_CU(cudaMalloc((void **)&p->d_R, per_combo * chunk));
+		p->R_combos = chunk;
+	}
+	float t_tr = 0, t_pc = 0;
+	for (int64_t c0 = 0; c0 < p->ncombo; c0 += chunk) {
+		int64_t c1 = c0 + chunk < p->ncombo ? c0 + chunk : p->ncombo;
+		SXS_CU(cudaEventRecord(p->ev[2], s));
+		SXS_K(sxsk_translate(p->d_U, p->d_tmat, p->d_combo + 3 * c0, (int)(c1 - c0), Q, L, p->d_R, s));
+		SXS_CU(cudaEventRecord(p->ev[3], s));
+		int64_t p0 = p->h_cstart[c0], p1 = p->h_cstart[c1];
+		SXS_K(sxsk_pose_cross(p->d_poses + p0, (int)(p1 - p0), (int)c0, p->d_P, p->d_R, p->d_tw, p->d_cst, Q, L,
+		                      p->d_cross, s));
+		SXS_CU(cudaEventRecord(p->ev[4], s));
+		sxs_count_launches(2);
+		if (p->ncombo > chunk) {
+			float a = 0, b = 0;
+			SXS_CU(cudaEventSynchronize(p->ev[4]));
+			cudaEventElapsedTime(&a, p->ev[2], p->ev[3]);
+			cudaEventElapsedTime(&b, p->ev[3], p->ev[4]);
+			t_tr += a; t_pc += b;
+		}
+	}
+	if (p->ncombo <= chunk && p->ncombo > 0) {
+		SXS_CU(cudaEventSynchronize(p->ev[4]));
+		cudaEventElapsedTime(&t_tr, p->ev[2], p->ev[3]);
+		cudaEventElapsedTime(&t_pc, p->ev[3], p->ev[4]);
+	}
+	SXS_CU(cudaEventRecord(p->ev[5], s));
+	int n = (int)p->npose;
+	if (fit_mode == SXSG_FIT_GRID) {
+		SXS_K(sxsk_fit_grid(p->d_cross, n, Q, p->d_q, p->d_a, p->a0sum, p->peak, p->d_gtab, p->d_c1g, p->n1, p->d_c2g,
+		                    p->n2, p->d_chi, p->d_c1, p->d_c2, p->d_cell, NULL, p->d_scaled, s));
+		sxs_count_launches(n > 0 ? 1 : 0);
+	} else if (fit_mode == SXSG_FIT_LBFGSB) {
+		/* rescale through the grid kernel is not needed: the L-BFGS-B kernel
+		 * rescales itself */
+		SXS_K(sxs_fit_lbfgsb_launch(p->d_cross, n, Q, p->d_q, p->d_a, p->mult, p->d_chi, p->d_c1, p->d_c2,
+		                            p->d_scale, p->d_iters, s));
+		sxs_count_launches(n > 0 ? 1 : 0);
+	}
+	p->last_fit = fit_mode;
+	p->grid_valid = 0;
+	cudaEvent_t end;
+	SXS_CU(cudaEventCreate(&end));
+	SXS_CU(cudaEventRecord(end, s));
+	SXS_CU(cudaEventSynchronize(end));
+	float t_tab = 0, t_fit = 0;
+	cudaEventElapsedTime(&t_tab, p->ev[0], p->ev[1]);
+	cudaEventElapsedTime(&t_fit, p->ev[5], end);
+	cudaEventDestroy(end);
+	p->ms[0] = t_tab; p->ms[1] = t_tr; p->ms[2] = t_pc; p->ms[3] = t_fit;
+	return 0;
+}
+
+int sxsg_plan_results(sxsg_plan *p, double *chi, double *c1, double *c2, int32_t *cell, double *cross, double *grid)
+{
+	if (!p) return sxs_fail(-2, "sxsg_plan_results: null plan");
+	size_t n = (size_t)p->npose;
+	cudaStream_t s = p->s;
+	if (n == 0) return 0;
+	if (chi) SXS_CU(cudaMemcpyAsync(chi, p->d_chi, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+	if (c1) SXS_CU(cudaMemcpyAsync(c1, p->d_c1, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+	if (c2) SXS_CU(cudaMemcpyAsync(c2, p->d_c2, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+	if (cell) SXS_CU(cudaMemcpyAsync(cell, p->d_cell, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+	if (cross) SXS_CU(cudaMemcpyAsync(cross, p->d_cross, sizeof(double) * n * 6 * p->Q, cudaMemcpyDeviceToHost, s));
+	if (grid) {
+		if (p->n1 <= 0 || p->n2 <= 0) return sxs_fail(-2, "no fit grid in this plan");
+		size_t gn = n * p->n1 * p->n2;
+		double *d_g = NULL;
+		SXS_CU(cudaMalloc((void **)&d_g, sizeof(double) * gn));
+		double *tc = NULL, *t1 = NULL, *t2 = NULL;
+		int32_t *tcell = NULL;
+		cudaError_t e = cudaMalloc((void **)&tc, sizeof(double) * n);
+		if (!e) e = cudaMalloc((void **)&t1, sizeof(double) * n);
+		if (!e) e = cudaMalloc((void **)&t2, sizeof(double) * n);
+		if (!e) e = cudaMalloc((void **)&tcell, sizeof(int32_t) * n);
+		if (!e) {
+			e = (cudaError_t)sxsk_fit_grid(p->d_cross, (int)n, p->Q, p->d_q, p->d_a, p->a0sum, p->peak, p->d_gtab,
+			                               p->d_c1g, p->n1, p->d_c2g, p->n2, tc, t1, t2, tcell, d_g, NULL, s);
+			sxs_count_launches(1);
+		}
+		if (!e) e = cudaMemcpyAsync(grid, d_g, sizeof(double) * gn, cudaMemcpyDeviceToHost, s);
+		if (!e) e = cudaStreamSynchronize(s);
+		cudaFree(d_g); cudaFree(tc); cudaFree(t1); cudaFree(t2); cudaFree(tcell);
+		if (e) return sxs_cuda_fail(e, "grid results");
+	}
+	SXS_CU(cudaStreamSynchronize(s));
+	return 0;
+}
+
+int sxsg_plan_timings(sxsg_plan *p, double *ms5)
+{
+	if (!p || !ms5) return sxs_fail(-2, "sxsg_plan_timings: bad arguments");
+	for (int i = 0; i < 5; i++) ms5[i] = p->ms[i];
+	ms5[4] = p->ms[0] + p->ms[1] + p->ms[2] + p->ms[3];
+	return 0;
+}

@@ -1,0 +1,70 @@
+/*
+ * Internal declarations shared by the host C files of fmftsaxs-gb300.
+ */
+#ifndef SXS_INTERNAL_H
+#define SXS_INTERNAL_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "fmftsaxs_gb300.h"
+#include "kernels.h"
+
+/* The reference is compiled with -std=c11, where <math.h> does not define
+ * M_PI, so src/define.h:14-16's fallback value is the pi of every formula on
+ * the path; the FFTW branch (exact DFT) uses the full-precision value. */
+#define SXS_PI 3.14159265358
+#define SXS_PI_FULL 3.14159265358979323846
+#define SXS_REL_ERR 0.05   /* src/define.h:21 */
+#define SXS_C1_LOWER 0.96  /* src/define.h:28-34 */
+#define SXS_C1_UPPER 1.04
+#define SXS_C2_LOWER -2.00
+#define SXS_C2_UPPER 4.00
+#define SXS_C1_DEFAULT 1.0
+#define SXS_C2_DEFAULT 0.0
+#define SXS_LMAX 60
+
+/* error state (thread-local message) */
+int sxs_fail(int code, const char *fmt, ...);
+int sxs_cuda_fail(cudaError_t e, const char *what);
+#define SXS_CU(call)                                                      \
+	do {                                                                  \
+		cudaError_t e_ = (call);                                          \
+		if (e_ != cudaSuccess) return sxs_cuda_fail(e_, #call);           \
+	} while (0)
+#define SXS_K(call)                                                       \
+	do {                                                                  \
+		int e_ = (call);                                                  \
+		if (e_ != 0) return sxs_cuda_fail((cudaError_t)e_, #call);        \
+	} while (0)
+/* abort the process like the reference's ERROR_MSG (src/common.h:26-30) */
+void sxs_die(const char *func, const char *msg);
+
+int sxs_ensure_init(void);
+cudaStream_t sxs_default_stream(void);
+void sxs_count_launches(int n);
+
+/* host tables (sxs_tables.c) */
+double sxs_sbessel_host(int l, double x);
+void sxs_wigner_d_host(int L, double beta, double *d);   /* [K][N][N] */
+void sxs_ynorm_host(int L, double *y);                    /* [K][N] (l, m+L) */
+void sxs_twiddles_host(int N, int exact, double *tw2);   /* [N][2] */
+const double *sxs_dsymb_cached(int L);                    /* [K2][K][N], built once per L */
+
+/* per-L device tables, cached for the process */
+typedef struct {
+	int L;
+	double *d_dtab;   /* [K][K][N][N] */
+	double *d_dsymb;  /* [K2][K][N] */
+	double *d_ynorm;  /* [K][N] */
+	int2 *d_ll1;      /* (l, l1 >= l) pairs */
+	int nll1;
+} sxs_ltables;
+int sxs_ltables_get(int L, const sxs_ltables **out);
+
+/* device L-BFGS-B over (c1, c2) for a batch of rescaled cross terms */
+int sxs_fit_lbfgsb_launch(const double *scaled, int npose, int Q, const double *q, const double *a, double mult,
+                          double *chi, double *c1, double *c2, double *scale, int *iters, cudaStream_t s);
+
+#endif
