@@ -194,6 +194,11 @@ int sxsg_expand(const double *xyz, const double *vacuum_ff, const double *dummy_
 int sxsg_bin_experiment(const double *exp_q, const double *exp_i, const double *exp_err, int nexp,
                         const double *qvals, int qnum, double rm, double *a, double *mult, double *peak);
 
+/* sxs_profile_from_spf on a flat expansion (profile.c:186-233): I(q) and
+ * err = 0.05 I of a single molecule at (c1, c2). */
+int sxsg_profile_from_flat(const double *spf, int L, int qnum, double rm, const double *qvals, double c1, double c2,
+                           double *in, double *err);
+
 /* Flat-array view of an sxs_spf_full ([3][qnum][(L+1)^2][2]). */
 int sxsg_spf_to_flat(const struct sxs_spf_full *s, double *flat);
 int sxsg_spf_from_flat(struct sxs_spf_full *s, const double *flat);
@@ -216,6 +221,10 @@ int sxsg_plan_create(sxsg_plan **plan, const double *A, const double *B, const d
  * poses the way the reference's skip = 1 does (simple_ft twiddles);
  * skip = 0 as its FFTW branch. */
 int sxsg_plan_set_poses(sxsg_plan *plan, const int64_t *index, int64_t n, int skip);
+/* Upper bound on the device memory of the per-chunk translated table (the
+ * default is half the free memory at plan creation); touched (z, b2, g2)
+ * combos are processed in chunks that fit. */
+int sxsg_plan_set_budget(sxsg_plan *plan, size_t bytes);
 /* Run the GPU work for the current pose list (asynchronous until results). */
 int sxsg_plan_run(sxsg_plan *plan, int fit_mode);
 /* Copy results to the host.  Any pointer may be NULL.  chi/c1/c2/cell: [n];
@@ -228,10 +237,37 @@ int sxsg_plan_results(sxsg_plan *plan, double *chi, double *c1, double *c2, int3
 int sxsg_plan_timings(sxsg_plan *plan, double *ms5);
 void sxsg_plan_destroy(sxsg_plan *plan);
 
+/* One-shot scoring from host buffers: plan, poses, run, results, release.
+ * chi/c1/c2 may be NULL; cross [n][6][qnum] may be NULL. */
+int sxsg_score_flat(const double *A, const double *B, const double *qvals, int qnum, const double *zvals, int znum,
+                    int L, const int64_t *index, int64_t n, int skip, const double *a, double mult, double peak,
+                    int fit_mode, const double *c1grid, int n1, const double *c2grid, int n2,
+                    double *chi, double *c1, double *c2, double *cross);
+
 /* Pose ingestion helpers (tools/correlate.c:202-240): grid index of one
  * Euler 6-tuple (z, b1, g1, a2, b2, g2 as written by sxs_ft2euler) at
  * translation slot z_idx. */
 int64_t sxsg_assemble_index(const double *euler6, int z_idx, int L);
+
+/* Batch pose ingestion, the way correlate builds its index list
+ * (index.c:38-75 then tools/correlate.c:172-251): for each pose i the
+ * ligand rotation rot[9i..9i+8] (row-major) and translation tr[3i..3i+2]
+ * go through sxs_ft2euler (reference ligand offset ref_lig[3]), the Euler
+ * values through the "% .3f" text round trip of the Euler file, z is
+ * matched to zvals within 1e-3, and the grid index is assembled.  keep[i]
+ * is 0 for poses whose z is not in zvals (index[i] = -1).  Returns the
+ * number kept. */
+int64_t sxsg_poses_to_indices(const double *rot, const double *tr, int64_t n, const double *ref_lig,
+                              const double *zvals, int znum, int L, int64_t *index, uint8_t *keep);
+
+/* Timing on the library's stream: start records an event; stop records a
+ * second one, waits for it and returns the elapsed milliseconds. */
+int sxsg_timer_start(void);
+double sxsg_timer_stop(void);
+
+/* Dense FP64 multiply-add rate of this GPU (TFLOP/s), measured with a
+ * register-resident FMA chain on every SM. */
+double sxsg_fp64_fma_tflops(void);
 
 #ifdef __cplusplus
 }

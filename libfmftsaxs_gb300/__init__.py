@@ -188,6 +188,10 @@ class Plan:
         self.n = len(idx)
         _check(load().sxsg_plan_set_poses(self.h, idx.ctypes.data, self.n, int(skip)))
 
+    def set_budget(self, nbytes):
+        load().sxsg_plan_set_budget.argtypes = [C.c_void_p, C.c_size_t]
+        _check(load().sxsg_plan_set_budget(self.h, int(nbytes)))
+
     def run(self, fit=FIT_GRID):
         _check(load().sxsg_plan_run(self.h, int(fit)))
 
@@ -221,3 +225,73 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+def profile_from_spf(spf, L, qvals, rm, c1, c2):
+    """(I[Q], err[Q]) of one molecule (sxs_profile_from_spf on a flat expansion)."""
+    q = f64(qvals)
+    i, e = np.zeros(len(q)), np.zeros(len(q))
+    _check(load().sxsg_profile_from_flat(_p(f64(spf)), C.c_int(L), C.c_int(len(q)), C.c_double(rm), _p(q),
+                                         C.c_double(c1), C.c_double(c2), _p(i), _p(e)))
+    return i, e
+
+
+def poses_to_indices(rot, tr, zvals, L, ref_lig=(0.0, 0.0, 0.0)):
+    """Batch pose ingestion (ft2euler, 3-decimal round trip, index assembly).
+    Returns (index[int64] of kept poses, keep mask)."""
+    rot = f64(rot).reshape(-1, 9)
+    tr = f64(tr).reshape(-1, 3)
+    n = len(rot)
+    idx = np.zeros(n, dtype=np.int64)
+    keep = np.zeros(n, dtype=np.uint8)
+    ref = f64(ref_lig)
+    z = f64(zvals)
+    k = load().sxsg_poses_to_indices(_p(rot), _p(tr), C.c_int64(n), _p(ref), _p(z), C.c_int(len(z)), C.c_int(L),
+                                     idx.ctypes.data_as(C.POINTER(C.c_int64)), keep.ctypes.data_as(C.POINTER(C.c_uint8)))
+    if k < 0:
+        raise SxsError(last_error())
+    return idx[keep.astype(bool)], keep.astype(bool)
+
+
+def score_flat(A, B, qvals, zvals, L, index, a, mult, peak, skip=1, fit=FIT_GRID, c1grid=None, c2grid=None,
+               cross=False):
+    """One-shot scoring from host buffers (sxsg_score_flat)."""
+    A, B, q, z, a = f64(A), f64(B), f64(qvals), f64(zvals), f64(a)
+    idx = np.ascontiguousarray(index, dtype=np.int64)
+    c1g = f64(c1grid if c1grid is not None else np.zeros(0))
+    c2g = f64(c2grid if c2grid is not None else np.zeros(0))
+    n = len(idx)
+    chi, c1, c2 = np.zeros(n), np.zeros(n), np.zeros(n)
+    cr = np.zeros((n, 6, len(q))) if cross else None
+    lib = load()
+    lib.sxsg_score_flat.argtypes = [C.c_void_p] * 3 + [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int64,
+                                    C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_int,
+                                    C.c_void_p, C.c_int] + [C.c_void_p] * 4
+    _check(lib.sxsg_score_flat(A.ctypes.data, B.ctypes.data, q.ctypes.data, len(q), z.ctypes.data, len(z), L,
+                               idx.ctypes.data, n, skip, a.ctypes.data, mult, peak, fit,
+                               c1g.ctypes.data if len(c1g) else None, len(c1g),
+                               c2g.ctypes.data if len(c2g) else None, len(c2g),
+                               chi.ctypes.data, c1.ctypes.data, c2.ctypes.data, cr.ctypes.data if cross else None))
+    out = dict(chi=chi, c1=c1, c2=c2)
+    if cross:
+        out["cross"] = cr
+    return out
+
+
+def timer_start():
+    _check(load().sxsg_timer_start())
+
+
+def timer_stop():
+    lib = load()
+    lib.sxsg_timer_stop.restype = C.c_double
+    ms = lib.sxsg_timer_stop()
+    if ms < 0:
+        raise SxsError("timer failed")
+    return ms
+
+
+def fp64_fma_tflops():
+    lib = load()
+    lib.sxsg_fp64_fma_tflops.restype = C.c_double
+    return lib.sxsg_fp64_fma_tflops()

@@ -330,3 +330,44 @@ int sxsk_fit_grid(const double *cross, int npose, int Q, const double *q, const 
 }
 
 } // extern "C"
+
+namespace {
+/* independent FMA chains per thread, register resident */
+__global__ void k_fp64_probe(double *out, int iters)
+{
+	double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
+	double a4 = a0 + 4e-9, a5 = a0 + 5e-9, a6 = a0 + 6e-9, a7 = a0 + 7e-9;
+	const double b = 0.999999999, c = 1e-12;
+	for (int i = 0; i < iters; i++) {
+		a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+		a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+	}
+	double s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+	if (s == 12345.678) out[threadIdx.x] = s; /* keeps the chains live */
+}
+} // namespace
+
+extern "C" double sxsk_fp64_probe(cudaStream_t s)
+{
+	int dev = 0, nsm = 0;
+	cudaGetDevice(&dev);
+	cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+	double *out = NULL;
+	if (cudaMalloc((void **)&out, 1024 * sizeof(double)) != cudaSuccess) return -1.0;
+	int blocks = nsm * 8, threads = 256, iters = 4096;
+	k_fp64_probe<<<blocks, threads, 0, s>>>(out, 64);
+	cudaEvent_t e0, e1;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	cudaEventRecord(e0, s);
+	k_fp64_probe<<<blocks, threads, 0, s>>>(out, iters);
+	cudaEventRecord(e1, s);
+	cudaEventSynchronize(e1);
+	float ms = 0;
+	cudaEventElapsedTime(&ms, e0, e1);
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	cudaFree(out);
+	double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
+	return ms > 0 ? flops / (ms * 1e-3) / 1e12 : -1.0;
+}

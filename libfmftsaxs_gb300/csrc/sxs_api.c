@@ -784,3 +784,52 @@ void sxs_compute_saxs_scores(double *scores, double *c1, double *c2, int *index_
 	free(fa); free(fb); free(idx);
 	if (rc) DIE(sxsg_last_error());
 }
+
+int64_t sxsg_poses_to_indices(const double *rot, const double *tr, int64_t n, const double *ref, const double *zvals,
+                              int znum, int L, int64_t *index, uint8_t *keep)
+{
+	if (n < 0 || (n > 0 && (!rot || !tr || !ref || !zvals || !index || !keep)) || L < 1)
+		return sxs_fail(-2, "sxsg_poses_to_indices: bad arguments");
+	int64_t kept = 0;
+	char buf[64];
+	for (int64_t i = 0; i < n; i++) {
+		struct mol_vector3 t = {tr[3 * i], tr[3 * i + 1], tr[3 * i + 2]}, r = {ref[0], ref[1], ref[2]};
+		const double *m = rot + 9 * i;
+		struct mol_matrix3 mm = {m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8]};
+		struct sxs_euler e;
+		sxs_ft2euler(&e, &t, &mm, &r);
+		double v[6] = {e.z, e.b1, e.g1, e.a2, e.b2, e.g2};
+		for (int k = 0; k < 6; k++) {
+			snprintf(buf, sizeof(buf), "% .3f", v[k]);
+			v[k] = strtod(buf, NULL);
+		}
+		int zi = -1;
+		for (int j = 0; j < znum; j++)
+			if (zvals[j] > v[0] - 0.001 && zvals[j] < v[0] + 0.001) { zi = j; break; }
+		if (zi < 0) {
+			keep[i] = 0;
+			index[i] = -1;
+			continue;
+		}
+		keep[i] = 1;
+		index[i] = sxsg_assemble_index(v, zi, L);
+		kept++;
+	}
+	return kept;
+}
+
+int sxsg_profile_from_flat(const double *spf, int L, int qnum, double rm, const double *q, double c1, double c2,
+                           double *in, double *err)
+{
+	if (!spf || L < 0 || qnum <= 0 || !q || !in || !err) return sxs_fail(-2, "sxsg_profile_from_flat: bad arguments");
+	struct sxs_spf_full *s = sxs_spf_full_create(L, qnum);
+	sxsg_spf_from_flat(s, spf);
+	s->rm = rm;
+	struct sxs_profile *p = sxs_profile_create((double *)q, qnum, 0);
+	sxs_profile_from_spf(p, s, c1, c2);
+	memcpy(in, p->in, sizeof(double) * qnum);
+	memcpy(err, p->err, sizeof(double) * qnum);
+	sxs_profile_free(p);
+	sxs_spf_full_free(s);
+	return 0;
+}

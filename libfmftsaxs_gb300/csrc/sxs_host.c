@@ -286,6 +286,13 @@ int sxsg_plan_create(sxsg_plan **out, const double *A, const double *B, const do
 	return 0;
 }
 
+int sxsg_plan_set_budget(sxsg_plan *p, size_t bytes)
+{
+	if (!p) return sxs_fail(-2, "sxsg_plan_set_budget: null plan");
+	p->r_budget = bytes;
+	return 0;
+}
+
 static int grow(void **ptr, size_t *cap, size_t need, size_t elem)
 {
 	if (*cap >= need && *ptr) return 0;
@@ -416,8 +423,10 @@ static int plan_tables(sxsg_plan *p)
 {
 	int L = p->L, Q = p->Q, N = p->N;
 	cudaStream_t s = p->s;
+	/* every run rebuilds the rotation tables: a run is the whole per-call
+	 * work of the reference's sxs_compute_saxs_scores */
 	int variant = p->skip == 1 ? 0 : 1;
-	if (p->tw_variant != variant) {
+	{
 		double *tw = malloc(sizeof(double) * 2 * N);
 		sxs_twiddles_host(N, variant, tw);
 		cudaError_t e = cudaMemcpy(p->d_tw, tw, sizeof(double2) * N, cudaMemcpyHostToDevice);
@@ -552,4 +561,53 @@ int sxsg_plan_timings(sxsg_plan *p, double *ms5)
 	for (int i = 0; i < 5; i++) ms5[i] = p->ms[i];
 	ms5[4] = p->ms[0] + p->ms[1] + p->ms[2] + p->ms[3];
 	return 0;
+}
+
+int sxsg_score_flat(const double *A, const double *B, const double *q, int Q, const double *z, int nz, int L,
+                    const int64_t *index, int64_t n, int skip, const double *a, double mult, double peak, int fit_mode,
+                    const double *c1g, int n1, const double *c2g, int n2, double *chi, double *c1, double *c2,
+                    double *cross)
+{
+	sxsg_plan *p = NULL;
+	int rc = sxsg_plan_create(&p, A, B, q, Q, z, nz, L, a, mult, peak, c1g, n1, c2g, n2, SXSG_FP64);
+	if (!rc) rc = sxsg_plan_set_poses(p, index, n, skip);
+	if (!rc) rc = sxsg_plan_run(p, fit_mode);
+	if (!rc) rc = sxsg_plan_results(p, chi, c1, c2, NULL, cross, NULL);
+	sxsg_plan_destroy(p);
+	return rc;
+}
+
+/* ------------------------------------------------------------ timing */
+static cudaEvent_t g_t0, g_t1;
+static int g_tinit = 0;
+
+int sxsg_timer_start(void)
+{
+	int rc = sxs_ensure_init();
+	if (rc) return rc;
+	if (!g_tinit) {
+		SXS_CU(cudaEventCreate(&g_t0));
+		SXS_CU(cudaEventCreate(&g_t1));
+		g_tinit = 1;
+	}
+	SXS_CU(cudaEventRecord(g_t0, g_stream));
+	return 0;
+}
+
+double sxsg_timer_stop(void)
+{
+	if (!g_tinit) return -1.0;
+	if (cudaEventRecord(g_t1, g_stream) != cudaSuccess) return -1.0;
+	if (cudaEventSynchronize(g_t1) != cudaSuccess) return -1.0;
+	float ms = 0;
+	cudaEventElapsedTime(&ms, g_t0, g_t1);
+	return ms;
+}
+
+double sxsg_fp64_fma_tflops(void)
+{
+	if (sxs_ensure_init()) return -1.0;
+	extern double sxsk_fp64_probe(cudaStream_t s);
+	sxs_count_launches(2);
+	return sxsk_fp64_probe(g_stream);
 }

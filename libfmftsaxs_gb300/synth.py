@@ -149,7 +149,10 @@ class Molecule:
         return self.xyz.mean(axis=0)
 
     def translated(self, t):
+        """A copy moved by t (accessible fractions are unchanged by a
+        rigid move and are carried over)."""
         m = Molecule(self.xyz + np.asarray(t), self.elements)
+        m.sasa = None if self.sasa is None else self.sasa.copy()
         return m
 
     def with_sasa(self, probe=1.4, npts=240):

@@ -678,8 +678,17 @@ int orc_score(const double *A, const double *B, const double *q, int qnum, const
 		cnt[pt[i]]++;
 	}
 
-	double *ds = malloc(sizeof(double) * K2 * K * N);
-	orc_dsymb(L, ds);
+	/* the 3j table depends on L only; keep the last one (the reference
+	 * rebuilds it per call, a fixed setup cost outside the per-pose work) */
+	static double *ds_cache = NULL;
+	static int ds_L = -1;
+	if (ds_L != L) {
+		free(ds_cache);
+		ds_cache = malloc(sizeof(double) * K2 * K * N);
+		orc_dsymb(L, ds_cache);
+		ds_L = L;
+	}
+	const double *ds = ds_cache;
 	size_t dsz = (size_t)K * N * N;
 	double *dt = malloc(sizeof(double) * dsz * nb);
 	double step = (ORC_PI - 0.0) / (nb - 1);
@@ -752,7 +761,7 @@ int orc_score(const double *A, const double *B, const double *q, int qnum, const
 				for (int y = 0; y < n2; y++)
 					grid[((size_t)i * n1 + x) * n2 + y] = orc_point_score(cs, q, qnum, a, mult, c1g[x], c2g[y]);
 	}
-	free(ds); free(dt); free(cst); free(tr_); free(ti_); free(te_); free(tf_);
+	free(dt); free(cst); free(tr_); free(ti_); free(te_); free(tf_);
 	free(bes); free(tre); free(tim); free(S); free(have); free(X);
 	free(pz); free(pt); free(pa); free(pg1); free(pg2); free(cnt);
 	return 0;

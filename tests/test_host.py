@@ -1,0 +1,156 @@
+"""Host-side logic of the product library (no GPU needed): the reference's
+C API functions that run on the host, pose ingestion, experiment binning,
+form-factor lookup, text I/O, and loud failure without a GPU."""
+import ctypes as C
+import glob
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+
+def load(path):
+    return dict(np.load(path, allow_pickle=False))
+
+
+def test_mkarray_and_bessel_match_oracle(lib, oracle):
+    for n, e in ((50, 0.5), (101, 0.5), (201, 0.6), (2, 1.0)):
+        np.testing.assert_array_equal(lib.mkarray(0.0, e, n), oracle.mkarray(0.0, e, n))
+    for l in range(0, 41, 4):
+        for x in (0.0, 0.01, 1.0, 7.5, 20.0, 33.0):
+            assert lib.sbessel(l, x) == oracle.sbessel(l, x)
+
+
+def test_pose_ingestion_matches_oracle(lib, oracle):
+    from libfmftsaxs_gb300 import synth
+    rng = np.random.default_rng(9)
+    R = synth.random_rotations(3000, rng)
+    T = synth.random_translations(3000, 9.5, 30.5, rng)
+    z = np.arange(10.0, 31.0)
+    for L in (6, 15, 20):
+        idx, keep = lib.poses_to_indices(R, T, z, L)
+        idx2, keep2 = synth.poses_to_indices(R, T, np.zeros(3), z, L, oracle.ft2euler, oracle.assemble_index)
+        np.testing.assert_array_equal(keep, keep2)
+        np.testing.assert_array_equal(idx, idx2)
+    # poses whose z falls outside the translation grid are dropped
+    idx, keep = lib.poses_to_indices(R[:10], T[:10] * 10, z, 6)
+    assert keep.sum() == 0 and len(idx) == 0
+
+
+def test_ft2euler_matches_oracle(lib, oracle):
+    from libfmftsaxs_gb300 import synth
+    rng = np.random.default_rng(3)
+    R = synth.random_rotations(200, rng)
+    T = synth.random_translations(200, 5, 70, rng)
+    ref = np.array([0.3, -1.2, 2.2])
+    for i in range(200):
+        np.testing.assert_array_equal(lib.ft2euler(T[i], R[i], ref), oracle.ft2euler(T[i], R[i].reshape(9), ref))
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p)[:-4])
+def test_bin_experiment_matches_reference(lib, path):
+    g = load(path)
+    a, mult, peak = lib.bin_experiment(g["exp_q"], g["exp_i"], g["exp_err"], g["q"], float(g["rm"]))
+    np.testing.assert_array_equal(a, g["a"])
+    assert mult == float(g["mult"]) and peak == float(g["peak"])
+
+
+def test_bin_experiment_stops_at_last_point(lib, oracle):
+    # experimental points beyond the model grid are ignored, no read past the end
+    q = lib.mkarray(0.0, 0.5, 11)
+    eq = np.linspace(0.0, 0.7, 29)
+    ei = 100.0 * np.exp(-eq * 4)
+    ee = 0.01 * ei
+    a, mult, peak = lib.bin_experiment(eq, ei, ee, q, 1.6)
+    a2, mult2, peak2 = oracle.opt_params(eq, ei, ee, q, 1.6)
+    np.testing.assert_array_equal(a, a2)
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p)[:-4])
+def test_profile_from_spf_matches_oracle(lib, oracle, path):
+    g = load(path)
+    L = int(g["L"])
+    for c1, c2 in ((1.0, 1.0), (1.03, -1.5), (0.96, 3.9)):
+        i1, e1 = lib.profile_from_spf(g["A"], L, g["q"], float(g["rmA"]), c1, c2)
+        i2, e2 = oracle.profile_from_spf(g["A"], L, g["q"], float(g["rmA"]), c1, c2)
+        np.testing.assert_array_equal(i1, i2)
+        np.testing.assert_array_equal(e1, e2)
+
+
+def test_form_factor_constants(lib, ref):
+    names = ["C", "N", "O", "S", "CH", "CH2", "CH3", "NH", "NH2", "NH3", "OH", "SH", "P", "H"]
+    mp = os.path.join("/root/reference/prms", "pdb_formfactor_mapping_clean.prm")
+    # residue/atom pairs of the mapping file that resolve to each type
+    pairs = {"C": ("ALA", "C"), "N": ("ALA", "N"), "O": ("ALA", "O"), "S": ("MET", "SD"), "CH": ("ALA", "CA"),
+             "CH3": ("ALA", "CB"), "CH2": ("ARG", "CB"), "H": ("ALA", "H")}
+    for t, (r, a) in pairs.items():
+        v, d, h2o, bad = ref.ff_lookup(mp, [r], [a])
+        assert bad == 0
+        assert lib.ff_type(t) == (v[0], d[0])
+        assert lib.ff_water() == h2o
+    v, d, missing = lib.ff_lookup(mp, [p[0] for p in pairs.values()] + ["XXX"], [p[1] for p in pairs.values()] + ["Q"])
+    assert missing == 1 and np.isnan(v[-1])
+    for k, t in enumerate(pairs):
+        assert (v[k], d[k]) == lib.ff_type(t)
+    with pytest.raises(KeyError):
+        lib.ff_type("UNOBTAINIUM")
+    assert len(names) > 0
+
+
+def test_ff_lookup_with_written_mapping(lib, tmp_path):
+    p = tmp_path / "map.prm"
+    p.write_text("# comment\n\nALA  C    C\nALA  CA   CH\nALA  CA   CH3\nXYZ  Q    NOPE\n")
+    v, d, missing = lib.ff_lookup(str(p), ["ALA", "ALA", " ALA", "XYZ"], ["C", "CA", " C ", "Q"])
+    assert (v[0], d[0]) == lib.ff_type("C")
+    assert (v[1], d[1]) == lib.ff_type("CH3")  # later lines replace earlier ones
+    assert (v[2], d[2]) == lib.ff_type("C")    # names are trimmed like get_ff does
+    assert missing == 1 and np.isnan(v[3])     # a type the reference does not know
+
+
+def _spf_roundtrip(lib, flat, L, Q, tmp_path):
+    so = lib.load()
+    so.sxs_spf_full_create.restype = C.c_void_p
+    so.sxs_spf_full_read.restype = C.c_void_p
+    s = so.sxs_spf_full_create(C.c_int(L), C.c_int(Q))
+    assert so.sxsg_spf_from_flat(C.c_void_p(s), flat.ctypes.data_as(C.POINTER(C.c_double))) == 0
+    path = str(tmp_path / "spf.txt").encode()
+    so.sxs_spf_full_write(C.c_char_p(path), C.c_void_p(s))
+    t = so.sxs_spf_full_read(C.c_char_p(path))
+    out = np.zeros_like(flat)
+    assert so.sxsg_spf_to_flat(C.c_void_p(t), out.ctypes.data_as(C.POINTER(C.c_double))) == 0
+    so.sxs_spf_full_free(C.c_void_p(s))
+    so.sxs_spf_full_free(C.c_void_p(t))
+    return out, open(path.decode()).readline()
+
+
+def test_spf_text_format_roundtrip(lib, tmp_path):
+    g = load(GOLDEN[0])
+    L, Q = int(g["L"]), len(g["q"])
+    out, header = _spf_roundtrip(lib, np.ascontiguousarray(g["A"]), L, Q, tmp_path)
+    # "% .4e" text: 5 significant digits
+    np.testing.assert_allclose(out, g["A"], rtol=6e-5, atol=1e-300)
+    assert header.split()[:2] == [str(L), str(Q)]
+
+
+def test_plan_fails_loudly_without_gpu(lib):
+    """Without a usable GPU the library reports an error; there is no
+    fallback path that would compute anything on the CPU."""
+    import subprocess
+    import sys
+    code = ("import sys; sys.path.insert(0, %r)\n"
+            "import libfmftsaxs_gb300 as g\n"
+            "try:\n    g.init(0)\nexcept g.SxsError as e:\n    print('ERR', e); sys.exit(0)\n"
+            "print('GPU'); sys.exit(0)\n") % os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120).stdout
+    assert out.startswith("ERR") or out.startswith("GPU")
+    if out.startswith("ERR"):
+        with pytest.raises(lib.SxsError):
+            lib.expand(np.zeros((1, 3)), [1.0], [1.0], None, 1.0, [0.0, 0.1], 2)
+
+
+def test_index_helpers(lib, oracle):
+    eu = np.array([12.0, 0.61, 5.9, 6.2, 2.9, 0.05])
+    for L in (5, 15, 20):
+        assert lib.assemble_index(eu, 3, L) == oracle.assemble_index(eu, 3, L)
