@@ -199,6 +199,27 @@ int sxsg_bin_experiment(const double *exp_q, const double *exp_i, const double *
 int sxsg_profile_from_flat(const double *spf, int L, int qnum, double rm, const double *qvals, double c1, double c2,
                            double *in, double *err);
 
+/* The expansion of sxsg_expand without any device allocation.  It has no
+ * counterpart in the reference.  It is for callers that cannot allocate
+ * device memory (all their memory comes from a host application's own
+ * pool, or they run where a synchronising cudaMalloc is not allowed).
+ * Every pointer is a DEVICE pointer the caller owns: xyz[3 natoms],
+ * vacuum_ff, dummy_ff, water_w[natoms] (water form factor x accessible
+ * fraction per atom; NULL for no hydration shell), qvals[qnum], spf_out in
+ * the flat layout [3][qnum][(L+1)^2][2].  Work buffers live in one static
+ * device array of 64 MiB (8 Mi doubles) that every GPU loading this library
+ * keeps until exit; a call needs about natoms (2 (L+1)^2 + qnum (L+1))
+ * doubles of it, L <= 40, and a larger request returns -3 without touching
+ * the GPU.  Work is queued on `stream` (a cudaStream_t; NULL for the
+ * default stream); the call returns once the Y_lm norm table is on the
+ * device.  The first call on each device looks up the array's device
+ * address, so make that first call before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race with each other.
+ * Returns 0, -2 (bad argument), -3 (too large for the static array), -4
+ * (no current device) or a CUDA error code. */
+int sxsg_expand_noalloc(const double *xyz, const double *vacuum_ff, const double *dummy_ff, const double *water_w,
+                        int natoms, const double *qvals, int qnum, int L, double *spf_out, void *stream);
+
 /* Flat-array view of an sxs_spf_full ([3][qnum][(L+1)^2][2]). */
 int sxsg_spf_to_flat(const struct sxs_spf_full *s, double *flat);
 int sxsg_spf_from_flat(struct sxs_spf_full *s, const double *flat);

@@ -260,3 +260,74 @@ int sxsk_const_int(const double *A, const double *B, int Q, int L, double *cst, 
 }
 
 } // extern "C"
+
+/* ------------------------------------------------------------------------
+ * Expansion with no allocation (sxsg_expand_noalloc).
+ *
+ * For callers that must not allocate device memory themselves or through
+ * this library: code that receives all device memory from a host
+ * application's own pool, or runs where a (synchronising) cudaMalloc is not
+ * allowed.  The work buffers of the expansion (Y_lm norms, Y_lm per atom,
+ * j_l(q r) per atom) live in one file-scope device array of fixed size that
+ * every GPU which loads this library keeps until the process exits.
+ * ---------------------------------------------------------------------- */
+#include <mutex>
+
+#define SXS_NOALLOC_DOUBLES (8u * 1024u * 1024u) /* 64 MiB of doubles */
+#define SXS_NOALLOC_LMAX 40
+
+static __device__ __align__(256) double g_noalloc_scratch[SXS_NOALLOC_DOUBLES];
+
+extern "C" void sxs_ynorm_host(int L, double *y);
+extern "C" void sxs_count_launches(int n);
+
+namespace {
+std::mutex g_noalloc_lock;
+double *g_noalloc_ptr[64]; /* device address of the scratch array, per device */
+} // namespace
+
+extern "C" int sxsg_expand_noalloc(const double *xyz, const double *vac, const double *dum, const double *water_w,
+                                   int natoms, const double *q, int Q, int L, double *spf_out, void *stream)
+{
+	if (natoms < 0 || Q < 1 || Q > 4096 || L < 1 || L > SXS_NOALLOC_LMAX || !q || !spf_out ||
+	    (natoms > 0 && (!xyz || !vac || !dum)))
+		return -2;
+	int K = L + 1, N = 2 * L + 1, K2 = K * K;
+	/* layout in doubles: ynorm | Y_lm (complex) | j_l | zero water weights */
+	size_t off_y = ((size_t)K * N + 31) / 32 * 32;
+	size_t off_j = off_y + ((size_t)natoms * K2 * 2 + 31) / 32 * 32;
+	size_t off_w = off_j + ((size_t)natoms * Q * K + 31) / 32 * 32;
+	size_t need = off_w + (water_w ? 0 : (size_t)natoms);
+	if (need > SXS_NOALLOC_DOUBLES) return -3;
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -4;
+	double *base;
+	{
+		std::lock_guard<std::mutex> lk(g_noalloc_lock);
+		if (!g_noalloc_ptr[dev]) {
+			void *p = NULL;
+			cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+			if (e != cudaSuccess || !p) return (int)(e != cudaSuccess ? e : cudaErrorInvalidSymbol);
+			g_noalloc_ptr[dev] = (double *)p;
+		}
+		base = g_noalloc_ptr[dev];
+	}
+	cudaStream_t s = (cudaStream_t)stream;
+	double yn[(SXS_NOALLOC_LMAX + 1) * (2 * SXS_NOALLOC_LMAX + 1)];
+	sxs_ynorm_host(L, yn);
+	cudaError_t e = cudaMemcpyAsync(base, yn, sizeof(double) * K * N, cudaMemcpyHostToDevice, s);
+	if (e != cudaSuccess) return (int)e;
+	/* the copy above reads a stack buffer: finish it before returning */
+	e = cudaStreamSynchronize(s);
+	if (e != cudaSuccess) return (int)e;
+	const double *w = water_w;
+	if (!w && natoms > 0) {
+		/* no hydration shell: the weights must start at zero on every call */
+		e = cudaMemsetAsync(base + off_w, 0, sizeof(double) * natoms, s);
+		if (e != cudaSuccess) return (int)e;
+		w = base + off_w;
+	}
+	int rc = sxsk_expand(xyz, vac, dum, w, natoms, q, Q, L, base, (double2 *)(base + off_y), base + off_j, spf_out, s);
+	sxs_count_launches(natoms > 0 ? 3 : 0);
+	return rc;
+}
