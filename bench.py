@@ -129,6 +129,12 @@ class Clocks:
 
 
 # ---------------------------------------------------------------- GPU side
+# DRAM bytes per pose of k_pose_cross from the ncu capture summarised in
+# profiles/k_pose_cross_c1_fp64.md (1.228 GB read + 4 MB written for 318
+# poses); the traffic of a launch scales with its pose count.
+TRAFFIC_PER_POSE = {"c1": 3.873e6}
+
+
 def pose_flops(L, Q):
     """Algorithmic FLOPs of the per-pose contraction for one pose: for each
     q, 9 complex multiply-adds (the 3x3 channel products) per (m, l) pair,
@@ -161,13 +167,17 @@ def run_ours(args):
     kind = cpu_kind()          # build the CPU checker before the first GPU call
     g.init(0)
     w = wl.build(args.config, seed=args.seed)
+    if args.poses:
+        w.index = w.index[:args.poses]
     n = len(w.index)
 
     # CPU baseline sample first (spawned processes, no GPU use)
     workers = max(1, min(os.cpu_count() or 1, 16))
-    cpu_rate, cpu_n, cpu_wall = cpu_sample(w, kind, workers)
+    cpu_rate, cpu_n, cpu_wall = cpu_sample(w, kind, workers) if not args.skip_cpu else (None, 0, 0)
 
     plan = g.Plan(w.A, w.B, w.q, w.z, w.L, w.a, w.mult, w.peak, w.c1g, w.c2g)
+    if args.budget_gb:
+        plan.set_budget(int(args.budget_gb * 2 ** 30))
     plan.set_poses(w.index, skip=1)
     for _ in range(args.warmup):
         plan.run(g.FIT_GRID)
@@ -188,11 +198,13 @@ def run_ours(args):
 
     # end to end through the one-shot C-ABI call from host buffers
     idx = np.ascontiguousarray(w.index, dtype=np.int64)
-    g.score_flat(w.A, w.B, w.q, w.z, w.L, idx, w.a, w.mult, w.peak, 1, g.FIT_GRID, w.c1g, w.c2g)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
+    e2e_s = float("nan")
+    if not args.skip_e2e:
         g.score_flat(w.A, w.B, w.q, w.z, w.L, idx, w.a, w.mult, w.peak, 1, g.FIT_GRID, w.c1g, w.c2g)
-    e2e_s = (time.perf_counter() - t0) / args.steps
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            g.score_flat(w.A, w.B, w.q, w.z, w.L, idx, w.a, w.mult, w.peak, 1, g.FIT_GRID, w.c1g, w.c2g)
+        e2e_s = (time.perf_counter() - t0) / args.steps
     h2d = w.A.nbytes + w.B.nbytes + w.q.nbytes + w.z.nbytes + w.a.nbytes + idx.nbytes + w.c1g.nbytes + w.c2g.nbytes
     d2h = 3 * 8 * n
 
@@ -221,7 +233,8 @@ def run_ours(args):
         "reference_equiv_tflops": fref / (ms / args.steps * 1e-3) / 1e12,
         "roofline": {"bound": "fp64", "kernel": "k_pose_cross", "achieved": achieved, "peak": fp64_peak,
                      "unit": "TFLOP/s", "frac": achieved / fp64_peak if fp64_peak > 0 else None,
-                     "traffic": None,
+                     "traffic": TRAFFIC_PER_POSE[args.config] * n if args.config in TRAFFIC_PER_POSE else None,
+                     "traffic_source": "ncu capture of 318 poses, scaled by poses per launch",
                      "peak_source": "measured in this run: register-resident FP64 FMA chains on every SM"},
         "cpu_baseline": {"value": cpu_rate, "unit": "poses/s", "cores": workers, "kind": kind,
                          "sample": "%d poses of %d (z,beta1,beta2) triples, one triple per process, grid fit"
@@ -274,6 +287,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2"])
     ap.add_argument("--seed", type=int, default=2026)
+    ap.add_argument("--poses", type=int, default=0, help="score only the first N poses (profiling cases)")
+    ap.add_argument("--budget-gb", type=float, default=0.0, help="cap on the translated-table chunk (GiB)")
+    ap.add_argument("--skip-cpu", action="store_true", help="no CPU baseline sample")
+    ap.add_argument("--skip-e2e", action="store_true", help="no end-to-end timing")
     args = ap.parse_args()
     if args.gpus > 1 and int(os.environ.get("RANK", "0")) != 0:
         return  # the path does not shard: one GPU runs, other ranks idle
