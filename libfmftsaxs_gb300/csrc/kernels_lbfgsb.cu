@@ -1,9 +1,67 @@
-/* L-BFGS-B over (c1, c2) on the device: placeholder until the batched
- * solver lands; the launcher reports that the fit is unavailable. */
+/*
+ * Batched L-BFGS-B fit of (c1, c2) on the device: one thread per pose,
+ * the solver of lbfgsb_core.h (the reference's fit, src/min_saxs.c:153-259).
+ * Compiled with -fmad=false so that every objective and solver step rounds
+ * like the reference's C code.
+ */
 #include "kernels.h"
+#include "lbfgsb_core.h"
 
-extern "C" int sxs_fit_lbfgsb_launch(const double *, int, int, const double *, const double *, double, double *,
-                                     double *, double *, double *, int *, cudaStream_t)
+namespace {
+
+/* raw [pose][6][Q] -> transposed [6*Q][pose], with the peak rescale of
+ * src/min_saxs.c:170-188 when rescale != 0 */
+__global__ void k_rescale_transpose(const double *__restrict__ cross, double *__restrict__ ct, int npose, int Q,
+                                    double peak, int rescale)
 {
-	return (int)cudaErrorNotSupported;
+	long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= (long)npose * 6 * Q) return;
+	int p = (int)(i % npose);
+	int cq = (int)(i / npose);
+	const double *src = cross + (size_t)p * 6 * Q;
+	double v = src[cq];
+	if (rescale) {
+		double s = src[0] + src[3 * Q] + src[5 * Q] + src[2 * Q] - src[Q] - src[4 * Q];
+		s = peak / s;
+		v *= s;
+	}
+	ct[i] = v;
+}
+
+__global__ void k_lbfgsb(const double *__restrict__ ct, int npose, int Q, const double *__restrict__ q,
+                         const double *__restrict__ a, double mult, int max_eval, double *__restrict__ chi,
+                         double *__restrict__ c1, double *__restrict__ c2, double *__restrict__ scale,
+                         int *__restrict__ nevals)
+{
+	int p = blockIdx.x * blockDim.x + threadIdx.x;
+	if (p >= npose) return;
+	lb_saxs o;
+	o.cr = ct + p;
+	o.stride = npose;
+	o.q = q;
+	o.a = a;
+	o.mult = mult;
+	o.Q = Q;
+	double x, y, z, w;
+	int ne = lb_saxs_fit(&o, &x, &y, &z, &w, max_eval);
+	chi[p] = x;
+	c1[p] = y;
+	c2[p] = z;
+	if (scale) scale[p] = w;
+	if (nevals) nevals[p] = ne;
+}
+
+} // namespace
+
+/* cross: [npose][6][Q] (raw when rescale != 0, already rescaled otherwise);
+ * ct: workspace of npose*6*Q doubles that receives the transposed terms. */
+extern "C" int sxs_fit_lbfgsb_launch(const double *cross, double *ct, int npose, int Q, const double *q,
+                                     const double *a, double mult, double peak, int rescale, double *chi, double *c1,
+                                     double *c2, double *scale, int *nevals, cudaStream_t s)
+{
+	if (npose <= 0) return 0;
+	long n = (long)npose * 6 * Q;
+	k_rescale_transpose<<<(int)((n + 255) / 256), 256, 0, s>>>(cross, ct, npose, Q, peak, rescale);
+	k_lbfgsb<<<(npose + 63) / 64, 64, 0, s>>>(ct, npose, Q, q, a, mult, 100000, chi, c1, c2, scale, nevals);
+	return (int)cudaGetLastError();
 }

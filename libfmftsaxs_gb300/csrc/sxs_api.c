@@ -489,9 +489,10 @@ static int fit_profiles_gpu(struct sxs_profile **profiles, const int *sel, int n
 		for (int c = 0; c < 6; c++)
 			for (int i = 0; i < Q; i++) dst[c * Q + i] = rescale ? src[c][i] * sc : src[c][i];
 	}
-	double *d_c = NULL, *d_q = NULL, *d_a = NULL, *d_o = NULL;
+	double *d_c = NULL, *d_t = NULL, *d_q = NULL, *d_a = NULL, *d_o = NULL;
 	int *d_it = NULL;
 	cudaError_t e = cudaMalloc((void **)&d_c, sizeof(double) * (size_t)n * 6 * Q);
+	if (!e) e = cudaMalloc((void **)&d_t, sizeof(double) * (size_t)n * 6 * Q);
 	if (!e) e = cudaMalloc((void **)&d_q, sizeof(double) * Q);
 	if (!e) e = cudaMalloc((void **)&d_a, sizeof(double) * 6 * Q);
 	if (!e) e = cudaMalloc((void **)&d_o, sizeof(double) * 4 * n);
@@ -500,14 +501,14 @@ static int fit_profiles_gpu(struct sxs_profile **profiles, const int *sel, int n
 	if (!e) e = cudaMemcpyAsync(d_q, profiles[sel[0]]->qvals, sizeof(double) * Q, cudaMemcpyHostToDevice, s);
 	if (!e) e = cudaMemcpyAsync(d_a, params->a, sizeof(double) * 6 * Q, cudaMemcpyHostToDevice, s);
 	if (!e) {
-		e = (cudaError_t)sxs_fit_lbfgsb_launch(d_c, n, Q, d_q, d_a, params->mult, d_o, d_o + n, d_o + 2 * n, d_o + 3 * n,
-		                                       d_it, s);
-		sxs_count_launches(1);
+		e = (cudaError_t)sxs_fit_lbfgsb_launch(d_c, d_t, n, Q, d_q, d_a, params->mult, params->peak, 0, d_o, d_o + n,
+		                                       d_o + 2 * n, d_o + 3 * n, d_it, s);
+		sxs_count_launches(2);
 	}
 	double *h_o = malloc(sizeof(double) * 4 * n);
 	if (!e) e = cudaMemcpyAsync(h_o, d_o, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, s);
 	if (!e) e = cudaStreamSynchronize(s);
-	cudaFree(d_c); cudaFree(d_q); cudaFree(d_a); cudaFree(d_o); cudaFree(d_it);
+	cudaFree(d_c); cudaFree(d_t); cudaFree(d_q); cudaFree(d_a); cudaFree(d_o); cudaFree(d_it);
 	if (!e) {
 		for (int k = 0; k < n; k++) {
 			struct sxs_profile *p = profiles[sel[k]];

@@ -499,11 +499,10 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 		                    p->n2, p->d_chi, p->d_c1, p->d_c2, p->d_cell, NULL, p->d_scaled, s));
 		sxs_count_launches(n > 0 ? 1 : 0);
 	} else if (fit_mode == SXSG_FIT_LBFGSB) {
-		/* rescale through the grid kernel is not needed: the L-BFGS-B kernel
-		 * rescales itself */
-		SXS_K(sxs_fit_lbfgsb_launch(p->d_cross, n, Q, p->d_q, p->d_a, p->mult, p->d_chi, p->d_c1, p->d_c2,
-		                            p->d_scale, p->d_iters, s));
-		sxs_count_launches(n > 0 ? 1 : 0);
+		SXS_K(sxs_fit_lbfgsb_launch(p->d_cross, p->d_scaled, n, Q, p->d_q, p->d_a, p->mult, p->peak, 1, p->d_chi,
+		                            p->d_c1, p->d_c2, p->d_scale, p->d_iters, s));
+		sxs_count_launches(n > 0 ? 2 : 0);
+		if (n > 0) SXS_CU(cudaMemsetAsync(p->d_cell, 0xff, sizeof(int32_t) * n, s));
 	}
 	p->last_fit = fit_mode;
 	p->grid_valid = 0;

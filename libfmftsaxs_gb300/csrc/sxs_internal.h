@@ -63,8 +63,11 @@ typedef struct {
 } sxs_ltables;
 int sxs_ltables_get(int L, const sxs_ltables **out);
 
-/* device L-BFGS-B over (c1, c2) for a batch of rescaled cross terms */
-int sxs_fit_lbfgsb_launch(const double *scaled, int npose, int Q, const double *q, const double *a, double mult,
-                          double *chi, double *c1, double *c2, double *scale, int *iters, cudaStream_t s);
+/* device L-BFGS-B over (c1, c2) for a batch of poses: cross [n][6][Q]
+ * (rescaled here by peak when rescale != 0), ct a workspace of n*6*Q
+ * doubles; two kernel launches */
+int sxs_fit_lbfgsb_launch(const double *cross, double *ct, int npose, int Q, const double *q, const double *a,
+                          double mult, double peak, int rescale, double *chi, double *c1, double *c2, double *scale,
+                          int *nevals, cudaStream_t s);
 
 #endif

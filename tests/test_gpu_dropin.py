@@ -1,0 +1,135 @@
+"""The drop-in sxs_compute_saxs_scores (the reference's own signature, structs
+and fit) against the reference's outputs, and the device L-BFGS-B.
+
+The continuous fit is path dependent: the cross terms reach the solver with
+~1e-14 relative differences and the device exp() may differ from glibc's
+in the last bit, so an iterate sequence can part from the reference's.  On
+the fixtures every fit lands on the reference's (c1, c2) to 1e-6 and chi to
+1e-8 relative (the reference's own test allows 1e-3 absolute).
+"""
+import ctypes as C
+import glob
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+CHI_TOL = 1e-8
+C_TOL = 1e-6
+
+
+def load(path):
+    return dict(np.load(path, allow_pickle=False))
+
+
+DP = C.POINTER(C.c_double)
+
+
+class Profile(C.Structure):
+    _fields_ = [("qnum", C.c_int), ("rerr", C.c_double), ("in_", DP), ("err", DP), ("qvals", DP),
+                ("VV", DP), ("VD", DP), ("VW", DP), ("DD", DP), ("DW", DP), ("WW", DP),
+                ("score", C.c_double), ("scale", C.c_double), ("c1", C.c_double), ("c2", C.c_double),
+                ("b1", C.c_double), ("g1", C.c_double), ("a2", C.c_double), ("b2", C.c_double), ("g2", C.c_double)]
+
+
+def _lib(gpu):
+    so = gpu.load()
+    so.sxs_spf_full_create.restype = C.c_void_p
+    so.sxs_profile_create.restype = C.POINTER(Profile)
+    so.sxs_opt_params_create.restype = C.c_void_p
+    so.sxs_opt_params_create.argtypes = [C.POINTER(Profile), DP, C.c_int, C.c_double]
+    so.sxs_compute_saxs_scores.argtypes = [DP, DP, DP, C.POINTER(C.c_int), C.c_int, C.c_void_p, C.c_void_p,
+                                           C.c_void_p, DP, C.c_int, DP, C.c_int, C.c_int, C.c_int]
+    so.sxs_compute_saxs_scores.restype = None
+    return so
+
+
+def _spf(so, flat, L, Q, rm):
+    s = so.sxs_spf_full_create(C.c_int(L), C.c_int(Q))
+    f = np.ascontiguousarray(flat)
+    assert so.sxsg_spf_from_flat(C.c_void_p(s), f.ctypes.data_as(DP)) == 0
+    # rm sits after two ints
+    C.cast(C.c_void_p(s + 8), DP)[0] = rm
+    return s
+
+
+def _exp_params(so, g, keep):
+    eq, ei, ee = (np.ascontiguousarray(g[k]) for k in ("exp_q", "exp_i", "exp_err"))
+    keep += [eq, ei, ee]
+    p = so.sxs_profile_create(eq.ctypes.data_as(DP), C.c_int(len(eq)), C.c_int(0))
+    for i in range(len(eq)):
+        p.contents.in_[i] = ei[i]
+        p.contents.err[i] = ee[i]
+    q = np.ascontiguousarray(g["q"])
+    keep.append(q)
+    return so.sxs_opt_params_create(p, q.ctypes.data_as(DP), len(q), float(g["rm"]))
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p)[:-4])
+def test_dropin_compute_saxs_scores_matches_reference(gpu, path):
+    g = load(path)
+    so = _lib(gpu)
+    L, Q = int(g["L"]), len(g["q"])
+    keep = []
+    A = _spf(so, g["A"], L, Q, float(g["rmA"]))
+    B = _spf(so, g["B"], L, Q, float(g["rmB"]))
+    params = _exp_params(so, g, keep)
+    idx = np.ascontiguousarray(g["index"], dtype=np.int32)
+    n = len(idx)
+    chi, c1, c2 = np.zeros(n), np.zeros(n), np.zeros(n)
+    q, z = np.ascontiguousarray(g["q"]), np.ascontiguousarray(g["z"])
+    so.sxs_compute_saxs_scores(chi.ctypes.data_as(DP), c1.ctypes.data_as(DP), c2.ctypes.data_as(DP),
+                               idx.ctypes.data_as(C.POINTER(C.c_int)), n, C.c_void_p(A), C.c_void_p(B),
+                               C.c_void_p(params), q.ctypes.data_as(DP), Q, z.ctypes.data_as(DP), len(z), L,
+                               int(g["skip"]))
+    np.testing.assert_allclose(chi, g["chi"], rtol=CHI_TOL, atol=0)
+    np.testing.assert_allclose(c1, g["c1"], rtol=0, atol=C_TOL)
+    np.testing.assert_allclose(c2, g["c2"], rtol=0, atol=C_TOL)
+    so.sxs_spf_full_free(C.c_void_p(A))
+    so.sxs_spf_full_free(C.c_void_p(B))
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p)[:-4])
+def test_plan_lbfgsb_fit_matches_reference(gpu, path):
+    g = load(path)
+    L = int(g["L"])
+    p = gpu.Plan(g["A"], g["B"], g["q"], g["z"], L, g["a"], float(g["mult"]), float(g["peak"]))
+    p.set_poses(g["index"], skip=int(g["skip"]))
+    p.run(gpu.FIT_LBFGSB)
+    r = p.results()
+    np.testing.assert_allclose(r["chi"], g["chi"], rtol=CHI_TOL, atol=0)
+    np.testing.assert_allclose(r["c1"], g["c1"], rtol=0, atol=C_TOL)
+    np.testing.assert_allclose(r["c2"], g["c2"], rtol=0, atol=C_TOL)
+    p.close()
+
+
+def test_single_profile_lbfgs_fitting(gpu):
+    """sxs_fit_params on caller profiles (src/min_saxs.h:94): rescaled cross
+    terms written back, chi/c1/c2/scale and the fitted intensity."""
+    g = load(GOLDEN[0])
+    so = _lib(gpu)
+    Q = len(g["q"])
+    keep = []
+    params = _exp_params(so, g, keep)
+    q = np.ascontiguousarray(g["q"])
+    k = 5
+    profs = []
+    for i in range(k):
+        p = so.sxs_profile_create(q.ctypes.data_as(DP), C.c_int(Q), C.c_int(1))
+        raw = g["raw"][i]
+        for c, name in enumerate(("VV", "VD", "VW", "DD", "DW", "WW")):
+            arr = getattr(p.contents, name)
+            for j in range(Q):
+                arr[j] = raw[c, j]
+        profs.append(p)
+    arr = (C.POINTER(Profile) * k)(*profs)
+    mask = np.ones(k, dtype=np.int32)
+    so.sxs_fit_params.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_int]
+    so.sxs_fit_params(C.cast(arr, C.c_void_p), C.c_void_p(params), mask.ctypes.data_as(C.POINTER(C.c_int)), k)
+    for i, p in enumerate(profs):
+        assert abs(p.contents.score - g["chi"][i]) <= CHI_TOL * g["chi"][i]
+        assert abs(p.contents.c1 - g["c1"][i]) <= C_TOL and abs(p.contents.c2 - g["c2"][i]) <= C_TOL
+        np.testing.assert_allclose([p.contents.VV[j] for j in range(Q)], g["scaled"][i][0], rtol=1e-12)
