@@ -175,7 +175,8 @@ def run_ours(args):
     workers = max(1, min(os.cpu_count() or 1, 16))
     cpu_rate, cpu_n, cpu_wall = cpu_sample(w, kind, workers) if not args.skip_cpu else (None, 0, 0)
 
-    plan = g.Plan(w.A, w.B, w.q, w.z, w.L, w.a, w.mult, w.peak, w.c1g, w.c2g)
+    prec = g.MIXED if args.precision == "mixed" else g.FP64
+    plan = g.Plan(w.A, w.B, w.q, w.z, w.L, w.a, w.mult, w.peak, w.c1g, w.c2g, precision=prec)
     if args.budget_gb:
         plan.set_budget(int(args.budget_gb * 2 ** 30))
     plan.set_poses(w.index, skip=1)
@@ -291,6 +292,7 @@ def main():
     ap.add_argument("--budget-gb", type=float, default=0.0, help="cap on the translated-table chunk (GiB)")
     ap.add_argument("--skip-cpu", action="store_true", help="no CPU baseline sample")
     ap.add_argument("--skip-e2e", action="store_true", help="no end-to-end timing")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     args = ap.parse_args()
     if args.gpus > 1 and int(os.environ.get("RANK", "0")) != 0:
         return  # the path does not shard: one GPU runs, other ranks idle

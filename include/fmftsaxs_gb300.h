@@ -229,7 +229,13 @@ int sxsg_spf_from_flat(struct sxs_spf_full *s, const double *flat);
 typedef struct sxsg_plan sxsg_plan;
 
 enum { SXSG_FIT_NONE = 0, SXSG_FIT_GRID = 1, SXSG_FIT_LBFGSB = 2 };
-enum { SXSG_FP64 = 0 };
+/* Precision of the contraction tables.  SXSG_FP64: every stage in FP64,
+ * matching the reference to ~1e-10 relative in I(q) and chi.  SXSG_MIXED:
+ * the expansion, Bessel, translation-coefficient and fit stages stay FP64;
+ * the rotation, translation and per-pose contractions run in FP32 (tables
+ * and accumulation) and the cross terms return to FP64 before the self
+ * terms are added; chi agrees with the FP64 path to ~1e-6 relative. */
+enum { SXSG_FP64 = 0, SXSG_MIXED = 1 };
 
 /* A, B: flat [3][qnum][(L+1)^2][2]; a[6 qnum], mult, peak: the binned
  * experiment of scoring_helper / sxs_opt_params (min_saxs.c:116-124,

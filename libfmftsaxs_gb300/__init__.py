@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(HERE, "libfmftsaxs_gb300.so")
 
 FIT_NONE, FIT_GRID, FIT_LBFGSB = 0, 1, 2
 FP64 = 0
+MIXED = 1
 
 _lib = None
 

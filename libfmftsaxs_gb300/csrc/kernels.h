@@ -3,15 +3,17 @@
  * Host C (sxs_host.c) calls these; every pointer is a device pointer unless
  * named h_*.  All launches go to the given stream; none synchronises.
  *
- * Device layouts (complex = double2 {re, im}; K = L+1, N = 2L+1, K2 = K*K):
- *   spf_t [3 ch][K2 lm][Q]            lm = l(l+1)+m, q fastest
- *   dtab  [K b][K l][N m+L][N m1+L]   Wigner small-d per beta_b = b*pi/L
+ * Device layouts (K = L+1, N = 2L+1, K2 = K*K, NP = K(K+1)/2; a table of
+ * precision S holds complex values as {re, im} pairs of S, S = double on the
+ * plain path and float on the mixed path):
+ *   spf_t [3 ch][K2 lm][Q]              lm = l(l+1)+m, q fastest (S)
+ *   dtab  [K b][K l][N m+L][N m1+L]     Wigner small-d per beta_b = b*pi/L
  *   dsymb [K2 lm][K l1][N p]
  *   bes   [nz][Q][N p]
- *   tmat  [nz][K |m|][K l][K l1][Q]   complex
- *   rot   [nb*N (b,g)][K2 pair][3 ch][Q]  pair = (m,l), l >= |m|, m-major
- *   trans [ncombo][K2 pair][3 ch][Q]
- *   cross [npose][6][Q]
+ *   tau   [nz][K m][K l][K l1][Q]       T^m_{l l1} = i^{l+l1} tau (real)
+ *   rot   [K*N (b,g)][NP pair][3 ch][Q] pair = (m >= 0, l >= m), m-major (S)
+ *   trans [ncombo][NP pair][3 ch][Q]    (S)
+ *   cross [npose][6][Q]                 (double)
  */
 #ifndef SXS_KERNELS_H
 #define SXS_KERNELS_H
@@ -39,40 +41,45 @@ int sxsk_expand(const double *xyz, const double *vac, const double *dum, const d
 size_t sxsk_expand_ws_ylm(int natoms, int L);
 size_t sxsk_expand_ws_jl(int natoms, int Q, int L);
 
-/* host-flat [3][Q][K2][2] -> spf_t [3][K2][Q] complex */
-int sxsk_spf_transpose(const double *flat, double2 *spf_t, int Q, int L, cudaStream_t s);
+/* host-flat [3][Q][K2][2] -> spf_t [3][K2][Q] complex, in float when fp32 */
+int sxsk_spf_transpose(const double *flat, void *spf_t, int Q, int L, int fp32, cudaStream_t s);
 
 /* j_p(q z) for p in [0,2L]: bes[nz][Q][N] (faithful series) */
 int sxsk_bessel_z(const double *z, int nz, const double *q, int Q, int L, double *bes, cudaStream_t s);
 
-/* translation matrix T^{|m|}_{l l1}(q z) -> tmat; ll1 lists the (l, l1 >= l) pairs */
+/* translation matrix T^m_{l l1}(q z) = i^{l+l1} tau -> tau; ll1 lists the
+ * (l, l1 >= l) pairs */
 int sxsk_tmatrix(const double *bes, const double *dsymb, int nz, int Q, int L, const int2 *ll1, int nll1,
-                 double2 *tmat, cudaStream_t s);
+                 double *tau, cudaStream_t s);
+
+/* b[i] = (float)a[i] */
+int sxsk_to_float(const double *a, float *b, long n, cudaStream_t s);
 
 /* self terms cst[6][Q] (already times {1,2,2,1,2,1}); A, B in the host flat layout */
 int sxsk_const_int(const double *A, const double *B, int Q, int L, double *cst, cudaStream_t s);
 
-/* rotation table: out[(b,g)][pair][ch][q] = sum_{m1} tw[(m1' g) mod N] d^l_{m m1}(beta_b) C[ch][l,m1][q]
+/* rotation table, m >= 0: out[(b,g)][pair][ch][q] = sum_{m1} tw[(m1' g) mod N] d^l_{m m1}(beta_b) C[ch][l,m1][q]
  * with C = spf_t, conjugated when conj != 0. */
-int sxsk_rotate(const double2 *spf_t, const double *dtab, const double2 *tw, int Q, int L, int conj,
-                double2 *out, cudaStream_t s);
+int sxsk_rotate(const void *spf_t, const double *dtab, const double2 *tw, int Q, int L, int conj, void *out,
+                int fp32, cudaStream_t s);
 
-/* translated ligand table for a list of combos (zi, b2, g2):
- * out[c][pair(m,l)][ch][q] = sum_{l1>=|m|} conj(T[zi][|m|][l][l1][q]) U[(b2,g2)][pair(m,l1)][ch][q] */
-int sxsk_translate(const double2 *U, const double2 *tmat, const int32_t *combo_zbg, int ncombo,
-                   int Q, int L, double2 *out, cudaStream_t s);
+/* translated ligand table for a list of combos (zi, b2, g2), m >= 0:
+ * out[c][pair(m,l)][ch][q] = sum_{l1>=m} conj(T[zi][m][l][l1][q]) U[(b2,g2)][pair(m,l1)][ch][q];
+ * tau is float when fp32 */
+int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, int ncombo, int Q, int L, void *out,
+                   int fp32, cudaStream_t s);
 
-/* per-pose raw cross terms: cross[p][c][q] = cst[c][q] + 2 Re sum_m tw(m' a2) sum_l P R */
-int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base,
-                    const double2 *P, const double2 *R, const double2 *tw, const double *cst,
-                    int Q, int L, double *cross, cudaStream_t s);
+/* per-pose raw cross terms: cross[p][c][q] = cst[c][q] + 2 Re sum_m tw(m' a2) sum_l P R,
+ * the m < 0 half folded in by symmetry */
+int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, const void *P, const void *R,
+                    const double2 *tw, const double *cst, int Q, int L, double *cross, int fp32, cudaStream_t s);
 
 /* grid fit: per pose, peak rescale then chi^2 at every (c1, c2) cell; best cell.
- * gtab[n1][Q] = c1^3 exp(-mult (c1^2-1) q^2); a[6Q] binned experiment; a0sum = sum_i a[6i]. */
-int sxsk_fit_grid(const double *cross, int npose, int Q, const double *q, const double *a, double a0sum,
-                  double peak, const double *gtab, const double *c1g, int n1, const double *c2g, int n2,
-                  double *chi, double *c1, double *c2, int32_t *cell, double *grid, double *scaled,
-                  cudaStream_t s);
+ * gtab[n1][Q] = c1^3 exp(-mult (c1^2-1) q^2); a[6Q] binned experiment; a0sum = sum_i a[6i];
+ * hinv[Q] = 1 / (q_i - q_{i-1}), q_{-1} = -1. */
+int sxsk_fit_grid(const double *cross, int npose, int Q, const double *q, const double *hinv, const double *a,
+                  double a0sum, double peak, const double *gtab, const double *c1g, int n1, const double *c2g, int n2,
+                  double *chi, double *c1, double *c2, int32_t *cell, double *grid, double *scaled, cudaStream_t s);
 
 #ifdef __cplusplus
 }

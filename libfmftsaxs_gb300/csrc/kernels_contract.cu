@@ -1,6 +1,6 @@
 /*
- * FP64 contraction kernels of the factorized correlation (multiply-add
- * fusion allowed; each output is a short fixed-order sum).
+ * Contraction kernels of the factorized correlation, in FP64 (plain path)
+ * or FP32 (mixed path); multiply-add fusion allowed.
  *
  * The reference evaluates, per touched (z, beta1, beta2) triple, the 6-channel
  * sums X[m,m1,m2] (src/fftsaxs.c:416-524) and then an angular DFT at each
@@ -13,27 +13,26 @@
  *   R^b[m,l]        = sum_{l1>=|m|} conj(T^{|m|}_{l l1}(q z)) U^b[m,l1]
  *   F^{ab}          = sum_m w^{m' a2} sum_{l>=|m|} P^a[m,l] R^b[m,l]
  *
- * (w = the twiddle table, x' = x mod N), which is the reference's F with the
- * same terms regrouped.  P depends on (b1, g1) only and U on (b2, g2) only, so
- * they are tabulated once per call; R is tabulated for each touched
- * (z, b2, g2); the per-pose work is the final K^2-term contraction.
+ * (w = the twiddle table, x' = x mod N), the reference's F with the same terms
+ * regrouped.  A and B expand real densities, so A_{l,-m} = (-1)^{l+m}
+ * conj(A_{lm}); with d^l_{-m,-m1} = (-1)^{m-m1} d^l_{m m1} and T real or
+ * imaginary by the parity of l + l1 this gives P[-m,l] = (-1)^{l+m} conj(P[m,l])
+ * and the same for U and R, so the m-sum is Re F = Re(w_0 G_0) +
+ * 2 sum_{m>0} Re(w_m G_m) with G_m = sum_l P[m,l] R[m,l].  Only m >= 0 is
+ * tabulated: pairs (m, l), m = 0..L, l = m..L, (L+1)(L+2)/2 of them.
  */
 #include "kernels.h"
 
 namespace {
 
+template <typename S> struct Cx;
+template <> struct Cx<double> { typedef double2 T; };
+template <> struct Cx<float> { typedef float2 T; };
+
 __device__ __forceinline__ int lm_index(int l, int m) { return l * (l + 1) + m; }
 
-/* index of the first (m, l) pair of row m, pairs ordered m = -L..L, l = |m|..L */
-__device__ __forceinline__ int pair_off(int m, int L)
-{
-	int K = L + 1;
-	if (m <= 0) {
-		int t = L + m; /* rows before: m' = -L .. m-1, sizes 1 .. L+m */
-		return t * (t + 1) / 2;
-	}
-	return L * (L + 1) / 2 + K + (m - 1) * K - (m - 1) * m / 2;
-}
+/* first pair of row m >= 0 */
+__device__ __forceinline__ int psym(int m, int K) { return m * K - m * (m - 1) / 2; }
 
 __device__ __forceinline__ void cfma(double2 &acc, double2 a, double2 b)
 {
@@ -42,91 +41,116 @@ __device__ __forceinline__ void cfma(double2 &acc, double2 a, double2 b)
 	acc.y = fma(a.x, b.y, acc.y);
 	acc.y = fma(a.y, b.x, acc.y);
 }
+__device__ __forceinline__ void cfma(float2 &acc, float2 a, float2 b)
+{
+	acc.x = fmaf(a.x, b.x, acc.x);
+	acc.x = fmaf(-a.y, b.y, acc.x);
+	acc.y = fmaf(a.x, b.y, acc.y);
+	acc.y = fmaf(a.y, b.x, acc.y);
+}
+template <typename V> __device__ __forceinline__ V zero2() { V v; v.x = 0; v.y = 0; return v; }
+template <typename V> __device__ __forceinline__ V from2(double2 a) { V v; v.x = a.x; v.y = a.y; return v; }
 
 /* [3][Q][K2][2] -> [3][K2][Q] complex */
-__global__ void k_spf_transpose(const double *__restrict__ flat, double2 *__restrict__ t, int Q, int K2)
+template <typename S>
+__global__ void k_spf_transpose(const double *__restrict__ flat, typename Cx<S>::T *__restrict__ t, int Q, int K2)
 {
+	typedef typename Cx<S>::T V;
 	long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= 3L * Q * K2) return;
 	int iq = (int)(i % Q);
 	long r = i / Q;
 	int lm = (int)(r % K2), ch = (int)(r / K2);
 	const double *s = flat + (((size_t)ch * Q + iq) * K2 + lm) * 2;
-	t[i] = make_double2(s[0], s[1]);
+	V v;
+	v.x = (S)s[0];
+	v.y = (S)s[1];
+	t[i] = v;
 }
 
-/* block = (b*N+g, m+L); threads over q */
-__global__ void k_rotate(const double2 *__restrict__ spf_t, const double *__restrict__ dtab,
-                         const double2 *__restrict__ tw, int Q, int L, int conj, double2 *__restrict__ out)
+/* block = (b*N+g, m >= 0); threads over q */
+template <typename S>
+__global__ void k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const double *__restrict__ dtab,
+                         const double2 *__restrict__ tw, int Q, int L, int conj, typename Cx<S>::T *__restrict__ out)
 {
-	int K = L + 1, N = 2 * L + 1, K2 = K * K;
-	int bg = blockIdx.x, mi = blockIdx.y, m = mi - L, am = m < 0 ? -m : m;
+	typedef typename Cx<S>::T V;
+	int K = L + 1, N = 2 * L + 1, K2 = K * K, NP = K * (K + 1) / 2;
+	int bg = blockIdx.x, m = blockIdx.y;
 	int b = bg / N, g = bg % N;
 	int iq = threadIdx.x;
 	if (iq >= Q) return;
 	const double *db = dtab + (size_t)b * K * N * N;
-	double sg = conj ? -1.0 : 1.0;
-	int po = pair_off(m, L);
-	for (int l = am; l <= L; l++) {
-		double2 acc0 = make_double2(0, 0), acc1 = acc0, acc2 = acc0;
-		const double *drow = db + ((size_t)l * N + mi) * N;
+	S sg = conj ? (S)-1 : (S)1;
+	int po = psym(m, K);
+	for (int l = m; l <= L; l++) {
+		V acc0 = zero2<V>(), acc1 = acc0, acc2 = acc0;
+		const double *drow = db + ((size_t)l * N + m + L) * N;
 		for (int m1 = -l; m1 <= l; m1++) {
 			int e = ((m1 < 0 ? m1 + N : m1) * g) % N;
 			double dv = drow[m1 + L];
-			double2 f = make_double2(tw[e].x * dv, tw[e].y * dv);
+			V f;
+			f.x = (S)(tw[e].x * dv);
+			f.y = (S)(tw[e].y * dv);
 			int lm = lm_index(l, m1);
-			double2 c0 = spf_t[((size_t)0 * K2 + lm) * Q + iq];
-			double2 c1 = spf_t[((size_t)1 * K2 + lm) * Q + iq];
-			double2 c2 = spf_t[((size_t)2 * K2 + lm) * Q + iq];
+			V c0 = spf_t[((size_t)0 * K2 + lm) * Q + iq];
+			V c1 = spf_t[((size_t)1 * K2 + lm) * Q + iq];
+			V c2 = spf_t[((size_t)2 * K2 + lm) * Q + iq];
 			c0.y *= sg; c1.y *= sg; c2.y *= sg;
 			cfma(acc0, f, c0);
 			cfma(acc1, f, c1);
 			cfma(acc2, f, c2);
 		}
-		double2 *o = out + (((size_t)bg * K2 + po + (l - am)) * 3) * Q + iq;
+		V *o = out + (((size_t)bg * NP + po + (l - m)) * 3) * Q + iq;
 		o[0] = acc0;
 		o[Q] = acc1;
 		o[2 * Q] = acc2;
 	}
 }
 
-/* block = (combo, m+L); threads over q; l blocked by LB for register reuse of U */
-template <int LB>
-__global__ void k_translate(const double2 *__restrict__ U, const double2 *__restrict__ tmat,
-                            const int32_t *__restrict__ combo_zbg, int Q, int L, double2 *__restrict__ out)
+/* block = (combo, m >= 0); threads over q; l blocked by LB for register
+ * reuse of U.  conj(T) U = tau U for even l + l1, tau (-i U) for odd. */
+template <typename S, int LB>
+__global__ void k_translate(const typename Cx<S>::T *__restrict__ U, const S *__restrict__ tau,
+                            const int32_t *__restrict__ combo_zbg, int Q, int L, typename Cx<S>::T *__restrict__ out)
 {
-	int K = L + 1, N = 2 * L + 1, K2 = K * K;
-	int c = blockIdx.x, mi = blockIdx.y, m = mi - L, am = m < 0 ? -m : m;
+	typedef typename Cx<S>::T V;
+	int K = L + 1, N = 2 * L + 1, NP = K * (K + 1) / 2;
+	int c = blockIdx.x, m = blockIdx.y;
 	int iq = threadIdx.x;
 	if (iq >= Q) return;
 	int zi = combo_zbg[3 * c], b2 = combo_zbg[3 * c + 1], g2 = combo_zbg[3 * c + 2];
-	const double2 *Ub = U + (size_t)(b2 * N + g2) * K2 * 3 * Q;
-	const double2 *Tm = tmat + ((size_t)zi * K + am) * K * K * Q;
-	int po = pair_off(m, L);
-	double2 *Ob = out + (size_t)c * K2 * 3 * Q;
-	for (int l0 = am; l0 <= L; l0 += LB) {
-		double2 acc[LB][3];
+	const V *Ub = U + (size_t)(b2 * N + g2) * NP * 3 * Q;
+	const S *Tm = tau + ((size_t)zi * K + m) * K * K * Q;
+	int po = psym(m, K);
+	V *Ob = out + (size_t)c * NP * 3 * Q;
+	for (int l0 = m; l0 <= L; l0 += LB) {
+		V acc[LB][3];
 #pragma unroll
-		for (int j = 0; j < LB; j++) acc[j][0] = acc[j][1] = acc[j][2] = make_double2(0, 0);
-		for (int l1 = am; l1 <= L; l1++) {
-			const double2 *u = Ub + ((size_t)(po + l1 - am) * 3) * Q + iq;
-			double2 u0 = u[0], u1 = u[Q], u2 = u[2 * Q];
+		for (int j = 0; j < LB; j++) acc[j][0] = acc[j][1] = acc[j][2] = zero2<V>();
+		for (int l1 = m; l1 <= L; l1++) {
+			const V *u = Ub + ((size_t)(po + l1 - m) * 3) * Q + iq;
+			V u0 = u[0], u1 = u[Q], u2 = u[2 * Q];
 #pragma unroll
 			for (int j = 0; j < LB; j++) {
 				int l = l0 + j;
 				if (l > L) break;
-				double2 t = Tm[((size_t)l * K + l1) * Q + iq];
-				t.y = -t.y;
-				cfma(acc[j][0], t, u0);
-				cfma(acc[j][1], t, u1);
-				cfma(acc[j][2], t, u2);
+				S t = Tm[((size_t)l * K + l1) * Q + iq];
+				if (((l + l1) & 1) == 0) {
+					acc[j][0].x += t * u0.x; acc[j][0].y += t * u0.y;
+					acc[j][1].x += t * u1.x; acc[j][1].y += t * u1.y;
+					acc[j][2].x += t * u2.x; acc[j][2].y += t * u2.y;
+				} else {
+					acc[j][0].x += t * u0.y; acc[j][0].y -= t * u0.x;
+					acc[j][1].x += t * u1.y; acc[j][1].y -= t * u1.x;
+					acc[j][2].x += t * u2.y; acc[j][2].y -= t * u2.x;
+				}
 			}
 		}
 #pragma unroll
 		for (int j = 0; j < LB; j++) {
 			int l = l0 + j;
 			if (l > L) break;
-			double2 *o = Ob + ((size_t)(po + l - am) * 3) * Q + iq;
+			V *o = Ob + ((size_t)(po + l - m) * 3) * Q + iq;
 			o[0] = acc[j][0];
 			o[Q] = acc[j][1];
 			o[2 * Q] = acc[j][2];
@@ -134,29 +158,30 @@ __global__ void k_translate(const double2 *__restrict__ U, const double2 *__rest
 	}
 }
 
-/* block = one pose; threads over q.  Writes cross[src][c][q]. */
-__global__ void k_pose_cross(const sxsk_pose *__restrict__ poses, int combo_base, const double2 *__restrict__ P,
-                             const double2 *__restrict__ R, const double2 *__restrict__ tw,
+/* block = one pose; threads over q.  Writes cross[src][c][q] (FP64). */
+template <typename S>
+__global__ void k_pose_cross(const sxsk_pose *__restrict__ poses, int combo_base, const typename Cx<S>::T *__restrict__ P,
+                             const typename Cx<S>::T *__restrict__ R, const double2 *__restrict__ tw,
                              const double *__restrict__ cst, int Q, int L, double *__restrict__ cross)
 {
-	int K = L + 1, N = 2 * L + 1, K2 = K * K;
+	typedef typename Cx<S>::T V;
+	int K = L + 1, N = 2 * L + 1, NP = K * (K + 1) / 2;
 	sxsk_pose ps = poses[blockIdx.x];
 	int iq = threadIdx.x;
 	if (iq >= Q) return;
-	const double2 *Pb = P + (size_t)(ps.b1 * N + ps.g1) * K2 * 3 * Q + iq;
-	const double2 *Rb = R + (size_t)(ps.combo - combo_base) * K2 * 3 * Q + iq;
-	double f[6] = {0, 0, 0, 0, 0, 0};
+	const V *Pb = P + (size_t)(ps.b1 * N + ps.g1) * NP * 3 * Q + iq;
+	const V *Rb = R + (size_t)(ps.combo - combo_base) * NP * 3 * Q + iq;
+	S f[6] = {0, 0, 0, 0, 0, 0};
 	int p = 0;
-	for (int m = -L; m <= L; m++) {
-		int am = m < 0 ? -m : m;
-		double2 g[6];
+	for (int m = 0; m <= L; m++) {
+		V g[6];
 #pragma unroll
-		for (int c = 0; c < 6; c++) g[c] = make_double2(0, 0);
-		for (int l = am; l <= L; l++, p++) {
-			const double2 *pp = Pb + (size_t)p * 3 * Q;
-			const double2 *rr = Rb + (size_t)p * 3 * Q;
-			double2 pv = pp[0], pd = pp[Q], pw = pp[2 * Q];
-			double2 rv = rr[0], rd = rr[Q], rw = rr[2 * Q];
+		for (int c = 0; c < 6; c++) g[c] = zero2<V>();
+		for (int l = m; l <= L; l++, p++) {
+			const V *pp = Pb + (size_t)p * 3 * Q;
+			const V *rr = Rb + (size_t)p * 3 * Q;
+			V pv = pp[0], pd = pp[Q], pw = pp[2 * Q];
+			V rv = rr[0], rd = rr[Q], rw = rr[2 * Q];
 			cfma(g[0], pv, rv);
 			cfma(g[1], pv, rd); cfma(g[1], pd, rv);
 			cfma(g[2], pv, rw); cfma(g[2], pw, rv);
@@ -164,17 +189,24 @@ __global__ void k_pose_cross(const sxsk_pose *__restrict__ poses, int combo_base
 			cfma(g[4], pd, rw); cfma(g[4], pw, rd);
 			cfma(g[5], pw, rw);
 		}
-		double2 w = tw[((m < 0 ? m + N : m) * ps.a2) % N];
+		V w = from2<V>(tw[(m * ps.a2) % N]);
+		S wt = m == 0 ? (S)1 : (S)2;
 #pragma unroll
-		for (int c = 0; c < 6; c++) f[c] += w.x * g[c].x - w.y * g[c].y;
+		for (int c = 0; c < 6; c++) f[c] += wt * (w.x * g[c].x - w.y * g[c].y);
 	}
 	double *o = cross + (size_t)ps.src * 6 * Q + iq;
 #pragma unroll
 	for (int c = 0; c < 6; c++) {
 		double v = cst[c * Q + iq];
-		v += 2.0 * f[c];
+		v += 2.0 * (double)f[c];
 		o[c * Q] = v;
 	}
+}
+
+__global__ void k_to_float(const double *__restrict__ a, float *__restrict__ b, long n)
+{
+	long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) b[i] = (float)a[i];
 }
 
 __device__ __forceinline__ double warp_sum(double v)
@@ -190,13 +222,15 @@ __device__ __forceinline__ double warp_sum(double v)
  * be = VW - G DW, ga = WW) the piecewise-linear model's tan_i and buf_i are
  * quadratics in c2, so best_scale's up(c2) (quadratic) and down(c2)
  * (quartic) are accumulated once per c1 as coefficients; each cell is then
- * chi^2 = sum a0 + k (-2 up + k down), k = up/down. */
+ * chi^2 = sum a0 + k (-2 up + k down), k = up/down.  hinv[i] = 1/(q_i -
+ * q_{i-1}) with q_{-1} = -1. */
 #define FIT_WARPS 4
 __global__ void k_fit_grid(const double *__restrict__ cross, int npose, int Q, const double *__restrict__ q,
-                           const double *__restrict__ a, double a0sum, double peak, const double *__restrict__ gtab,
-                           const double *__restrict__ c1g, int n1, const double *__restrict__ c2g, int n2,
-                           double *__restrict__ chi, double *__restrict__ c1o, double *__restrict__ c2o,
-                           int32_t *__restrict__ cello, double *__restrict__ grid, double *__restrict__ scaled)
+                           const double *__restrict__ hinv, const double *__restrict__ a, double a0sum, double peak,
+                           const double *__restrict__ gtab, const double *__restrict__ c1g, int n1,
+                           const double *__restrict__ c2g, int n2, double *__restrict__ chi, double *__restrict__ c1o,
+                           double *__restrict__ c2o, int32_t *__restrict__ cello, double *__restrict__ grid,
+                           double *__restrict__ scaled)
 {
 	extern __shared__ double sm[];
 	int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -228,19 +262,19 @@ __global__ void k_fit_grid(const double *__restrict__ cross, int npose, int Q, c
 			double alp = VV[ip] - gp * VD[ip] + gp * gp * DD[ip];
 			double bep = VW[ip] - gp * DW[ip];
 			double gap = WW[ip];
-			double qc = q[i], qp = i > 0 ? q[i - 1] : -1.0;
-			double h = qc - qp;
-			double t0 = (al - alp) / h, t1 = (be - bep) / h, t2 = (ga - gap) / h;
+			double qc = q[i], hi = hinv[i];
+			double t0 = (al - alp) * hi, t1 = (be - bep) * hi, t2 = (ga - gap) * hi;
 			double b0 = al - t0 * qc, b1 = be - t1 * qc, b2 = ga - t2 * qc;
 			double a1 = a[6 * i + 1], a2 = a[6 * i + 2], a3 = a[6 * i + 3], a4 = a[6 * i + 4], a5 = a[6 * i + 5];
 			U0 += b0 * a1 + t0 * a2;
 			U1 += b1 * a1 + t1 * a2;
 			U2 += b2 * a1 + t2 * a2;
-			D0 += b0 * b0 * a3 + 2.0 * t0 * b0 * a4 + t0 * t0 * a5;
-			D1 += 2.0 * b0 * b1 * a3 + 2.0 * (t0 * b1 + t1 * b0) * a4 + 2.0 * t0 * t1 * a5;
-			D2 += (b1 * b1 + 2.0 * b0 * b2) * a3 + 2.0 * (t0 * b2 + t1 * b1 + t2 * b0) * a4 + (t1 * t1 + 2.0 * t0 * t2) * a5;
-			D3 += 2.0 * b1 * b2 * a3 + 2.0 * (t1 * b2 + t2 * b1) * a4 + 2.0 * t1 * t2 * a5;
-			D4 += b2 * b2 * a3 + 2.0 * t2 * b2 * a4 + t2 * t2 * a5;
+			double a4x2 = 2.0 * a4;
+			D0 += b0 * (b0 * a3 + t0 * a4x2) + t0 * t0 * a5;
+			D1 += 2.0 * (b0 * (b1 * a3 + t1 * a4) + t0 * (b1 * a4 + t1 * a5));
+			D2 += b1 * (b1 * a3 + t1 * a4x2) + t1 * t1 * a5 + 2.0 * (b0 * (b2 * a3 + t2 * a4) + t0 * (b2 * a4 + t2 * a5));
+			D3 += 2.0 * (b1 * (b2 * a3 + t2 * a4) + t1 * (b2 * a4 + t2 * a5));
+			D4 += b2 * (b2 * a3 + t2 * a4x2) + t2 * t2 * a5;
 		}
 		U0 = warp_sum(U0); U1 = warp_sum(U1); U2 = warp_sum(U2);
 		D0 = warp_sum(D0); D1 = warp_sum(D1); D2 = warp_sum(D2); D3 = warp_sum(D3); D4 = warp_sum(D4);
@@ -283,49 +317,67 @@ inline int qthreads(int Q) { return ((Q + 31) / 32) * 32; }
 
 extern "C" {
 
-int sxsk_spf_transpose(const double *flat, double2 *spf_t, int Q, int L, cudaStream_t s)
+int sxsk_spf_transpose(const double *flat, void *spf_t, int Q, int L, int fp32, cudaStream_t s)
 {
 	int K2 = (L + 1) * (L + 1);
-	k_spf_transpose<<<nblk(3L * Q * K2, 256), 256, 0, s>>>(flat, spf_t, Q, K2);
+	if (fp32) k_spf_transpose<float><<<nblk(3L * Q * K2, 256), 256, 0, s>>>(flat, (float2 *)spf_t, Q, K2);
+	else k_spf_transpose<double><<<nblk(3L * Q * K2, 256), 256, 0, s>>>(flat, (double2 *)spf_t, Q, K2);
 	return cudaGetLastError();
 }
 
-int sxsk_rotate(const double2 *spf_t, const double *dtab, const double2 *tw, int Q, int L, int conj,
-                double2 *out, cudaStream_t s)
+int sxsk_rotate(const void *spf_t, const double *dtab, const double2 *tw, int Q, int L, int conj, void *out, int fp32,
+                cudaStream_t s)
 {
 	int K = L + 1, N = 2 * L + 1;
-	dim3 grid(K * N, N);
-	k_rotate<<<grid, qthreads(Q), 0, s>>>(spf_t, dtab, tw, Q, L, conj, out);
+	dim3 grid(K * N, K);
+	if (fp32) k_rotate<float><<<grid, qthreads(Q), 0, s>>>((const float2 *)spf_t, dtab, tw, Q, L, conj, (float2 *)out);
+	else k_rotate<double><<<grid, qthreads(Q), 0, s>>>((const double2 *)spf_t, dtab, tw, Q, L, conj, (double2 *)out);
 	return cudaGetLastError();
 }
 
-int sxsk_translate(const double2 *U, const double2 *tmat, const int32_t *combo_zbg, int ncombo,
-                   int Q, int L, double2 *out, cudaStream_t s)
+int sxsk_to_float(const double *a, float *b, long n, cudaStream_t s)
+{
+	if (n <= 0) return 0;
+	k_to_float<<<nblk(n, 256), 256, 0, s>>>(a, b, n);
+	return cudaGetLastError();
+}
+
+int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, int ncombo, int Q, int L, void *out,
+                   int fp32, cudaStream_t s)
 {
 	if (ncombo <= 0) return 0;
-	dim3 grid(ncombo, 2 * L + 1);
-	k_translate<4><<<grid, qthreads(Q), 0, s>>>(U, tmat, combo_zbg, Q, L, out);
+	dim3 grid(ncombo, L + 1);
+	if (fp32)
+		k_translate<float, 4><<<grid, qthreads(Q), 0, s>>>((const float2 *)U, (const float *)tau, combo_zbg, Q, L,
+		                                                    (float2 *)out);
+	else
+		k_translate<double, 4><<<grid, qthreads(Q), 0, s>>>((const double2 *)U, (const double *)tau, combo_zbg, Q, L,
+		                                                     (double2 *)out);
 	return cudaGetLastError();
 }
 
-int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, const double2 *P, const double2 *R,
-                    const double2 *tw, const double *cst, int Q, int L, double *cross, cudaStream_t s)
+int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, const void *P, const void *R,
+                    const double2 *tw, const double *cst, int Q, int L, double *cross, int fp32, cudaStream_t s)
 {
 	if (npose <= 0) return 0;
-	k_pose_cross<<<npose, qthreads(Q), 0, s>>>(poses, combo_base, P, R, tw, cst, Q, L, cross);
+	if (fp32)
+		k_pose_cross<float><<<npose, qthreads(Q), 0, s>>>(poses, combo_base, (const float2 *)P, (const float2 *)R, tw,
+		                                                   cst, Q, L, cross);
+	else
+		k_pose_cross<double><<<npose, qthreads(Q), 0, s>>>(poses, combo_base, (const double2 *)P, (const double2 *)R,
+		                                                    tw, cst, Q, L, cross);
 	return cudaGetLastError();
 }
 
-int sxsk_fit_grid(const double *cross, int npose, int Q, const double *q, const double *a, double a0sum,
-                  double peak, const double *gtab, const double *c1g, int n1, const double *c2g, int n2,
-                  double *chi, double *c1, double *c2, int32_t *cell, double *grid, double *scaled,
-                  cudaStream_t s)
+int sxsk_fit_grid(const double *cross, int npose, int Q, const double *q, const double *hinv, const double *a,
+                  double a0sum, double peak, const double *gtab, const double *c1g, int n1, const double *c2g, int n2,
+                  double *chi, double *c1, double *c2, int32_t *cell, double *grid, double *scaled, cudaStream_t s)
 {
 	if (npose <= 0) return 0;
 	size_t smem = (size_t)FIT_WARPS * 6 * Q * sizeof(double);
 	if (smem > 48 * 1024) cudaFuncSetAttribute(k_fit_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-	k_fit_grid<<<nblk(npose, FIT_WARPS), FIT_WARPS * 32, smem, s>>>(cross, npose, Q, q, a, a0sum, peak, gtab, c1g,
-	                                                               n1, c2g, n2, chi, c1, c2, cell, grid, scaled);
+	k_fit_grid<<<nblk(npose, FIT_WARPS), FIT_WARPS * 32, smem, s>>>(cross, npose, Q, q, hinv, a, a0sum, peak, gtab,
+	                                                               c1g, n1, c2g, n2, chi, c1, c2, cell, grid, scaled);
 	return cudaGetLastError();
 }
 

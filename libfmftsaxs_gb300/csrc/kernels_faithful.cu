@@ -156,9 +156,13 @@ __global__ void k_bessel_z(const double *__restrict__ z, int nz, const double *_
 }
 
 /* T^{|m|}_{l l1}(q z) = sum_p (-1)^m i^p j_p d_lm(l1,p) for l <= l1, mirrored
- * (src/fftsaxs.c:182-243).  Thread = (iz, m, l, l1 >= l, q), q fastest. */
+ * (src/fftsaxs.c:182-243).  Thread = (iz, m, l, l1 >= l, q), q fastest.
+ * The 3j factor 3j(l p l1; 0 0 0) vanishes unless l + p + l1 is even, so T
+ * is real for even l + l1 and imaginary for odd l + l1 (the other part is
+ * the sum of exact zeros and binary128 round-off below 1e-30 relative); the
+ * table keeps that one real number, tau = Re T (even) or Im T (odd). */
 __global__ void k_tmatrix(const double *__restrict__ bes, const double *__restrict__ ds, int nz, int Q, int L,
-                          const int2 *__restrict__ ll1, int nll1, double2 *__restrict__ tmat)
+                          const int2 *__restrict__ ll1, int nll1, double *__restrict__ tau)
 {
 	const double ipr[4] = {1.0, 0.0, -1.0, 0.0};
 	const double ipi[4] = {0.0, 1.0, 0.0, -1.0};
@@ -182,9 +186,10 @@ __global__ void k_tmatrix(const double *__restrict__ bes, const double *__restri
 		re += ipr[p % 4] * v;
 		im += ipi[p % 4] * v;
 	}
+	double v = ((l + l1) & 1) ? im : re;
 	size_t base = ((size_t)iz * K + m) * K;
-	tmat[((base + l) * K + l1) * Q + iq] = make_double2(re, im);
-	tmat[((base + l1) * K + l) * Q + iq] = make_double2(re, im);
+	tau[((base + l) * K + l1) * Q + iq] = v;
+	tau[((base + l1) * K + l) * Q + iq] = v;
 }
 
 /* Self terms of fill_const (src/fftsaxs.c:27-50, 52-85): per channel pair
@@ -243,13 +248,13 @@ int sxsk_bessel_z(const double *z, int nz, const double *q, int Q, int L, double
 }
 
 int sxsk_tmatrix(const double *bes, const double *dsymb, int nz, int Q, int L, const int2 *ll1, int nll1,
-                  double2 *tmat, cudaStream_t s)
+                 double *tau, cudaStream_t s)
 {
 	int K = L + 1;
 	long n = (long)nz * K * nll1 * Q;
 	if (n == 0) return 0;
-	cudaMemsetAsync(tmat, 0, (size_t)nz * K * K * K * Q * sizeof(double2), s);
-	k_tmatrix<<<nblk(n, 128), 128, 0, s>>>(bes, dsymb, nz, Q, L, ll1, nll1, tmat);
+	cudaMemsetAsync(tau, 0, (size_t)nz * K * K * K * Q * sizeof(double), s);
+	k_tmatrix<<<nblk(n, 128), 128, 0, s>>>(bes, dsymb, nz, Q, L, ll1, nll1, tau);
 	return cudaGetLastError();
 }
 

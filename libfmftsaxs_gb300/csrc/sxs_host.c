@@ -149,11 +149,15 @@ struct sxsg_plan {
 	cudaStream_t s;
 	double mult, peak, a0sum;
 	/* resident inputs */
-	double *d_A, *d_B, *d_q, *d_a, *d_gtab, *d_c1g, *d_c2g, *d_cst;
-	double2 *d_At, *d_Bt, *d_tw;
+	double *d_A, *d_B, *d_q, *d_hinv, *d_a, *d_gtab, *d_c1g, *d_c2g, *d_cst;
+	double2 *d_tw;
+	void *d_At, *d_Bt;          /* transposed coefficients, table precision */
 	double *h_z;
+	int fp32;                   /* tables in float (mixed path) */
+	size_t celem;               /* bytes of one complex table entry */
+	int NP;                     /* (m >= 0, l >= m) pairs */
 	/* rotation tables (depend on the twiddle variant) */
-	double2 *d_P, *d_U;
+	void *d_P, *d_U;
 	int tw_variant; /* -1 none, 0 simple_ft, 1 exact */
 	/* poses */
 	int64_t npose;
@@ -165,10 +169,11 @@ struct sxsg_plan {
 	int nzt;                    /* touched z count */
 	double *h_zt, *d_zt;        /* touched z values */
 	double *d_bes;
-	double2 *d_tmat;
+	double *d_tau;              /* [nzt][K][K][K][Q] */
+	float *d_tauf;              /* float copy (mixed path) */
 	size_t pose_cap, combo_cap, zt_cap;
 	/* per-chunk translated table */
-	double2 *d_R;
+	void *d_R;
 	int64_t R_combos;
 	size_t r_budget;
 	/* outputs */
@@ -185,9 +190,10 @@ struct sxsg_plan {
 static void plan_free_poses(sxsg_plan *p)
 {
 	free(p->h_poses); free(p->h_combo); free(p->h_cstart); free(p->h_zt);
-	cudaFree(p->d_poses); cudaFree(p->d_combo); cudaFree(p->d_zt); cudaFree(p->d_bes); cudaFree(p->d_tmat);
+	cudaFree(p->d_poses); cudaFree(p->d_combo); cudaFree(p->d_zt); cudaFree(p->d_bes); cudaFree(p->d_tau);
+	cudaFree(p->d_tauf);
 	p->h_poses = NULL; p->h_combo = NULL; p->h_cstart = NULL; p->h_zt = NULL;
-	p->d_poses = NULL; p->d_combo = NULL; p->d_zt = NULL; p->d_bes = NULL; p->d_tmat = NULL;
+	p->d_poses = NULL; p->d_combo = NULL; p->d_zt = NULL; p->d_bes = NULL; p->d_tau = NULL; p->d_tauf = NULL;
 	p->pose_cap = p->combo_cap = p->zt_cap = 0;
 }
 
@@ -196,7 +202,7 @@ void sxsg_plan_destroy(sxsg_plan *p)
 	if (!p) return;
 	cudaStreamSynchronize(p->s);
 	plan_free_poses(p);
-	cudaFree(p->d_A); cudaFree(p->d_B); cudaFree(p->d_q); cudaFree(p->d_a); cudaFree(p->d_gtab);
+	cudaFree(p->d_A); cudaFree(p->d_B); cudaFree(p->d_q); cudaFree(p->d_hinv); cudaFree(p->d_a); cudaFree(p->d_gtab);
 	cudaFree(p->d_c1g); cudaFree(p->d_c2g); cudaFree(p->d_cst); cudaFree(p->d_At); cudaFree(p->d_Bt);
 	cudaFree(p->d_tw); cudaFree(p->d_P); cudaFree(p->d_U); cudaFree(p->d_R);
 	cudaFree(p->d_cross); cudaFree(p->d_chi); cudaFree(p->d_c1); cudaFree(p->d_c2); cudaFree(p->d_grid);
@@ -214,7 +220,8 @@ int sxsg_plan_create(sxsg_plan **out, const double *A, const double *B, const do
 		return sxs_fail(-2, "sxsg_plan_create: bad arguments (Q must be in [1, 1024])");
 	if ((n1 > 0 && !c1g) || (n2 > 0 && !c2g) || n1 < 0 || n2 < 0)
 		return sxs_fail(-2, "sxsg_plan_create: bad fit grid");
-	if (precision != SXSG_FP64) return sxs_fail(-2, "sxsg_plan_create: unknown precision %d", precision);
+	if (precision != SXSG_FP64 && precision != SXSG_MIXED)
+		return sxs_fail(-2, "sxsg_plan_create: unknown precision %d", precision);
 	const sxs_ltables *lt;
 	int rc = sxs_ltables_get(L, &lt);
 	if (rc) return rc;
@@ -222,6 +229,9 @@ int sxsg_plan_create(sxsg_plan **out, const double *A, const double *B, const do
 	p->L = L; p->K = L + 1; p->N = 2 * L + 1; p->K2 = p->K * p->K; p->Q = Q; p->nz = nz;
 	p->n1 = n1; p->n2 = n2; p->precision = precision; p->lt = lt; p->s = g_stream;
 	p->mult = mult; p->peak = peak; p->tw_variant = -1;
+	p->fp32 = precision == SXSG_MIXED;
+	p->celem = p->fp32 ? 2 * sizeof(float) : 2 * sizeof(double);
+	p->NP = p->K * (p->K + 1) / 2;
 	double s0 = 0.0;
 	for (int i = 0; i < Q; i++) s0 += a[6 * i];
 	p->a0sum = s0;
@@ -232,18 +242,19 @@ int sxsg_plan_create(sxsg_plan **out, const double *A, const double *B, const do
 	for (int i = 0; i < 6 && !e; i++) e = cudaEventCreate(&p->ev[i]);
 	if (!e) e = cudaMalloc((void **)&p->d_A, sizeof(double) * spf_n);
 	if (!e) e = cudaMalloc((void **)&p->d_B, sizeof(double) * spf_n);
-	if (!e) e = cudaMalloc((void **)&p->d_At, sizeof(double) * spf_n);
-	if (!e) e = cudaMalloc((void **)&p->d_Bt, sizeof(double) * spf_n);
+	if (!e) e = cudaMalloc(&p->d_At, p->celem * spf_n / 2);
+	if (!e) e = cudaMalloc(&p->d_Bt, p->celem * spf_n / 2);
 	if (!e) e = cudaMalloc((void **)&p->d_q, sizeof(double) * Q);
+	if (!e) e = cudaMalloc((void **)&p->d_hinv, sizeof(double) * Q);
 	if (!e) e = cudaMalloc((void **)&p->d_a, sizeof(double) * 6 * Q);
 	if (!e) e = cudaMalloc((void **)&p->d_cst, sizeof(double) * 6 * Q);
 	if (!e) e = cudaMalloc((void **)&p->d_tw, sizeof(double2) * p->N);
 	if (!e && n1 > 0) e = cudaMalloc((void **)&p->d_gtab, sizeof(double) * n1 * Q);
 	if (!e && n1 > 0) e = cudaMalloc((void **)&p->d_c1g, sizeof(double) * n1);
 	if (!e && n2 > 0) e = cudaMalloc((void **)&p->d_c2g, sizeof(double) * n2);
-	size_t rot_n = (size_t)p->K * p->N * p->K2 * 3 * Q;
-	if (!e) e = cudaMalloc((void **)&p->d_P, sizeof(double2) * rot_n);
-	if (!e) e = cudaMalloc((void **)&p->d_U, sizeof(double2) * rot_n);
+	size_t rot_n = (size_t)p->K * p->N * p->NP * 3 * Q;
+	if (!e) e = cudaMalloc(&p->d_P, p->celem * rot_n);
+	if (!e) e = cudaMalloc(&p->d_U, p->celem * rot_n);
 	if (e) {
 		sxsg_plan_destroy(p);
 		return sxs_cuda_fail(e, "sxsg_plan_create allocation");
@@ -252,6 +263,14 @@ int sxsg_plan_create(sxsg_plan **out, const double *A, const double *B, const do
 	e = cudaMemcpyAsync(p->d_A, A, sizeof(double) * spf_n, cudaMemcpyHostToDevice, s);
 	if (!e) e = cudaMemcpyAsync(p->d_B, B, sizeof(double) * spf_n, cudaMemcpyHostToDevice, s);
 	if (!e) e = cudaMemcpyAsync(p->d_q, q, sizeof(double) * Q, cudaMemcpyHostToDevice, s);
+	if (!e) {
+		/* 1 / (q_i - q_{i-1}) with q_{-1} = -1: the spacing of the
+		 * piecewise-linear model (src/min_saxs.c:400-417) */
+		double *hi = malloc(sizeof(double) * Q);
+		for (int i = 0; i < Q; i++) hi[i] = 1.0 / (q[i] - (i > 0 ? q[i - 1] : -1.0));
+		e = cudaMemcpy(p->d_hinv, hi, sizeof(double) * Q, cudaMemcpyHostToDevice);
+		free(hi);
+	}
 	if (!e) e = cudaMemcpyAsync(p->d_a, a, sizeof(double) * 6 * Q, cudaMemcpyHostToDevice, s);
 	if (!e && n1 > 0) {
 		/* G(c1, q) = c1^3 exp(-mult (c1^2 - 1) q^2) exactly as point_score
@@ -269,8 +288,8 @@ int sxsg_plan_create(sxsg_plan **out, const double *A, const double *B, const do
 	}
 	if (!e && n2 > 0) e = cudaMemcpyAsync(p->d_c2g, c2g, sizeof(double) * n2, cudaMemcpyHostToDevice, s);
 	if (!e) {
-		e = (cudaError_t)sxsk_spf_transpose(p->d_A, p->d_At, Q, L, s);
-		if (!e) e = (cudaError_t)sxsk_spf_transpose(p->d_B, p->d_Bt, Q, L, s);
+		e = (cudaError_t)sxsk_spf_transpose(p->d_A, p->d_At, Q, L, p->fp32, s);
+		if (!e) e = (cudaError_t)sxsk_spf_transpose(p->d_B, p->d_Bt, Q, L, p->fp32, s);
 		if (!e) e = (cudaError_t)sxsk_const_int(p->d_A, p->d_B, Q, L, p->d_cst, s);
 		sxs_count_launches(3);
 	}
@@ -395,7 +414,9 @@ int sxsg_plan_set_poses(sxsg_plan *p, const int64_t *index, int64_t n, int skip)
 	if (!e) e = cudaMalloc((void **)&p->d_combo, sizeof(int32_t) * 3 * (ncombo > 0 ? ncombo : 1));
 	if (!e) e = cudaMalloc((void **)&p->d_zt, sizeof(double) * (nzt > 0 ? nzt : 1));
 	if (!e && nzt > 0) e = cudaMalloc((void **)&p->d_bes, sizeof(double) * (size_t)nzt * p->Q * N);
-	if (!e && nzt > 0) e = cudaMalloc((void **)&p->d_tmat, sizeof(double2) * (size_t)nzt * p->K * p->K * p->K * p->Q);
+	size_t tau_n = (size_t)nzt * p->K * p->K * p->K * p->Q;
+	if (!e && nzt > 0) e = cudaMalloc((void **)&p->d_tau, sizeof(double) * tau_n);
+	if (!e && nzt > 0 && p->fp32) e = cudaMalloc((void **)&p->d_tauf, sizeof(float) * tau_n);
 	if (!e && n > 0) e = cudaMemcpyAsync(p->d_poses, p->h_poses, sizeof(sxsk_pose) * n, cudaMemcpyHostToDevice, p->s);
 	if (!e && ncombo > 0) e = cudaMemcpyAsync(p->d_combo, p->h_combo, sizeof(int32_t) * 3 * ncombo, cudaMemcpyHostToDevice, p->s);
 	if (!e && nzt > 0) e = cudaMemcpyAsync(p->d_zt, p->h_zt, sizeof(double) * nzt, cudaMemcpyHostToDevice, p->s);
@@ -432,15 +453,19 @@ static int plan_tables(sxsg_plan *p)
 		cudaError_t e = cudaMemcpy(p->d_tw, tw, sizeof(double2) * N, cudaMemcpyHostToDevice);
 		free(tw);
 		if (e) return sxs_cuda_fail(e, "twiddle upload");
-		SXS_K(sxsk_rotate(p->d_At, p->lt->d_dtab, p->d_tw, Q, L, 0, p->d_P, s));
-		SXS_K(sxsk_rotate(p->d_Bt, p->lt->d_dtab, p->d_tw, Q, L, 1, p->d_U, s));
+		SXS_K(sxsk_rotate(p->d_At, p->lt->d_dtab, p->d_tw, Q, L, 0, p->d_P, p->fp32, s));
+		SXS_K(sxsk_rotate(p->d_Bt, p->lt->d_dtab, p->d_tw, Q, L, 1, p->d_U, p->fp32, s));
 		sxs_count_launches(2);
 		p->tw_variant = variant;
 	}
 	if (p->nzt > 0) {
 		SXS_K(sxsk_bessel_z(p->d_zt, p->nzt, p->d_q, Q, L, p->d_bes, s));
-		SXS_K(sxsk_tmatrix(p->d_bes, p->lt->d_dsymb, p->nzt, Q, L, p->lt->d_ll1, p->lt->nll1, p->d_tmat, s));
+		SXS_K(sxsk_tmatrix(p->d_bes, p->lt->d_dsymb, p->nzt, Q, L, p->lt->d_ll1, p->lt->nll1, p->d_tau, s));
 		sxs_count_launches(2);
+		if (p->fp32) {
+			SXS_K(sxsk_to_float(p->d_tau, p->d_tauf, (long)p->nzt * p->K * p->K * p->K * Q, s));
+			sxs_count_launches(1);
+		}
 	}
 	return 0;
 }
@@ -458,25 +483,26 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 	if ((rc = plan_tables(p))) return rc;
 	SXS_CU(cudaEventRecord(p->ev[1], s));
 	/* translated table in chunks of combos that fit the budget */
-	size_t per_combo = (size_t)p->K2 * 3 * Q * sizeof(double2);
+	size_t per_combo = (size_t)p->NP * 3 * Q * p->celem;
 	int64_t chunk = (int64_t)(p->r_budget / per_combo);
 	if (chunk < 1) chunk = 1;
 	if (chunk > p->ncombo) chunk = p->ncombo;
 	if (chunk > 0 && p->R_combos < chunk) {
 		cudaFree(p->d_R);
 		p->d_R = NULL;
-		SXS_CU(cudaMalloc((void **)&p->d_R, per_combo * chunk));
+		SXS_CU(cudaMalloc(&p->d_R, per_combo * chunk));
 		p->R_combos = chunk;
 	}
 	float t_tr = 0, t_pc = 0;
 	for (int64_t c0 = 0; c0 < p->ncombo; c0 += chunk) {
 		int64_t c1 = c0 + chunk < p->ncombo ? c0 + chunk : p->ncombo;
 		SXS_CU(cudaEventRecord(p->ev[2], s));
-		SXS_K(sxsk_translate(p->d_U, p->d_tmat, p->d_combo + 3 * c0, (int)(c1 - c0), Q, L, p->d_R, s));
+		const void *tau = p->fp32 ? (const void *)p->d_tauf : (const void *)p->d_tau;
+		SXS_K(sxsk_translate(p->d_U, tau, p->d_combo + 3 * c0, (int)(c1 - c0), Q, L, p->d_R, p->fp32, s));
 		SXS_CU(cudaEventRecord(p->ev[3], s));
 		int64_t p0 = p->h_cstart[c0], p1 = p->h_cstart[c1];
 		SXS_K(sxsk_pose_cross(p->d_poses + p0, (int)(p1 - p0), (int)c0, p->d_P, p->d_R, p->d_tw, p->d_cst, Q, L,
-		                      p->d_cross, s));
+		                      p->d_cross, p->fp32, s));
 		SXS_CU(cudaEventRecord(p->ev[4], s));
 		sxs_count_launches(2);
 		if (p->ncombo > chunk) {
@@ -495,7 +521,7 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 	SXS_CU(cudaEventRecord(p->ev[5], s));
 	int n = (int)p->npose;
 	if (fit_mode == SXSG_FIT_GRID) {
-		SXS_K(sxsk_fit_grid(p->d_cross, n, Q, p->d_q, p->d_a, p->a0sum, p->peak, p->d_gtab, p->d_c1g, p->n1, p->d_c2g,
+		SXS_K(sxsk_fit_grid(p->d_cross, n, Q, p->d_q, p->d_hinv, p->d_a, p->a0sum, p->peak, p->d_gtab, p->d_c1g, p->n1, p->d_c2g,
 		                    p->n2, p->d_chi, p->d_c1, p->d_c2, p->d_cell, NULL, p->d_scaled, s));
 		sxs_count_launches(n > 0 ? 1 : 0);
 	} else if (fit_mode == SXSG_FIT_LBFGSB) {
@@ -541,7 +567,7 @@ int sxsg_plan_results(sxsg_plan *p, double *chi, double *c1, double *c2, int32_t
 		if (!e) e = cudaMalloc((void **)&t2, sizeof(double) * n);
 		if (!e) e = cudaMalloc((void **)&tcell, sizeof(int32_t) * n);
 		if (!e) {
-			e = (cudaError_t)sxsk_fit_grid(p->d_cross, (int)n, p->Q, p->d_q, p->d_a, p->a0sum, p->peak, p->d_gtab,
+			e = (cudaError_t)sxsk_fit_grid(p->d_cross, (int)n, p->Q, p->d_q, p->d_hinv, p->d_a, p->a0sum, p->peak, p->d_gtab,
 			                               p->d_c1g, p->n1, p->d_c2g, p->n2, tc, t1, t2, tcell, d_g, NULL, s);
 			sxs_count_launches(1);
 		}

@@ -1,0 +1,93 @@
+"""The mixed-precision path (SXSG_MIXED: FP32 rotation, translation and
+per-pose contractions, FP64 everywhere else) against the reference.
+
+The stated bound for this path is |chi_mixed - chi_ref| <= 1e-4 chi_ref.
+Checked here:
+  * golden fixtures (the reference's own outputs): best chi of the grid fit
+    and of the L-BFGS-B fit within 1e-4 relative; the chosen grid cell is the
+    reference's, or one whose reference chi^2 is within 2e-4 of the best;
+  * raw cross terms within 1e-5 of each pose's channel scale;
+  * random cases against the oracle for L from 1 to 15;
+  * a dimer at lmax = 20, Q = 101 (the headline shapes, fewer atoms and
+    poses) against the FP64 GPU path, which the other tests pin to the
+    reference at 1e-10.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from test_gpu_parity import _random_case, chan_err, load
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+CHI_TOL = 1e-4
+CROSS_TOL = 1e-5
+
+
+def check_grid(res, grid_ref):
+    g = grid_ref.reshape(len(grid_ref), -1)
+    best = g.min(axis=1)
+    n = len(g)
+    np.testing.assert_allclose(res["chi"][:n], np.sqrt(best), rtol=CHI_TOL, atol=0)
+    chosen = g[np.arange(n), res["cell"][:n]]
+    assert np.all(chosen <= best * (1 + 2 * CHI_TOL))
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p)[:-4])
+def test_mixed_grid_fit_matches_reference_fixture(gpu, path):
+    g = load(path)
+    L, skip = int(g["L"]), int(g["skip"])
+    p = gpu.Plan(g["A"], g["B"], g["q"], g["z"], L, g["a"], float(g["mult"]), float(g["peak"]), g["c1g"], g["c2g"],
+                 precision=gpu.MIXED)
+    p.set_poses(g["index"], skip=skip)
+    p.run(gpu.FIT_GRID)
+    res = p.results(cross=True)
+    assert chan_err(res["cross"], g["raw"]) <= CROSS_TOL
+    check_grid(res, g["grid"])
+    p.close()
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p)[:-4])
+def test_mixed_lbfgsb_fit_matches_reference_fixture(gpu, path):
+    g = load(path)
+    L = int(g["L"])
+    p = gpu.Plan(g["A"], g["B"], g["q"], g["z"], L, g["a"], float(g["mult"]), float(g["peak"]), precision=gpu.MIXED)
+    p.set_poses(g["index"], skip=int(g["skip"]))
+    p.run(gpu.FIT_LBFGSB)
+    r = p.results()
+    np.testing.assert_allclose(r["chi"], g["chi"], rtol=CHI_TOL, atol=0)
+    p.close()
+
+
+@pytest.mark.parametrize("L,Q,skip", [(1, 4, 1), (4, 9, 0), (9, 12, 1), (15, 8, 0)])
+def test_mixed_matches_oracle_random(gpu, oracle, L, Q, skip):
+    from libfmftsaxs_gb300 import synth
+    c = _random_case(oracle, L, Q, 60, 40, 120, seed=L * 100 + Q + 7)
+    raw, scl, grid, br = oracle.score(c["A"], c["B"], c["q"], c["z"], L, c["index"], skip, c["peak"], c["a"],
+                                      c["mult"], synth.C1_GRID, synth.C2_GRID)
+    p = gpu.Plan(c["A"], c["B"], c["q"], c["z"], L, c["a"], c["mult"], c["peak"], synth.C1_GRID, synth.C2_GRID,
+                 precision=gpu.MIXED)
+    p.set_poses(c["index"], skip=skip)
+    p.run(gpu.FIT_GRID)
+    res = p.results(cross=True)
+    assert chan_err(res["cross"], raw) <= CROSS_TOL
+    check_grid(res, grid)
+
+
+def test_mixed_matches_fp64_at_lmax20(gpu):
+    from libfmftsaxs_gb300 import workload
+    w = workload.build("c1", seed=3, lib=gpu, overrides=dict(rec=(500, 12.0), lig=(300, 10.0), lists=(3000,),
+                                                             t=(18.0, 30.0)))
+    out = {}
+    for prec in (gpu.FP64, gpu.MIXED):
+        p = gpu.Plan(w.A, w.B, w.q, w.z, w.L, w.a, w.mult, w.peak, w.c1g, w.c2g, precision=prec)
+        p.set_poses(w.index, skip=1)
+        p.run(gpu.FIT_GRID)
+        out[prec] = p.results(cross=True, grid=True)
+        p.close()
+    ref, mix = out[gpu.FP64], out[gpu.MIXED]
+    assert chan_err(mix["cross"], ref["cross"]) <= CROSS_TOL
+    check_grid(mix, ref["grid"])
