@@ -87,10 +87,10 @@ __global__ void k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const doub
 		const double *drow = db + ((size_t)l * N + m + L) * N;
 		for (int m1 = -l; m1 <= l; m1++) {
 			int e = ((m1 < 0 ? m1 + N : m1) * g) % N;
-			double dv = drow[m1 + L];
+			S dv = (S)drow[m1 + L];
 			V f;
-			f.x = (S)(tw[e].x * dv);
-			f.y = (S)(tw[e].y * dv);
+			f.x = (S)tw[e].x * dv;
+			f.y = (S)tw[e].y * dv;
 			int lm = lm_index(l, m1);
 			V c0 = spf_t[((size_t)0 * K2 + lm) * Q + iq];
 			V c1 = spf_t[((size_t)1 * K2 + lm) * Q + iq];
@@ -216,89 +216,166 @@ __device__ __forceinline__ double warp_sum(double v)
 	return v;
 }
 
-/* One warp per pose: peak rescale (src/min_saxs.c:170-188), then for each c1
- * the scale-optimal chi^2 of point_score (391-448) as a function of c2.  With
- * I_i(c2) = al_i + be_i c2 + ga_i c2^2 (al = VV - G VD + G^2 DD,
- * be = VW - G DW, ga = WW) the piecewise-linear model's tan_i and buf_i are
- * quadratics in c2, so best_scale's up(c2) (quadratic) and down(c2)
- * (quartic) are accumulated once per c1 as coefficients; each cell is then
- * chi^2 = sum a0 + k (-2 up + k down), k = up/down.  hinv[i] = 1/(q_i -
- * q_{i-1}) with q_{-1} = -1. */
-#define FIT_WARPS 4
-__global__ void k_fit_grid(const double *__restrict__ cross, int npose, int Q, const double *__restrict__ q,
-                           const double *__restrict__ hinv, const double *__restrict__ a, double a0sum, double peak,
-                           const double *__restrict__ gtab, const double *__restrict__ c1g, int n1,
-                           const double *__restrict__ c2g, int n2, double *__restrict__ chi, double *__restrict__ c1o,
-                           double *__restrict__ c2o, int32_t *__restrict__ cello, double *__restrict__ grid,
-                           double *__restrict__ scaled)
+/* Grid fit (src/min_saxs.c:170-188 peak rescale, 261-320 best scale,
+ * 391-448 point_score).  For one pose and one (c1, c2) cell the model at q_i
+ * is in_i = al_i + c2 be_i + c2^2 ga_i with G_i = c1^3 exp(-mult (c1^2-1) q_i^2),
+ * al = VV - G VD + G^2 DD, be = VW - G DW, ga = WW; point_score's piecewise
+ * line is tan_i = (in_i - in_{i-1}) h_i (tan_0 = 0), buf_i = in_i - tan_i q_i,
+ * and with the best scale k = up/down the score is sum a0 + k(-2 up + k down),
+ *   up   = sum_i a1 buf + a2 tan = sum_i a1 in + u_i D_i
+ *   down = sum_i a3 buf^2 + 2 a4 buf tan + a5 tan^2
+ *        = sum_i a3 in^2 + 2 e_i in D_i + f_i D_i^2
+ * where D_i = in_i - in_{i-1} and the per-q constants are folded on the host:
+ *   fc[i] = {a3, e = (a4 - q a3) h, f = (a5 - 2 q a4 + q^2 a3) h^2, a1,
+ *            u = (a2 - q a1) h}.
+ * up is quadratic and down quartic in c2, so per (pose, c1) one pass over q
+ * yields their coefficients and every c2 cell costs a few multiply-adds.
+ * One thread per (pose, c1): no reductions and no repeated q work.  Within
+ * a thread cells are ranked by up^2/down (score = sum a0 - up^2/down); the
+ * threads of a pose then compare their best scores, ties going to the lower
+ * cell index as in a c1-major scan. */
+#define FIT_THREADS 128
+#define FIT_NFC 5
+__global__ void __launch_bounds__(FIT_THREADS)
+k_fit_grid(const double *__restrict__ cross, int npose, int Q, const double *__restrict__ fc, double a0sum,
+           double peak, const double *__restrict__ gtab, const double *__restrict__ c1g, int n1,
+           const double *__restrict__ c2g, int n2, int tp, int ppb, double *__restrict__ chi,
+           double *__restrict__ c1o, double *__restrict__ c2o, int32_t *__restrict__ cello,
+           double *__restrict__ grid, double *__restrict__ scaled)
 {
 	extern __shared__ double sm[];
-	int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	int pid = blockIdx.x * FIT_WARPS + w;
-	if (pid >= npose) return;
-	double *sc = sm + (size_t)w * 6 * Q;
-	const double *src = cross + (size_t)pid * 6 * Q;
-	for (int i = lane; i < 6 * Q; i += 32) sc[i] = src[i];
-	__syncwarp();
-	double s = sc[0] + sc[3 * Q] + sc[5 * Q] + sc[2 * Q] - sc[Q] - sc[4 * Q];
-	s = peak / s;
-	__syncwarp();
-	for (int i = lane; i < 6 * Q; i += 32) sc[i] *= s;
-	__syncwarp();
-	if (scaled)
-		for (int i = lane; i < 6 * Q; i += 32) scaled[(size_t)pid * 6 * Q + i] = sc[i];
-	const double *VV = sc, *VD = sc + Q, *VW = sc + 2 * Q, *DD = sc + 3 * Q, *DW = sc + 4 * Q, *WW = sc + 5 * Q;
-	double best = __longlong_as_double(0x7ff0000000000000LL);
+	double *cs = sm;                                   /* [ppb][8][Q]: VV VD VW DD DW WW P3 P4 */
+	double *fs = cs + (size_t)ppb * 8 * Q;             /* [FIT_NFC][Q] */
+	double *c2s = fs + (size_t)FIT_NFC * Q;            /* [n2] */
+	double *red = c2s + n2;                            /* [ppb*tp][2] partials / best score */
+	int *redc = (int *)(red + 2 * ppb * tp);           /* [ppb*tp] best cell */
+	double *sf = (double *)(redc + ((ppb * tp + 1) & ~1)); /* [ppb][3]: scale, U2, D4 */
+	int tid = threadIdx.x;
+	int nthr = ppb * tp;
+	int lp = tid / tp, lt = tid % tp;
+	int pid = blockIdx.x * ppb + lp;
+	int pose0 = blockIdx.x * ppb;
+	int nhere = min(ppb, npose - pose0);
+	bool live = tid < nthr && lp < nhere;
+
+	for (int k = tid; k < FIT_NFC * Q; k += blockDim.x) fs[k] = fc[(k % Q) * FIT_NFC + k / Q];
+	for (int k = tid; k < n2; k += blockDim.x) c2s[k] = c2g[k];
+	for (int k = tid; k < nhere * 6 * Q; k += blockDim.x) {
+		int p = k / (6 * Q), r = k % (6 * Q);
+		cs[(size_t)p * 8 * Q + r] = cross[(size_t)(pose0 + p) * 6 * Q + r];
+	}
+	__syncthreads();
+	if (live && lt == 0) {
+		const double *c = cs + (size_t)lp * 8 * Q;
+		double s = c[0] + c[3 * Q] + c[5 * Q] + c[2 * Q] - c[Q] - c[4 * Q];
+		sf[3 * lp] = peak / s;
+	}
+	__syncthreads();
+	for (int k = tid; k < nhere * 6 * Q; k += blockDim.x) {
+		int p = k / (6 * Q), r = k % (6 * Q);
+		double v = cs[(size_t)p * 8 * Q + r] * sf[3 * p];
+		cs[(size_t)p * 8 * Q + r] = v;
+		if (scaled) scaled[(size_t)(pose0 + p) * 6 * Q + r] = v;
+	}
+	__syncthreads();
+	const double *F3 = fs, *FE = fs + Q, *FF = fs + 2 * Q, *F1 = fs + 3 * Q, *FU = fs + 4 * Q;
+	double *c = cs + (size_t)lp * 8 * Q;
+	const double *VV = c, *VD = c + Q, *VW = c + 2 * Q, *DD = c + 3 * Q, *DW = c + 4 * Q, *WW = c + 5 * Q;
+	double *P3 = c + 6 * Q, *P4 = c + 7 * Q;
+	/* c1-independent part: M (ga, D_ga) per q, and the c2^2 coefficients */
+	if (live) {
+		double u2 = 0, d4 = 0;
+		for (int i = lt; i < Q; i += tp) {
+			double ga = WW[i], dg = i > 0 ? ga - WW[i - 1] : 0.0;
+			double p3 = fma(F3[i], ga, FE[i] * dg);
+			double p4 = fma(FE[i], ga, FF[i] * dg);
+			P3[i] = p3;
+			P4[i] = p4;
+			u2 = fma(F1[i], ga, fma(FU[i], dg, u2));
+			d4 = fma(ga, p3, fma(dg, p4, d4));
+		}
+		red[2 * tid] = u2;
+		red[2 * tid + 1] = d4;
+	}
+	__syncthreads();
+	if (live && lt == 0) {
+		double u2 = 0, d4 = 0;
+		for (int t = 0; t < tp; t++) {
+			u2 += red[2 * (tid + t)];
+			d4 += red[2 * (tid + t) + 1];
+		}
+		sf[3 * lp + 1] = u2;
+		sf[3 * lp + 2] = d4;
+	}
+	__syncthreads();
+	double bscore = __longlong_as_double(0x7ff0000000000000LL);
 	int bcell = -1;
-	for (int i1 = 0; i1 < n1; i1++) {
-		const double *G = gtab + (size_t)i1 * Q;
-		double U0 = 0, U1 = 0, U2 = 0, D0 = 0, D1 = 0, D2 = 0, D3 = 0, D4 = 0;
-		for (int i = lane; i < Q; i += 32) {
-			int ip = i > 0 ? i - 1 : 0;
-			double gi = G[i], gp = G[ip];
-			double al = VV[i] - gi * VD[i] + gi * gi * DD[i];
-			double be = VW[i] - gi * DW[i];
-			double ga = WW[i];
-			double alp = VV[ip] - gp * VD[ip] + gp * gp * DD[ip];
-			double bep = VW[ip] - gp * DW[ip];
-			double gap = WW[ip];
-			double qc = q[i], hi = hinv[i];
-			double t0 = (al - alp) * hi, t1 = (be - bep) * hi, t2 = (ga - gap) * hi;
-			double b0 = al - t0 * qc, b1 = be - t1 * qc, b2 = ga - t2 * qc;
-			double a1 = a[6 * i + 1], a2 = a[6 * i + 2], a3 = a[6 * i + 3], a4 = a[6 * i + 4], a5 = a[6 * i + 5];
-			U0 += b0 * a1 + t0 * a2;
-			U1 += b1 * a1 + t1 * a2;
-			U2 += b2 * a1 + t2 * a2;
-			double a4x2 = 2.0 * a4;
-			D0 += b0 * (b0 * a3 + t0 * a4x2) + t0 * t0 * a5;
-			D1 += 2.0 * (b0 * (b1 * a3 + t1 * a4) + t0 * (b1 * a4 + t1 * a5));
-			D2 += b1 * (b1 * a3 + t1 * a4x2) + t1 * t1 * a5 + 2.0 * (b0 * (b2 * a3 + t2 * a4) + t0 * (b2 * a4 + t2 * a5));
-			D3 += 2.0 * (b1 * (b2 * a3 + t2 * a4) + t1 * (b2 * a4 + t2 * a5));
-			D4 += b2 * (b2 * a3 + t2 * a4x2) + t2 * t2 * a5;
+	if (live) {
+		double U2 = sf[3 * lp + 1], D4 = sf[3 * lp + 2];
+		for (int j = lt; j < n1; j += tp) {
+			const double *G = gtab + (size_t)j * Q;
+			double U0 = 0, U1 = 0, D0 = 0, D1 = 0, D2a = 0, D2b = 0, D3 = 0;
+			double g = __ldg(G);
+			double alp = fma(g, fma(g, DD[0], -VD[0]), VV[0]);
+			double bep = fma(-g, DW[0], VW[0]);
+			for (int i = 0; i < Q; i++) {
+				g = __ldg(G + i);
+				double al = fma(g, fma(g, DD[i], -VD[i]), VV[i]);
+				double be = fma(-g, DW[i], VW[i]);
+				double d0 = al - alp, d1 = be - bep;
+				double f3 = F3[i], fe = FE[i], ff = FF[i];
+				double m0a = fma(f3, al, fe * d0), m0b = fma(fe, al, ff * d0);
+				double m1a = fma(f3, be, fe * d1), m1b = fma(fe, be, ff * d1);
+				double p3 = P3[i], p4 = P4[i];
+				D0 = fma(al, m0a, fma(d0, m0b, D0));
+				D1 = fma(be, m0a, fma(d1, m0b, D1));
+				D2a = fma(be, m1a, fma(d1, m1b, D2a));
+				D2b = fma(al, p3, fma(d0, p4, D2b));
+				D3 = fma(be, p3, fma(d1, p4, D3));
+				double f1 = F1[i], fu = FU[i];
+				U0 = fma(f1, al, fma(fu, d0, U0));
+				U1 = fma(f1, be, fma(fu, d1, U1));
+				alp = al;
+				bep = be;
+			}
+			D1 *= 2.0;
+			double D2 = fma(2.0, D2b, D2a);
+			D3 *= 2.0;
+			/* best c2 of this c1 by up^2/down, then its score */
+			double bu = 0, bd = 0;
+			int bi = -1;
+			for (int i2 = 0; i2 < n2; i2++) {
+				double c2 = c2s[i2];
+				double up = fma(c2, fma(c2, U2, U1), U0);
+				double down = fma(c2, fma(c2, fma(c2, fma(c2, D4, D3), D2), D1), D0);
+				if (grid) {
+					double k = up / down;
+					grid[((size_t)pid * n1 + j) * n2 + i2] = a0sum + k * (-2.0 * up + k * down);
+				}
+				if (down > 0.0) {
+					double num = up * up;
+					if (bi < 0 || num * bd > bu * bu * down) { bu = up; bd = down; bi = i2; }
+				}
+			}
+			if (bi >= 0) {
+				double k = bu / bd;
+				double score = a0sum + k * (-2.0 * bu + k * bd);
+				int cell = j * n2 + bi;
+				if (score < bscore || (score == bscore && cell < bcell)) { bscore = score; bcell = cell; }
+			}
 		}
-		U0 = warp_sum(U0); U1 = warp_sum(U1); U2 = warp_sum(U2);
-		D0 = warp_sum(D0); D1 = warp_sum(D1); D2 = warp_sum(D2); D3 = warp_sum(D3); D4 = warp_sum(D4);
-		for (int i2 = lane; i2 < n2; i2 += 32) {
-			double c2 = c2g[i2];
-			double up = U0 + c2 * (U1 + c2 * U2);
-			double down = D0 + c2 * (D1 + c2 * (D2 + c2 * (D3 + c2 * D4)));
-			double k = up / down;
-			double score = a0sum + k * (-2.0 * up + k * down);
-			if (grid) grid[((size_t)pid * n1 + i1) * n2 + i2] = score;
-			int cell = i1 * n2 + i2;
-			if (score < best || (score == best && cell < bcell)) { best = score; bcell = cell; }
+		red[2 * tid] = bscore;
+		redc[tid] = bcell;
+	}
+	__syncthreads();
+	if (live && lt == 0) {
+		for (int t = 1; t < tp; t++) {
+			double os = red[2 * (tid + t)];
+			int oc = redc[tid + t];
+			if (oc >= 0 && (bcell < 0 || os < bscore || (os == bscore && oc < bcell))) { bscore = os; bcell = oc; }
 		}
-	}
-#pragma unroll
-	for (int o = 16; o > 0; o >>= 1) {
-		double ob = __shfl_xor_sync(0xffffffffu, best, o);
-		int oc = __shfl_xor_sync(0xffffffffu, bcell, o);
-		bool take = (oc >= 0) && (bcell < 0 || ob < best || (ob == best && oc < bcell));
-		if (take) { best = ob; bcell = oc; }
-	}
-	if (lane == 0) {
 		if (bcell >= 0) {
-			chi[pid] = sqrt(best);
+			chi[pid] = sqrt(bscore);
 			c1o[pid] = c1g[bcell / n2];
 			c2o[pid] = c2g[bcell % n2];
 		} else {
@@ -369,15 +446,30 @@ int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, const voi
 	return cudaGetLastError();
 }
 
-int sxsk_fit_grid(const double *cross, int npose, int Q, const double *q, const double *hinv, const double *a,
-                  double a0sum, double peak, const double *gtab, const double *c1g, int n1, const double *c2g, int n2,
-                  double *chi, double *c1, double *c2, int32_t *cell, double *grid, double *scaled, cudaStream_t s)
+int sxsk_fit_grid(const double *cross, int npose, int Q, const double *fc, double a0sum, double peak,
+                  const double *gtab, const double *c1g, int n1, const double *c2g, int n2, double *chi, double *c1,
+                  double *c2, int32_t *cell, double *grid, double *scaled, cudaStream_t s)
 {
 	if (npose <= 0) return 0;
-	size_t smem = (size_t)FIT_WARPS * 6 * Q * sizeof(double);
-	if (smem > 48 * 1024) cudaFuncSetAttribute(k_fit_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-	k_fit_grid<<<nblk(npose, FIT_WARPS), FIT_WARPS * 32, smem, s>>>(cross, npose, Q, q, hinv, a, a0sum, peak, gtab,
-	                                                               c1g, n1, c2g, n2, chi, c1, c2, cell, grid, scaled);
+	if (n1 <= 0 || n2 <= 0) return cudaErrorInvalidValue;
+	int tp = n1 < FIT_THREADS ? n1 : FIT_THREADS;
+	int ppb = FIT_THREADS / tp;
+	size_t nthr = (size_t)ppb * tp;
+	size_t smem = sizeof(double) * ((size_t)ppb * 8 * Q + (size_t)FIT_NFC * Q + n2 + 2 * nthr + 3 * ppb) +
+	              sizeof(int) * ((nthr + 1) & ~(size_t)1);
+	if (smem > 227 * 1024) {
+		ppb = 1;
+		nthr = tp;
+		smem = sizeof(double) * ((size_t)8 * Q + (size_t)FIT_NFC * Q + n2 + 2 * nthr + 3) +
+		       sizeof(int) * ((nthr + 1) & ~(size_t)1);
+		if (smem > 227 * 1024) return cudaErrorInvalidValue;
+	}
+	if (smem > 48 * 1024) {
+		cudaError_t e = cudaFuncSetAttribute(k_fit_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		if (e != cudaSuccess) return e;
+	}
+	k_fit_grid<<<nblk(npose, ppb), FIT_THREADS, smem, s>>>(cross, npose, Q, fc, a0sum, peak, gtab, c1g, n1, c2g, n2,
+	                                                        tp, ppb, chi, c1, c2, cell, grid, scaled);
 	return cudaGetLastError();
 }
 

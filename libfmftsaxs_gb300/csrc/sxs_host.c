@@ -142,6 +142,24 @@ int sxsg_expand(const double *xyz, const double *vac, const double *dum, const d
 	return 0;
 }
 
+/* Per-q constants of the grid fit, fc[i][5] = {a3, (a4 - q a3) h,
+ * (a5 - 2 q a4 + q^2 a3) h^2, a1, (a2 - q a1) h} with h = 1 / (q_i - q_{i-1})
+ * and q_{-1} = -1: point_score's buf = in - tan q and tan = D h
+ * (src/min_saxs.c:391-448) substituted into its sums so that the device
+ * works with in and D = in_i - in_{i-1} directly. */
+void sxs_fit_constants(const double *q, const double *a, int Q, double *fc)
+{
+	for (int i = 0; i < Q; i++) {
+		double qi = q[i], h = 1.0 / (qi - (i > 0 ? q[i - 1] : -1.0));
+		const double *ai = a + 6 * i;
+		fc[5 * i] = ai[3];
+		fc[5 * i + 1] = (ai[4] - qi * ai[3]) * h;
+		fc[5 * i + 2] = ((ai[5] - 2.0 * qi * ai[4]) + qi * qi * ai[3]) * (h * h);
+		fc[5 * i + 3] = ai[1];
+		fc[5 * i + 4] = (ai[2] - qi * ai[1]) * h;
+	}
+}
+
 /* --------------------------------------------------------------- plan */
 struct sxsg_plan {
 	int L, K, N, K2, Q, nz, n1, n2, precision;
@@ -149,7 +167,7 @@ struct sxsg_plan {
 	cudaStream_t s;
 	double mult, peak, a0sum;
 	/* resident inputs */
-	double *d_A, *d_B, *d_q, *d_hinv, *d_a, *d_gtab, *d_c1g, *d_c2g, *d_cst;
+	double *d_A, *d_B, *d_q, *d_fc, *d_a, *d_gtab, *d_c1g, *d_c2g, *d_cst;
 	double2 *d_tw;
 	void *d_At, *d_Bt;          /* transposed coefficients, table precision */
 	double *h_z;
@@ -202,7 +220,7 @@ void sxsg_plan_destroy(sxsg_plan *p)
 	if (!p) return;
 	cudaStreamSynchronize(p->s);
 	plan_free_poses(p);
-	cudaFree(p->d_A); cudaFree(p->d_B); cudaFree(p->d_q); cudaFree(p->d_hinv); cudaFree(p->d_a); cudaFree(p->d_gtab);
+	cudaFree(p->d_A); cudaFree(p->d_B); cudaFree(p->d_q); cudaFree(p->d_fc); cudaFree(p->d_a); cudaFree(p->d_gtab);
 	cudaFree(p->d_c1g); cudaFree(p->d_c2g); cudaFree(p->d_cst); cudaFree(p->d_At); cudaFree(p->d_Bt);
 	cudaFree(p->d_tw); cudaFree(p->d_P); cudaFree(p->d_U); cudaFree(p->d_R);
 	cudaFree(p->d_cross); cudaFree(p->d_chi); cudaFree(p->d_c1); cudaFree(p->d_c2); cudaFree(p->d_grid);
@@ -245,7 +263,7 @@ int sxsg_plan_create(sxsg_plan **out, const double *A, const double *B, const do
 	if (!e) e = cudaMalloc(&p->d_At, p->celem * spf_n / 2);
 	if (!e) e = cudaMalloc(&p->d_Bt, p->celem * spf_n / 2);
 	if (!e) e = cudaMalloc((void **)&p->d_q, sizeof(double) * Q);
-	if (!e) e = cudaMalloc((void **)&p->d_hinv, sizeof(double) * Q);
+	if (!e) e = cudaMalloc((void **)&p->d_fc, sizeof(double) * 5 * Q);
 	if (!e) e = cudaMalloc((void **)&p->d_a, sizeof(double) * 6 * Q);
 	if (!e) e = cudaMalloc((void **)&p->d_cst, sizeof(double) * 6 * Q);
 	if (!e) e = cudaMalloc((void **)&p->d_tw, sizeof(double2) * p->N);
@@ -264,12 +282,10 @@ int sxsg_plan_create(sxsg_plan **out, const double *A, const double *B, const do
 	if (!e) e = cudaMemcpyAsync(p->d_B, B, sizeof(double) * spf_n, cudaMemcpyHostToDevice, s);
 	if (!e) e = cudaMemcpyAsync(p->d_q, q, sizeof(double) * Q, cudaMemcpyHostToDevice, s);
 	if (!e) {
-		/* 1 / (q_i - q_{i-1}) with q_{-1} = -1: the spacing of the
-		 * piecewise-linear model (src/min_saxs.c:400-417) */
-		double *hi = malloc(sizeof(double) * Q);
-		for (int i = 0; i < Q; i++) hi[i] = 1.0 / (q[i] - (i > 0 ? q[i - 1] : -1.0));
-		e = cudaMemcpy(p->d_hinv, hi, sizeof(double) * Q, cudaMemcpyHostToDevice);
-		free(hi);
+		double *fc = malloc(sizeof(double) * 5 * Q);
+		sxs_fit_constants(q, a, Q, fc);
+		e = cudaMemcpy(p->d_fc, fc, sizeof(double) * 5 * Q, cudaMemcpyHostToDevice);
+		free(fc);
 	}
 	if (!e) e = cudaMemcpyAsync(p->d_a, a, sizeof(double) * 6 * Q, cudaMemcpyHostToDevice, s);
 	if (!e && n1 > 0) {
@@ -521,7 +537,7 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 	SXS_CU(cudaEventRecord(p->ev[5], s));
 	int n = (int)p->npose;
 	if (fit_mode == SXSG_FIT_GRID) {
-		SXS_K(sxsk_fit_grid(p->d_cross, n, Q, p->d_q, p->d_hinv, p->d_a, p->a0sum, p->peak, p->d_gtab, p->d_c1g, p->n1, p->d_c2g,
+		SXS_K(sxsk_fit_grid(p->d_cross, n, Q, p->d_fc, p->a0sum, p->peak, p->d_gtab, p->d_c1g, p->n1, p->d_c2g,
 		                    p->n2, p->d_chi, p->d_c1, p->d_c2, p->d_cell, NULL, p->d_scaled, s));
 		sxs_count_launches(n > 0 ? 1 : 0);
 	} else if (fit_mode == SXSG_FIT_LBFGSB) {
@@ -567,7 +583,7 @@ int sxsg_plan_results(sxsg_plan *p, double *chi, double *c1, double *c2, int32_t
 		if (!e) e = cudaMalloc((void **)&t2, sizeof(double) * n);
 		if (!e) e = cudaMalloc((void **)&tcell, sizeof(int32_t) * n);
 		if (!e) {
-			e = (cudaError_t)sxsk_fit_grid(p->d_cross, (int)n, p->Q, p->d_q, p->d_hinv, p->d_a, p->a0sum, p->peak, p->d_gtab,
+			e = (cudaError_t)sxsk_fit_grid(p->d_cross, (int)n, p->Q, p->d_fc, p->a0sum, p->peak, p->d_gtab,
 			                               p->d_c1g, p->n1, p->d_c2g, p->n2, tc, t1, t2, tcell, d_g, NULL, s);
 			sxs_count_launches(1);
 		}

@@ -63,6 +63,9 @@ typedef struct {
 } sxs_ltables;
 int sxs_ltables_get(int L, const sxs_ltables **out);
 
+/* per-q constants of the grid fit: fc[Q][5] */
+void sxs_fit_constants(const double *q, const double *a, int Q, double *fc);
+
 /* device L-BFGS-B over (c1, c2) for a batch of poses: cross [n][6][Q]
  * (rescaled here by peak when rescale != 0), ct a workspace of n*6*Q
  * doubles; two kernel launches */
