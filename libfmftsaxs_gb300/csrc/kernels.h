@@ -75,11 +75,15 @@ int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, const voi
                     const double2 *tw, const double *cst, int Q, int L, double *cross, int fp32, cudaStream_t s);
 
 /* grid fit: per pose, peak rescale then chi^2 at every (c1, c2) cell; best cell.
+ * Scores the poses at slots [slot0, slot0 + nslot) of order (order[i].src
+ * indexes cross and every output; the slot itself when order is NULL).
  * gtab[n1][Q] = c1^3 exp(-mult (c1^2-1) q^2); fc[Q][5] per-q constants of the
- * binned experiment (see sxs_fit_constants); a0sum = sum_i a[6i]. */
-int sxsk_fit_grid(const double *cross, int npose, int Q, const double *fc, double a0sum, double peak,
-                  const double *gtab, const double *c1g, int n1, const double *c2g, int n2, double *chi, double *c1,
-                  double *c2, int32_t *cell, double *grid, double *scaled, cudaStream_t s);
+ * binned experiment (sxs_fit_constants); a0sum = sum_i a[6i]; at most
+ * max_blocks resident blocks (persistent loop; <= 0: one block per group). */
+int sxsk_fit_grid(const double *cross, const sxsk_pose *order, int slot0, int nslot, int Q, const double *fc,
+                  double a0sum, double peak, const double *gtab, const double *c1g, int n1, const double *c2g, int n2,
+                  int max_blocks, double *chi, double *c1, double *c2, int32_t *cell, double *grid, double *scaled,
+                  cudaStream_t s);
 
 #ifdef __cplusplus
 }

@@ -236,11 +236,14 @@ __device__ __forceinline__ double warp_sum(double v)
  * cell index as in a c1-major scan. */
 #define FIT_THREADS 128
 #define FIT_NFC 5
+/* Persistent: block b handles pose groups b, b + gridDim.x, ...; a group is
+ * ppb consecutive slots of the pose order (order[slot].src is the pose's
+ * position in cross and in the outputs; slot itself when order is NULL). */
 __global__ void __launch_bounds__(FIT_THREADS)
-k_fit_grid(const double *__restrict__ cross, int npose, int Q, const double *__restrict__ fc, double a0sum,
-           double peak, const double *__restrict__ gtab, const double *__restrict__ c1g, int n1,
-           const double *__restrict__ c2g, int n2, int tp, int ppb, double *__restrict__ chi,
-           double *__restrict__ c1o, double *__restrict__ c2o, int32_t *__restrict__ cello,
+k_fit_grid(const double *__restrict__ cross, const sxsk_pose *__restrict__ order, int slot0, int nslot, int Q,
+           const double *__restrict__ fc, double a0sum, double peak, const double *__restrict__ gtab,
+           const double *__restrict__ c1g, int n1, const double *__restrict__ c2g, int n2, int tp, int ppb,
+           double *__restrict__ chi, double *__restrict__ c1o, double *__restrict__ c2o, int32_t *__restrict__ cello,
            double *__restrict__ grid, double *__restrict__ scaled)
 {
 	extern __shared__ double sm[];
@@ -250,140 +253,147 @@ k_fit_grid(const double *__restrict__ cross, int npose, int Q, const double *__r
 	double *red = c2s + n2;                            /* [ppb*tp][2] partials / best score */
 	int *redc = (int *)(red + 2 * ppb * tp);           /* [ppb*tp] best cell */
 	double *sf = (double *)(redc + ((ppb * tp + 1) & ~1)); /* [ppb][3]: scale, U2, D4 */
+	int *srcs = (int *)(sf + 3 * ppb);                 /* [ppb] pose index of each slot */
 	int tid = threadIdx.x;
 	int nthr = ppb * tp;
 	int lp = tid / tp, lt = tid % tp;
-	int pid = blockIdx.x * ppb + lp;
-	int pose0 = blockIdx.x * ppb;
-	int nhere = min(ppb, npose - pose0);
-	bool live = tid < nthr && lp < nhere;
+	const double *F3 = fs, *FE = fs + Q, *FF = fs + 2 * Q, *F1 = fs + 3 * Q, *FU = fs + 4 * Q;
 
 	for (int k = tid; k < FIT_NFC * Q; k += blockDim.x) fs[k] = fc[(k % Q) * FIT_NFC + k / Q];
 	for (int k = tid; k < n2; k += blockDim.x) c2s[k] = c2g[k];
-	for (int k = tid; k < nhere * 6 * Q; k += blockDim.x) {
-		int p = k / (6 * Q), r = k % (6 * Q);
-		cs[(size_t)p * 8 * Q + r] = cross[(size_t)(pose0 + p) * 6 * Q + r];
-	}
-	__syncthreads();
-	if (live && lt == 0) {
-		const double *c = cs + (size_t)lp * 8 * Q;
-		double s = c[0] + c[3 * Q] + c[5 * Q] + c[2 * Q] - c[Q] - c[4 * Q];
-		sf[3 * lp] = peak / s;
-	}
-	__syncthreads();
-	for (int k = tid; k < nhere * 6 * Q; k += blockDim.x) {
-		int p = k / (6 * Q), r = k % (6 * Q);
-		double v = cs[(size_t)p * 8 * Q + r] * sf[3 * p];
-		cs[(size_t)p * 8 * Q + r] = v;
-		if (scaled) scaled[(size_t)(pose0 + p) * 6 * Q + r] = v;
-	}
-	__syncthreads();
-	const double *F3 = fs, *FE = fs + Q, *FF = fs + 2 * Q, *F1 = fs + 3 * Q, *FU = fs + 4 * Q;
-	double *c = cs + (size_t)lp * 8 * Q;
-	const double *VV = c, *VD = c + Q, *VW = c + 2 * Q, *DD = c + 3 * Q, *DW = c + 4 * Q, *WW = c + 5 * Q;
-	double *P3 = c + 6 * Q, *P4 = c + 7 * Q;
-	/* c1-independent part: M (ga, D_ga) per q, and the c2^2 coefficients */
-	if (live) {
-		double u2 = 0, d4 = 0;
-		for (int i = lt; i < Q; i += tp) {
-			double ga = WW[i], dg = i > 0 ? ga - WW[i - 1] : 0.0;
-			double p3 = fma(F3[i], ga, FE[i] * dg);
-			double p4 = fma(FE[i], ga, FF[i] * dg);
-			P3[i] = p3;
-			P4[i] = p4;
-			u2 = fma(F1[i], ga, fma(FU[i], dg, u2));
-			d4 = fma(ga, p3, fma(dg, p4, d4));
+	int ngroup = (nslot + ppb - 1) / ppb;
+	for (int grp = blockIdx.x; grp < ngroup; grp += gridDim.x) {
+		int s0 = grp * ppb;
+		int nhere = min(ppb, nslot - s0);
+		bool live = tid < nthr && lp < nhere;
+		__syncthreads();   /* previous group done with the shared arrays */
+		if (tid < nhere) srcs[tid] = order ? order[slot0 + s0 + tid].src : slot0 + s0 + tid;
+		__syncthreads();
+		for (int k = tid; k < nhere * 6 * Q; k += blockDim.x) {
+			int p = k / (6 * Q), r = k % (6 * Q);
+			cs[(size_t)p * 8 * Q + r] = cross[(size_t)srcs[p] * 6 * Q + r];
 		}
-		red[2 * tid] = u2;
-		red[2 * tid + 1] = d4;
-	}
-	__syncthreads();
-	if (live && lt == 0) {
-		double u2 = 0, d4 = 0;
-		for (int t = 0; t < tp; t++) {
-			u2 += red[2 * (tid + t)];
-			d4 += red[2 * (tid + t) + 1];
+		__syncthreads();
+		if (live && lt == 0) {
+			const double *c = cs + (size_t)lp * 8 * Q;
+			double sc = c[0] + c[3 * Q] + c[5 * Q] + c[2 * Q] - c[Q] - c[4 * Q];
+			sf[3 * lp] = peak / sc;
 		}
-		sf[3 * lp + 1] = u2;
-		sf[3 * lp + 2] = d4;
-	}
-	__syncthreads();
-	double bscore = __longlong_as_double(0x7ff0000000000000LL);
-	int bcell = -1;
-	if (live) {
-		double U2 = sf[3 * lp + 1], D4 = sf[3 * lp + 2];
-		for (int j = lt; j < n1; j += tp) {
-			const double *G = gtab + (size_t)j * Q;
-			double U0 = 0, U1 = 0, D0 = 0, D1 = 0, D2a = 0, D2b = 0, D3 = 0;
-			double g = __ldg(G);
-			double alp = fma(g, fma(g, DD[0], -VD[0]), VV[0]);
-			double bep = fma(-g, DW[0], VW[0]);
-			for (int i = 0; i < Q; i++) {
-				g = __ldg(G + i);
-				double al = fma(g, fma(g, DD[i], -VD[i]), VV[i]);
-				double be = fma(-g, DW[i], VW[i]);
-				double d0 = al - alp, d1 = be - bep;
-				double f3 = F3[i], fe = FE[i], ff = FF[i];
-				double m0a = fma(f3, al, fe * d0), m0b = fma(fe, al, ff * d0);
-				double m1a = fma(f3, be, fe * d1), m1b = fma(fe, be, ff * d1);
-				double p3 = P3[i], p4 = P4[i];
-				D0 = fma(al, m0a, fma(d0, m0b, D0));
-				D1 = fma(be, m0a, fma(d1, m0b, D1));
-				D2a = fma(be, m1a, fma(d1, m1b, D2a));
-				D2b = fma(al, p3, fma(d0, p4, D2b));
-				D3 = fma(be, p3, fma(d1, p4, D3));
-				double f1 = F1[i], fu = FU[i];
-				U0 = fma(f1, al, fma(fu, d0, U0));
-				U1 = fma(f1, be, fma(fu, d1, U1));
-				alp = al;
-				bep = be;
+		__syncthreads();
+		for (int k = tid; k < nhere * 6 * Q; k += blockDim.x) {
+			int p = k / (6 * Q), r = k % (6 * Q);
+			double v = cs[(size_t)p * 8 * Q + r] * sf[3 * p];
+			cs[(size_t)p * 8 * Q + r] = v;
+			if (scaled) scaled[(size_t)srcs[p] * 6 * Q + r] = v;
+		}
+		__syncthreads();
+		double *c = cs + (size_t)lp * 8 * Q;
+		const double *VV = c, *VD = c + Q, *VW = c + 2 * Q, *DD = c + 3 * Q, *DW = c + 4 * Q, *WW = c + 5 * Q;
+		double *P3 = c + 6 * Q, *P4 = c + 7 * Q;
+		/* c1-independent part: M (ga, D_ga) per q, and the c2^2 coefficients */
+		if (live) {
+			double u2 = 0, d4 = 0;
+			for (int i = lt; i < Q; i += tp) {
+				double ga = WW[i], dg = i > 0 ? ga - WW[i - 1] : 0.0;
+				double p3 = fma(F3[i], ga, FE[i] * dg);
+				double p4 = fma(FE[i], ga, FF[i] * dg);
+				P3[i] = p3;
+				P4[i] = p4;
+				u2 = fma(F1[i], ga, fma(FU[i], dg, u2));
+				d4 = fma(ga, p3, fma(dg, p4, d4));
 			}
-			D1 *= 2.0;
-			double D2 = fma(2.0, D2b, D2a);
-			D3 *= 2.0;
-			/* best c2 of this c1 by up^2/down, then its score */
-			double bu = 0, bd = 0;
-			int bi = -1;
-			for (int i2 = 0; i2 < n2; i2++) {
-				double c2 = c2s[i2];
-				double up = fma(c2, fma(c2, U2, U1), U0);
-				double down = fma(c2, fma(c2, fma(c2, fma(c2, D4, D3), D2), D1), D0);
-				if (grid) {
-					double k = up / down;
-					grid[((size_t)pid * n1 + j) * n2 + i2] = a0sum + k * (-2.0 * up + k * down);
+			red[2 * tid] = u2;
+			red[2 * tid + 1] = d4;
+		}
+		__syncthreads();
+		if (live && lt == 0) {
+			double u2 = 0, d4 = 0;
+			for (int t = 0; t < tp; t++) {
+				u2 += red[2 * (tid + t)];
+				d4 += red[2 * (tid + t) + 1];
+			}
+			sf[3 * lp + 1] = u2;
+			sf[3 * lp + 2] = d4;
+		}
+		__syncthreads();
+		double bscore = __longlong_as_double(0x7ff0000000000000LL);
+		int bcell = -1;
+		int pid = live ? srcs[lp] : 0;
+		if (live) {
+			double U2 = sf[3 * lp + 1], D4 = sf[3 * lp + 2];
+			for (int j = lt; j < n1; j += tp) {
+				const double *G = gtab + (size_t)j * Q;
+				double U0 = 0, U1 = 0, D0 = 0, D1 = 0, D2a = 0, D2b = 0, D3 = 0;
+				double g = __ldg(G);
+				double alp = fma(g, fma(g, DD[0], -VD[0]), VV[0]);
+				double bep = fma(-g, DW[0], VW[0]);
+				for (int i = 0; i < Q; i++) {
+					g = __ldg(G + i);
+					double al = fma(g, fma(g, DD[i], -VD[i]), VV[i]);
+					double be = fma(-g, DW[i], VW[i]);
+					double d0 = al - alp, d1 = be - bep;
+					double f3 = F3[i], fe = FE[i], ff = FF[i];
+					double m0a = fma(f3, al, fe * d0), m0b = fma(fe, al, ff * d0);
+					double m1a = fma(f3, be, fe * d1), m1b = fma(fe, be, ff * d1);
+					double p3 = P3[i], p4 = P4[i];
+					D0 = fma(al, m0a, fma(d0, m0b, D0));
+					D1 = fma(be, m0a, fma(d1, m0b, D1));
+					D2a = fma(be, m1a, fma(d1, m1b, D2a));
+					D2b = fma(al, p3, fma(d0, p4, D2b));
+					D3 = fma(be, p3, fma(d1, p4, D3));
+					double f1 = F1[i], fu = FU[i];
+					U0 = fma(f1, al, fma(fu, d0, U0));
+					U1 = fma(f1, be, fma(fu, d1, U1));
+					alp = al;
+					bep = be;
 				}
-				if (down > 0.0) {
-					double num = up * up;
-					if (bi < 0 || num * bd > bu * bu * down) { bu = up; bd = down; bi = i2; }
+				D1 *= 2.0;
+				double D2 = fma(2.0, D2b, D2a);
+				D3 *= 2.0;
+				/* best c2 of this c1 by up^2/down, then its score */
+				double bu = 0, bd = 0;
+				int bi = -1;
+				for (int i2 = 0; i2 < n2; i2++) {
+					double c2 = c2s[i2];
+					double up = fma(c2, fma(c2, U2, U1), U0);
+					double down = fma(c2, fma(c2, fma(c2, fma(c2, D4, D3), D2), D1), D0);
+					if (grid) {
+						double k = up / down;
+						grid[((size_t)pid * n1 + j) * n2 + i2] = a0sum + k * (-2.0 * up + k * down);
+					}
+					if (down > 0.0) {
+						double num = up * up;
+						if (bi < 0 || num * bd > bu * bu * down) { bu = up; bd = down; bi = i2; }
+					}
+				}
+				if (bi >= 0) {
+					double k = bu / bd;
+					double score = a0sum + k * (-2.0 * bu + k * bd);
+					int cell = j * n2 + bi;
+					if (score < bscore || (score == bscore && cell < bcell)) { bscore = score; bcell = cell; }
 				}
 			}
-			if (bi >= 0) {
-				double k = bu / bd;
-				double score = a0sum + k * (-2.0 * bu + k * bd);
-				int cell = j * n2 + bi;
-				if (score < bscore || (score == bscore && cell < bcell)) { bscore = score; bcell = cell; }
+			red[2 * tid] = bscore;
+			redc[tid] = bcell;
+		}
+		__syncthreads();
+		if (live && lt == 0) {
+			for (int t = 1; t < tp; t++) {
+				double os = red[2 * (tid + t)];
+				int oc = redc[tid + t];
+				if (oc >= 0 && (bcell < 0 || os < bscore || (os == bscore && oc < bcell))) { bscore = os; bcell = oc; }
 			}
+			if (bcell >= 0) {
+				chi[pid] = sqrt(bscore);
+				c1o[pid] = c1g[bcell / n2];
+				c2o[pid] = c2g[bcell % n2];
+			} else {
+				chi[pid] = __longlong_as_double(0x7ff8000000000000LL);
+				c1o[pid] = __longlong_as_double(0x7ff8000000000000LL);
+				c2o[pid] = __longlong_as_double(0x7ff8000000000000LL);
+			}
+			if (cello) cello[pid] = bcell;
 		}
-		red[2 * tid] = bscore;
-		redc[tid] = bcell;
-	}
-	__syncthreads();
-	if (live && lt == 0) {
-		for (int t = 1; t < tp; t++) {
-			double os = red[2 * (tid + t)];
-			int oc = redc[tid + t];
-			if (oc >= 0 && (bcell < 0 || os < bscore || (os == bscore && oc < bcell))) { bscore = os; bcell = oc; }
-		}
-		if (bcell >= 0) {
-			chi[pid] = sqrt(bscore);
-			c1o[pid] = c1g[bcell / n2];
-			c2o[pid] = c2g[bcell % n2];
-		} else {
-			chi[pid] = __longlong_as_double(0x7ff8000000000000LL);
-			c1o[pid] = __longlong_as_double(0x7ff8000000000000LL);
-			c2o[pid] = __longlong_as_double(0x7ff8000000000000LL);
-		}
-		if (cello) cello[pid] = bcell;
 	}
 }
 
@@ -446,30 +456,32 @@ int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, const voi
 	return cudaGetLastError();
 }
 
-int sxsk_fit_grid(const double *cross, int npose, int Q, const double *fc, double a0sum, double peak,
-                  const double *gtab, const double *c1g, int n1, const double *c2g, int n2, double *chi, double *c1,
-                  double *c2, int32_t *cell, double *grid, double *scaled, cudaStream_t s)
+int sxsk_fit_grid(const double *cross, const sxsk_pose *order, int slot0, int nslot, int Q, const double *fc,
+                  double a0sum, double peak, const double *gtab, const double *c1g, int n1, const double *c2g, int n2,
+                  int max_blocks, double *chi, double *c1, double *c2, int32_t *cell, double *grid, double *scaled,
+                  cudaStream_t s)
 {
-	if (npose <= 0) return 0;
+	if (nslot <= 0) return 0;
 	if (n1 <= 0 || n2 <= 0) return cudaErrorInvalidValue;
 	int tp = n1 < FIT_THREADS ? n1 : FIT_THREADS;
 	int ppb = FIT_THREADS / tp;
-	size_t nthr = (size_t)ppb * tp;
-	size_t smem = sizeof(double) * ((size_t)ppb * 8 * Q + (size_t)FIT_NFC * Q + n2 + 2 * nthr + 3 * ppb) +
-	              sizeof(int) * ((nthr + 1) & ~(size_t)1);
-	if (smem > 227 * 1024) {
-		ppb = 1;
-		nthr = tp;
-		smem = sizeof(double) * ((size_t)8 * Q + (size_t)FIT_NFC * Q + n2 + 2 * nthr + 3) +
-		       sizeof(int) * ((nthr + 1) & ~(size_t)1);
-		if (smem > 227 * 1024) return cudaErrorInvalidValue;
+	size_t smem;
+	for (;;) {
+		size_t nthr = (size_t)ppb * tp;
+		smem = sizeof(double) * ((size_t)ppb * 8 * Q + (size_t)FIT_NFC * Q + n2 + 2 * nthr + 3 * ppb) +
+		       sizeof(int) * (((nthr + 1) & ~(size_t)1) + ppb);
+		if (smem <= 227 * 1024 || ppb == 1) break;
+		ppb = (ppb + 1) / 2;
 	}
+	if (smem > 227 * 1024) return cudaErrorInvalidValue;
 	if (smem > 48 * 1024) {
 		cudaError_t e = cudaFuncSetAttribute(k_fit_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 		if (e != cudaSuccess) return e;
 	}
-	k_fit_grid<<<nblk(npose, ppb), FIT_THREADS, smem, s>>>(cross, npose, Q, fc, a0sum, peak, gtab, c1g, n1, c2g, n2,
-	                                                        tp, ppb, chi, c1, c2, cell, grid, scaled);
+	long ngroup = (nslot + ppb - 1) / ppb;
+	int grid_n = (int)(ngroup < (long)max_blocks || max_blocks <= 0 ? ngroup : max_blocks);
+	k_fit_grid<<<grid_n, FIT_THREADS, smem, s>>>(cross, order, slot0, nslot, Q, fc, a0sum, peak, gtab, c1g, n1, c2g,
+	                                              n2, tp, ppb, chi, c1, c2, cell, grid, scaled);
 	return cudaGetLastError();
 }
 

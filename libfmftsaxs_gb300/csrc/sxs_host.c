@@ -165,6 +165,10 @@ struct sxsg_plan {
 	int L, K, N, K2, Q, nz, n1, n2, precision;
 	const sxs_ltables *lt;
 	cudaStream_t s;
+	cudaStream_t sf;            /* fit stream, high priority: overlaps the contractions */
+	int nsm;
+	cudaEvent_t *cev;           /* per-chunk events, 5 per chunk */
+	int ncev;
 	double mult, peak, a0sum;
 	/* resident inputs */
 	double *d_A, *d_B, *d_q, *d_fc, *d_a, *d_gtab, *d_c1g, *d_c2g, *d_cst;
@@ -226,6 +230,9 @@ void sxsg_plan_destroy(sxsg_plan *p)
 	cudaFree(p->d_cross); cudaFree(p->d_chi); cudaFree(p->d_c1); cudaFree(p->d_c2); cudaFree(p->d_grid);
 	cudaFree(p->d_scaled); cudaFree(p->d_scale); cudaFree(p->d_cell); cudaFree(p->d_iters);
 	for (int i = 0; i < 6; i++) if (p->ev[i]) cudaEventDestroy(p->ev[i]);
+	for (int i = 0; i < p->ncev; i++) cudaEventDestroy(p->cev[i]);
+	free(p->cev);
+	if (p->sf) cudaStreamDestroy(p->sf);
 	free(p->h_z);
 	free(p);
 }
@@ -258,6 +265,16 @@ int sxsg_plan_create(sxsg_plan **out, const double *A, const double *B, const do
 	size_t spf_n = (size_t)3 * Q * p->K2 * 2;
 	cudaError_t e = cudaSuccess;
 	for (int i = 0; i < 6 && !e; i++) e = cudaEventCreate(&p->ev[i]);
+	if (!e) {
+		int lo = 0, hi = 0;
+		e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
+		if (!e) e = cudaStreamCreateWithPriority(&p->sf, cudaStreamNonBlocking, hi);
+	}
+	if (!e) {
+		int dev = 0;
+		e = cudaGetDevice(&dev);
+		if (!e) e = cudaDeviceGetAttribute(&p->nsm, cudaDevAttrMultiProcessorCount, dev);
+	}
 	if (!e) e = cudaMalloc((void **)&p->d_A, sizeof(double) * spf_n);
 	if (!e) e = cudaMalloc((void **)&p->d_B, sizeof(double) * spf_n);
 	if (!e) e = cudaMalloc(&p->d_At, p->celem * spf_n / 2);
@@ -486,6 +503,25 @@ static int plan_tables(sxsg_plan *p)
 	return 0;
 }
 
+/* Chunks the grid-fit run is split into at least, so that the fit of one
+ * chunk (FP64 pipe) overlaps the contractions of the next (HBM / FP32). */
+#define SXS_PIPE_CHUNKS 8
+/* resident fit blocks per SM while it overlaps the contractions */
+#define SXS_FIT_BLOCKS_PER_SM 2
+
+static int plan_events(sxsg_plan *p, int need)
+{
+	if (need <= p->ncev) return 0;
+	cudaEvent_t *ev = realloc(p->cev, sizeof(cudaEvent_t) * need);
+	if (!ev) return sxs_fail(-5, "out of host memory");
+	p->cev = ev;
+	while (p->ncev < need) {
+		SXS_CU(cudaEventCreate(&p->cev[p->ncev]));
+		p->ncev++;
+	}
+	return 0;
+}
+
 int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 {
 	if (!p) return sxs_fail(-2, "sxsg_plan_run: null plan");
@@ -502,43 +538,53 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 	size_t per_combo = (size_t)p->NP * 3 * Q * p->celem;
 	int64_t chunk = (int64_t)(p->r_budget / per_combo);
 	if (chunk < 1) chunk = 1;
+	int pipe = fit_mode == SXSG_FIT_GRID && p->ncombo > 0;
+	if (pipe) {
+		int64_t c = (p->ncombo + SXS_PIPE_CHUNKS - 1) / SXS_PIPE_CHUNKS;
+		if (c < chunk) chunk = c;
+	}
 	if (chunk > p->ncombo) chunk = p->ncombo;
+	int64_t nch = chunk > 0 ? (p->ncombo + chunk - 1) / chunk : 0;
+	if (nch > INT32_MAX / 5) return sxs_fail(-2, "sxsg_plan_run: too many chunks");
+	if ((rc = plan_events(p, (int)(5 * nch + 1)))) return rc;
 	if (chunk > 0 && p->R_combos < chunk) {
 		cudaFree(p->d_R);
 		p->d_R = NULL;
 		SXS_CU(cudaMalloc(&p->d_R, per_combo * chunk));
 		p->R_combos = chunk;
 	}
-	float t_tr = 0, t_pc = 0;
-	for (int64_t c0 = 0; c0 < p->ncombo; c0 += chunk) {
-		int64_t c1 = c0 + chunk < p->ncombo ? c0 + chunk : p->ncombo;
-		SXS_CU(cudaEventRecord(p->ev[2], s));
-		const void *tau = p->fp32 ? (const void *)p->d_tauf : (const void *)p->d_tau;
+	const void *tau = p->fp32 ? (const void *)p->d_tauf : (const void *)p->d_tau;
+	for (int64_t k = 0; k < nch; k++) {
+		int64_t c0 = k * chunk, c1 = c0 + chunk < p->ncombo ? c0 + chunk : p->ncombo;
+		cudaEvent_t *e = p->cev + 5 * k;
+		SXS_CU(cudaEventRecord(e[0], s));
 		SXS_K(sxsk_translate(p->d_U, tau, p->d_combo + 3 * c0, (int)(c1 - c0), Q, L, p->d_R, p->fp32, s));
-		SXS_CU(cudaEventRecord(p->ev[3], s));
+		SXS_CU(cudaEventRecord(e[1], s));
 		int64_t p0 = p->h_cstart[c0], p1 = p->h_cstart[c1];
 		SXS_K(sxsk_pose_cross(p->d_poses + p0, (int)(p1 - p0), (int)c0, p->d_P, p->d_R, p->d_tw, p->d_cst, Q, L,
 		                      p->d_cross, p->fp32, s));
-		SXS_CU(cudaEventRecord(p->ev[4], s));
+		SXS_CU(cudaEventRecord(e[2], s));
 		sxs_count_launches(2);
-		if (p->ncombo > chunk) {
-			float a = 0, b = 0;
-			SXS_CU(cudaEventSynchronize(p->ev[4]));
-			cudaEventElapsedTime(&a, p->ev[2], p->ev[3]);
-			cudaEventElapsedTime(&b, p->ev[3], p->ev[4]);
-			t_tr += a; t_pc += b;
+		if (pipe) {
+			SXS_CU(cudaStreamWaitEvent(p->sf, e[2], 0));
+			SXS_CU(cudaEventRecord(e[3], p->sf));
+			SXS_K(sxsk_fit_grid(p->d_cross, p->d_poses, (int)p0, (int)(p1 - p0), Q, p->d_fc, p->a0sum, p->peak,
+			                    p->d_gtab, p->d_c1g, p->n1, p->d_c2g, p->n2, SXS_FIT_BLOCKS_PER_SM * p->nsm,
+			                    p->d_chi, p->d_c1, p->d_c2, p->d_cell, NULL, p->d_scaled, p->sf));
+			SXS_CU(cudaEventRecord(e[4], p->sf));
+			sxs_count_launches(p1 > p0 ? 1 : 0);
 		}
 	}
-	if (p->ncombo <= chunk && p->ncombo > 0) {
-		SXS_CU(cudaEventSynchronize(p->ev[4]));
-		cudaEventElapsedTime(&t_tr, p->ev[2], p->ev[3]);
-		cudaEventElapsedTime(&t_pc, p->ev[3], p->ev[4]);
+	if (pipe) {
+		cudaEvent_t j = p->cev[5 * nch];
+		SXS_CU(cudaEventRecord(j, p->sf));
+		SXS_CU(cudaStreamWaitEvent(s, j, 0));
 	}
 	SXS_CU(cudaEventRecord(p->ev[5], s));
 	int n = (int)p->npose;
-	if (fit_mode == SXSG_FIT_GRID) {
-		SXS_K(sxsk_fit_grid(p->d_cross, n, Q, p->d_fc, p->a0sum, p->peak, p->d_gtab, p->d_c1g, p->n1, p->d_c2g,
-		                    p->n2, p->d_chi, p->d_c1, p->d_c2, p->d_cell, NULL, p->d_scaled, s));
+	if (fit_mode == SXSG_FIT_GRID && !pipe) {
+		SXS_K(sxsk_fit_grid(p->d_cross, NULL, 0, n, Q, p->d_fc, p->a0sum, p->peak, p->d_gtab, p->d_c1g, p->n1,
+		                    p->d_c2g, p->n2, 0, p->d_chi, p->d_c1, p->d_c2, p->d_cell, NULL, p->d_scaled, s));
 		sxs_count_launches(n > 0 ? 1 : 0);
 	} else if (fit_mode == SXSG_FIT_LBFGSB) {
 		SXS_K(sxs_fit_lbfgsb_launch(p->d_cross, p->d_scaled, n, Q, p->d_q, p->d_a, p->mult, p->peak, 1, p->d_chi,
@@ -552,11 +598,25 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 	SXS_CU(cudaEventCreate(&end));
 	SXS_CU(cudaEventRecord(end, s));
 	SXS_CU(cudaEventSynchronize(end));
-	float t_tab = 0, t_fit = 0;
+	float t_tab = 0, t_fit = 0, t_all = 0;
+	double t_tr = 0, t_pc = 0;
 	cudaEventElapsedTime(&t_tab, p->ev[0], p->ev[1]);
-	cudaEventElapsedTime(&t_fit, p->ev[5], end);
+	cudaEventElapsedTime(&t_all, p->ev[0], end);
+	for (int64_t k = 0; k < nch; k++) {
+		cudaEvent_t *e = p->cev + 5 * k;
+		float a = 0, b = 0, c = 0;
+		cudaEventElapsedTime(&a, e[0], e[1]);
+		cudaEventElapsedTime(&b, e[1], e[2]);
+		t_tr += a;
+		t_pc += b;
+		if (pipe) {
+			cudaEventElapsedTime(&c, e[3], e[4]);
+			t_fit += c;
+		}
+	}
+	if (!pipe) cudaEventElapsedTime(&t_fit, p->ev[5], end);
 	cudaEventDestroy(end);
-	p->ms[0] = t_tab; p->ms[1] = t_tr; p->ms[2] = t_pc; p->ms[3] = t_fit;
+	p->ms[0] = t_tab; p->ms[1] = t_tr; p->ms[2] = t_pc; p->ms[3] = t_fit; p->ms[4] = t_all;
 	return 0;
 }
 
@@ -583,8 +643,9 @@ int sxsg_plan_results(sxsg_plan *p, double *chi, double *c1, double *c2, int32_t
 		if (!e) e = cudaMalloc((void **)&t2, sizeof(double) * n);
 		if (!e) e = cudaMalloc((void **)&tcell, sizeof(int32_t) * n);
 		if (!e) {
-			e = (cudaError_t)sxsk_fit_grid(p->d_cross, (int)n, p->Q, p->d_fc, p->a0sum, p->peak, p->d_gtab,
-			                               p->d_c1g, p->n1, p->d_c2g, p->n2, tc, t1, t2, tcell, d_g, NULL, s);
+			e = (cudaError_t)sxsk_fit_grid(p->d_cross, NULL, 0, (int)n, p->Q, p->d_fc, p->a0sum, p->peak,
+			                               p->d_gtab, p->d_c1g, p->n1, p->d_c2g, p->n2, 0, tc, t1, t2, tcell, d_g,
+			                               NULL, s);
 			sxs_count_launches(1);
 		}
 		if (!e) e = cudaMemcpyAsync(grid, d_g, sizeof(double) * gn, cudaMemcpyDeviceToHost, s);
@@ -600,7 +661,6 @@ int sxsg_plan_timings(sxsg_plan *p, double *ms5)
 {
 	if (!p || !ms5) return sxs_fail(-2, "sxsg_plan_timings: bad arguments");
 	for (int i = 0; i < 5; i++) ms5[i] = p->ms[i];
-	ms5[4] = p->ms[0] + p->ms[1] + p->ms[2] + p->ms[3];
 	return 0;
 }
 
