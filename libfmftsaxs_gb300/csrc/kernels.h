@@ -3,17 +3,19 @@
  * Host C (sxs_host.c) calls these; every pointer is a device pointer unless
  * named h_*.  All launches go to the given stream; none synchronises.
  *
- * Device layouts (K = L+1, N = 2L+1, K2 = K*K, NP = K(K+1)/2; a table of
- * precision S holds complex values as {re, im} pairs of S, S = double on the
- * plain path and float on the mixed path):
- *   spf_t [3 ch][K2 lm][Q]              lm = l(l+1)+m, q fastest (S)
- *   dtab  [K b][K l][N m+L][N m1+L]     Wigner small-d per beta_b = b*pi/L
+ * Device layouts (K = L+1, N = 2L+1, K2 = K*K, NP = K(K+1)/2, NT = ceil(Q/8)
+ * q tiles of 8; a table of precision S holds complex values as {re, im}
+ * pairs of S, S = double on the plain path and float on the mixed path):
+ *   spf_t [3 ch][K2 lm][Q]                     lm = l(l+1)+m, q fastest (S)
+ *   dtab  [K b][K l][N m+L][N m1+L]            Wigner small-d per beta_b = b*pi/L
  *   dsymb [K2 lm][K l1][N p]
  *   bes   [nz][Q][N p]
- *   tau   [nz][K m][K l][K l1][Q]       T^m_{l l1} = i^{l+l1} tau (real)
- *   rot   [K*N (b,g)][NP pair][3 ch][Q] pair = (m >= 0, l >= m), m-major (S)
- *   trans [ncombo][NP pair][3 ch][Q]    (S)
- *   cross [npose][6][Q]                 (double)
+ *   tau   [NT][nz][K m][K l][K l1][8]          T^m_{l l1} = i^{l+l1} tau (real)
+ *   rot   [NT][K*N (b,g)][NP pair][3 ch][8]    pair = (m >= 0, l >= m), m-major (S)
+ *   trans [NT][ncombo][NP pair][3 ch][8]       (S)
+ *   cross [npose][6][Q]                        (double)
+ * Entries of the q tiles past Q are padding: never written by the kernels
+ * that fill a table and never read into a result.
  */
 #ifndef SXS_KERNELS_H
 #define SXS_KERNELS_H
@@ -63,15 +65,15 @@ int sxsk_const_int(const double *A, const double *B, int Q, int L, double *cst, 
 int sxsk_rotate(const void *spf_t, const double *dtab, const double2 *tw, int Q, int L, int conj, void *out,
                 int fp32, cudaStream_t s);
 
-/* translated ligand table for a list of combos (zi, b2, g2), m >= 0:
- * out[c][pair(m,l)][ch][q] = sum_{l1>=m} conj(T[zi][m][l][l1][q]) U[(b2,g2)][pair(m,l1)][ch][q];
- * tau is float when fp32 */
-int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, int ncombo, int Q, int L, void *out,
-                   int fp32, cudaStream_t s);
+/* translated ligand table for a list of combos (zi, b2, g2), m >= 0, all q tiles:
+ * R[t][c][pair(m,l)][ch][q] = sum_{l1>=m} conj(T[t][zi][m][l][l1][q]) U[t][(b2,g2)][pair(m,l1)][ch][q];
+ * tau is float when fp32; nzt = z count of tau */
+int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, int ncombo, int nzt, int Q, int L,
+                   void *R, int fp32, cudaStream_t s);
 
 /* per-pose raw cross terms: cross[p][c][q] = cst[c][q] + 2 Re sum_m tw(m' a2) sum_l P R,
- * the m < 0 half folded in by symmetry */
-int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, const void *P, const void *R,
+ * the m < 0 half folded in by symmetry; R holds the ncombo combos from combo_base */
+int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, int ncombo, const void *P, const void *R,
                     const double2 *tw, const double *cst, int Q, int L, double *cross, int fp32, cudaStream_t s);
 
 /* grid fit: per pose, peak rescale then chi^2 at every (c1, c2) cell; best cell.

@@ -68,13 +68,46 @@ __global__ void k_spf_transpose(const double *__restrict__ flat, typename Cx<S>:
 	t[i] = v;
 }
 
-/* block = (b*N+g, m >= 0); threads over q */
+/* Contraction tables are q-tiled: a tile holds QT = 8 consecutive q, and a
+ * table row is stored as [tile][row][pair][ch][8], so the slice of one tile
+ * (an eighth of the table at Q ~ 100) stays in L2 while the blocks of that
+ * tile run, and each thread moves 2 adjacent q (16 or 32 bytes) per load. */
+#define SXS_QT 8
+
+template <typename S> struct Pair2 { typename Cx<S>::T a, b; };
+__device__ __forceinline__ Pair2<float> ld2(const float2 *p)
+{
+	float4 v = *reinterpret_cast<const float4 *>(p);
+	Pair2<float> r;
+	r.a = make_float2(v.x, v.y);
+	r.b = make_float2(v.z, v.w);
+	return r;
+}
+__device__ __forceinline__ Pair2<double> ld2(const double2 *p)
+{
+	Pair2<double> r;
+	r.a = p[0];
+	r.b = p[1];
+	return r;
+}
+__device__ __forceinline__ void st2(float2 *p, float2 a, float2 b)
+{
+	*reinterpret_cast<float4 *>(p) = make_float4(a.x, a.y, b.x, b.y);
+}
+__device__ __forceinline__ void st2(double2 *p, double2 a, double2 b)
+{
+	p[0] = a;
+	p[1] = b;
+}
+
+/* block = (b*N+g, m >= 0); threads over q.  Output in the q-tiled layout. */
 template <typename S>
 __global__ void k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const double *__restrict__ dtab,
                          const double2 *__restrict__ tw, int Q, int L, int conj, typename Cx<S>::T *__restrict__ out)
 {
 	typedef typename Cx<S>::T V;
 	int K = L + 1, N = 2 * L + 1, K2 = K * K, NP = K * (K + 1) / 2;
+	int nrow = K * N;
 	int bg = blockIdx.x, m = blockIdx.y;
 	int b = bg / N, g = bg % N;
 	int iq = threadIdx.x;
@@ -82,6 +115,7 @@ __global__ void k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const doub
 	const double *db = dtab + (size_t)b * K * N * N;
 	S sg = conj ? (S)-1 : (S)1;
 	int po = psym(m, K);
+	V *ob = out + (((size_t)(iq / SXS_QT) * nrow + bg) * NP + po) * 3 * SXS_QT + iq % SXS_QT;
 	for (int l = m; l <= L; l++) {
 		V acc0 = zero2<V>(), acc1 = acc0, acc2 = acc0;
 		const double *drow = db + ((size_t)l * N + m + L) * N;
@@ -100,106 +134,146 @@ __global__ void k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const doub
 			cfma(acc1, f, c1);
 			cfma(acc2, f, c2);
 		}
-		V *o = out + (((size_t)bg * NP + po + (l - m)) * 3) * Q + iq;
+		V *o = ob + (size_t)(l - m) * 3 * SXS_QT;
 		o[0] = acc0;
-		o[Q] = acc1;
-		o[2 * Q] = acc2;
+		o[SXS_QT] = acc1;
+		o[2 * SXS_QT] = acc2;
 	}
 }
 
-/* block = (combo, m >= 0); threads over q; l blocked by LB for register
- * reuse of U.  conj(T) U = tau U for even l + l1, tau (-i U) for odd. */
+/* Translated ligand rows of one chunk of combos, all q tiles:
+ * R[tile][c][pair(m,l)][ch][8] = sum_{l1>=m} conj(T^m_{l l1}) U[tile][(b2,g2)][pair(m,l1)][ch][8].
+ * conj(T) U = tau U for even l + l1, tau (-i U) for odd.  Thread = (combo,
+ * 2 adjacent q); block = 32 combos x 4 q pairs of one (tile, m); blocks
+ * ordered tile-major so one tile's U and tau slices are live at a time.
+ * l blocked by LB for register reuse of U. */
 template <typename S, int LB>
-__global__ void k_translate(const typename Cx<S>::T *__restrict__ U, const S *__restrict__ tau,
-                            const int32_t *__restrict__ combo_zbg, int Q, int L, typename Cx<S>::T *__restrict__ out)
+__global__ void __launch_bounds__(128)
+k_translate(const typename Cx<S>::T *__restrict__ U, const S *__restrict__ tau, const int32_t *__restrict__ combo_zbg,
+            int ncombo, int L, int nzt, typename Cx<S>::T *__restrict__ R)
 {
 	typedef typename Cx<S>::T V;
-	int K = L + 1, N = 2 * L + 1, NP = K * (K + 1) / 2;
-	int c = blockIdx.x, m = blockIdx.y;
-	int iq = threadIdx.x;
-	if (iq >= Q) return;
+	int K = L + 1, N = 2 * L + 1, NP = K * (K + 1) / 2, nrow = K * N;
+	int cpt = (ncombo + 31) / 32;
+	int bid = blockIdx.x;
+	int cb = bid % cpt;
+	bid /= cpt;
+	int m = bid % K, t = bid / K;
+	int c = cb * 32 + (threadIdx.x >> 2), j2 = 2 * (threadIdx.x & 3);
+	if (c >= ncombo) return;
 	int zi = combo_zbg[3 * c], b2 = combo_zbg[3 * c + 1], g2 = combo_zbg[3 * c + 2];
-	const V *Ub = U + (size_t)(b2 * N + g2) * NP * 3 * Q;
-	const S *Tm = tau + ((size_t)zi * K + m) * K * K * Q;
 	int po = psym(m, K);
-	V *Ob = out + (size_t)c * NP * 3 * Q;
+	const V *Ub = U + (((size_t)t * nrow + b2 * N + g2) * NP + po) * 3 * SXS_QT + j2;
+	const S *Tm = tau + ((((size_t)t * nzt + zi) * K + m) * K) * K * SXS_QT + j2;
+	V *Ob = R + (((size_t)t * ncombo + c) * NP + po) * 3 * SXS_QT + j2;
 	for (int l0 = m; l0 <= L; l0 += LB) {
-		V acc[LB][3];
+		V acc[LB][3][2];
 #pragma unroll
-		for (int j = 0; j < LB; j++) acc[j][0] = acc[j][1] = acc[j][2] = zero2<V>();
+		for (int i = 0; i < LB; i++)
+#pragma unroll
+			for (int ch = 0; ch < 3; ch++) acc[i][ch][0] = acc[i][ch][1] = zero2<V>();
 		for (int l1 = m; l1 <= L; l1++) {
-			const V *u = Ub + ((size_t)(po + l1 - m) * 3) * Q + iq;
-			V u0 = u[0], u1 = u[Q], u2 = u[2 * Q];
+			const V *u = Ub + (size_t)(l1 - m) * 3 * SXS_QT;
+			Pair2<S> uv[3];
 #pragma unroll
-			for (int j = 0; j < LB; j++) {
-				int l = l0 + j;
+			for (int ch = 0; ch < 3; ch++) uv[ch] = ld2(u + ch * SXS_QT);
+#pragma unroll
+			for (int i = 0; i < LB; i++) {
+				int l = l0 + i;
 				if (l > L) break;
-				S t = Tm[((size_t)l * K + l1) * Q + iq];
+				const S *tl = Tm + ((size_t)l * K + l1) * SXS_QT;
+				S t0 = tl[0], t1 = tl[1];
 				if (((l + l1) & 1) == 0) {
-					acc[j][0].x += t * u0.x; acc[j][0].y += t * u0.y;
-					acc[j][1].x += t * u1.x; acc[j][1].y += t * u1.y;
-					acc[j][2].x += t * u2.x; acc[j][2].y += t * u2.y;
+#pragma unroll
+					for (int ch = 0; ch < 3; ch++) {
+						acc[i][ch][0].x += t0 * uv[ch].a.x; acc[i][ch][0].y += t0 * uv[ch].a.y;
+						acc[i][ch][1].x += t1 * uv[ch].b.x; acc[i][ch][1].y += t1 * uv[ch].b.y;
+					}
 				} else {
-					acc[j][0].x += t * u0.y; acc[j][0].y -= t * u0.x;
-					acc[j][1].x += t * u1.y; acc[j][1].y -= t * u1.x;
-					acc[j][2].x += t * u2.y; acc[j][2].y -= t * u2.x;
+#pragma unroll
+					for (int ch = 0; ch < 3; ch++) {
+						acc[i][ch][0].x += t0 * uv[ch].a.y; acc[i][ch][0].y -= t0 * uv[ch].a.x;
+						acc[i][ch][1].x += t1 * uv[ch].b.y; acc[i][ch][1].y -= t1 * uv[ch].b.x;
+					}
 				}
 			}
 		}
 #pragma unroll
-		for (int j = 0; j < LB; j++) {
-			int l = l0 + j;
+		for (int i = 0; i < LB; i++) {
+			int l = l0 + i;
 			if (l > L) break;
-			V *o = Ob + ((size_t)(po + l - m) * 3) * Q + iq;
-			o[0] = acc[j][0];
-			o[Q] = acc[j][1];
-			o[2 * Q] = acc[j][2];
+			V *o = Ob + (size_t)(l - m) * 3 * SXS_QT;
+#pragma unroll
+			for (int ch = 0; ch < 3; ch++) st2(o + ch * SXS_QT, acc[i][ch][0], acc[i][ch][1]);
 		}
 	}
 }
 
-/* block = one pose; threads over q.  Writes cross[src][c][q] (FP64). */
+/* Per-pose cross terms of one chunk, all q tiles.  Thread = (pose, 2
+ * adjacent q); block = 32 consecutive poses (sorted by combo, so their R
+ * rows repeat and hit in L1) x 4 q pairs of one tile; blocks ordered
+ * tile-major.  The pose's phase w_m = tw[(m a2) mod N] (doubled for m > 0)
+ * is applied to R first, so each channel product needs only its real part:
+ *   cross[src][c][q] = cst[c][q] + 2 sum_{m,l} Re(P_a[m,l] (w_m R_b[m,l])). */
 template <typename S>
-__global__ void k_pose_cross(const sxsk_pose *__restrict__ poses, int combo_base, const typename Cx<S>::T *__restrict__ P,
-                             const typename Cx<S>::T *__restrict__ R, const double2 *__restrict__ tw,
-                             const double *__restrict__ cst, int Q, int L, double *__restrict__ cross)
+__global__ void __launch_bounds__(128)
+k_pose_cross(const sxsk_pose *__restrict__ poses, int npose, int combo_base, int ncombo,
+             const typename Cx<S>::T *__restrict__ P, const typename Cx<S>::T *__restrict__ R,
+             const double2 *__restrict__ tw, const double *__restrict__ cst, int Q, int L, double *__restrict__ cross)
 {
 	typedef typename Cx<S>::T V;
-	int K = L + 1, N = 2 * L + 1, NP = K * (K + 1) / 2;
-	sxsk_pose ps = poses[blockIdx.x];
-	int iq = threadIdx.x;
-	if (iq >= Q) return;
-	const V *Pb = P + (size_t)(ps.b1 * N + ps.g1) * NP * 3 * Q + iq;
-	const V *Rb = R + (size_t)(ps.combo - combo_base) * NP * 3 * Q + iq;
-	S f[6] = {0, 0, 0, 0, 0, 0};
+	int K = L + 1, N = 2 * L + 1, NP = K * (K + 1) / 2, nrow = K * N;
+	int bpt = (npose + 31) / 32;
+	int t = blockIdx.x / bpt, pb = blockIdx.x % bpt;
+	int pi = pb * 32 + (threadIdx.x >> 2), j2 = 2 * (threadIdx.x & 3);
+	if (pi >= npose) return;
+	int q0 = t * SXS_QT + j2;
+	if (q0 >= Q) return;
+	sxsk_pose ps = poses[pi];
+	const V *Pr = P + (((size_t)t * nrow + ps.b1 * N + ps.g1) * NP) * 3 * SXS_QT + j2;
+	const V *Rr = R + (((size_t)t * ncombo + ps.combo - combo_base) * NP) * 3 * SXS_QT + j2;
+	S f[2][6];
+#pragma unroll
+	for (int k = 0; k < 2; k++)
+#pragma unroll
+		for (int c = 0; c < 6; c++) f[k][c] = 0;
 	int p = 0;
 	for (int m = 0; m <= L; m++) {
-		V g[6];
-#pragma unroll
-		for (int c = 0; c < 6; c++) g[c] = zero2<V>();
-		for (int l = m; l <= L; l++, p++) {
-			const V *pp = Pb + (size_t)p * 3 * Q;
-			const V *rr = Rb + (size_t)p * 3 * Q;
-			V pv = pp[0], pd = pp[Q], pw = pp[2 * Q];
-			V rv = rr[0], rd = rr[Q], rw = rr[2 * Q];
-			cfma(g[0], pv, rv);
-			cfma(g[1], pv, rd); cfma(g[1], pd, rv);
-			cfma(g[2], pv, rw); cfma(g[2], pw, rv);
-			cfma(g[3], pd, rd);
-			cfma(g[4], pd, rw); cfma(g[4], pw, rd);
-			cfma(g[5], pw, rw);
-		}
-		V w = from2<V>(tw[(m * ps.a2) % N]);
+		double2 wd = tw[(m * ps.a2) % N];
 		S wt = m == 0 ? (S)1 : (S)2;
+		S wx = (S)wd.x * wt, wy = (S)wd.y * wt;
+#pragma unroll 2
+		for (int l = m; l <= L; l++, p++) {
+			const V *pp = Pr + (size_t)p * 3 * SXS_QT;
+			const V *rr = Rr + (size_t)p * 3 * SXS_QT;
+			Pair2<S> pv = ld2(pp), pd = ld2(pp + SXS_QT), pw = ld2(pp + 2 * SXS_QT);
+			Pair2<S> rv = ld2(rr), rd = ld2(rr + SXS_QT), rw = ld2(rr + 2 * SXS_QT);
 #pragma unroll
-		for (int c = 0; c < 6; c++) f[c] += wt * (w.x * g[c].x - w.y * g[c].y);
+			for (int k = 0; k < 2; k++) {
+				V a0 = k ? pv.b : pv.a, a1 = k ? pd.b : pd.a, a2 = k ? pw.b : pw.a;
+				V r0 = k ? rv.b : rv.a, r1 = k ? rd.b : rd.a, r2 = k ? rw.b : rw.a;
+				/* R' = w R */
+				V s0, s1, s2;
+				s0.x = wx * r0.x - wy * r0.y; s0.y = wx * r0.y + wy * r0.x;
+				s1.x = wx * r1.x - wy * r1.y; s1.y = wx * r1.y + wy * r1.x;
+				s2.x = wx * r2.x - wy * r2.y; s2.y = wx * r2.y + wy * r2.x;
+				f[k][0] += a0.x * s0.x - a0.y * s0.y;
+				f[k][1] += a0.x * s1.x - a0.y * s1.y + a1.x * s0.x - a1.y * s0.y;
+				f[k][2] += a0.x * s2.x - a0.y * s2.y + a2.x * s0.x - a2.y * s0.y;
+				f[k][3] += a1.x * s1.x - a1.y * s1.y;
+				f[k][4] += a1.x * s2.x - a1.y * s2.y + a2.x * s1.x - a2.y * s1.y;
+				f[k][5] += a2.x * s2.x - a2.y * s2.y;
+			}
+		}
 	}
-	double *o = cross + (size_t)ps.src * 6 * Q + iq;
+	double *o = cross + (size_t)ps.src * 6 * Q;
 #pragma unroll
-	for (int c = 0; c < 6; c++) {
-		double v = cst[c * Q + iq];
-		v += 2.0 * (double)f[c];
-		o[c * Q] = v;
+	for (int k = 0; k < 2; k++) {
+		int q = q0 + k;
+		if (q < Q) {
+#pragma unroll
+			for (int c = 0; c < 6; c++) o[c * Q + q] = cst[c * Q + q] + 2.0 * (double)f[k][c];
+		}
 	}
 }
 
@@ -429,30 +503,35 @@ int sxsk_to_float(const double *a, float *b, long n, cudaStream_t s)
 	return cudaGetLastError();
 }
 
-int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, int ncombo, int Q, int L, void *out,
-                   int fp32, cudaStream_t s)
+int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, int ncombo, int nzt, int Q, int L,
+                   void *R, int fp32, cudaStream_t s)
 {
 	if (ncombo <= 0) return 0;
-	dim3 grid(ncombo, L + 1);
+	int NT = (Q + SXS_QT - 1) / SXS_QT;
+	long nb = (long)NT * (L + 1) * ((ncombo + 31) / 32);
+	if (nb > 0x7fffffffL) return cudaErrorInvalidValue;
 	if (fp32)
-		k_translate<float, 4><<<grid, qthreads(Q), 0, s>>>((const float2 *)U, (const float *)tau, combo_zbg, Q, L,
-		                                                    (float2 *)out);
+		k_translate<float, 4><<<(unsigned)nb, 128, 0, s>>>((const float2 *)U, (const float *)tau, combo_zbg, ncombo, L,
+		                                                    nzt, (float2 *)R);
 	else
-		k_translate<double, 4><<<grid, qthreads(Q), 0, s>>>((const double2 *)U, (const double *)tau, combo_zbg, Q, L,
-		                                                     (double2 *)out);
+		k_translate<double, 4><<<(unsigned)nb, 128, 0, s>>>((const double2 *)U, (const double *)tau, combo_zbg, ncombo,
+		                                                     L, nzt, (double2 *)R);
 	return cudaGetLastError();
 }
 
-int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, const void *P, const void *R,
+int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, int ncombo, const void *P, const void *R,
                     const double2 *tw, const double *cst, int Q, int L, double *cross, int fp32, cudaStream_t s)
 {
 	if (npose <= 0) return 0;
+	int NT = (Q + SXS_QT - 1) / SXS_QT;
+	long nb = (long)NT * ((npose + 31) / 32);
+	if (nb > 0x7fffffffL) return cudaErrorInvalidValue;
 	if (fp32)
-		k_pose_cross<float><<<npose, qthreads(Q), 0, s>>>(poses, combo_base, (const float2 *)P, (const float2 *)R, tw,
-		                                                   cst, Q, L, cross);
+		k_pose_cross<float><<<(unsigned)nb, 128, 0, s>>>(poses, npose, combo_base, ncombo, (const float2 *)P,
+		                                                  (const float2 *)R, tw, cst, Q, L, cross);
 	else
-		k_pose_cross<double><<<npose, qthreads(Q), 0, s>>>(poses, combo_base, (const double2 *)P, (const double2 *)R,
-		                                                    tw, cst, Q, L, cross);
+		k_pose_cross<double><<<(unsigned)nb, 128, 0, s>>>(poses, npose, combo_base, ncombo, (const double2 *)P,
+		                                                   (const double2 *)R, tw, cst, Q, L, cross);
 	return cudaGetLastError();
 }
 

@@ -178,6 +178,7 @@ struct sxsg_plan {
 	int fp32;                   /* tables in float (mixed path) */
 	size_t celem;               /* bytes of one complex table entry */
 	int NP;                     /* (m >= 0, l >= m) pairs */
+	int NT;                     /* q tiles of 8 */
 	/* rotation tables (depend on the twiddle variant) */
 	void *d_P, *d_U;
 	int tw_variant; /* -1 none, 0 simple_ft, 1 exact */
@@ -257,6 +258,7 @@ int sxsg_plan_create(sxsg_plan **out, const double *A, const double *B, const do
 	p->fp32 = precision == SXSG_MIXED;
 	p->celem = p->fp32 ? 2 * sizeof(float) : 2 * sizeof(double);
 	p->NP = p->K * (p->K + 1) / 2;
+	p->NT = (Q + 7) / 8;
 	double s0 = 0.0;
 	for (int i = 0; i < Q; i++) s0 += a[6 * i];
 	p->a0sum = s0;
@@ -287,9 +289,12 @@ int sxsg_plan_create(sxsg_plan **out, const double *A, const double *B, const do
 	if (!e && n1 > 0) e = cudaMalloc((void **)&p->d_gtab, sizeof(double) * n1 * Q);
 	if (!e && n1 > 0) e = cudaMalloc((void **)&p->d_c1g, sizeof(double) * n1);
 	if (!e && n2 > 0) e = cudaMalloc((void **)&p->d_c2g, sizeof(double) * n2);
-	size_t rot_n = (size_t)p->K * p->N * p->NP * 3 * Q;
+	size_t rot_n = (size_t)p->NT * p->K * p->N * p->NP * 3 * 8;
 	if (!e) e = cudaMalloc(&p->d_P, p->celem * rot_n);
 	if (!e) e = cudaMalloc(&p->d_U, p->celem * rot_n);
+	/* q-tile padding stays zero */
+	if (!e) e = cudaMemsetAsync(p->d_P, 0, p->celem * rot_n, p->s);
+	if (!e) e = cudaMemsetAsync(p->d_U, 0, p->celem * rot_n, p->s);
 	if (e) {
 		sxsg_plan_destroy(p);
 		return sxs_cuda_fail(e, "sxsg_plan_create allocation");
@@ -447,7 +452,7 @@ int sxsg_plan_set_poses(sxsg_plan *p, const int64_t *index, int64_t n, int skip)
 	if (!e) e = cudaMalloc((void **)&p->d_combo, sizeof(int32_t) * 3 * (ncombo > 0 ? ncombo : 1));
 	if (!e) e = cudaMalloc((void **)&p->d_zt, sizeof(double) * (nzt > 0 ? nzt : 1));
 	if (!e && nzt > 0) e = cudaMalloc((void **)&p->d_bes, sizeof(double) * (size_t)nzt * p->Q * N);
-	size_t tau_n = (size_t)nzt * p->K * p->K * p->K * p->Q;
+	size_t tau_n = (size_t)p->NT * nzt * p->K * p->K * p->K * 8;
 	if (!e && nzt > 0) e = cudaMalloc((void **)&p->d_tau, sizeof(double) * tau_n);
 	if (!e && nzt > 0 && p->fp32) e = cudaMalloc((void **)&p->d_tauf, sizeof(float) * tau_n);
 	if (!e && n > 0) e = cudaMemcpyAsync(p->d_poses, p->h_poses, sizeof(sxsk_pose) * n, cudaMemcpyHostToDevice, p->s);
@@ -496,7 +501,7 @@ static int plan_tables(sxsg_plan *p)
 		SXS_K(sxsk_tmatrix(p->d_bes, p->lt->d_dsymb, p->nzt, Q, L, p->lt->d_ll1, p->lt->nll1, p->d_tau, s));
 		sxs_count_launches(2);
 		if (p->fp32) {
-			SXS_K(sxsk_to_float(p->d_tau, p->d_tauf, (long)p->nzt * p->K * p->K * p->K * Q, s));
+			SXS_K(sxsk_to_float(p->d_tau, p->d_tauf, (long)p->NT * p->nzt * p->K * p->K * p->K * 8, s));
 			sxs_count_launches(1);
 		}
 	}
@@ -535,7 +540,7 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 	if ((rc = plan_tables(p))) return rc;
 	SXS_CU(cudaEventRecord(p->ev[1], s));
 	/* translated table in chunks of combos that fit the budget */
-	size_t per_combo = (size_t)p->NP * 3 * Q * p->celem;
+	size_t per_combo = (size_t)p->NP * 3 * 8 * p->NT * p->celem;
 	int64_t chunk = (int64_t)(p->r_budget / per_combo);
 	if (chunk < 1) chunk = 1;
 	int pipe = fit_mode == SXSG_FIT_GRID && p->ncombo > 0;
@@ -558,10 +563,11 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 		int64_t c0 = k * chunk, c1 = c0 + chunk < p->ncombo ? c0 + chunk : p->ncombo;
 		cudaEvent_t *e = p->cev + 5 * k;
 		SXS_CU(cudaEventRecord(e[0], s));
-		SXS_K(sxsk_translate(p->d_U, tau, p->d_combo + 3 * c0, (int)(c1 - c0), Q, L, p->d_R, p->fp32, s));
+		SXS_K(sxsk_translate(p->d_U, tau, p->d_combo + 3 * c0, (int)(c1 - c0), p->nzt, Q, L, p->d_R, p->fp32, s));
 		SXS_CU(cudaEventRecord(e[1], s));
 		int64_t p0 = p->h_cstart[c0], p1 = p->h_cstart[c1];
-		SXS_K(sxsk_pose_cross(p->d_poses + p0, (int)(p1 - p0), (int)c0, p->d_P, p->d_R, p->d_tw, p->d_cst, Q, L,
+		SXS_K(sxsk_pose_cross(p->d_poses + p0, (int)(p1 - p0), (int)c0, (int)(c1 - c0), p->d_P, p->d_R, p->d_tw,
+		                      p->d_cst, Q, L,
 		                      p->d_cross, p->fp32, s));
 		SXS_CU(cudaEventRecord(e[2], s));
 		sxs_count_launches(2);
