@@ -87,6 +87,14 @@ int sxsk_fit_grid(const double *cross, const sxsk_pose *order, int slot0, int ns
                   int max_blocks, double *chi, double *c1, double *c2, int32_t *cell, double *grid, double *scaled,
                   cudaStream_t s);
 
+/* the grid fit of the mixed path in double-float arithmetic (FP32 pipe);
+ * same arguments as sxsk_fit_grid, with gdf[n1][Q] = gtab split into
+ * {hi, lo} floats */
+int sxsk_fit_grid_df(const double *cross, const sxsk_pose *order, int slot0, int nslot, int Q, const double *fc,
+                     double a0sum, double peak, const float2 *gdf, const double *c1g, int n1, const double *c2g,
+                     int n2, int max_blocks, double *chi, double *c1, double *c2, int32_t *cell, double *grid,
+                     double *scaled, cudaStream_t s);
+
 #ifdef __cplusplus
 }
 #endif

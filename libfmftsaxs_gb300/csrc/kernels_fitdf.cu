@@ -1,0 +1,178 @@
+/*
+ * Grid fit of the mixed-precision path in double-float arithmetic: every
+ * quantity is an unevaluated sum hi + lo of two floats (about 48 significant
+ * bits), so the fit runs on the FP32 pipe, 64 times wider than the FP64 pipe
+ * on this GPU.  The score sum a0 - up^2/down cancels by A0/chi^2 (10^3 to
+ * 10^4 on SAXS data), which rules out plain FP32; 48 bits leave it far
+ * inside the mixed path's |dchi| <= 1e-4 chi.
+ *
+ * Same algorithm and thread layout as k_fit_grid in kernels_contract.cu
+ * (point_score of src/min_saxs.c:391-448 with the per-q constants folded on
+ * the host); the model is normalised to 1 at q_0 instead of to the peak, and
+ * the constants are scaled by peak (a1, u) and peak^2 (a3, e, f), which
+ * leaves up and down unchanged and keeps every intermediate near 1.
+ *
+ * Compiled with -fmad=false: the error-free transformations of
+ * fitdf_core.h must not be contracted.
+ */
+#include "kernels.h"
+#include "fitdf_core.h"
+
+namespace {
+
+#define FITD_THREADS 128
+#define FITD_NFC 5
+
+__global__ void __launch_bounds__(FITD_THREADS)
+k_fit_grid_df(const double *__restrict__ cross, const sxsk_pose *__restrict__ order, int slot0, int nslot, int Q,
+              const double *__restrict__ fc, double a0sum, double peak, const float2 *__restrict__ gdf,
+              const double *__restrict__ c1g, int n1, const double *__restrict__ c2g, int n2, int tp, int ppb,
+              double *__restrict__ chi, double *__restrict__ c1o, double *__restrict__ c2o,
+              int32_t *__restrict__ cello, double *__restrict__ grid, double *__restrict__ scaled)
+{
+	extern __shared__ double sm[];
+	dfl *cs = reinterpret_cast<dfl *>(sm);             /* [ppb][8][Q]: VV VD VW DD DW WW P3 P4 */
+	dfl *fs = cs + (size_t)ppb * 8 * Q;                /* [FITD_NFC][Q] */
+	dfl *c2s = fs + (size_t)FITD_NFC * Q;              /* [n2] */
+	double *red = reinterpret_cast<double *>(c2s + n2); /* [ppb*tp][2] */
+	int *redc = (int *)(red + 2 * ppb * tp);           /* [ppb*tp] */
+	double *sf = (double *)(redc + ((ppb * tp + 1) & ~1)); /* [ppb][2]: 1/norm, peak/norm */
+	dfl *sfd = reinterpret_cast<dfl *>(sf + 2 * ppb);  /* [ppb][2]: U2, D4 */
+	int *srcs = (int *)(sfd + 2 * ppb);                /* [ppb] */
+	int tid = threadIdx.x;
+	int nthr = ppb * tp;
+	int lp = tid / tp, lt = tid % tp;
+	double pk2 = peak * peak;
+	for (int k = tid; k < FITD_NFC * Q; k += blockDim.x) {
+		int c = k / Q, i = k % Q;
+		fs[k] = df_from(fc[i * FITD_NFC + c] * (c < 3 ? pk2 : peak));
+	}
+	for (int k = tid; k < n2; k += blockDim.x) c2s[k] = df_from(c2g[k]);
+	int ngroup = (nslot + ppb - 1) / ppb;
+	for (int grp = blockIdx.x; grp < ngroup; grp += gridDim.x) {
+		int s0 = grp * ppb;
+		int nhere = min(ppb, nslot - s0);
+		bool live = tid < nthr && lp < nhere;
+		__syncthreads();
+		if (tid < nhere) srcs[tid] = order ? order[slot0 + s0 + tid].src : slot0 + s0 + tid;
+		__syncthreads();
+		if (tid < nhere) {
+			const double *c = cross + (size_t)srcs[tid] * 6 * Q;
+			double sc = c[0] + c[3 * Q] + c[5 * Q] + c[2 * Q] - c[Q] - c[4 * Q];
+			sf[2 * tid] = 1.0 / sc;
+			sf[2 * tid + 1] = peak / sc;
+		}
+		__syncthreads();
+		for (int k = tid; k < nhere * 6 * Q; k += blockDim.x) {
+			int p = k / (6 * Q), r = k % (6 * Q);
+			double v = cross[(size_t)srcs[p] * 6 * Q + r];
+			cs[(size_t)p * 8 * Q + r] = df_from(v * sf[2 * p]);
+			if (scaled) scaled[(size_t)srcs[p] * 6 * Q + r] = v * sf[2 * p + 1];
+		}
+		__syncthreads();
+		dfl *c = cs + (size_t)lp * 8 * Q;
+		if (live) {
+			dfl u2, d4;
+			df_pose_prep(c, fs, Q, lt, tp, &u2, &d4);
+			red[2 * tid] = df_to(u2);
+			red[2 * tid + 1] = df_to(d4);
+		}
+		__syncthreads();
+		if (live && lt == 0) {
+			/* partial sums added in double: exact enough and order-fixed */
+			double u2 = 0, d4 = 0;
+			for (int t = 0; t < tp; t++) {
+				u2 += red[2 * (tid + t)];
+				d4 += red[2 * (tid + t) + 1];
+			}
+			sfd[2 * lp] = df_from(u2);
+			sfd[2 * lp + 1] = df_from(d4);
+		}
+		__syncthreads();
+		double bscore = __longlong_as_double(0x7ff0000000000000LL);
+		int bcell = -1;
+		int pid = live ? srcs[lp] : 0;
+		if (live) {
+			dfl U2 = sfd[2 * lp], D4 = sfd[2 * lp + 1];
+			for (int j = lt; j < n1; j += tp) {
+				const dfl *G = reinterpret_cast<const dfl *>(gdf) + (size_t)j * Q;
+				dfl u[2], d[4];
+				df_row(c, fs, G, Q, u, d);
+				if (grid) {
+					for (int i2 = 0; i2 < n2; i2++) {
+						double uu = df_to(df_up(u, U2, c2s[i2])), dd = df_to(df_down(d, D4, c2s[i2]));
+						double k = uu / dd;
+						grid[((size_t)pid * n1 + j) * n2 + i2] = a0sum + k * (-2.0 * uu + k * dd);
+					}
+				}
+				dfl bu, bd;
+				int bi = df_best_c2(u, U2, d, D4, c2s, n2, &bu, &bd);
+				if (bi >= 0) {
+					double uu = df_to(bu), dd = df_to(bd);
+					double k = uu / dd;
+					double score = a0sum + k * (-2.0 * uu + k * dd);
+					int cell = j * n2 + bi;
+					if (score < bscore || (score == bscore && cell < bcell)) {
+						bscore = score;
+						bcell = cell;
+					}
+				}
+			}
+			red[2 * tid] = bscore;
+			redc[tid] = bcell;
+		}
+		__syncthreads();
+		if (live && lt == 0) {
+			for (int t = 1; t < tp; t++) {
+				double os = red[2 * (tid + t)];
+				int oc = redc[tid + t];
+				if (oc >= 0 && (bcell < 0 || os < bscore || (os == bscore && oc < bcell))) {
+					bscore = os;
+					bcell = oc;
+				}
+			}
+			if (bcell >= 0) {
+				chi[pid] = sqrt(bscore);
+				c1o[pid] = c1g[bcell / n2];
+				c2o[pid] = c2g[bcell % n2];
+			} else {
+				chi[pid] = __longlong_as_double(0x7ff8000000000000LL);
+				c1o[pid] = __longlong_as_double(0x7ff8000000000000LL);
+				c2o[pid] = __longlong_as_double(0x7ff8000000000000LL);
+			}
+			if (cello) cello[pid] = bcell;
+		}
+	}
+}
+
+} // namespace
+
+extern "C" int sxsk_fit_grid_df(const double *cross, const sxsk_pose *order, int slot0, int nslot, int Q,
+                                const double *fc, double a0sum, double peak, const float2 *gdf, const double *c1g,
+                                int n1, const double *c2g, int n2, int max_blocks, double *chi, double *c1,
+                                double *c2, int32_t *cell, double *grid, double *scaled, cudaStream_t s)
+{
+	if (nslot <= 0) return 0;
+	if (n1 <= 0 || n2 <= 0) return cudaErrorInvalidValue;
+	int tp = n1 < FITD_THREADS ? n1 : FITD_THREADS;
+	int ppb = FITD_THREADS / tp;
+	size_t smem;
+	for (;;) {
+		size_t nthr = (size_t)ppb * tp;
+		smem = sizeof(dfl) * ((size_t)ppb * 8 * Q + (size_t)FITD_NFC * Q + n2) +
+		       sizeof(double) * (2 * nthr + 2 * ppb) + sizeof(int) * ((nthr + 1) & ~(size_t)1) +
+		       sizeof(dfl) * 2 * ppb + sizeof(int) * ppb;
+		if (smem <= 227 * 1024 || ppb == 1) break;
+		ppb = (ppb + 1) / 2;
+	}
+	if (smem > 227 * 1024) return cudaErrorInvalidValue;
+	if (smem > 48 * 1024) {
+		cudaError_t e = cudaFuncSetAttribute(k_fit_grid_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		if (e != cudaSuccess) return e;
+	}
+	long ngroup = (nslot + ppb - 1) / ppb;
+	int grid_n = (int)(ngroup < (long)max_blocks || max_blocks <= 0 ? ngroup : max_blocks);
+	k_fit_grid_df<<<grid_n, FITD_THREADS, smem, s>>>(cross, order, slot0, nslot, Q, fc, a0sum, peak, gdf, c1g, n1,
+	                                                  c2g, n2, tp, ppb, chi, c1, c2, cell, grid, scaled);
+	return cudaGetLastError();
+}

@@ -172,6 +172,7 @@ struct sxsg_plan {
 	double mult, peak, a0sum;
 	/* resident inputs */
 	double *d_A, *d_B, *d_q, *d_fc, *d_a, *d_gtab, *d_c1g, *d_c2g, *d_cst;
+	float2 *d_gdf;              /* gtab as {hi, lo} floats (mixed path fit) */
 	double2 *d_tw;
 	void *d_At, *d_Bt;          /* transposed coefficients, table precision */
 	double *h_z;
@@ -225,7 +226,7 @@ void sxsg_plan_destroy(sxsg_plan *p)
 	if (!p) return;
 	cudaStreamSynchronize(p->s);
 	plan_free_poses(p);
-	cudaFree(p->d_A); cudaFree(p->d_B); cudaFree(p->d_q); cudaFree(p->d_fc); cudaFree(p->d_a); cudaFree(p->d_gtab);
+	cudaFree(p->d_A); cudaFree(p->d_B); cudaFree(p->d_q); cudaFree(p->d_fc); cudaFree(p->d_a); cudaFree(p->d_gtab); cudaFree(p->d_gdf);
 	cudaFree(p->d_c1g); cudaFree(p->d_c2g); cudaFree(p->d_cst); cudaFree(p->d_At); cudaFree(p->d_Bt);
 	cudaFree(p->d_tw); cudaFree(p->d_P); cudaFree(p->d_U); cudaFree(p->d_R);
 	cudaFree(p->d_cross); cudaFree(p->d_chi); cudaFree(p->d_c1); cudaFree(p->d_c2); cudaFree(p->d_grid);
@@ -321,6 +322,17 @@ int sxsg_plan_create(sxsg_plan **out, const double *A, const double *B, const do
 			for (int k = 0; k < Q; k++) g[(size_t)i * Q + k] = c1c * exp(corr * q[k] * q[k]);
 		}
 		e = cudaMemcpy(p->d_gtab, g, sizeof(double) * n1 * Q, cudaMemcpyHostToDevice);
+		if (!e && p->fp32) {
+			float *gd = malloc(sizeof(float) * 2 * n1 * Q);
+			for (size_t k = 0; k < (size_t)n1 * Q; k++) {
+				float h = (float)g[k];
+				gd[2 * k] = h;
+				gd[2 * k + 1] = (float)(g[k] - (double)h);
+			}
+			e = cudaMalloc((void **)&p->d_gdf, sizeof(float2) * n1 * Q);
+			if (!e) e = cudaMemcpy(p->d_gdf, gd, sizeof(float2) * n1 * Q, cudaMemcpyHostToDevice);
+			free(gd);
+		}
 		free(g);
 		if (!e) e = cudaMemcpyAsync(p->d_c1g, c1g, sizeof(double) * n1, cudaMemcpyHostToDevice, s);
 	}
@@ -508,6 +520,19 @@ static int plan_tables(sxsg_plan *p)
 	return 0;
 }
 
+/* grid fit of slots [slot0, slot0 + nslot) of order (all poses in list
+ * order when order is NULL) in the plan's precision: FP64 on the plain path,
+ * double-float on the FP32 pipe on the mixed path */
+static int plan_fit_grid(sxsg_plan *p, const sxsk_pose *order, int slot0, int nslot, int max_blocks, double *chi,
+                         double *c1, double *c2, int32_t *cell, double *grid, double *scaled, cudaStream_t st)
+{
+	if (p->fp32)
+		return sxsk_fit_grid_df(p->d_cross, order, slot0, nslot, p->Q, p->d_fc, p->a0sum, p->peak, p->d_gdf,
+		                        p->d_c1g, p->n1, p->d_c2g, p->n2, max_blocks, chi, c1, c2, cell, grid, scaled, st);
+	return sxsk_fit_grid(p->d_cross, order, slot0, nslot, p->Q, p->d_fc, p->a0sum, p->peak, p->d_gtab, p->d_c1g,
+	                     p->n1, p->d_c2g, p->n2, max_blocks, chi, c1, c2, cell, grid, scaled, st);
+}
+
 /* Chunks the grid-fit run is split into at least, so that the fit of one
  * chunk (FP64 pipe) overlaps the contractions of the next (HBM / FP32). */
 #define SXS_PIPE_CHUNKS 8
@@ -574,9 +599,8 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 		if (pipe) {
 			SXS_CU(cudaStreamWaitEvent(p->sf, e[2], 0));
 			SXS_CU(cudaEventRecord(e[3], p->sf));
-			SXS_K(sxsk_fit_grid(p->d_cross, p->d_poses, (int)p0, (int)(p1 - p0), Q, p->d_fc, p->a0sum, p->peak,
-			                    p->d_gtab, p->d_c1g, p->n1, p->d_c2g, p->n2, SXS_FIT_BLOCKS_PER_SM * p->nsm,
-			                    p->d_chi, p->d_c1, p->d_c2, p->d_cell, NULL, p->d_scaled, p->sf));
+			SXS_K(plan_fit_grid(p, p->d_poses, (int)p0, (int)(p1 - p0), SXS_FIT_BLOCKS_PER_SM * p->nsm, p->d_chi,
+			                    p->d_c1, p->d_c2, p->d_cell, NULL, p->d_scaled, p->sf));
 			SXS_CU(cudaEventRecord(e[4], p->sf));
 			sxs_count_launches(p1 > p0 ? 1 : 0);
 		}
@@ -589,8 +613,7 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 	SXS_CU(cudaEventRecord(p->ev[5], s));
 	int n = (int)p->npose;
 	if (fit_mode == SXSG_FIT_GRID && !pipe) {
-		SXS_K(sxsk_fit_grid(p->d_cross, NULL, 0, n, Q, p->d_fc, p->a0sum, p->peak, p->d_gtab, p->d_c1g, p->n1,
-		                    p->d_c2g, p->n2, 0, p->d_chi, p->d_c1, p->d_c2, p->d_cell, NULL, p->d_scaled, s));
+		SXS_K(plan_fit_grid(p, NULL, 0, n, 0, p->d_chi, p->d_c1, p->d_c2, p->d_cell, NULL, p->d_scaled, s));
 		sxs_count_launches(n > 0 ? 1 : 0);
 	} else if (fit_mode == SXSG_FIT_LBFGSB) {
 		SXS_K(sxs_fit_lbfgsb_launch(p->d_cross, p->d_scaled, n, Q, p->d_q, p->d_a, p->mult, p->peak, 1, p->d_chi,
@@ -649,9 +672,7 @@ int sxsg_plan_results(sxsg_plan *p, double *chi, double *c1, double *c2, int32_t
 		if (!e) e = cudaMalloc((void **)&t2, sizeof(double) * n);
 		if (!e) e = cudaMalloc((void **)&tcell, sizeof(int32_t) * n);
 		if (!e) {
-			e = (cudaError_t)sxsk_fit_grid(p->d_cross, NULL, 0, (int)n, p->Q, p->d_fc, p->a0sum, p->peak,
-			                               p->d_gtab, p->d_c1g, p->n1, p->d_c2g, p->n2, 0, tc, t1, t2, tcell, d_g,
-			                               NULL, s);
+			e = (cudaError_t)plan_fit_grid(p, NULL, 0, (int)n, 0, tc, t1, t2, tcell, d_g, NULL, s);
 			sxs_count_launches(1);
 		}
 		if (!e) e = cudaMemcpyAsync(grid, d_g, sizeof(double) * gn, cudaMemcpyDeviceToHost, s);
