@@ -65,11 +65,13 @@ int sxsk_const_int(const double *A, const double *B, int Q, int L, double *cst, 
 int sxsk_rotate(const void *spf_t, const double *dtab, const double2 *tw, int Q, int L, int conj, void *out,
                 int fp32, cudaStream_t s);
 
-/* translated ligand table for a list of combos (zi, b2, g2), m >= 0, all q tiles:
- * R[t][c][pair(m,l)][ch][q] = sum_{l1>=m} conj(T[t][zi][m][l][l1][q]) U[t][(b2,g2)][pair(m,l1)][ch][q];
- * tau is float when fp32; nzt = z count of tau */
-int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, int ncombo, int nzt, int Q, int L,
-                   void *R, int fp32, cudaStream_t s);
+/* translated ligand table for the combos of a run of slices, m >= 0, all q tiles:
+ * R[t][c][pair(m,l)][ch][q] = sum_{l1>=m} conj(T[t][zi][m][l][l1][q]) U[t][(b2,g2)][pair(m,l1)][ch][q].
+ * combo_zbg = the combos of the chunk (cbase = the first one's index),
+ * slices[nslice][2] = {first combo, count} runs of <= 16 combos sharing z;
+ * R holds ncombo combos; tau is float when fp32; nzt = z count of tau */
+int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, const int32_t *slices, int nslice,
+                   int cbase, int ncombo, int nzt, int Q, int L, void *R, int fp32, cudaStream_t s);
 
 /* per-pose raw cross terms: cross[p][c][q] = cst[c][q] + 2 Re sum_m tw(m' a2) sum_l P R,
  * the m < 0 half folded in by symmetry; R holds the ncombo combos from combo_base */

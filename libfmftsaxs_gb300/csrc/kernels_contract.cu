@@ -141,71 +141,161 @@ __global__ void k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const doub
 	}
 }
 
-/* Translated ligand rows of one chunk of combos, all q tiles:
- * R[tile][c][pair(m,l)][ch][8] = sum_{l1>=m} conj(T^m_{l l1}) U[tile][(b2,g2)][pair(m,l1)][ch][8].
- * conj(T) U = tau U for even l + l1, tau (-i U) for odd.  Thread = (combo,
- * 2 adjacent q); block = 32 combos x 4 q pairs of one (tile, m); blocks
- * ordered tile-major so one tile's U and tau slices are live at a time.
- * l blocked by LB for register reuse of U. */
-template <typename S, int LB>
+/* Translated ligand rows, q-tiled:
+ * R[tile][c][pair(m,l)][ch][8] = sum_{l1>=m} conj(T^m_{l l1}) U[tile][(b2,g2)][pair(m,l1)][ch][8],
+ * conj(T) U = tau U for even l + l1 and tau (-i U) for odd.
+ * Block = (tile, slice of <= 16 combos sharing one z, 32 consecutive pairs);
+ * thread = (pair, 2 adjacent q).  The block stages the tau rows of its 32
+ * pairs (the same for every combo of the slice) in shared memory once, then
+ * streams the slice's U rows: each thread accumulates its pair for the 3
+ * channels and 2 q.  Threads of a warp with the same m read the same U
+ * entries (broadcast).  Blocks are ordered tile-major. */
+template <typename S>
 __global__ void __launch_bounds__(128)
 k_translate(const typename Cx<S>::T *__restrict__ U, const S *__restrict__ tau, const int32_t *__restrict__ combo_zbg,
-            int ncombo, int L, int nzt, typename Cx<S>::T *__restrict__ R)
+            const int32_t *__restrict__ slices, int nslice, int cbase, int ncombo, int L, int nzt, int tstride,
+            typename Cx<S>::T *__restrict__ R)
 {
 	typedef typename Cx<S>::T V;
+	extern __shared__ __align__(16) unsigned char tsm_raw[];
+	S *ts = reinterpret_cast<S *>(tsm_raw);   /* [32 pairs][tstride]: tau[l1][8 q] of each pair */
 	int K = L + 1, N = 2 * L + 1, NP = K * (K + 1) / 2, nrow = K * N;
-	int cpt = (ncombo + 31) / 32;
+	int npb = (NP + 31) / 32;
 	int bid = blockIdx.x;
-	int cb = bid % cpt;
-	bid /= cpt;
-	int m = bid % K, t = bid / K;
-	int c = cb * 32 + (threadIdx.x >> 2), j2 = 2 * (threadIdx.x & 3);
-	if (c >= ncombo) return;
-	int zi = combo_zbg[3 * c], b2 = combo_zbg[3 * c + 1], g2 = combo_zbg[3 * c + 2];
+	int pb = bid % npb;
+	bid /= npb;
+	int si = bid % nslice, t = bid / nslice;
+	int cfirst = slices[2 * si] - cbase, nc = slices[2 * si + 1];
+	int zi = combo_zbg[3 * cfirst];
+	for (int k = threadIdx.x; k < 32 * K * SXS_QT; k += blockDim.x) {
+		int pl = k / (K * SXS_QT), r = k % (K * SXS_QT);
+		int l1 = r / SXS_QT, qq = r % SXS_QT;
+		int pr = pb * 32 + pl;
+		S v = 0;
+		if (pr < NP) {
+			int m = 0;
+			while (pr >= psym(m + 1, K)) m++;
+			int l = m + pr - psym(m, K);
+			if (l1 >= m) v = tau[(((((size_t)t * nzt + zi) * K + m) * K + l) * K + l1) * SXS_QT + qq];
+		}
+		ts[pl * tstride + r] = v;
+	}
+	__syncthreads();
+	int pl = threadIdx.x >> 2, j2 = 2 * (threadIdx.x & 3);
+	int pr = pb * 32 + pl;
+	if (pr >= NP) return;
+	int m = 0;
+	while (pr >= psym(m + 1, K)) m++;
+	int l = m + pr - psym(m, K);
+	const S *tp = ts + pl * tstride + j2;
 	int po = psym(m, K);
-	const V *Ub = U + (((size_t)t * nrow + b2 * N + g2) * NP + po) * 3 * SXS_QT + j2;
-	const S *Tm = tau + ((((size_t)t * nzt + zi) * K + m) * K) * K * SXS_QT + j2;
-	V *Ob = R + (((size_t)t * ncombo + c) * NP + po) * 3 * SXS_QT + j2;
-	for (int l0 = m; l0 <= L; l0 += LB) {
-		V acc[LB][3][2];
+	for (int c = cfirst; c < cfirst + nc; c++) {
+		int b2 = combo_zbg[3 * c + 1], g2 = combo_zbg[3 * c + 2];
+		const V *Ub = U + (((size_t)t * nrow + b2 * N + g2) * NP + po) * 3 * SXS_QT + j2;
+		V acc[3][2];
 #pragma unroll
-		for (int i = 0; i < LB; i++)
-#pragma unroll
-			for (int ch = 0; ch < 3; ch++) acc[i][ch][0] = acc[i][ch][1] = zero2<V>();
+		for (int ch = 0; ch < 3; ch++) acc[ch][0] = acc[ch][1] = zero2<V>();
 		for (int l1 = m; l1 <= L; l1++) {
+			S t0 = tp[l1 * SXS_QT], t1 = tp[l1 * SXS_QT + 1];
 			const V *u = Ub + (size_t)(l1 - m) * 3 * SXS_QT;
-			Pair2<S> uv[3];
+			if (((l + l1) & 1) == 0) {
 #pragma unroll
-			for (int ch = 0; ch < 3; ch++) uv[ch] = ld2(u + ch * SXS_QT);
+				for (int ch = 0; ch < 3; ch++) {
+					Pair2<S> uv = ld2(u + ch * SXS_QT);
+					acc[ch][0].x += t0 * uv.a.x; acc[ch][0].y += t0 * uv.a.y;
+					acc[ch][1].x += t1 * uv.b.x; acc[ch][1].y += t1 * uv.b.y;
+				}
+			} else {
 #pragma unroll
-			for (int i = 0; i < LB; i++) {
-				int l = l0 + i;
-				if (l > L) break;
-				const S *tl = Tm + ((size_t)l * K + l1) * SXS_QT;
-				S t0 = tl[0], t1 = tl[1];
-				if (((l + l1) & 1) == 0) {
-#pragma unroll
-					for (int ch = 0; ch < 3; ch++) {
-						acc[i][ch][0].x += t0 * uv[ch].a.x; acc[i][ch][0].y += t0 * uv[ch].a.y;
-						acc[i][ch][1].x += t1 * uv[ch].b.x; acc[i][ch][1].y += t1 * uv[ch].b.y;
-					}
-				} else {
-#pragma unroll
-					for (int ch = 0; ch < 3; ch++) {
-						acc[i][ch][0].x += t0 * uv[ch].a.y; acc[i][ch][0].y -= t0 * uv[ch].a.x;
-						acc[i][ch][1].x += t1 * uv[ch].b.y; acc[i][ch][1].y -= t1 * uv[ch].b.x;
-					}
+				for (int ch = 0; ch < 3; ch++) {
+					Pair2<S> uv = ld2(u + ch * SXS_QT);
+					acc[ch][0].x += t0 * uv.a.y; acc[ch][0].y -= t0 * uv.a.x;
+					acc[ch][1].x += t1 * uv.b.y; acc[ch][1].y -= t1 * uv.b.x;
 				}
 			}
 		}
+		V *o = R + (((size_t)t * ncombo + c) * NP + pr) * 3 * SXS_QT + j2;
 #pragma unroll
-		for (int i = 0; i < LB; i++) {
-			int l = l0 + i;
-			if (l > L) break;
-			V *o = Ob + (size_t)(l - m) * 3 * SXS_QT;
+		for (int ch = 0; ch < 3; ch++) st2(o + ch * SXS_QT, acc[ch][0], acc[ch][1]);
+	}
+}
+
+__device__ __forceinline__ void ld4(const float *p, float *v)
+{
+	float4 x = *reinterpret_cast<const float4 *>(p);
+	v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+}
+__device__ __forceinline__ void ld4(const double *p, double *v)
+{
+	double2 x = *reinterpret_cast<const double2 *>(p), y = *reinterpret_cast<const double2 *>(p + 2);
+	v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
+}
+
+/* Column form of the translation, for L < 32: thread = one column
+ * (combo c, channel ch, q) of one m; it holds U[c][pair(m, m+k)][ch][q],
+ * k < n = L + 1 - m, in registers (NB = n rounded up to 4, unrolled) and
+ * applies the n x n matrix tau^m(q z) staged in shared memory:
+ *   R[c][pair(m, m+i)][ch][q] = sum_k tau[i][k] (U[k] or -i U[k] by the
+ *   parity of i + k).
+ * Block = (tile, slice of <= 16 combos sharing z, m) with 8 q x 3 ch x 16
+ * combos = 384 threads; tau rows are read as float4/double2 chunks that
+ * lanes of the same q share.  One launch per NB covers the m with
+ * n in (NB - 4, NB]. */
+template <typename S, int NB>
+__global__ void __launch_bounds__(384)
+k_translate_col(const typename Cx<S>::T *__restrict__ U, const S *__restrict__ tau,
+                const int32_t *__restrict__ combo_zbg, const int32_t *__restrict__ slices, int nslice, int cbase,
+                int ncombo, int L, int nzt, int m_lo, int nm, typename Cx<S>::T *__restrict__ R)
+{
+	typedef typename Cx<S>::T V;
+	extern __shared__ __align__(16) unsigned char tcs_raw[];
+	S *ts = reinterpret_cast<S *>(tcs_raw);   /* [8 q][NB i][NB k] (+ pad per q) */
+	const int qstride = NB * NB + 4;
+	int K = L + 1, N = 2 * L + 1, NP = K * (K + 1) / 2, nrow = K * N;
+	int bid = blockIdx.x;
+	int mi = bid % nm;
+	bid /= nm;
+	int si = bid % nslice, t = bid / nslice;
+	int m = m_lo + mi, n = K - m;
+	int cfirst = slices[2 * si] - cbase, nc = slices[2 * si + 1];
+	int zi = combo_zbg[3 * cfirst];
+	const S *tz = tau + ((((size_t)t * nzt + zi) * K + m) * K) * K * SXS_QT;
+	for (int k = threadIdx.x; k < SXS_QT * NB * NB; k += blockDim.x) {
+		int q = k % SXS_QT, r = k / SXS_QT;
+		int i = r / NB, kk = r % NB;
+		S v = 0;
+		if (i < n && kk < n) v = tz[((size_t)(m + i) * K + m + kk) * SXS_QT + q];
+		ts[q * qstride + i * NB + kk] = v;
+	}
+	__syncthreads();
+	int q = threadIdx.x % SXS_QT, ch = (threadIdx.x / SXS_QT) % 3, cl = threadIdx.x / (3 * SXS_QT);
+	if (cl >= nc) return;
+	int c = cfirst + cl;
+	int b2 = combo_zbg[3 * c + 1], g2 = combo_zbg[3 * c + 2];
+	int po = psym(m, K);
+	const V *Ub = U + (((size_t)t * nrow + b2 * N + g2) * NP + po) * 3 * SXS_QT + ch * SXS_QT + q;
+	V u[NB];
 #pragma unroll
-			for (int ch = 0; ch < 3; ch++) st2(o + ch * SXS_QT, acc[i][ch][0], acc[i][ch][1]);
+	for (int k = 0; k < NB; k++) u[k] = k < n ? Ub[(size_t)k * 3 * SXS_QT] : zero2<V>();
+	const S *tq = ts + q * qstride;
+	V *Rb = R + (((size_t)t * ncombo + c) * NP + po) * 3 * SXS_QT + ch * SXS_QT + q;
+	for (int i = 0; i < n; i++) {
+		const S *row = tq + i * NB;
+		V acc = zero2<V>();
+		int par = i & 1;
+#pragma unroll
+		for (int k4 = 0; k4 < NB; k4 += 4) {
+			S tv[4];
+			ld4(row + k4, tv);
+#pragma unroll
+			for (int kk = 0; kk < 4; kk++) {
+				int k = k4 + kk;
+				/* even i + k: tau U; odd: tau (-i U) */
+				if ((kk & 1) == par) { acc.x += tv[kk] * u[k].x; acc.y += tv[kk] * u[k].y; }
+				else { acc.x += tv[kk] * u[k].y; acc.y -= tv[kk] * u[k].x; }
+			}
 		}
+		Rb[(size_t)i * 3 * SXS_QT] = acc;
 	}
 }
 
@@ -476,6 +566,81 @@ inline int qthreads(int Q) { return ((Q + 31) / 32) * 32; }
 
 } // namespace
 
+template <typename S, int NB>
+static cudaError_t translate_col_launch(const void *U, const void *tau, const int32_t *combo_zbg,
+                                        const int32_t *slices, int nslice, int cbase, int ncombo, int nzt, int NT,
+                                        int L, void *R, cudaStream_t s)
+{
+	typedef typename Cx<S>::T V;
+	int K = L + 1;
+	/* m with n = K - m in (NB - 4, NB] */
+	int m_hi = K - (NB - 3), m_lo = K - NB;
+	if (m_hi > L) m_hi = L;
+	if (m_lo < 0) m_lo = 0;
+	if (m_hi < m_lo) return cudaSuccess;
+	int nm = m_hi - m_lo + 1;
+	long nb = (long)NT * nslice * nm;
+	if (nb > 0x7fffffffL) return cudaErrorInvalidValue;
+	size_t smem = sizeof(S) * SXS_QT * (NB * NB + 4);
+	if (smem > 48 * 1024) {
+		cudaError_t e = cudaFuncSetAttribute(k_translate_col<S, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                                     (int)smem);
+		if (e != cudaSuccess) return e;
+	}
+	k_translate_col<S, NB><<<(unsigned)nb, 384, smem, s>>>((const V *)U, (const S *)tau, combo_zbg, slices, nslice,
+	                                                        cbase, ncombo, L, nzt, m_lo, nm, (V *)R);
+	return cudaGetLastError();
+}
+
+template <typename S>
+static cudaError_t translate_col_all(const void *U, const void *tau, const int32_t *combo_zbg, const int32_t *slices,
+                                     int nslice, int cbase, int ncombo, int nzt, int NT, int L, void *R,
+                                     cudaStream_t s)
+{
+	cudaError_t e = cudaSuccess;
+	if (!e) e = translate_col_launch<S, 4>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, s);
+	if (!e) e = translate_col_launch<S, 8>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, s);
+	if (!e) e = translate_col_launch<S, 12>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, s);
+	if (!e) e = translate_col_launch<S, 16>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, s);
+	if (!e) e = translate_col_launch<S, 20>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, s);
+	if (!e) e = translate_col_launch<S, 24>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, s);
+	if (!e) e = translate_col_launch<S, 28>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, s);
+	if (!e) e = translate_col_launch<S, 32>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, s);
+	return e;
+}
+
+static int translate_slices(const void *U, const void *tau, const int32_t *combo_zbg, const int32_t *slices, int nslice,
+                   int cbase, int ncombo, int nzt, int Q, int L, void *R, int fp32, cudaStream_t s)
+{
+	int K = L + 1, NT = (Q + SXS_QT - 1) / SXS_QT, NP = K * (K + 1) / 2;
+	long nb = (long)NT * nslice * ((NP + 31) / 32);
+	if (nb > 0x7fffffffL) return cudaErrorInvalidValue;
+	/* row stride of the staged tau, = 8 (mod 32) words so the 4 pairs of a
+	 * half warp hit distinct banks */
+	int ts = K * SXS_QT;
+	while (ts % 32 != 8) ts += SXS_QT;
+	size_t smem = (size_t)32 * ts * (fp32 ? sizeof(float) : sizeof(double));
+	if (fp32) {
+		if (smem > 48 * 1024) {
+			cudaError_t e = cudaFuncSetAttribute(k_translate<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			                                     (int)smem);
+			if (e != cudaSuccess) return e;
+		}
+		k_translate<float><<<(unsigned)nb, 128, smem, s>>>((const float2 *)U, (const float *)tau, combo_zbg, slices,
+		                                                    nslice, cbase, ncombo, L, nzt, ts, (float2 *)R);
+	} else {
+		if (smem > 48 * 1024) {
+			cudaError_t e = cudaFuncSetAttribute(k_translate<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			                                     (int)smem);
+			if (e != cudaSuccess) return e;
+		}
+		k_translate<double><<<(unsigned)nb, 128, smem, s>>>((const double2 *)U, (const double *)tau, combo_zbg,
+		                                                     slices, nslice, cbase, ncombo, L, nzt, ts,
+		                                                     (double2 *)R);
+	}
+	return cudaGetLastError();
+}
+
 extern "C" {
 
 int sxsk_spf_transpose(const double *flat, void *spf_t, int Q, int L, int fp32, cudaStream_t s)
@@ -503,20 +668,17 @@ int sxsk_to_float(const double *a, float *b, long n, cudaStream_t s)
 	return cudaGetLastError();
 }
 
-int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, int ncombo, int nzt, int Q, int L,
-                   void *R, int fp32, cudaStream_t s)
+int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, const int32_t *slices, int nslice,
+                   int cbase, int ncombo, int nzt, int Q, int L, void *R, int fp32, cudaStream_t s)
 {
-	if (ncombo <= 0) return 0;
+	if (nslice <= 0) return 0;
 	int NT = (Q + SXS_QT - 1) / SXS_QT;
-	long nb = (long)NT * (L + 1) * ((ncombo + 31) / 32);
-	if (nb > 0x7fffffffL) return cudaErrorInvalidValue;
-	if (fp32)
-		k_translate<float, 4><<<(unsigned)nb, 128, 0, s>>>((const float2 *)U, (const float *)tau, combo_zbg, ncombo, L,
-		                                                    nzt, (float2 *)R);
-	else
-		k_translate<double, 4><<<(unsigned)nb, 128, 0, s>>>((const double2 *)U, (const double *)tau, combo_zbg, ncombo,
-		                                                     L, nzt, (double2 *)R);
-	return cudaGetLastError();
+	if (L + 1 <= 32) {
+		if (fp32)
+			return translate_col_all<float>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, s);
+		return translate_col_all<double>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, s);
+	}
+	return translate_slices(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, Q, L, R, fp32, s);
 }
 
 int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, int ncombo, const void *P, const void *R,

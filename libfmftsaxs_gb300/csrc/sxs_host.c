@@ -161,6 +161,9 @@ void sxs_fit_constants(const double *q, const double *a, int Q, double *fc)
 }
 
 /* --------------------------------------------------------------- plan */
+/* combos per translation slice (a run of combos sharing z) */
+#define SXS_SLICE 16
+
 struct sxsg_plan {
 	int L, K, N, K2, Q, nz, n1, n2, precision;
 	const sxs_ltables *lt;
@@ -190,6 +193,8 @@ struct sxsg_plan {
 	int ncombo;
 	int32_t *h_combo, *d_combo; /* [ncombo][3]: tslot, b2, g2 */
 	int64_t *h_cstart;          /* [ncombo+1] first sorted pose of each combo */
+	int nslice;                 /* runs of <= SXS_SLICE combos sharing z */
+	int32_t *h_slices, *d_slices; /* [nslice][2]: first combo, count */
 	int nzt;                    /* touched z count */
 	double *h_zt, *d_zt;        /* touched z values */
 	double *d_bes;
@@ -213,7 +218,9 @@ struct sxsg_plan {
 
 static void plan_free_poses(sxsg_plan *p)
 {
-	free(p->h_poses); free(p->h_combo); free(p->h_cstart); free(p->h_zt);
+	free(p->h_poses); free(p->h_combo); free(p->h_cstart); free(p->h_zt); free(p->h_slices);
+	cudaFree(p->d_slices);
+	p->h_slices = NULL; p->d_slices = NULL; p->nslice = 0;
 	cudaFree(p->d_poses); cudaFree(p->d_combo); cudaFree(p->d_zt); cudaFree(p->d_bes); cudaFree(p->d_tau);
 	cudaFree(p->d_tauf);
 	p->h_poses = NULL; p->h_combo = NULL; p->h_cstart = NULL; p->h_zt = NULL;
@@ -449,6 +456,19 @@ int sxsg_plan_set_poses(sxsg_plan *p, const int64_t *index, int64_t n, int skip)
 	for (int64_t k = 0; k < nkey; k++)
 		if (cid[k] >= 0) p->h_cstart[c++] = pos[k];
 	p->h_cstart[ncombo] = n;
+	/* slices for the translation kernel */
+	p->h_slices = malloc(sizeof(int32_t) * 2 * (ncombo > 0 ? ncombo : 1));
+	p->nslice = 0;
+	for (int k = 0; k < ncombo; k++) {
+		int ns = p->nslice;
+		if (ns > 0 && p->h_slices[2 * ns - 1] < SXS_SLICE && p->h_combo[3 * (k - 1)] == p->h_combo[3 * k]) {
+			p->h_slices[2 * ns - 1]++;
+		} else {
+			p->h_slices[2 * ns] = k;
+			p->h_slices[2 * ns + 1] = 1;
+			p->nslice++;
+		}
+	}
 	for (int64_t i = 0; i < n; i++) {
 		int64_t dst = pos[key[i]]++;
 		sxsk_pose ps = tmp[i];
@@ -469,6 +489,9 @@ int sxsg_plan_set_poses(sxsg_plan *p, const int64_t *index, int64_t n, int skip)
 	if (!e && nzt > 0 && p->fp32) e = cudaMalloc((void **)&p->d_tauf, sizeof(float) * tau_n);
 	if (!e && n > 0) e = cudaMemcpyAsync(p->d_poses, p->h_poses, sizeof(sxsk_pose) * n, cudaMemcpyHostToDevice, p->s);
 	if (!e && ncombo > 0) e = cudaMemcpyAsync(p->d_combo, p->h_combo, sizeof(int32_t) * 3 * ncombo, cudaMemcpyHostToDevice, p->s);
+	if (!e) e = cudaMalloc((void **)&p->d_slices, sizeof(int32_t) * 2 * (p->nslice > 0 ? p->nslice : 1));
+	if (!e && p->nslice > 0)
+		e = cudaMemcpyAsync(p->d_slices, p->h_slices, sizeof(int32_t) * 2 * p->nslice, cudaMemcpyHostToDevice, p->s);
 	if (!e && nzt > 0) e = cudaMemcpyAsync(p->d_zt, p->h_zt, sizeof(double) * nzt, cudaMemcpyHostToDevice, p->s);
 	if (e) return sxs_cuda_fail(e, "sxsg_plan_set_poses upload");
 	size_t need = (size_t)nn;
@@ -564,31 +587,35 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 	SXS_CU(cudaEventRecord(p->ev[0], s));
 	if ((rc = plan_tables(p))) return rc;
 	SXS_CU(cudaEventRecord(p->ev[1], s));
-	/* translated table in chunks of combos that fit the budget */
+	/* translated table in chunks of whole slices that fit the budget */
 	size_t per_combo = (size_t)p->NP * 3 * 8 * p->NT * p->celem;
-	int64_t chunk = (int64_t)(p->r_budget / per_combo);
+	int64_t chunk = (int64_t)(p->r_budget / (per_combo * SXS_SLICE));   /* slices per chunk */
 	if (chunk < 1) chunk = 1;
 	int pipe = fit_mode == SXSG_FIT_GRID && p->ncombo > 0;
 	if (pipe) {
-		int64_t c = (p->ncombo + SXS_PIPE_CHUNKS - 1) / SXS_PIPE_CHUNKS;
+		int64_t c = (p->nslice + SXS_PIPE_CHUNKS - 1) / SXS_PIPE_CHUNKS;
 		if (c < chunk) chunk = c;
 	}
-	if (chunk > p->ncombo) chunk = p->ncombo;
-	int64_t nch = chunk > 0 ? (p->ncombo + chunk - 1) / chunk : 0;
+	if (chunk > p->nslice) chunk = p->nslice;
+	int64_t nch = chunk > 0 ? (p->nslice + chunk - 1) / chunk : 0;
 	if (nch > INT32_MAX / 5) return sxs_fail(-2, "sxsg_plan_run: too many chunks");
 	if ((rc = plan_events(p, (int)(5 * nch + 1)))) return rc;
-	if (chunk > 0 && p->R_combos < chunk) {
+	int64_t rcap = chunk * SXS_SLICE;
+	if (rcap > p->ncombo) rcap = p->ncombo;
+	if (rcap > 0 && p->R_combos < rcap) {
 		cudaFree(p->d_R);
 		p->d_R = NULL;
-		SXS_CU(cudaMalloc(&p->d_R, per_combo * chunk));
-		p->R_combos = chunk;
+		SXS_CU(cudaMalloc(&p->d_R, per_combo * rcap));
+		p->R_combos = rcap;
 	}
 	const void *tau = p->fp32 ? (const void *)p->d_tauf : (const void *)p->d_tau;
 	for (int64_t k = 0; k < nch; k++) {
-		int64_t c0 = k * chunk, c1 = c0 + chunk < p->ncombo ? c0 + chunk : p->ncombo;
+		int64_t s0 = k * chunk, s1 = s0 + chunk < p->nslice ? s0 + chunk : p->nslice;
+		int64_t c0 = p->h_slices[2 * s0], c1 = p->h_slices[2 * (s1 - 1)] + p->h_slices[2 * (s1 - 1) + 1];
 		cudaEvent_t *e = p->cev + 5 * k;
 		SXS_CU(cudaEventRecord(e[0], s));
-		SXS_K(sxsk_translate(p->d_U, tau, p->d_combo + 3 * c0, (int)(c1 - c0), p->nzt, Q, L, p->d_R, p->fp32, s));
+		SXS_K(sxsk_translate(p->d_U, tau, p->d_combo + 3 * c0, p->d_slices + 2 * s0, (int)(s1 - s0), (int)c0,
+		                     (int)(c1 - c0), p->nzt, Q, L, p->d_R, p->fp32, s));
 		SXS_CU(cudaEventRecord(e[1], s));
 		int64_t p0 = p->h_cstart[c0], p1 = p->h_cstart[c1];
 		SXS_K(sxsk_pose_cross(p->d_poses + p0, (int)(p1 - p0), (int)c0, (int)(c1 - c0), p->d_P, p->d_R, p->d_tw,
