@@ -266,6 +266,55 @@ int sxsg_plan_results(sxsg_plan *plan, double *chi, double *c1, double *c2, int3
 int sxsg_plan_timings(sxsg_plan *plan, double *ms5);
 void sxsg_plan_destroy(sxsg_plan *plan);
 
+/* ------------------------------------------------------------ serving
+ * A persistent pool of workers that keeps the GPU busy with many scoring
+ * jobs (the FFT-correlate work of sxs_compute_saxs_scores for one dimer
+ * each).  Jobs are admitted in arrival order as device memory frees up under
+ * an HBM cap, run concurrently on separate streams, and their results are
+ * bitwise those of the same job run alone.  Rotation tables of molecules
+ * with a nonzero key are cached on the device across jobs. */
+typedef struct sxsg_server sxsg_server;
+
+typedef struct {
+	const double *A, *B;          /* flat expansions [3][qnum][(L+1)^2][2] */
+	uint64_t keyA, keyB;          /* molecule keys for the table cache; 0 = not cached */
+	const double *qvals;
+	int qnum;
+	const double *zvals;
+	int znum;
+	int L;
+	const double *a;              /* binned experiment a[6 qnum], mult, peak */
+	double mult, peak;
+	const double *c1grid;         /* fit grid (grid fit) */
+	int n1;
+	const double *c2grid;
+	int n2;
+	const int64_t *index;         /* packed grid indices of the poses */
+	int64_t n;
+	int skip;
+	int fit_mode;                 /* SXSG_FIT_* */
+	int precision;                /* SXSG_FP64 or SXSG_MIXED */
+} sxsg_request;
+
+/* hbm_cap: device bytes the server may hold (0 = 90% of the free memory);
+ * max_active: jobs on the device at once (workers, 1..64). */
+int sxsg_server_create(sxsg_server **server, size_t hbm_cap, int max_active);
+/* Queue a job; every input is copied, so the caller may reuse its buffers.
+ * Returns the ticket (>= 0) or a negative error. */
+int64_t sxsg_server_submit(sxsg_server *server, const sxsg_request *request);
+/* 1 when the job is done, 0 while queued or running. */
+int sxsg_server_poll(sxsg_server *server, int64_t ticket);
+/* Block until the job is done and collect chi, c1, c2 [n] (any may be
+ * NULL) and ms3 = {queued, running, submit-to-done} milliseconds.  A ticket
+ * is collected once.  Returns the job's status (0 or the error of the run,
+ * with its message in sxsg_last_error). */
+int sxsg_server_wait(sxsg_server *server, int64_t ticket, double *chi, double *c1, double *c2, double *ms3);
+/* out8 = {jobs done, poses done, jobs queued, bytes held by running jobs,
+ * bytes of cached tables, cached tables, cache hits, cache misses} */
+int sxsg_server_stats(sxsg_server *server, double *out8);
+/* Finish every queued job, then release the workers and the cache. */
+void sxsg_server_destroy(sxsg_server *server);
+
 /* One-shot scoring from host buffers: plan, poses, run, results, release.
  * chi/c1/c2 may be NULL; cross [n][6][qnum] may be NULL. */
 int sxsg_score_flat(const double *A, const double *B, const double *qvals, int qnum, const double *zvals, int znum,

@@ -228,6 +228,81 @@ class Plan:
             pass
 
 
+class _Request(C.Structure):
+    _fields_ = [("A", C.c_void_p), ("B", C.c_void_p), ("keyA", C.c_uint64), ("keyB", C.c_uint64),
+                ("qvals", C.c_void_p), ("qnum", C.c_int), ("zvals", C.c_void_p), ("znum", C.c_int), ("L", C.c_int),
+                ("a", C.c_void_p), ("mult", C.c_double), ("peak", C.c_double), ("c1grid", C.c_void_p),
+                ("n1", C.c_int), ("c2grid", C.c_void_p), ("n2", C.c_int), ("index", C.c_void_p),
+                ("n", C.c_int64), ("skip", C.c_int), ("fit_mode", C.c_int), ("precision", C.c_int)]
+
+
+class Server:
+    """The serving loop (sxsg_server_*): jobs are admitted in arrival order
+    under an HBM cap, run concurrently on the device and keep molecule
+    rotation tables cached by key."""
+
+    def __init__(self, hbm_cap=0, max_active=4):
+        lib = load()
+        lib.sxsg_server_create.argtypes = [C.POINTER(C.c_void_p), C.c_size_t, C.c_int]
+        lib.sxsg_server_submit.argtypes = [C.c_void_p, C.POINTER(_Request)]
+        lib.sxsg_server_submit.restype = C.c_int64
+        lib.sxsg_server_poll.argtypes = [C.c_void_p, C.c_int64]
+        lib.sxsg_server_wait.argtypes = [C.c_void_p, C.c_int64] + [C.c_void_p] * 4
+        lib.sxsg_server_stats.argtypes = [C.c_void_p, C.c_void_p]
+        lib.sxsg_server_destroy.argtypes = [C.c_void_p]
+        lib.sxsg_server_destroy.restype = None
+        self.h = C.c_void_p()
+        _check(lib.sxsg_server_create(C.byref(self.h), int(hbm_cap), int(max_active)))
+        self.sizes = {}
+
+    def submit(self, A, B, qvals, zvals, L, a, mult, peak, index, c1grid=None, c2grid=None, skip=1, fit=FIT_GRID,
+               precision=MIXED, keyA=0, keyB=0):
+        A, B, q, z, a = f64(A), f64(B), f64(qvals), f64(zvals), f64(a)
+        c1 = f64(c1grid if c1grid is not None else np.zeros(0))
+        c2 = f64(c2grid if c2grid is not None else np.zeros(0))
+        idx = np.ascontiguousarray(index, dtype=np.int64)
+        r = _Request(A.ctypes.data, B.ctypes.data, int(keyA), int(keyB), q.ctypes.data, len(q), z.ctypes.data,
+                     len(z), int(L), a.ctypes.data, float(mult), float(peak), c1.ctypes.data if len(c1) else None,
+                     len(c1), c2.ctypes.data if len(c2) else None, len(c2), idx.ctypes.data if len(idx) else None,
+                     len(idx), int(skip), int(fit), int(precision))
+        t = load().sxsg_server_submit(self.h, C.byref(r))
+        if t < 0:
+            raise SxsError(last_error())
+        self.sizes[t] = len(idx)
+        return t
+
+    def done(self, ticket):
+        rc = load().sxsg_server_poll(self.h, ticket)
+        if rc < 0:
+            raise SxsError(last_error())
+        return bool(rc)
+
+    def wait(self, ticket):
+        """dict(chi, c1, c2, queued_ms, run_ms, latency_ms)"""
+        n = self.sizes.pop(ticket)
+        chi, c1, c2, ms = np.zeros(n), np.zeros(n), np.zeros(n), np.zeros(3)
+        _check(load().sxsg_server_wait(self.h, ticket, chi.ctypes.data, c1.ctypes.data, c2.ctypes.data,
+                                       ms.ctypes.data))
+        return dict(chi=chi, c1=c1, c2=c2, queued_ms=ms[0], run_ms=ms[1], latency_ms=ms[2])
+
+    def stats(self):
+        o = np.zeros(8)
+        _check(load().sxsg_server_stats(self.h, o.ctypes.data))
+        return dict(done=int(o[0]), poses=int(o[1]), queued=int(o[2]), running_bytes=int(o[3]),
+                    cache_bytes=int(o[4]), cache_entries=int(o[5]), cache_hits=int(o[6]), cache_misses=int(o[7]))
+
+    def close(self):
+        if self.h:
+            load().sxsg_server_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def profile_from_spf(spf, L, qvals, rm, c1, c2):
     """(I[Q], err[Q]) of one molecule (sxs_profile_from_spf on a flat expansion)."""
     q = f64(qvals)

@@ -185,6 +185,8 @@ struct sxsg_plan {
 	int NT;                     /* q tiles of 8 */
 	/* rotation tables (depend on the twiddle variant) */
 	void *d_P, *d_U;
+	int ext_tables;             /* P and U belong to the caller (serving cache) */
+	int P_valid, U_valid;       /* caller tables already hold this run's rows */
 	int tw_variant; /* -1 none, 0 simple_ft, 1 exact */
 	/* poses */
 	int64_t npose;
@@ -216,13 +218,21 @@ struct sxsg_plan {
 	double ms[5];
 };
 
+/* stream-ordered allocation on the plan's stream: plans on different
+ * streams (the serving loop) never synchronise the device through the
+ * allocator */
+static void pfree(const sxsg_plan *p, void *x)
+{
+	if (x) cudaFreeAsync(x, p->s);
+}
+
 static void plan_free_poses(sxsg_plan *p)
 {
 	free(p->h_poses); free(p->h_combo); free(p->h_cstart); free(p->h_zt); free(p->h_slices);
-	cudaFree(p->d_slices);
+	pfree(p, p->d_slices);
 	p->h_slices = NULL; p->d_slices = NULL; p->nslice = 0;
-	cudaFree(p->d_poses); cudaFree(p->d_combo); cudaFree(p->d_zt); cudaFree(p->d_bes); cudaFree(p->d_tau);
-	cudaFree(p->d_tauf);
+	pfree(p, p->d_poses); pfree(p, p->d_combo); pfree(p, p->d_zt); pfree(p, p->d_bes); pfree(p, p->d_tau);
+	pfree(p, p->d_tauf);
 	p->h_poses = NULL; p->h_combo = NULL; p->h_cstart = NULL; p->h_zt = NULL;
 	p->d_poses = NULL; p->d_combo = NULL; p->d_zt = NULL; p->d_bes = NULL; p->d_tau = NULL; p->d_tauf = NULL;
 	p->pose_cap = p->combo_cap = p->zt_cap = 0;
@@ -233,11 +243,15 @@ void sxsg_plan_destroy(sxsg_plan *p)
 	if (!p) return;
 	cudaStreamSynchronize(p->s);
 	plan_free_poses(p);
-	cudaFree(p->d_A); cudaFree(p->d_B); cudaFree(p->d_q); cudaFree(p->d_fc); cudaFree(p->d_a); cudaFree(p->d_gtab); cudaFree(p->d_gdf);
-	cudaFree(p->d_c1g); cudaFree(p->d_c2g); cudaFree(p->d_cst); cudaFree(p->d_At); cudaFree(p->d_Bt);
-	cudaFree(p->d_tw); cudaFree(p->d_P); cudaFree(p->d_U); cudaFree(p->d_R);
-	cudaFree(p->d_cross); cudaFree(p->d_chi); cudaFree(p->d_c1); cudaFree(p->d_c2); cudaFree(p->d_grid);
-	cudaFree(p->d_scaled); cudaFree(p->d_scale); cudaFree(p->d_cell); cudaFree(p->d_iters);
+	pfree(p, p->d_A); pfree(p, p->d_B); pfree(p, p->d_q); pfree(p, p->d_fc); pfree(p, p->d_a); pfree(p, p->d_gtab); pfree(p, p->d_gdf);
+	pfree(p, p->d_c1g); pfree(p, p->d_c2g); pfree(p, p->d_cst); pfree(p, p->d_At); pfree(p, p->d_Bt);
+	pfree(p, p->d_tw); pfree(p, p->d_R);
+	if (!p->ext_tables) {
+		pfree(p, p->d_P);
+		pfree(p, p->d_U);
+	}
+	pfree(p, p->d_cross); pfree(p, p->d_chi); pfree(p, p->d_c1); pfree(p, p->d_c2); pfree(p, p->d_grid);
+	pfree(p, p->d_scaled); pfree(p, p->d_scale); pfree(p, p->d_cell); pfree(p, p->d_iters);
 	for (int i = 0; i < 6; i++) if (p->ev[i]) cudaEventDestroy(p->ev[i]);
 	for (int i = 0; i < p->ncev; i++) cudaEventDestroy(p->cev[i]);
 	free(p->cev);
@@ -250,6 +264,13 @@ int sxsg_plan_create(sxsg_plan **out, const double *A, const double *B, const do
                      int nz, int L, const double *a, double mult, double peak, const double *c1g, int n1,
                      const double *c2g, int n2, int precision)
 {
+	return sxs_plan_create_on(out, A, B, q, Q, z, nz, L, a, mult, peak, c1g, n1, c2g, n2, precision, NULL, 0);
+}
+
+int sxs_plan_create_on(sxsg_plan **out, const double *A, const double *B, const double *q, int Q, const double *z,
+                       int nz, int L, const double *a, double mult, double peak, const double *c1g, int n1,
+                       const double *c2g, int n2, int precision, cudaStream_t stream, int ext_tables)
+{
 	if (!out || !A || !B || !q || Q <= 0 || Q > 1024 || !z || nz <= 0 || !a)
 		return sxs_fail(-2, "sxsg_plan_create: bad arguments (Q must be in [1, 1024])");
 	if ((n1 > 0 && !c1g) || (n2 > 0 && !c2g) || n1 < 0 || n2 < 0)
@@ -261,7 +282,8 @@ int sxsg_plan_create(sxsg_plan **out, const double *A, const double *B, const do
 	if (rc) return rc;
 	sxsg_plan *p = calloc(1, sizeof(*p));
 	p->L = L; p->K = L + 1; p->N = 2 * L + 1; p->K2 = p->K * p->K; p->Q = Q; p->nz = nz;
-	p->n1 = n1; p->n2 = n2; p->precision = precision; p->lt = lt; p->s = g_stream;
+	p->n1 = n1; p->n2 = n2; p->precision = precision; p->lt = lt; p->s = stream ? stream : g_stream;
+	p->ext_tables = ext_tables;
 	p->mult = mult; p->peak = peak; p->tw_variant = -1;
 	p->fp32 = precision == SXSG_MIXED;
 	p->celem = p->fp32 ? 2 * sizeof(float) : 2 * sizeof(double);
@@ -285,24 +307,26 @@ int sxsg_plan_create(sxsg_plan **out, const double *A, const double *B, const do
 		e = cudaGetDevice(&dev);
 		if (!e) e = cudaDeviceGetAttribute(&p->nsm, cudaDevAttrMultiProcessorCount, dev);
 	}
-	if (!e) e = cudaMalloc((void **)&p->d_A, sizeof(double) * spf_n);
-	if (!e) e = cudaMalloc((void **)&p->d_B, sizeof(double) * spf_n);
-	if (!e) e = cudaMalloc(&p->d_At, p->celem * spf_n / 2);
-	if (!e) e = cudaMalloc(&p->d_Bt, p->celem * spf_n / 2);
-	if (!e) e = cudaMalloc((void **)&p->d_q, sizeof(double) * Q);
-	if (!e) e = cudaMalloc((void **)&p->d_fc, sizeof(double) * 5 * Q);
-	if (!e) e = cudaMalloc((void **)&p->d_a, sizeof(double) * 6 * Q);
-	if (!e) e = cudaMalloc((void **)&p->d_cst, sizeof(double) * 6 * Q);
-	if (!e) e = cudaMalloc((void **)&p->d_tw, sizeof(double2) * p->N);
-	if (!e && n1 > 0) e = cudaMalloc((void **)&p->d_gtab, sizeof(double) * n1 * Q);
-	if (!e && n1 > 0) e = cudaMalloc((void **)&p->d_c1g, sizeof(double) * n1);
-	if (!e && n2 > 0) e = cudaMalloc((void **)&p->d_c2g, sizeof(double) * n2);
+	if (!e) e = cudaMallocAsync((void **)&p->d_A, sizeof(double) * spf_n, p->s);
+	if (!e) e = cudaMallocAsync((void **)&p->d_B, sizeof(double) * spf_n, p->s);
+	if (!e) e = cudaMallocAsync(&p->d_At, p->celem * spf_n / 2, p->s);
+	if (!e) e = cudaMallocAsync(&p->d_Bt, p->celem * spf_n / 2, p->s);
+	if (!e) e = cudaMallocAsync((void **)&p->d_q, sizeof(double) * Q, p->s);
+	if (!e) e = cudaMallocAsync((void **)&p->d_fc, sizeof(double) * 5 * Q, p->s);
+	if (!e) e = cudaMallocAsync((void **)&p->d_a, sizeof(double) * 6 * Q, p->s);
+	if (!e) e = cudaMallocAsync((void **)&p->d_cst, sizeof(double) * 6 * Q, p->s);
+	if (!e) e = cudaMallocAsync((void **)&p->d_tw, sizeof(double2) * p->N, p->s);
+	if (!e && n1 > 0) e = cudaMallocAsync((void **)&p->d_gtab, sizeof(double) * n1 * Q, p->s);
+	if (!e && n1 > 0) e = cudaMallocAsync((void **)&p->d_c1g, sizeof(double) * n1, p->s);
+	if (!e && n2 > 0) e = cudaMallocAsync((void **)&p->d_c2g, sizeof(double) * n2, p->s);
 	size_t rot_n = (size_t)p->NT * p->K * p->N * p->NP * 3 * 8;
-	if (!e) e = cudaMalloc(&p->d_P, p->celem * rot_n);
-	if (!e) e = cudaMalloc(&p->d_U, p->celem * rot_n);
-	/* q-tile padding stays zero */
-	if (!e) e = cudaMemsetAsync(p->d_P, 0, p->celem * rot_n, p->s);
-	if (!e) e = cudaMemsetAsync(p->d_U, 0, p->celem * rot_n, p->s);
+	if (!ext_tables) {
+		if (!e) e = cudaMallocAsync(&p->d_P, p->celem * rot_n, p->s);
+		if (!e) e = cudaMallocAsync(&p->d_U, p->celem * rot_n, p->s);
+		/* q-tile padding stays zero */
+		if (!e) e = cudaMemsetAsync(p->d_P, 0, p->celem * rot_n, p->s);
+		if (!e) e = cudaMemsetAsync(p->d_U, 0, p->celem * rot_n, p->s);
+	}
 	if (e) {
 		sxsg_plan_destroy(p);
 		return sxs_cuda_fail(e, "sxsg_plan_create allocation");
@@ -314,7 +338,7 @@ int sxsg_plan_create(sxsg_plan **out, const double *A, const double *B, const do
 	if (!e) {
 		double *fc = malloc(sizeof(double) * 5 * Q);
 		sxs_fit_constants(q, a, Q, fc);
-		e = cudaMemcpy(p->d_fc, fc, sizeof(double) * 5 * Q, cudaMemcpyHostToDevice);
+		e = cudaMemcpyAsync(p->d_fc, fc, sizeof(double) * 5 * Q, cudaMemcpyHostToDevice, p->s);
 		free(fc);
 	}
 	if (!e) e = cudaMemcpyAsync(p->d_a, a, sizeof(double) * 6 * Q, cudaMemcpyHostToDevice, s);
@@ -328,7 +352,7 @@ int sxsg_plan_create(sxsg_plan **out, const double *A, const double *B, const do
 			double c1c = c1 * c1 * c1;
 			for (int k = 0; k < Q; k++) g[(size_t)i * Q + k] = c1c * exp(corr * q[k] * q[k]);
 		}
-		e = cudaMemcpy(p->d_gtab, g, sizeof(double) * n1 * Q, cudaMemcpyHostToDevice);
+		e = cudaMemcpyAsync(p->d_gtab, g, sizeof(double) * n1 * Q, cudaMemcpyHostToDevice, p->s);
 		if (!e && p->fp32) {
 			float *gd = malloc(sizeof(float) * 2 * n1 * Q);
 			for (size_t k = 0; k < (size_t)n1 * Q; k++) {
@@ -336,8 +360,8 @@ int sxsg_plan_create(sxsg_plan **out, const double *A, const double *B, const do
 				gd[2 * k] = h;
 				gd[2 * k + 1] = (float)(g[k] - (double)h);
 			}
-			e = cudaMalloc((void **)&p->d_gdf, sizeof(float2) * n1 * Q);
-			if (!e) e = cudaMemcpy(p->d_gdf, gd, sizeof(float2) * n1 * Q, cudaMemcpyHostToDevice);
+			e = cudaMallocAsync((void **)&p->d_gdf, sizeof(float2) * n1 * Q, p->s);
+			if (!e) e = cudaMemcpyAsync(p->d_gdf, gd, sizeof(float2) * n1 * Q, cudaMemcpyHostToDevice, p->s);
 			free(gd);
 		}
 		free(g);
@@ -369,13 +393,13 @@ int sxsg_plan_set_budget(sxsg_plan *p, size_t bytes)
 	return 0;
 }
 
-static int grow(void **ptr, size_t *cap, size_t need, size_t elem)
+static int grow(sxsg_plan *p, void **ptr, size_t *cap, size_t need, size_t elem)
 {
 	if (*cap >= need && *ptr) return 0;
-	cudaFree(*ptr);
+	pfree(p, *ptr);
 	*ptr = NULL;
 	size_t n = need > 0 ? need : 1;
-	cudaError_t e = cudaMalloc(ptr, n * elem);
+	cudaError_t e = cudaMallocAsync(ptr, n * elem, p->s);
 	if (e) {
 		*cap = 0;
 		return sxs_cuda_fail(e, "device allocation");
@@ -480,34 +504,34 @@ int sxsg_plan_set_poses(sxsg_plan *p, const int64_t *index, int64_t n, int skip)
 	/* upload */
 	size_t nn = (size_t)(n > 0 ? n : 1);
 	int rc = 0;
-	cudaError_t e = cudaMalloc((void **)&p->d_poses, sizeof(sxsk_pose) * nn);
-	if (!e) e = cudaMalloc((void **)&p->d_combo, sizeof(int32_t) * 3 * (ncombo > 0 ? ncombo : 1));
-	if (!e) e = cudaMalloc((void **)&p->d_zt, sizeof(double) * (nzt > 0 ? nzt : 1));
-	if (!e && nzt > 0) e = cudaMalloc((void **)&p->d_bes, sizeof(double) * (size_t)nzt * p->Q * N);
+	cudaError_t e = cudaMallocAsync((void **)&p->d_poses, sizeof(sxsk_pose) * nn, p->s);
+	if (!e) e = cudaMallocAsync((void **)&p->d_combo, sizeof(int32_t) * 3 * (ncombo > 0 ? ncombo : 1), p->s);
+	if (!e) e = cudaMallocAsync((void **)&p->d_zt, sizeof(double) * (nzt > 0 ? nzt : 1), p->s);
+	if (!e && nzt > 0) e = cudaMallocAsync((void **)&p->d_bes, sizeof(double) * (size_t)nzt * p->Q * N, p->s);
 	size_t tau_n = (size_t)p->NT * nzt * p->K * p->K * p->K * 8;
-	if (!e && nzt > 0) e = cudaMalloc((void **)&p->d_tau, sizeof(double) * tau_n);
-	if (!e && nzt > 0 && p->fp32) e = cudaMalloc((void **)&p->d_tauf, sizeof(float) * tau_n);
+	if (!e && nzt > 0) e = cudaMallocAsync((void **)&p->d_tau, sizeof(double) * tau_n, p->s);
+	if (!e && nzt > 0 && p->fp32) e = cudaMallocAsync((void **)&p->d_tauf, sizeof(float) * tau_n, p->s);
 	if (!e && n > 0) e = cudaMemcpyAsync(p->d_poses, p->h_poses, sizeof(sxsk_pose) * n, cudaMemcpyHostToDevice, p->s);
 	if (!e && ncombo > 0) e = cudaMemcpyAsync(p->d_combo, p->h_combo, sizeof(int32_t) * 3 * ncombo, cudaMemcpyHostToDevice, p->s);
-	if (!e) e = cudaMalloc((void **)&p->d_slices, sizeof(int32_t) * 2 * (p->nslice > 0 ? p->nslice : 1));
+	if (!e) e = cudaMallocAsync((void **)&p->d_slices, sizeof(int32_t) * 2 * (p->nslice > 0 ? p->nslice : 1), p->s);
 	if (!e && p->nslice > 0)
 		e = cudaMemcpyAsync(p->d_slices, p->h_slices, sizeof(int32_t) * 2 * p->nslice, cudaMemcpyHostToDevice, p->s);
 	if (!e && nzt > 0) e = cudaMemcpyAsync(p->d_zt, p->h_zt, sizeof(double) * nzt, cudaMemcpyHostToDevice, p->s);
 	if (e) return sxs_cuda_fail(e, "sxsg_plan_set_poses upload");
 	size_t need = (size_t)nn;
-	if ((rc = grow((void **)&p->d_cross, &p->out_cap, need * 6 * p->Q, sizeof(double)))) return rc;
+	if ((rc = grow(p, (void **)&p->d_cross, &p->out_cap, need * 6 * p->Q, sizeof(double)))) return rc;
 	/* out_cap tracks d_cross in doubles; the per-pose vectors follow it */
-	cudaFree(p->d_chi); cudaFree(p->d_c1); cudaFree(p->d_c2); cudaFree(p->d_cell); cudaFree(p->d_scaled);
-	cudaFree(p->d_scale); cudaFree(p->d_iters); cudaFree(p->d_grid);
+	pfree(p, p->d_chi); pfree(p, p->d_c1); pfree(p, p->d_c2); pfree(p, p->d_cell); pfree(p, p->d_scaled);
+	pfree(p, p->d_scale); pfree(p, p->d_iters); pfree(p, p->d_grid);
 	p->d_chi = p->d_c1 = p->d_c2 = p->d_scaled = p->d_scale = p->d_grid = NULL;
 	p->d_cell = NULL; p->d_iters = NULL;
-	e = cudaMalloc((void **)&p->d_chi, sizeof(double) * nn);
-	if (!e) e = cudaMalloc((void **)&p->d_c1, sizeof(double) * nn);
-	if (!e) e = cudaMalloc((void **)&p->d_c2, sizeof(double) * nn);
-	if (!e) e = cudaMalloc((void **)&p->d_cell, sizeof(int32_t) * nn);
-	if (!e) e = cudaMalloc((void **)&p->d_scale, sizeof(double) * nn);
-	if (!e) e = cudaMalloc((void **)&p->d_iters, sizeof(int) * nn);
-	if (!e) e = cudaMalloc((void **)&p->d_scaled, sizeof(double) * nn * 6 * p->Q);
+	e = cudaMallocAsync((void **)&p->d_chi, sizeof(double) * nn, p->s);
+	if (!e) e = cudaMallocAsync((void **)&p->d_c1, sizeof(double) * nn, p->s);
+	if (!e) e = cudaMallocAsync((void **)&p->d_c2, sizeof(double) * nn, p->s);
+	if (!e) e = cudaMallocAsync((void **)&p->d_cell, sizeof(int32_t) * nn, p->s);
+	if (!e) e = cudaMallocAsync((void **)&p->d_scale, sizeof(double) * nn, p->s);
+	if (!e) e = cudaMallocAsync((void **)&p->d_iters, sizeof(int) * nn, p->s);
+	if (!e) e = cudaMallocAsync((void **)&p->d_scaled, sizeof(double) * nn * 6 * p->Q, p->s);
 	if (e) return sxs_cuda_fail(e, "sxsg_plan_set_poses outputs");
 	(void)L;
 	return 0;
@@ -523,12 +547,18 @@ static int plan_tables(sxsg_plan *p)
 	{
 		double *tw = malloc(sizeof(double) * 2 * N);
 		sxs_twiddles_host(N, variant, tw);
-		cudaError_t e = cudaMemcpy(p->d_tw, tw, sizeof(double2) * N, cudaMemcpyHostToDevice);
+		cudaError_t e = cudaMemcpyAsync(p->d_tw, tw, sizeof(double2) * N, cudaMemcpyHostToDevice, p->s);
 		free(tw);
 		if (e) return sxs_cuda_fail(e, "twiddle upload");
-		SXS_K(sxsk_rotate(p->d_At, p->lt->d_dtab, p->d_tw, Q, L, 0, p->d_P, p->fp32, s));
-		SXS_K(sxsk_rotate(p->d_Bt, p->lt->d_dtab, p->d_tw, Q, L, 1, p->d_U, p->fp32, s));
-		sxs_count_launches(2);
+		if (!p->ext_tables || !p->P_valid) {
+			SXS_K(sxsk_rotate(p->d_At, p->lt->d_dtab, p->d_tw, Q, L, 0, p->d_P, p->fp32, s));
+			sxs_count_launches(1);
+		}
+		if (!p->ext_tables || !p->U_valid) {
+			SXS_K(sxsk_rotate(p->d_Bt, p->lt->d_dtab, p->d_tw, Q, L, 1, p->d_U, p->fp32, s));
+			sxs_count_launches(1);
+		}
+		if (p->ext_tables) p->P_valid = p->U_valid = 1;
 		p->tw_variant = variant;
 	}
 	if (p->nzt > 0) {
@@ -603,9 +633,9 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 	int64_t rcap = chunk * SXS_SLICE;
 	if (rcap > p->ncombo) rcap = p->ncombo;
 	if (rcap > 0 && p->R_combos < rcap) {
-		cudaFree(p->d_R);
+		pfree(p, p->d_R);
 		p->d_R = NULL;
-		SXS_CU(cudaMalloc(&p->d_R, per_combo * rcap));
+		SXS_CU(cudaMallocAsync(&p->d_R, per_combo * rcap, p->s));
 		p->R_combos = rcap;
 	}
 	const void *tau = p->fp32 ? (const void *)p->d_tauf : (const void *)p->d_tau;
@@ -691,20 +721,20 @@ int sxsg_plan_results(sxsg_plan *p, double *chi, double *c1, double *c2, int32_t
 		if (p->n1 <= 0 || p->n2 <= 0) return sxs_fail(-2, "no fit grid in this plan");
 		size_t gn = n * p->n1 * p->n2;
 		double *d_g = NULL;
-		SXS_CU(cudaMalloc((void **)&d_g, sizeof(double) * gn));
+		SXS_CU(cudaMallocAsync((void **)&d_g, sizeof(double) * gn, p->s));
 		double *tc = NULL, *t1 = NULL, *t2 = NULL;
 		int32_t *tcell = NULL;
-		cudaError_t e = cudaMalloc((void **)&tc, sizeof(double) * n);
-		if (!e) e = cudaMalloc((void **)&t1, sizeof(double) * n);
-		if (!e) e = cudaMalloc((void **)&t2, sizeof(double) * n);
-		if (!e) e = cudaMalloc((void **)&tcell, sizeof(int32_t) * n);
+		cudaError_t e = cudaMallocAsync((void **)&tc, sizeof(double) * n, p->s);
+		if (!e) e = cudaMallocAsync((void **)&t1, sizeof(double) * n, p->s);
+		if (!e) e = cudaMallocAsync((void **)&t2, sizeof(double) * n, p->s);
+		if (!e) e = cudaMallocAsync((void **)&tcell, sizeof(int32_t) * n, p->s);
 		if (!e) {
 			e = (cudaError_t)plan_fit_grid(p, NULL, 0, (int)n, 0, tc, t1, t2, tcell, d_g, NULL, s);
 			sxs_count_launches(1);
 		}
 		if (!e) e = cudaMemcpyAsync(grid, d_g, sizeof(double) * gn, cudaMemcpyDeviceToHost, s);
 		if (!e) e = cudaStreamSynchronize(s);
-		cudaFree(d_g); cudaFree(tc); cudaFree(t1); cudaFree(t2); cudaFree(tcell);
+		pfree(p, d_g); pfree(p, tc); pfree(p, t1); pfree(p, t2); pfree(p, tcell);
 		if (e) return sxs_cuda_fail(e, "grid results");
 	}
 	SXS_CU(cudaStreamSynchronize(s));
@@ -730,6 +760,46 @@ int sxsg_score_flat(const double *A, const double *B, const double *q, int Q, co
 	if (!rc) rc = sxsg_plan_results(p, chi, c1, c2, NULL, cross, NULL);
 	sxsg_plan_destroy(p);
 	return rc;
+}
+
+/* Caller-owned rotation tables for a plan created with ext_tables (the
+ * serving cache): P and U of sxs_plan_table_bytes each, zero-filled by the
+ * owner; *_valid says whether they already hold this plan's rows (same
+ * molecule, L, q grid, twiddle variant and precision). */
+void sxs_plan_set_tables(sxsg_plan *p, void *P, int P_valid, void *U, int U_valid)
+{
+	p->d_P = P;
+	p->d_U = U;
+	p->P_valid = P_valid;
+	p->U_valid = U_valid;
+}
+
+size_t sxs_plan_table_bytes(int L, int Q, int precision)
+{
+	size_t K = L + 1, N = 2 * L + 1, NP = K * (K + 1) / 2, NT = (Q + 7) / 8;
+	return NT * K * N * NP * 3 * 8 * (precision == SXSG_MIXED ? 2 * sizeof(float) : 2 * sizeof(double));
+}
+
+/* Device bytes of a plan besides its rotation tables and translated-table
+ * chunk: molecules, per-z tables for nzt touched z, pose lists and outputs. */
+size_t sxs_plan_base_bytes(int L, int Q, int nzt, int64_t npose, int n1, int precision)
+{
+	size_t K = L + 1, N = 2 * L + 1, NT = (Q + 7) / 8, K2 = K * K;
+	size_t celem = precision == SXSG_MIXED ? 8 : 16;
+	size_t spf = (size_t)3 * Q * K2;
+	size_t b = spf * (16 * 2 + celem * 2);                       /* A, B, At, Bt */
+	b += (size_t)nzt * Q * N * 8;                                /* Bessel */
+	b += NT * nzt * K * K * K * 8 * (precision == SXSG_MIXED ? 12 : 8); /* tau */
+	b += (size_t)npose * (sizeof(sxsk_pose) + 12 * Q * 8 + 40);  /* poses, cross, scaled, outputs */
+	b += (size_t)n1 * Q * 16 + (size_t)64 * Q + (1 << 20);
+	return b;
+}
+
+/* bytes of one combo of the translated table */
+size_t sxs_plan_combo_bytes(int L, int Q, int precision)
+{
+	size_t K = L + 1, NP = K * (K + 1) / 2, NT = (Q + 7) / 8;
+	return NP * 3 * 8 * NT * (precision == SXSG_MIXED ? 8 : 16);
 }
 
 /* ------------------------------------------------------------ timing */

@@ -63,6 +63,16 @@ typedef struct {
 } sxs_ltables;
 int sxs_ltables_get(int L, const sxs_ltables **out);
 
+/* plans for the serving loop: on a caller stream (NULL = the library's),
+ * with caller-owned rotation tables when ext_tables != 0 */
+int sxs_plan_create_on(sxsg_plan **out, const double *A, const double *B, const double *q, int Q, const double *z,
+                       int nz, int L, const double *a, double mult, double peak, const double *c1g, int n1,
+                       const double *c2g, int n2, int precision, cudaStream_t stream, int ext_tables);
+void sxs_plan_set_tables(sxsg_plan *p, void *P, int P_valid, void *U, int U_valid);
+size_t sxs_plan_table_bytes(int L, int Q, int precision);
+size_t sxs_plan_base_bytes(int L, int Q, int nzt, int64_t npose, int n1, int precision);
+size_t sxs_plan_combo_bytes(int L, int Q, int precision);
+
 /* per-q constants of the grid fit: fc[Q][5] */
 void sxs_fit_constants(const double *q, const double *a, int Q, double *fc);
 
