@@ -129,23 +129,26 @@ class Clocks:
 
 
 # ---------------------------------------------------------------- GPU side
-# DRAM bytes per pose of k_pose_cross from the ncu capture summarised in
-# profiles/k_pose_cross_c1_fp64.md (1.228 GB read + 4 MB written for 318
-# poses); the traffic of a launch scales with its pose count.
-TRAFFIC_PER_POSE = {"c1": 3.873e6}
+# DRAM bytes per pose of the dominant kernel from ncu captures of the same
+# kernel on a smaller pose list of this workload (profiles/): the traffic of
+# a launch scales with the poses it processes.
+TRAFFIC_PER_POSE = {("c1", "mixed"): 2.444e5, ("c1", "fp64"): 3.873e6}
 
 
-def pose_flops(L, Q):
-    """Algorithmic FLOPs of the per-pose contraction for one pose: for each
-    q, 9 complex multiply-adds (the 3x3 channel products) per (m, l) pair,
-    (L+1)^2 pairs, 8 FLOPs per complex multiply-add."""
-    return Q * (L + 1) ** 2 * 9 * 8
+def pose_flops(L, Q, precision):
+    """Algorithmic FLOPs of the per-pose contraction for one pose, over the
+    (L+1)(L+2)/2 pairs (m >= 0, l >= m) and Q q values.  Mixed path: the
+    phase w_m applied to the 3 channels of R (3 complex multiplies, 18
+    FLOPs) and the real parts of the 9 channel products (36 FLOPs).  Plain
+    path: the 9 complex multiply-adds (72 FLOPs) of the same contraction."""
+    NP = (L + 1) * (L + 2) // 2
+    return Q * NP * (54 if precision == "mixed" else 72)
 
 
 def reference_flops(w):
     """F_ref of the reference algorithm on this pose list: per touched
-    (z, b1, b2) triple 72 Q N S(L) (sum2) + 30 Q N^3 log2 N (6-channel DFT),
-    per touched (z, b2) 24 Q sum_{m,m2} sum_{l>=|m|} (K - max(|m|,|m2|,l))."""
+    (z, beta1, beta2) triple 72 Q N S(L) (sum2) + 30 Q N^3 log2 N (6-channel DFT),
+    per touched (z, beta2) 24 Q sum_{m,m2} sum_{l>=|m|} (K - max(|m|,|m2|,l))."""
     from libfmftsaxs_gb300.workload import decode
     L, Q = w.L, w.Q
     K, N = L + 1, 2 * L + 1
@@ -156,6 +159,127 @@ def reference_flops(w):
     ntrip = len(np.unique((z * K + b1) * K + b2))
     nzb2 = len(np.unique(z * K + b2))
     return ntrip * (72.0 * Q * N * S + 30.0 * Q * N ** 3 * np.log2(N)) + nzb2 * 24.0 * Q * s1
+
+
+def time_plan(g, w, precision, args, clocks=None):
+    """K timed runs of a resident plan (inputs on the device); returns
+    (ms per run from events on the library stream, stage ms, launches, results)."""
+    plan = g.Plan(w.A, w.B, w.q, w.z, w.L, w.a, w.mult, w.peak, w.c1g, w.c2g, precision=precision)
+    if args.budget_gb:
+        plan.set_budget(int(args.budget_gb * 2 ** 30))
+    plan.set_poses(w.index, skip=1)
+    for _ in range(args.warmup):
+        plan.run(g.FIT_GRID)
+    l0 = g.launch_count()
+    stage = np.zeros(5)
+    ctx = clocks if clocks is not None else _Null()
+    with ctx:
+        g.timer_start()
+        for _ in range(args.steps):
+            plan.run(g.FIT_GRID)
+            t = plan.timings()
+            stage += np.array([t["tables"], t["translate"], t["pose"], t["fit"], t["total"]])
+        ms = g.timer_stop()
+    launches = g.launch_count() - l0
+    res = plan.results()
+    plan.close()
+    return ms / args.steps, stage / args.steps, launches, res
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        pass
+
+
+def accuracy(mix, ref, k=100):
+    rel = np.abs(mix["chi"] - ref["chi"]) / ref["chi"]
+    top_m = set(np.argsort(mix["chi"], kind="stable")[:k].tolist())
+    top_r = set(np.argsort(ref["chi"], kind="stable")[:k].tolist())
+    return {"vs": "FP64 GPU path (pinned to the reference at 1e-10)", "dchi_rel_max": float(rel.max()),
+            "dchi_rel_median": float(np.median(rel)), "bound": 1e-4, "top%d_overlap" % k: len(top_m & top_r) / k,
+            "same_cell": float(np.mean(mix["cell"] == ref["cell"]))}
+
+
+def run_serving(g, args):
+    """Serving scenario: Poisson arrivals of scoring requests (each one dimer
+    with its own lmax, q grid, experiment and pose list) into the serving
+    loop; latency = submit to results on the host."""
+    from libfmftsaxs_gb300 import synth, workload as wl
+    rng = np.random.default_rng(args.seed + 77)
+    nreq = max(1, int(round(args.serve_rate * args.serve_window)))
+    Ls, Qs = (10, 15, 20, 25, 30), (51, 101, 201)
+    nrec, nlig = 4, 4
+    def mol(lo, hi, seed):
+        na = int(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        return synth.make_molecule(na, 2.2 * (na / 8.0) ** 0.38, seed)   # Rg of a compact protein of na/8 residues
+    recs = [mol(500, 8000, 900 + i) for i in range(nrec)]
+    ligs = [mol(300, 5000, 950 + i) for i in range(nlig)]
+    recs = [m.translated(-m.center_of_extrema()).with_sasa() for m in recs]
+    ligs = [m.translated(-m.centroid()).with_sasa() for m in ligs]
+    expd = {}
+
+    def expansion(kind, i, L, Q):
+        key = (kind, i, L, Q)
+        if key not in expd:
+            m = (recs if kind == "r" else ligs)[i]
+            v, d = wl.form_factors(g, m)
+            q = g.mkarray(0.0, 0.5, Q)
+            expd[key] = g.expand(m.xyz, v, d, m.sasa, g.ff_water(), q, L)
+        return expd[key]
+
+    reqs, used_rec = [], []
+    for k in range(nreq):
+        if used_rec and rng.random() < 0.3:
+            ri, L, Q = used_rec[rng.integers(len(used_rec))]
+        else:
+            ri, L, Q = int(rng.integers(nrec)), int(rng.choice(Ls)), int(rng.choice(Qs))
+            used_rec.append((ri, L, Q))
+        li = int(rng.integers(nlig))
+        q = g.mkarray(0.0, 0.5, Q)
+        A, B = expansion("r", ri, L, Q), expansion("l", li, L, Q)
+        I, _ = g.profile_from_spf(A, L, q, 1.7, 1.0, 1.0)
+        exp = synth.noisy_experiment(q, I, 0.01, rng)
+        a, mult, peak = g.bin_experiment(exp[0], exp[1], exp[2], q, 1.7)
+        npose = int(np.exp(rng.uniform(np.log(args.serve_min_poses), np.log(args.serve_max_poses))))
+        z = np.arange(25.0, 46.0)
+        R = synth.random_rotations(npose, rng)
+        T = synth.random_translations(npose, 25.0, 45.0, rng)
+        idx, _ = g.poses_to_indices(R, T, z, L)
+        reqs.append(dict(A=A, B=B, qvals=q, zvals=z, L=L, a=a, mult=mult, peak=peak, index=idx,
+                         c1grid=synth.C1_GRID, c2grid=synth.C2_GRID, keyA=1000 * ri + 1, keyB=2000 * li + 2))
+    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, size=nreq))
+    out = {}
+    for prec, name in ((g.MIXED, "mixed"), (g.FP64, "fp64")):
+        if name == "fp64" and not args.serve_fp64:
+            continue
+        srv = g.Server(hbm_cap=int(args.serve_cap_gb * 2 ** 30), max_active=args.serve_active)
+        t0 = time.perf_counter()
+        tickets = []
+        for r, ta in zip(reqs, arrivals):
+            dt = ta - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            tickets.append(srv.submit(precision=prec, **r))
+        lat = np.array([srv.wait(t)["latency_ms"] for t in tickets])
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        poses = sum(len(r["index"]) for r in reqs)
+        out[name] = {"p50_ms": float(np.percentile(lat, 50)), "p95_ms": float(np.percentile(lat, 95)),
+                     "p99_ms": float(np.percentile(lat, 99)), "poses_per_s": poses / wall,
+                     "requests_per_s": nreq / wall, "cache_hits": st["cache_hits"],
+                     "cache_misses": st["cache_misses"]}
+    out["scenario"] = ("%d requests, Poisson arrivals at %.0f/s; each one dimer: receptor %d-%d atoms, ligand %d-%d "
+                       "(pools of %d and %d molecules, 30%% of requests reuse a served receptor), L in %s, Q in %s, "
+                       "%d-%d poses log-uniform, |t| in [25,45] A, grid fit 11x41; up to %d jobs on the device "
+                       "under a %.0f GB cap"
+                       % (nreq, args.serve_rate, min(r.natoms for r in recs), max(r.natoms for r in recs),
+                          min(m.natoms for m in ligs), max(m.natoms for m in ligs), nrec, nlig, list(Ls), list(Qs),
+                          args.serve_min_poses, args.serve_max_poses, args.serve_active, args.serve_cap_gb))
+    return out
 
 
 def run_ours(args):
@@ -175,68 +299,75 @@ def run_ours(args):
     workers = max(1, min(os.cpu_count() or 1, 16))
     cpu_rate, cpu_n, cpu_wall = cpu_sample(w, kind, workers) if not args.skip_cpu else (None, 0, 0)
 
-    prec = g.MIXED if args.precision == "mixed" else g.FP64
-    plan = g.Plan(w.A, w.B, w.q, w.z, w.L, w.a, w.mult, w.peak, w.c1g, w.c2g, precision=prec)
-    if args.budget_gb:
-        plan.set_budget(int(args.budget_gb * 2 ** 30))
-    plan.set_poses(w.index, skip=1)
-    for _ in range(args.warmup):
-        plan.run(g.FIT_GRID)
     fp64_peak = max(g.fp64_fma_tflops() for _ in range(3))
-    l0 = g.launch_count()
-    with Clocks() as clk:
-        g.timer_start()
-        stage = np.zeros(5)
-        for _ in range(args.steps):
-            plan.run(g.FIT_GRID)
-            t = plan.timings()
-            stage += np.array([t["tables"], t["translate"], t["pose"], t["fit"], t["total"]])
-        ms = g.timer_stop()
-    launches = g.launch_count() - l0
-    clocks = clk.summary()
-    value = n * args.steps / (ms * 1e-3)
-    stage /= args.steps
+    fp32_peak = max(g.fp32_fma_tflops() for _ in range(3))
+    head = args.precision
+    prec = {"mixed": g.MIXED, "fp64": g.FP64}
+    runs = {}
+    for name in (["fp64", "mixed"] if head == "mixed" else ["fp64"]):
+        if name == head:
+            with Clocks() as clk:
+                runs[name] = time_plan(g, w, prec[name], args)
+            clocks = clk.summary()
+        else:
+            runs[name] = time_plan(g, w, prec[name], args)
+    ms, stage, launches, res = runs[head]
+    value = n / (ms * 1e-3)
 
     # end to end through the one-shot C-ABI call from host buffers
     idx = np.ascontiguousarray(w.index, dtype=np.int64)
     e2e_s = float("nan")
     if not args.skip_e2e:
-        g.score_flat(w.A, w.B, w.q, w.z, w.L, idx, w.a, w.mult, w.peak, 1, g.FIT_GRID, w.c1g, w.c2g)
+        g.score_flat(w.A, w.B, w.q, w.z, w.L, idx, w.a, w.mult, w.peak, 1, g.FIT_GRID, w.c1g, w.c2g,
+                     precision=prec[head])
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            g.score_flat(w.A, w.B, w.q, w.z, w.L, idx, w.a, w.mult, w.peak, 1, g.FIT_GRID, w.c1g, w.c2g)
+            g.score_flat(w.A, w.B, w.q, w.z, w.L, idx, w.a, w.mult, w.peak, 1, g.FIT_GRID, w.c1g, w.c2g,
+                         precision=prec[head])
         e2e_s = (time.perf_counter() - t0) / args.steps
     h2d = w.A.nbytes + w.B.nbytes + w.q.nbytes + w.z.nbytes + w.a.nbytes + idx.nbytes + w.c1g.nbytes + w.c2g.nbytes
     d2h = 3 * 8 * n
 
-    pf = pose_flops(w.L, w.Q) * n
+    pf = pose_flops(w.L, w.Q, head) * n
     achieved = pf / (stage[2] * 1e-3) / 1e12
+    peak = fp32_peak if head == "mixed" else fp64_peak
     fref = reference_flops(w)
+    nchunks = 8
+    tkey = (args.config, head)
+    traffic = TRAFFIC_PER_POSE[tkey] * n / nchunks if tkey in TRAFFIC_PER_POSE else None
     out = {
-        "metric": "poses/s @lmax=20 (FP64 plain GPU path, grid fit)",
+        "metric": "poses/s @lmax=20 (%s GPU path, grid fit)" % ("mixed-precision" if head == "mixed" else "FP64 plain"),
         "value": value,
         "unit": "poses/s",
         "n_gpus": 1,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": ms / args.steps,
+        "ms_per_step": ms,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64",
+        "dtype": "f32+f64" if head == "mixed" else "f64",
         "data": "synthetic (seeded random-walk dimers, poses and noisy experiment)",
         "config": {"workload": "%s: receptor %d / ligand %d atoms, L=%d, Q=%d, %d poses, fit grid %dx%d"
                                % (args.config, w.rec.natoms, w.lig.natoms, w.L, w.Q, n, len(w.c1g), len(w.c2g)),
-                   "precision": "fp64", "skip": 1,
-                   "l2": "inputs larger than L2 (rotation/translation tables of several GB per step)"},
-        "stages_ms": {"tables": stage[0], "translate": stage[1], "pose": stage[2], "fit": stage[3]},
+                   "precision": head, "skip": 1,
+                   "l2": "inputs larger than L2 (rotation tables of ~1 GB and translated tables of several GB per step)"},
+        "stages_ms": {"tables": stage[0], "translate": stage[1], "pose": stage[2], "fit": stage[3],
+                      "note": "per-chunk stage times on two streams; the fit of one chunk overlaps the next chunk"},
+        "fp64": {"value": n / (runs["fp64"][0] * 1e-3), "unit": "poses/s", "ms_per_step": runs["fp64"][0],
+                 "stages_ms": dict(zip(("tables", "translate", "pose", "fit"), runs["fp64"][1][:4].tolist()))},
         "reference_flops_per_step": fref,
-        "reference_equiv_tflops": fref / (ms / args.steps * 1e-3) / 1e12,
-        "roofline": {"bound": "fp64", "kernel": "k_pose_cross", "achieved": achieved, "peak": fp64_peak,
-                     "unit": "TFLOP/s", "frac": achieved / fp64_peak if fp64_peak > 0 else None,
-                     "traffic": TRAFFIC_PER_POSE[args.config] * n if args.config in TRAFFIC_PER_POSE else None,
-                     "traffic_source": "ncu capture of 318 poses, scaled by poses per launch",
-                     "peak_source": "measured in this run: register-resident FP64 FMA chains on every SM"},
+        "reference_equiv_tflops": fref / (ms * 1e-3) / 1e12,
+        "roofline": {"bound": "fp32" if head == "mixed" else "fp64",
+                     "kernel": "k_pose_cross<%s>" % ("float" if head == "mixed" else "double"),
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak if peak > 0 else None,
+                     "traffic": traffic,
+                     "traffic_source": "ncu DRAM read+write per pose of the same kernel on a smaller pose list, "
+                                       "scaled to the poses of one launch (one of %d chunks)" % nchunks,
+                     "hbm_frac": (traffic * nchunks / (stage[2] * 1e-3) / 1e9 / 6773.5) if traffic else None,
+                     "peak_source": "measured in this run: register-resident %s FMA chains on every SM"
+                                    % ("FP32" if head == "mixed" else "FP64")},
         "cpu_baseline": {"value": cpu_rate, "unit": "poses/s", "cores": workers, "kind": kind,
                          "sample": "%d poses of %d (z,beta1,beta2) triples, one triple per process, grid fit"
                                    % (cpu_n, workers)},
@@ -244,6 +375,10 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "clocks": clocks,
     }
+    if head == "mixed":
+        out["accuracy"] = accuracy(res, runs["fp64"][3])
+    if not args.skip_serve:
+        out["serving"] = run_serving(g, args)
     print(json.dumps(out))
 
 
@@ -293,6 +428,14 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true", help="no CPU baseline sample")
     ap.add_argument("--skip-e2e", action="store_true", help="no end-to-end timing")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--skip-serve", action="store_true", help="no serving scenario")
+    ap.add_argument("--serve-rate", type=float, default=50.0, help="serving: mean arrivals per second")
+    ap.add_argument("--serve-window", type=float, default=2.0, help="serving: seconds of arrivals")
+    ap.add_argument("--serve-min-poses", type=int, default=5000)
+    ap.add_argument("--serve-max-poses", type=int, default=50000)
+    ap.add_argument("--serve-active", type=int, default=4, help="serving: jobs on the device at once")
+    ap.add_argument("--serve-cap-gb", type=float, default=150.0, help="serving: HBM cap")
+    ap.add_argument("--serve-fp64", action="store_true", help="serving: also run the FP64 path")
     args = ap.parse_args()
     if args.gpus > 1 and int(os.environ.get("RANK", "0")) != 0:
         return  # the path does not shard: one GPU runs, other ranks idle

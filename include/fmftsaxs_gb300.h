@@ -316,11 +316,12 @@ int sxsg_server_stats(sxsg_server *server, double *out8);
 void sxsg_server_destroy(sxsg_server *server);
 
 /* One-shot scoring from host buffers: plan, poses, run, results, release.
- * chi/c1/c2 may be NULL; cross [n][6][qnum] may be NULL. */
+ * chi/c1/c2 may be NULL; cross [n][6][qnum] may be NULL; precision is
+ * SXSG_FP64 or SXSG_MIXED. */
 int sxsg_score_flat(const double *A, const double *B, const double *qvals, int qnum, const double *zvals, int znum,
                     int L, const int64_t *index, int64_t n, int skip, const double *a, double mult, double peak,
                     int fit_mode, const double *c1grid, int n1, const double *c2grid, int n2,
-                    double *chi, double *c1, double *c2, double *cross);
+                    double *chi, double *c1, double *c2, double *cross, int precision);
 
 /* Pose ingestion helpers (tools/correlate.c:202-240): grid index of one
  * Euler 6-tuple (z, b1, g1, a2, b2, g2 as written by sxs_ft2euler) at
@@ -346,6 +347,8 @@ double sxsg_timer_stop(void);
 /* Dense FP64 multiply-add rate of this GPU (TFLOP/s), measured with a
  * register-resident FMA chain on every SM. */
 double sxsg_fp64_fma_tflops(void);
+/* Dense FP32 multiply-add rate of this GPU (TFLOP/s), measured the same way. */
+double sxsg_fp32_fma_tflops(void);
 
 #ifdef __cplusplus
 }

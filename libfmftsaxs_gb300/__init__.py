@@ -330,7 +330,7 @@ def poses_to_indices(rot, tr, zvals, L, ref_lig=(0.0, 0.0, 0.0)):
 
 
 def score_flat(A, B, qvals, zvals, L, index, a, mult, peak, skip=1, fit=FIT_GRID, c1grid=None, c2grid=None,
-               cross=False):
+               cross=False, precision=FP64):
     """One-shot scoring from host buffers (sxsg_score_flat)."""
     A, B, q, z, a = f64(A), f64(B), f64(qvals), f64(zvals), f64(a)
     idx = np.ascontiguousarray(index, dtype=np.int64)
@@ -342,12 +342,13 @@ def score_flat(A, B, qvals, zvals, L, index, a, mult, peak, skip=1, fit=FIT_GRID
     lib = load()
     lib.sxsg_score_flat.argtypes = [C.c_void_p] * 3 + [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int64,
                                     C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_int,
-                                    C.c_void_p, C.c_int] + [C.c_void_p] * 4
+                                    C.c_void_p, C.c_int] + [C.c_void_p] * 4 + [C.c_int]
     _check(lib.sxsg_score_flat(A.ctypes.data, B.ctypes.data, q.ctypes.data, len(q), z.ctypes.data, len(z), L,
                                idx.ctypes.data, n, skip, a.ctypes.data, mult, peak, fit,
                                c1g.ctypes.data if len(c1g) else None, len(c1g),
                                c2g.ctypes.data if len(c2g) else None, len(c2g),
-                               chi.ctypes.data, c1.ctypes.data, c2.ctypes.data, cr.ctypes.data if cross else None))
+                               chi.ctypes.data, c1.ctypes.data, c2.ctypes.data, cr.ctypes.data if cross else None,
+                               int(precision)))
     out = dict(chi=chi, c1=c1, c2=c2)
     if cross:
         out["cross"] = cr
@@ -371,3 +372,9 @@ def fp64_fma_tflops():
     lib = load()
     lib.sxsg_fp64_fma_tflops.restype = C.c_double
     return lib.sxsg_fp64_fma_tflops()
+
+
+def fp32_fma_tflops():
+    lib = load()
+    lib.sxsg_fp32_fma_tflops.restype = C.c_double
+    return lib.sxsg_fp32_fma_tflops()

@@ -742,7 +742,47 @@ __global__ void k_fp64_probe(double *out, int iters)
 	double s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
 	if (s == 12345.678) out[threadIdx.x] = s; /* keeps the chains live */
 }
+/* FP32 FMA chains: 8 independent per thread, enough threads to fill every
+ * SM's FP32 pipes */
+__global__ void k_fp32_probe(float *out, int iters)
+{
+	float a[8];
+#pragma unroll
+	for (int k = 0; k < 8; k++) a[k] = threadIdx.x * 1e-6f + k * 1e-6f;
+	const float b = 0.9999999f, c = 1e-9f;
+	for (int i = 0; i < iters; i++) {
+#pragma unroll
+		for (int k = 0; k < 8; k++) a[k] = fmaf(a[k], b, c);
+	}
+	float s = a[0] + a[1] + a[2] + a[3] + a[4] + a[5] + a[6] + a[7];
+	if (s == 12345.678f) out[threadIdx.x] = s;
+}
 } // namespace
+
+extern "C" double sxsk_fp32_probe(cudaStream_t s)
+{
+	int dev = 0, nsm = 0;
+	cudaGetDevice(&dev);
+	cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+	float *out = NULL;
+	if (cudaMalloc((void **)&out, 1024 * sizeof(float)) != cudaSuccess) return -1.0;
+	int blocks = nsm * 8, threads = 256, iters = 65536;
+	k_fp32_probe<<<blocks, threads, 0, s>>>(out, 64);
+	cudaEvent_t e0, e1;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	cudaEventRecord(e0, s);
+	k_fp32_probe<<<blocks, threads, 0, s>>>(out, iters);
+	cudaEventRecord(e1, s);
+	cudaEventSynchronize(e1);
+	float ms = 0;
+	cudaEventElapsedTime(&ms, e0, e1);
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	cudaFree(out);
+	double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
+	return ms > 0 ? flops / (ms * 1e-3) / 1e12 : -1.0;
+}
 
 extern "C" double sxsk_fp64_probe(cudaStream_t s)
 {

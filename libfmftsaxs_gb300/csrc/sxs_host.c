@@ -751,10 +751,10 @@ int sxsg_plan_timings(sxsg_plan *p, double *ms5)
 int sxsg_score_flat(const double *A, const double *B, const double *q, int Q, const double *z, int nz, int L,
                     const int64_t *index, int64_t n, int skip, const double *a, double mult, double peak, int fit_mode,
                     const double *c1g, int n1, const double *c2g, int n2, double *chi, double *c1, double *c2,
-                    double *cross)
+                    double *cross, int precision)
 {
 	sxsg_plan *p = NULL;
-	int rc = sxsg_plan_create(&p, A, B, q, Q, z, nz, L, a, mult, peak, c1g, n1, c2g, n2, SXSG_FP64);
+	int rc = sxsg_plan_create(&p, A, B, q, Q, z, nz, L, a, mult, peak, c1g, n1, c2g, n2, precision);
 	if (!rc) rc = sxsg_plan_set_poses(p, index, n, skip);
 	if (!rc) rc = sxsg_plan_run(p, fit_mode);
 	if (!rc) rc = sxsg_plan_results(p, chi, c1, c2, NULL, cross, NULL);
@@ -827,6 +827,14 @@ double sxsg_timer_stop(void)
 	float ms = 0;
 	cudaEventElapsedTime(&ms, g_t0, g_t1);
 	return ms;
+}
+
+double sxsg_fp32_fma_tflops(void)
+{
+	if (sxs_ensure_init()) return -1.0;
+	extern double sxsk_fp32_probe(cudaStream_t s);
+	sxs_count_launches(2);
+	return sxsk_fp32_probe(g_stream);
 }
 
 double sxsg_fp64_fma_tflops(void)
