@@ -62,8 +62,8 @@ int sxsk_const_int(const double *A, const double *B, int Q, int L, double *cst, 
 
 /* rotation table, m >= 0: out[(b,g)][pair][ch][q] = sum_{m1} tw[(m1' g) mod N] d^l_{m m1}(beta_b) C[ch][l,m1][q]
  * with C = spf_t, conjugated when conj != 0. */
-int sxsk_rotate(const void *spf_t, const double *dtab, const double2 *tw, int Q, int L, int conj, void *out,
-                int fp32, cudaStream_t s);
+int sxsk_rotate(const void *spf_t, const void *dtab, const double2 *tw, int Q, int L, int conj, void *out,
+                int fp32, cudaStream_t s);   /* dtab in float when fp32 */
 
 /* translated ligand table for the combos of a run of slices, m >= 0, all q tiles:
  * R[t][c][pair(m,l)][ch][q] = sum_{l1>=m} conj(T[t][zi][m][l][l1][q]) U[t][(b2,g2)][pair(m,l1)][ch][q].

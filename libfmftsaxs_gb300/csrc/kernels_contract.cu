@@ -100,39 +100,74 @@ __device__ __forceinline__ void st2(double2 *p, double2 a, double2 b)
 	p[1] = b;
 }
 
-/* block = (b*N+g, m >= 0); threads over q.  Output in the q-tiled layout. */
+/* Rotation tables in the q-tiled layout:
+ *   out[t][b*N+g][pair(m,l)][ch][q] = sum_{m1=-l..l} tw[(m1' g) mod N] d^l_{m m1}(beta_b) C[ch][l,m1][q]
+ * (C = spf_t, conjugated when conj != 0).  Block = (b, m, QS q of a tile),
+ * thread = (g, q): the block stages its coefficients C[ch][l >= m][m1][QS q],
+ * the d row d^l_{m m1}(beta_b) and the twiddles in shared memory once and
+ * every gamma thread reuses them; the twiddle index (m1' g) mod N advances
+ * by g per m1. */
 template <typename S>
-__global__ void k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const double *__restrict__ dtab,
-                         const double2 *__restrict__ tw, int Q, int L, int conj, typename Cx<S>::T *__restrict__ out)
+__global__ void k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const S *__restrict__ dtab,
+                         const double2 *__restrict__ tw, int Q, int L, int conj, int QS,
+                         typename Cx<S>::T *__restrict__ out)
 {
 	typedef typename Cx<S>::T V;
-	int K = L + 1, N = 2 * L + 1, K2 = K * K, NP = K * (K + 1) / 2;
-	int nrow = K * N;
-	int bg = blockIdx.x, m = blockIdx.y;
-	int b = bg / N, g = bg % N;
-	int iq = threadIdx.x;
-	if (iq >= Q) return;
-	const double *db = dtab + (size_t)b * K * N * N;
+	extern __shared__ __align__(16) unsigned char rsm_raw[];
+	int K = L + 1, N = 2 * L + 1, K2 = K * K, NP = K * (K + 1) / 2, nrow = K * N;
+	int NT = (Q + SXS_QT - 1) / SXS_QT, nsub = SXS_QT / QS;
+	int bid = blockIdx.x;
+	int t = bid % (NT * nsub);
+	bid /= NT * nsub;
+	int q0 = t * QS;                         /* first q of the block */
+	t = q0 / SXS_QT;
+	int m = bid % K, b = bid / K;
+	int lm0 = m * m;                         /* first lm with l >= m */
+	int nlm = K2 - lm0;
+	V *cs = reinterpret_cast<V *>(rsm_raw);  /* [3][nlm][QS] */
+	V *ws = cs + 3 * nlm * QS;               /* [N] twiddles */
+	S *ds = reinterpret_cast<S *>(ws + N);   /* [nlm] d^l_{m m1}(beta_b), indexed like lm */
 	S sg = conj ? (S)-1 : (S)1;
+	for (int k = threadIdx.x; k < 3 * nlm * QS; k += blockDim.x) {
+		int qq = k % QS, r = k / QS;
+		int lm = lm0 + r % nlm, ch = r / nlm;
+		int q = q0 + qq;
+		V v = zero2<V>();
+		if (q < Q) {
+			v = spf_t[((size_t)ch * K2 + lm) * Q + q];
+			v.y *= sg;
+		}
+		cs[k] = v;
+	}
+	for (int k = threadIdx.x; k < N; k += blockDim.x) ws[k] = from2<V>(tw[k]);
+	for (int k = threadIdx.x; k < nlm; k += blockDim.x) {
+		int lm = lm0 + k;
+		int l = 0;
+		while ((l + 1) * (l + 1) <= lm) l++;
+		int m1 = lm - l * (l + 1);
+		ds[k] = dtab[(((size_t)b * K + l) * N + m + L) * N + m1 + L];
+	}
+	__syncthreads();
+	int g = threadIdx.x / QS, qq = threadIdx.x % QS;
+	if (g >= N) return;
 	int po = psym(m, K);
-	V *ob = out + (((size_t)(iq / SXS_QT) * nrow + bg) * NP + po) * 3 * SXS_QT + iq % SXS_QT;
+	V *ob = out + (((size_t)t * nrow + b * N + g) * NP + po) * 3 * SXS_QT + q0 % SXS_QT + qq;
 	for (int l = m; l <= L; l++) {
 		V acc0 = zero2<V>(), acc1 = acc0, acc2 = acc0;
-		const double *drow = db + ((size_t)l * N + m + L) * N;
-		for (int m1 = -l; m1 <= l; m1++) {
-			int e = ((m1 < 0 ? m1 + N : m1) * g) % N;
-			S dv = (S)drow[m1 + L];
+		int r0 = l * l - lm0;                /* lm = l^2 + (m1 + l) */
+		int e = ((N - l) * g) % N;           /* (m1' g) mod N at m1 = -l */
+		for (int j = 0; j < 2 * l + 1; j++) {
+			S dv = ds[r0 + j];
+			V w = ws[e];
 			V f;
-			f.x = (S)tw[e].x * dv;
-			f.y = (S)tw[e].y * dv;
-			int lm = lm_index(l, m1);
-			V c0 = spf_t[((size_t)0 * K2 + lm) * Q + iq];
-			V c1 = spf_t[((size_t)1 * K2 + lm) * Q + iq];
-			V c2 = spf_t[((size_t)2 * K2 + lm) * Q + iq];
-			c0.y *= sg; c1.y *= sg; c2.y *= sg;
-			cfma(acc0, f, c0);
-			cfma(acc1, f, c1);
-			cfma(acc2, f, c2);
+			f.x = w.x * dv;
+			f.y = w.y * dv;
+			const V *c = cs + (size_t)(r0 + j) * QS + qq;
+			cfma(acc0, f, c[0]);
+			cfma(acc1, f, c[(size_t)nlm * QS]);
+			cfma(acc2, f, c[(size_t)2 * nlm * QS]);
+			e += g;
+			if (e >= N) e -= N;
 		}
 		V *o = ob + (size_t)(l - m) * 3 * SXS_QT;
 		o[0] = acc0;
@@ -651,13 +686,40 @@ int sxsk_spf_transpose(const double *flat, void *spf_t, int Q, int L, int fp32, 
 	return cudaGetLastError();
 }
 
-int sxsk_rotate(const void *spf_t, const double *dtab, const double2 *tw, int Q, int L, int conj, void *out, int fp32,
+int sxsk_rotate(const void *spf_t, const void *dtab, const double2 *tw, int Q, int L, int conj, void *out, int fp32,
                 cudaStream_t s)
 {
-	int K = L + 1, N = 2 * L + 1;
-	dim3 grid(K * N, K);
-	if (fp32) k_rotate<float><<<grid, qthreads(Q), 0, s>>>((const float2 *)spf_t, dtab, tw, Q, L, conj, (float2 *)out);
-	else k_rotate<double><<<grid, qthreads(Q), 0, s>>>((const double2 *)spf_t, dtab, tw, Q, L, conj, (double2 *)out);
+	int K = L + 1, N = 2 * L + 1, NT = (Q + SXS_QT - 1) / SXS_QT;
+	size_t nlm = (size_t)K * K;  /* at m = 0, the largest */
+	size_t celem = fp32 ? sizeof(float2) : sizeof(double2);
+	/* q per block: the largest of 8, 4, 2, 1 whose staged coefficients fit */
+	int QS = SXS_QT;
+	size_t smem;
+	for (;;) {
+		smem = celem * (3 * nlm * QS + N) + (fp32 ? sizeof(float) : sizeof(double)) * nlm;
+		if (smem <= 200 * 1024 || QS == 1) break;
+		QS /= 2;
+	}
+	if (smem > 227 * 1024) return cudaErrorInvalidValue;
+	long nb = (long)K * K * NT * (SXS_QT / QS);
+	int threads = ((N * QS + 31) / 32) * 32;
+	if (fp32) {
+		if (smem > 48 * 1024) {
+			cudaError_t e = cudaFuncSetAttribute(k_rotate<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			                                     (int)smem);
+			if (e != cudaSuccess) return e;
+		}
+		k_rotate<float><<<(unsigned)nb, threads, smem, s>>>((const float2 *)spf_t, (const float *)dtab, tw, Q, L,
+		                                                    conj, QS, (float2 *)out);
+	} else {
+		if (smem > 48 * 1024) {
+			cudaError_t e = cudaFuncSetAttribute(k_rotate<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			                                     (int)smem);
+			if (e != cudaSuccess) return e;
+		}
+		k_rotate<double><<<(unsigned)nb, threads, smem, s>>>((const double2 *)spf_t, (const double *)dtab, tw, Q,
+		                                                     L, conj, QS, (double2 *)out);
+	}
 	return cudaGetLastError();
 }
 

@@ -550,12 +550,13 @@ static int plan_tables(sxsg_plan *p)
 		cudaError_t e = cudaMemcpyAsync(p->d_tw, tw, sizeof(double2) * N, cudaMemcpyHostToDevice, p->s);
 		free(tw);
 		if (e) return sxs_cuda_fail(e, "twiddle upload");
+		const void *dtab = p->fp32 ? (const void *)p->lt->d_dtabf : (const void *)p->lt->d_dtab;
 		if (!p->ext_tables || !p->P_valid) {
-			SXS_K(sxsk_rotate(p->d_At, p->lt->d_dtab, p->d_tw, Q, L, 0, p->d_P, p->fp32, s));
+			SXS_K(sxsk_rotate(p->d_At, dtab, p->d_tw, Q, L, 0, p->d_P, p->fp32, s));
 			sxs_count_launches(1);
 		}
 		if (!p->ext_tables || !p->U_valid) {
-			SXS_K(sxsk_rotate(p->d_Bt, p->lt->d_dtab, p->d_tw, Q, L, 1, p->d_U, p->fp32, s));
+			SXS_K(sxsk_rotate(p->d_Bt, dtab, p->d_tw, Q, L, 1, p->d_U, p->fp32, s));
 			sxs_count_launches(1);
 		}
 		if (p->ext_tables) p->P_valid = p->U_valid = 1;

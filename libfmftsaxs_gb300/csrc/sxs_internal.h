@@ -56,6 +56,7 @@ const double *sxs_dsymb_cached(int L);                    /* [K2][K][N], built o
 typedef struct {
 	int L;
 	double *d_dtab;   /* [K][K][N][N] */
+	float *d_dtabf;   /* the same in float (mixed-path rotation) */
 	double *d_dsymb;  /* [K2][K][N] */
 	double *d_ynorm;  /* [K][N] */
 	int2 *d_ll1;      /* (l, l1 >= l) pairs */

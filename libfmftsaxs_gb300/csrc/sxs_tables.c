@@ -283,16 +283,23 @@ int sxs_ltables_get(int L, const sxs_ltables **out)
 	t->nll1 = nll;
 	cudaError_t e = cudaSuccess;
 	if (e == cudaSuccess) e = cudaMalloc((void **)&t->d_dtab, sizeof(double) * dsz * K);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&t->d_dtabf, sizeof(float) * dsz * K);
 	if (e == cudaSuccess) e = cudaMalloc((void **)&t->d_dsymb, sizeof(double) * (size_t)K * K * K * N);
 	if (e == cudaSuccess) e = cudaMalloc((void **)&t->d_ynorm, sizeof(double) * K * N);
 	if (e == cudaSuccess) e = cudaMalloc((void **)&t->d_ll1, sizeof(int2) * nll);
 	if (e == cudaSuccess) e = cudaMemcpy(t->d_dtab, h_dt, sizeof(double) * dsz * K, cudaMemcpyHostToDevice);
+	if (e == cudaSuccess) {
+		float *h_df = malloc(sizeof(float) * dsz * K);
+		for (size_t i = 0; i < dsz * K; i++) h_df[i] = (float)h_dt[i];
+		e = cudaMemcpy(t->d_dtabf, h_df, sizeof(float) * dsz * K, cudaMemcpyHostToDevice);
+		free(h_df);
+	}
 	if (e == cudaSuccess) e = cudaMemcpy(t->d_dsymb, h_ds, sizeof(double) * (size_t)K * K * K * N, cudaMemcpyHostToDevice);
 	if (e == cudaSuccess) e = cudaMemcpy(t->d_ynorm, h_yn, sizeof(double) * K * N, cudaMemcpyHostToDevice);
 	if (e == cudaSuccess) e = cudaMemcpy(t->d_ll1, h_ll, sizeof(int2) * nll, cudaMemcpyHostToDevice);
 	free(h_dt); free(h_yn); free(h_ll);
 	if (e != cudaSuccess) {
-		cudaFree(t->d_dtab); cudaFree(t->d_dsymb); cudaFree(t->d_ynorm); cudaFree(t->d_ll1);
+		cudaFree(t->d_dtab); cudaFree(t->d_dtabf); cudaFree(t->d_dsymb); cudaFree(t->d_ynorm); cudaFree(t->d_ll1);
 		free(t);
 		pthread_mutex_unlock(&g_lt_lock);
 		return sxs_cuda_fail(e, "per-L table upload");
