@@ -591,7 +591,7 @@ static int plan_fit_grid(sxsg_plan *p, const sxsk_pose *order, int slot0, int ns
  * chunk (FP64 pipe) overlaps the contractions of the next (HBM / FP32). */
 #define SXS_PIPE_CHUNKS 8
 /* resident fit blocks per SM while it overlaps the contractions */
-#define SXS_FIT_BLOCKS_PER_SM 2
+#define SXS_FIT_BLOCKS_PER_SM 1
 
 static int plan_events(sxsg_plan *p, int need)
 {
