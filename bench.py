@@ -132,17 +132,17 @@ class Clocks:
 # DRAM bytes per pose of the dominant kernel from ncu captures of the same
 # kernel on a smaller pose list of this workload (profiles/): the traffic of
 # a launch scales with the poses it processes.
-TRAFFIC_PER_POSE = {("c1", "mixed"): 2.444e5, ("c1", "fp64"): 3.873e6}
+TRAFFIC_PER_POSE = {("c1", "mixed"): 2.36e5, ("c1", "fp64"): 5.73e5}
 
 
 def pose_flops(L, Q, precision):
-    """Algorithmic FLOPs of the per-pose contraction for one pose, over the
-    (L+1)(L+2)/2 pairs (m >= 0, l >= m) and Q q values.  Mixed path: the
-    phase w_m applied to the 3 channels of R (3 complex multiplies, 18
-    FLOPs) and the real parts of the 9 channel products (36 FLOPs).  Plain
-    path: the 9 complex multiply-adds (72 FLOPs) of the same contraction."""
+    """Algorithmic FLOPs of the per-pose contraction for one pose (both
+    precisions run the same kernel): over the (L+1)(L+2)/2 pairs
+    (m >= 0, l >= m) and Q q values, the phase w_m applied to the 3 channels
+    of R (3 complex multiplies, 18 FLOPs) and the real parts of the 9
+    channel products (36 FLOPs)."""
     NP = (L + 1) * (L + 2) // 2
-    return Q * NP * (54 if precision == "mixed" else 72)
+    return Q * NP * 54
 
 
 def reference_flops(w):
