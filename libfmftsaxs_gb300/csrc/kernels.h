@@ -3,16 +3,16 @@
  * Host C (sxs_host.c) calls these; every pointer is a device pointer unless
  * named h_*.  All launches go to the given stream; none synchronises.
  *
- * Device layouts (K = L+1, N = 2L+1, K2 = K*K, NP = K(K+1)/2, NT = ceil(Q/8)
- * q tiles of 8; a table of precision S holds complex values as {re, im}
+ * Device layouts (K = L+1, N = 2L+1, K2 = K*K, NP = K(K+1)/2, NT = ceil(Q/QT)
+ * q tiles of QT = SXS_QT; a table of precision S holds complex values as {re, im}
  * pairs of S, S = double on the plain path and float on the mixed path):
  *   spf_t [3 ch][K2 lm][Q]                     lm = l(l+1)+m, q fastest (S)
  *   dtab  [K b][K l][N m+L][N m1+L]            Wigner small-d per beta_b = b*pi/L
  *   dsymb [K2 lm][K l1][N p]
  *   bes   [nz][Q][N p]
- *   tau   [NT][nz][K m][K l][K l1][8]          T^m_{l l1} = i^{l+l1} tau (real)
- *   rot   [NT][K*N (b,g)][NP pair][3 ch][8]    pair = (m >= 0, l >= m), m-major (S)
- *   trans [NT][ncombo][NP pair][3 ch][8]       (S)
+ *   tau   [NT][nz][K m][K l][K l1][QT]         T^m_{l l1} = i^{l+l1} tau (real)
+ *   rot   [NT][K*N (b,g)][NP pair][3 ch][QT]   pair = (m >= 0, l >= m), m-major (S)
+ *   trans [NT][ncombo][NP pair][3 ch][QT]      (S)
  *   cross [npose][6][Q]                        (double)
  * Entries of the q tiles past Q are padding: never written by the kernels
  * that fill a table and never read into a result.
@@ -22,6 +22,16 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+/* q values per tile of the contraction tables; kernels move 2 adjacent q
+ * per thread, SXS_QT / 2 threads per tile row */
+#define SXS_QT 8
+#define SXS_QP (SXS_QT / 2)
+/* combos per translation slice (a run of combos sharing z): one block of
+ * the column translation kernel holds SXS_QT q x 3 channels x SXS_SLICE */
+#define SXS_SLICE (384 / (3 * SXS_QT))
+/* largest L + 1 the plans accept */
+#define SXS_LMAX_K 61
 
 #ifdef __cplusplus
 extern "C" {

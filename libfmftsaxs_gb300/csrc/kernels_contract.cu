@@ -72,7 +72,11 @@ __global__ void k_spf_transpose(const double *__restrict__ flat, typename Cx<S>:
  * table row is stored as [tile][row][pair][ch][8], so the slice of one tile
  * (an eighth of the table at Q ~ 100) stays in L2 while the blocks of that
  * tile run, and each thread moves 2 adjacent q (16 or 32 bytes) per load. */
-#define SXS_QT 8
+
+/* pairs per block of the slice translation kernel, poses per block of the
+ * per-pose kernel: 128 threads of SXS_QP q pairs */
+#define TR_PB (128 / SXS_QP)
+#define PC_PPB (128 / SXS_QP)
 
 template <typename S> struct Pair2 { typename Cx<S>::T a, b; };
 __device__ __forceinline__ Pair2<float> ld2(const float2 *p)
@@ -179,7 +183,7 @@ __global__ void k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const S *_
 /* Translated ligand rows, q-tiled:
  * R[tile][c][pair(m,l)][ch][8] = sum_{l1>=m} conj(T^m_{l l1}) U[tile][(b2,g2)][pair(m,l1)][ch][8],
  * conj(T) U = tau U for even l + l1 and tau (-i U) for odd.
- * Block = (tile, slice of <= 16 combos sharing one z, 32 consecutive pairs);
+ * Block = (tile, slice of combos sharing one z, TR_PB consecutive pairs);
  * thread = (pair, 2 adjacent q).  The block stages the tau rows of its 32
  * pairs (the same for every combo of the slice) in shared memory once, then
  * streams the slice's U rows: each thread accumulates its pair for the 3
@@ -193,19 +197,19 @@ k_translate(const typename Cx<S>::T *__restrict__ U, const S *__restrict__ tau, 
 {
 	typedef typename Cx<S>::T V;
 	extern __shared__ __align__(16) unsigned char tsm_raw[];
-	S *ts = reinterpret_cast<S *>(tsm_raw);   /* [32 pairs][tstride]: tau[l1][8 q] of each pair */
+	S *ts = reinterpret_cast<S *>(tsm_raw);   /* [TR_PB pairs][tstride]: tau[l1][QT q] of each pair */
 	int K = L + 1, N = 2 * L + 1, NP = K * (K + 1) / 2, nrow = K * N;
-	int npb = (NP + 31) / 32;
+	int npb = (NP + TR_PB - 1) / TR_PB;
 	int bid = blockIdx.x;
 	int pb = bid % npb;
 	bid /= npb;
 	int si = bid % nslice, t = bid / nslice;
 	int cfirst = slices[2 * si] - cbase, nc = slices[2 * si + 1];
 	int zi = combo_zbg[3 * cfirst];
-	for (int k = threadIdx.x; k < 32 * K * SXS_QT; k += blockDim.x) {
+	for (int k = threadIdx.x; k < TR_PB * K * SXS_QT; k += blockDim.x) {
 		int pl = k / (K * SXS_QT), r = k % (K * SXS_QT);
 		int l1 = r / SXS_QT, qq = r % SXS_QT;
-		int pr = pb * 32 + pl;
+		int pr = pb * TR_PB + pl;
 		S v = 0;
 		if (pr < NP) {
 			int m = 0;
@@ -216,8 +220,8 @@ k_translate(const typename Cx<S>::T *__restrict__ U, const S *__restrict__ tau, 
 		ts[pl * tstride + r] = v;
 	}
 	__syncthreads();
-	int pl = threadIdx.x >> 2, j2 = 2 * (threadIdx.x & 3);
-	int pr = pb * 32 + pl;
+	int pl = threadIdx.x / SXS_QP, j2 = 2 * (threadIdx.x % SXS_QP);
+	int pr = pb * TR_PB + pl;
 	if (pr >= NP) return;
 	int m = 0;
 	while (pr >= psym(m + 1, K)) m++;
@@ -272,8 +276,8 @@ __device__ __forceinline__ void ld4(const double *p, double *v)
  * applies the n x n matrix tau^m(q z) staged in shared memory:
  *   R[c][pair(m, m+i)][ch][q] = sum_k tau[i][k] (U[k] or -i U[k] by the
  *   parity of i + k).
- * Block = (tile, slice of <= 16 combos sharing z, m) with 8 q x 3 ch x 16
- * combos = 384 threads; tau rows are read as float4/double2 chunks that
+ * Block = (tile, slice of <= SXS_SLICE combos sharing z, m) with
+ * SXS_QT q x 3 ch x SXS_SLICE combos = 384 threads; tau rows are read as float4/double2 chunks that
  * lanes of the same q share.  One launch per NB covers the m with
  * n in (NB - 4, NB]. */
 template <typename S, int NB>
@@ -347,10 +351,13 @@ k_pose_cross(const sxsk_pose *__restrict__ poses, int npose, int combo_base, int
              const double2 *__restrict__ tw, const double *__restrict__ cst, int Q, int L, double *__restrict__ cross)
 {
 	typedef typename Cx<S>::T V;
+	__shared__ V tws[2 * SXS_LMAX_K - 1];
 	int K = L + 1, N = 2 * L + 1, NP = K * (K + 1) / 2, nrow = K * N;
-	int bpt = (npose + 31) / 32;
+	for (int k = threadIdx.x; k < N; k += blockDim.x) tws[k] = from2<V>(tw[k]);
+	__syncthreads();
+	int bpt = (npose + PC_PPB - 1) / PC_PPB;
 	int t = blockIdx.x / bpt, pb = blockIdx.x % bpt;
-	int pi = pb * 32 + (threadIdx.x >> 2), j2 = 2 * (threadIdx.x & 3);
+	int pi = pb * PC_PPB + threadIdx.x / SXS_QP, j2 = 2 * (threadIdx.x % SXS_QP);
 	if (pi >= npose) return;
 	int q0 = t * SXS_QT + j2;
 	if (q0 >= Q) return;
@@ -362,33 +369,43 @@ k_pose_cross(const sxsk_pose *__restrict__ poses, int npose, int combo_base, int
 	for (int k = 0; k < 2; k++)
 #pragma unroll
 		for (int c = 0; c < 6; c++) f[k][c] = 0;
-	int p = 0;
-	for (int m = 0; m <= L; m++) {
-		double2 wd = tw[(m * ps.a2) % N];
-		S wt = m == 0 ? (S)1 : (S)2;
-		S wx = (S)wd.x * wt, wy = (S)wd.y * wt;
+	/* pairs in m-major order; the phase tw[(m a2) mod N] (doubled for m > 0)
+	 * changes where a row of m starts */
+	int m = 0, mend = K, e = 0;
+	S wx = tws[0].x, wy = tws[0].y;
 #pragma unroll 2
-		for (int l = m; l <= L; l++, p++) {
-			const V *pp = Pr + (size_t)p * 3 * SXS_QT;
-			const V *rr = Rr + (size_t)p * 3 * SXS_QT;
-			Pair2<S> pv = ld2(pp), pd = ld2(pp + SXS_QT), pw = ld2(pp + 2 * SXS_QT);
-			Pair2<S> rv = ld2(rr), rd = ld2(rr + SXS_QT), rw = ld2(rr + 2 * SXS_QT);
+	for (int p = 0; p < NP; p++) {
+		if (p == mend) {
+			m++;
+			mend += K - m;
+			e += ps.a2;
+			if (e >= N) e -= N;
+			wx = (S)2 * tws[e].x;
+			wy = (S)2 * tws[e].y;
+		}
+		const V *pp = Pr + (size_t)p * 3 * SXS_QT;
+		const V *rr = Rr + (size_t)p * 3 * SXS_QT;
+		Pair2<S> cp[3], cr[3];
 #pragma unroll
-			for (int k = 0; k < 2; k++) {
-				V a0 = k ? pv.b : pv.a, a1 = k ? pd.b : pd.a, a2 = k ? pw.b : pw.a;
-				V r0 = k ? rv.b : rv.a, r1 = k ? rd.b : rd.a, r2 = k ? rw.b : rw.a;
-				/* R' = w R */
-				V s0, s1, s2;
-				s0.x = wx * r0.x - wy * r0.y; s0.y = wx * r0.y + wy * r0.x;
-				s1.x = wx * r1.x - wy * r1.y; s1.y = wx * r1.y + wy * r1.x;
-				s2.x = wx * r2.x - wy * r2.y; s2.y = wx * r2.y + wy * r2.x;
-				f[k][0] += a0.x * s0.x - a0.y * s0.y;
-				f[k][1] += a0.x * s1.x - a0.y * s1.y + a1.x * s0.x - a1.y * s0.y;
-				f[k][2] += a0.x * s2.x - a0.y * s2.y + a2.x * s0.x - a2.y * s0.y;
-				f[k][3] += a1.x * s1.x - a1.y * s1.y;
-				f[k][4] += a1.x * s2.x - a1.y * s2.y + a2.x * s1.x - a2.y * s1.y;
-				f[k][5] += a2.x * s2.x - a2.y * s2.y;
-			}
+		for (int c = 0; c < 3; c++) {
+			cp[c] = ld2(pp + c * SXS_QT);
+			cr[c] = ld2(rr + c * SXS_QT);
+		}
+#pragma unroll
+		for (int k = 0; k < 2; k++) {
+			V a0 = k ? cp[0].b : cp[0].a, a1 = k ? cp[1].b : cp[1].a, a2 = k ? cp[2].b : cp[2].a;
+			V r0 = k ? cr[0].b : cr[0].a, r1 = k ? cr[1].b : cr[1].a, r2 = k ? cr[2].b : cr[2].a;
+			/* R' = w R */
+			V s0, s1, s2;
+			s0.x = wx * r0.x - wy * r0.y; s0.y = wx * r0.y + wy * r0.x;
+			s1.x = wx * r1.x - wy * r1.y; s1.y = wx * r1.y + wy * r1.x;
+			s2.x = wx * r2.x - wy * r2.y; s2.y = wx * r2.y + wy * r2.x;
+			f[k][0] += a0.x * s0.x - a0.y * s0.y;
+			f[k][1] += a0.x * s1.x - a0.y * s1.y + a1.x * s0.x - a1.y * s0.y;
+			f[k][2] += a0.x * s2.x - a0.y * s2.y + a2.x * s0.x - a2.y * s0.y;
+			f[k][3] += a1.x * s1.x - a1.y * s1.y;
+			f[k][4] += a1.x * s2.x - a1.y * s2.y + a2.x * s1.x - a2.y * s1.y;
+			f[k][5] += a2.x * s2.x - a2.y * s2.y;
 		}
 	}
 	double *o = cross + (size_t)ps.src * 6 * Q;
@@ -648,13 +665,13 @@ static int translate_slices(const void *U, const void *tau, const int32_t *combo
                    int cbase, int ncombo, int nzt, int Q, int L, void *R, int fp32, cudaStream_t s)
 {
 	int K = L + 1, NT = (Q + SXS_QT - 1) / SXS_QT, NP = K * (K + 1) / 2;
-	long nb = (long)NT * nslice * ((NP + 31) / 32);
+	long nb = (long)NT * nslice * ((NP + TR_PB - 1) / TR_PB);
 	if (nb > 0x7fffffffL) return cudaErrorInvalidValue;
-	/* row stride of the staged tau, = 8 (mod 32) words so the 4 pairs of a
-	 * half warp hit distinct banks */
-	int ts = K * SXS_QT;
-	while (ts % 32 != 8) ts += SXS_QT;
-	size_t smem = (size_t)32 * ts * (fp32 ? sizeof(float) : sizeof(double));
+	/* row stride of the staged tau: the pairs of a half warp start on
+	 * distinct banks */
+	int ts = K * SXS_QT, tgt = SXS_QT >= 16 ? 16 : 8;
+	while (ts % 32 != tgt) ts += SXS_QT;
+	size_t smem = (size_t)TR_PB * ts * (fp32 ? sizeof(float) : sizeof(double));
 	if (fp32) {
 		if (smem > 48 * 1024) {
 			cudaError_t e = cudaFuncSetAttribute(k_translate<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -748,7 +765,7 @@ int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, int ncomb
 {
 	if (npose <= 0) return 0;
 	int NT = (Q + SXS_QT - 1) / SXS_QT;
-	long nb = (long)NT * ((npose + 31) / 32);
+	long nb = (long)NT * ((npose + PC_PPB - 1) / PC_PPB);
 	if (nb > 0x7fffffffL) return cudaErrorInvalidValue;
 	if (fp32)
 		k_pose_cross<float><<<(unsigned)nb, 128, 0, s>>>(poses, npose, combo_base, ncombo, (const float2 *)P,

@@ -157,7 +157,7 @@ __global__ void k_bessel_z(const double *__restrict__ z, int nz, const double *_
 
 /* T^{|m|}_{l l1}(q z) = sum_p (-1)^m i^p j_p d_lm(l1,p) for l <= l1, mirrored
  * (src/fftsaxs.c:182-243).  Thread = (iz, m, l, l1 >= l, q), q fastest.
- * Output in the q-tiled layout of the contraction tables (tiles of 8 q).
+ * Output in the q-tiled layout of the contraction tables (tiles of SXS_QT q).
  * The 3j factor 3j(l p l1; 0 0 0) vanishes unless l + p + l1 is even, so T
  * is real for even l + l1 and imaginary for odd l + l1 (the other part is
  * the sum of exact zeros and binary128 round-off below 1e-30 relative); the
@@ -188,10 +188,10 @@ __global__ void k_tmatrix(const double *__restrict__ bes, const double *__restri
 		im += ipi[p % 4] * v;
 	}
 	double v = ((l + l1) & 1) ? im : re;
-	/* q-tiled: [tile][iz][m][l][l1][8], tile = q / 8 */
-	size_t base = (((size_t)(iq / 8) * nz + iz) * K + m) * K;
-	tau[((base + l) * K + l1) * 8 + iq % 8] = v;
-	tau[((base + l1) * K + l) * 8 + iq % 8] = v;
+	/* q-tiled: [tile][iz][m][l][l1][SXS_QT], tile = q / SXS_QT */
+	size_t base = (((size_t)(iq / SXS_QT) * nz + iz) * K + m) * K;
+	tau[((base + l) * K + l1) * SXS_QT + iq % SXS_QT] = v;
+	tau[((base + l1) * K + l) * SXS_QT + iq % SXS_QT] = v;
 }
 
 /* Self terms of fill_const (src/fftsaxs.c:27-50, 52-85): per channel pair
@@ -255,8 +255,8 @@ int sxsk_tmatrix(const double *bes, const double *dsymb, int nz, int Q, int L, c
 	int K = L + 1;
 	long n = (long)nz * K * nll1 * Q;
 	if (n == 0) return 0;
-	size_t nt = (size_t)(Q + 7) / 8;
-	cudaMemsetAsync(tau, 0, nt * nz * K * K * K * 8 * sizeof(double), s);
+	size_t nt = (size_t)(Q + SXS_QT - 1) / SXS_QT;
+	cudaMemsetAsync(tau, 0, nt * nz * K * K * K * SXS_QT * sizeof(double), s);
 	k_tmatrix<<<nblk(n, 128), 128, 0, s>>>(bes, dsymb, nz, Q, L, ll1, nll1, tau);
 	return cudaGetLastError();
 }

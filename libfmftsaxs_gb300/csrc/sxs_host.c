@@ -161,8 +161,6 @@ void sxs_fit_constants(const double *q, const double *a, int Q, double *fc)
 }
 
 /* --------------------------------------------------------------- plan */
-/* combos per translation slice (a run of combos sharing z) */
-#define SXS_SLICE 16
 
 struct sxsg_plan {
 	int L, K, N, K2, Q, nz, n1, n2, precision;
@@ -195,7 +193,7 @@ struct sxsg_plan {
 	int ncombo;
 	int32_t *h_combo, *d_combo; /* [ncombo][3]: tslot, b2, g2 */
 	int64_t *h_cstart;          /* [ncombo+1] first sorted pose of each combo */
-	int nslice;                 /* runs of <= SXS_SLICE combos sharing z */
+	int nslice;                 /* runs of <= SXS_SLICE combos sharing z (kernels.h) */
 	int32_t *h_slices, *d_slices; /* [nslice][2]: first combo, count */
 	int nzt;                    /* touched z count */
 	double *h_zt, *d_zt;        /* touched z values */
@@ -288,7 +286,7 @@ int sxs_plan_create_on(sxsg_plan **out, const double *A, const double *B, const 
 	p->fp32 = precision == SXSG_MIXED;
 	p->celem = p->fp32 ? 2 * sizeof(float) : 2 * sizeof(double);
 	p->NP = p->K * (p->K + 1) / 2;
-	p->NT = (Q + 7) / 8;
+	p->NT = (Q + SXS_QT - 1) / SXS_QT;
 	double s0 = 0.0;
 	for (int i = 0; i < Q; i++) s0 += a[6 * i];
 	p->a0sum = s0;
@@ -319,7 +317,7 @@ int sxs_plan_create_on(sxsg_plan **out, const double *A, const double *B, const 
 	if (!e && n1 > 0) e = cudaMallocAsync((void **)&p->d_gtab, sizeof(double) * n1 * Q, p->s);
 	if (!e && n1 > 0) e = cudaMallocAsync((void **)&p->d_c1g, sizeof(double) * n1, p->s);
 	if (!e && n2 > 0) e = cudaMallocAsync((void **)&p->d_c2g, sizeof(double) * n2, p->s);
-	size_t rot_n = (size_t)p->NT * p->K * p->N * p->NP * 3 * 8;
+	size_t rot_n = (size_t)p->NT * p->K * p->N * p->NP * 3 * SXS_QT;
 	if (!ext_tables) {
 		if (!e) e = cudaMallocAsync(&p->d_P, p->celem * rot_n, p->s);
 		if (!e) e = cudaMallocAsync(&p->d_U, p->celem * rot_n, p->s);
@@ -508,7 +506,7 @@ int sxsg_plan_set_poses(sxsg_plan *p, const int64_t *index, int64_t n, int skip)
 	if (!e) e = cudaMallocAsync((void **)&p->d_combo, sizeof(int32_t) * 3 * (ncombo > 0 ? ncombo : 1), p->s);
 	if (!e) e = cudaMallocAsync((void **)&p->d_zt, sizeof(double) * (nzt > 0 ? nzt : 1), p->s);
 	if (!e && nzt > 0) e = cudaMallocAsync((void **)&p->d_bes, sizeof(double) * (size_t)nzt * p->Q * N, p->s);
-	size_t tau_n = (size_t)p->NT * nzt * p->K * p->K * p->K * 8;
+	size_t tau_n = (size_t)p->NT * nzt * p->K * p->K * p->K * SXS_QT;
 	if (!e && nzt > 0) e = cudaMallocAsync((void **)&p->d_tau, sizeof(double) * tau_n, p->s);
 	if (!e && nzt > 0 && p->fp32) e = cudaMallocAsync((void **)&p->d_tauf, sizeof(float) * tau_n, p->s);
 	if (!e && n > 0) e = cudaMemcpyAsync(p->d_poses, p->h_poses, sizeof(sxsk_pose) * n, cudaMemcpyHostToDevice, p->s);
@@ -567,7 +565,7 @@ static int plan_tables(sxsg_plan *p)
 		SXS_K(sxsk_tmatrix(p->d_bes, p->lt->d_dsymb, p->nzt, Q, L, p->lt->d_ll1, p->lt->nll1, p->d_tau, s));
 		sxs_count_launches(2);
 		if (p->fp32) {
-			SXS_K(sxsk_to_float(p->d_tau, p->d_tauf, (long)p->NT * p->nzt * p->K * p->K * p->K * 8, s));
+			SXS_K(sxsk_to_float(p->d_tau, p->d_tauf, (long)p->NT * p->nzt * p->K * p->K * p->K * SXS_QT, s));
 			sxs_count_launches(1);
 		}
 	}
@@ -619,7 +617,7 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 	if ((rc = plan_tables(p))) return rc;
 	SXS_CU(cudaEventRecord(p->ev[1], s));
 	/* translated table in chunks of whole slices that fit the budget */
-	size_t per_combo = (size_t)p->NP * 3 * 8 * p->NT * p->celem;
+	size_t per_combo = (size_t)p->NP * 3 * SXS_QT * p->NT * p->celem;
 	int64_t chunk = (int64_t)(p->r_budget / (per_combo * SXS_SLICE));   /* slices per chunk */
 	if (chunk < 1) chunk = 1;
 	int pipe = fit_mode == SXSG_FIT_GRID && p->ncombo > 0;
@@ -777,20 +775,20 @@ void sxs_plan_set_tables(sxsg_plan *p, void *P, int P_valid, void *U, int U_vali
 
 size_t sxs_plan_table_bytes(int L, int Q, int precision)
 {
-	size_t K = L + 1, N = 2 * L + 1, NP = K * (K + 1) / 2, NT = (Q + 7) / 8;
-	return NT * K * N * NP * 3 * 8 * (precision == SXSG_MIXED ? 2 * sizeof(float) : 2 * sizeof(double));
+	size_t K = L + 1, N = 2 * L + 1, NP = K * (K + 1) / 2, NT = (Q + SXS_QT - 1) / SXS_QT;
+	return NT * K * N * NP * 3 * SXS_QT * (precision == SXSG_MIXED ? 2 * sizeof(float) : 2 * sizeof(double));
 }
 
 /* Device bytes of a plan besides its rotation tables and translated-table
  * chunk: molecules, per-z tables for nzt touched z, pose lists and outputs. */
 size_t sxs_plan_base_bytes(int L, int Q, int nzt, int64_t npose, int n1, int precision)
 {
-	size_t K = L + 1, N = 2 * L + 1, NT = (Q + 7) / 8, K2 = K * K;
+	size_t K = L + 1, N = 2 * L + 1, NT = (Q + SXS_QT - 1) / SXS_QT, K2 = K * K;
 	size_t celem = precision == SXSG_MIXED ? 8 : 16;
 	size_t spf = (size_t)3 * Q * K2;
 	size_t b = spf * (16 * 2 + celem * 2);                       /* A, B, At, Bt */
 	b += (size_t)nzt * Q * N * 8;                                /* Bessel */
-	b += NT * nzt * K * K * K * 8 * (precision == SXSG_MIXED ? 12 : 8); /* tau */
+	b += NT * nzt * K * K * K * SXS_QT * (precision == SXSG_MIXED ? 12 : 8); /* tau */
 	b += (size_t)npose * (sizeof(sxsk_pose) + 12 * Q * 8 + 40);  /* poses, cross, scaled, outputs */
 	b += (size_t)n1 * Q * 16 + (size_t)64 * Q + (1 << 20);
 	return b;
@@ -799,8 +797,8 @@ size_t sxs_plan_base_bytes(int L, int Q, int nzt, int64_t npose, int n1, int pre
 /* bytes of one combo of the translated table */
 size_t sxs_plan_combo_bytes(int L, int Q, int precision)
 {
-	size_t K = L + 1, NP = K * (K + 1) / 2, NT = (Q + 7) / 8;
-	return NP * 3 * 8 * NT * (precision == SXSG_MIXED ? 8 : 16);
+	size_t K = L + 1, NP = K * (K + 1) / 2, NT = (Q + SXS_QT - 1) / SXS_QT;
+	return NP * 3 * SXS_QT * NT * (precision == SXSG_MIXED ? 8 : 16);
 }
 
 /* ------------------------------------------------------------ timing */
