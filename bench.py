@@ -404,11 +404,17 @@ def run_reference(args):
         r, n, wall = cpu_sample(w, kind, workers, seed=k)
         rates.append(r); ns.append(n); walls.append(wall)
     value = sum(ns) / sum(walls)
-    out = {"impl": "reference", "metric": "poses/s @lmax=20 (FP64 plain GPU path, grid fit)", "value": value,
-           "unit": "poses/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+    out = {"impl": "reference",
+           "metric": "poses/s @lmax=20 (%s GPU path, grid fit)"
+                     % ("mixed-precision" if args.precision == "mixed" else "FP64 plain"),
+           "value": value, "unit": "poses/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": 1e3 * float(np.mean(walls)), "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": args.config, "sample": "one (z,beta1,beta2) triple per host process"},
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random-walk dimers, poses and noisy experiment)",
+           "config": {"workload": "%s: receptor %d / ligand %d atoms, L=%d, Q=%d, %d poses, fit grid %dx%d"
+                                  % (args.config, w.rec.natoms, w.lig.natoms, w.L, w.Q, len(w.index), len(w.c1g),
+                                     len(w.c2g)),
+                      "precision": "fp64 (the reference's CPU arithmetic)", "skip": 1,
+                      "sample": "each step: one (z,beta1,beta2) triple of the pose list per host process"},
            "cpu_baseline": {"value": value, "unit": "poses/s", "cores": workers, "kind": kind,
                             "sample": "%d processes x 1 triple per step" % workers},
            "e2e": {"value": value, "unit": "poses/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

@@ -323,6 +323,24 @@ int sxsg_score_flat(const double *A, const double *B, const double *qvals, int q
                     int fit_mode, const double *c1grid, int n1, const double *c2grid, int n2,
                     double *chi, double *c1, double *c2, double *cross, int precision);
 
+/* Exact per-pose scoring, the reference's score_ft_naive flow
+ * (tools/score_ft_naive.c:156-212), for cross-checking the grid method:
+ * for each Euler pose eu[6 i .. 6 i + 5] = (z, beta1, gamma1, alpha2,
+ * beta2, gamma2) the receptor (rec_xyz[3 nrec], centred at its centre of
+ * extrema) is turned by the active rotation R(0, beta1, gamma1), the ligand
+ * (lig_xyz[3 nlig], centred at its centroid) by R(alpha2, beta2, gamma2)
+ * and moved by (0, 0, z); the joined complex (receptor first) is centred at
+ * its centroid, expanded to A_lm at L on qvals (the kernels of
+ * sxsg_expand), reduced to its cross terms (sxs_spf2cross_terms) and fitted
+ * by L-BFGS-B without the peak rescale (sxs_spf2fitted_profile).
+ * vac, dum, water_w: per atom of the joined order (water_w = water form
+ * factor x accessible fraction, NULL for none); a[6 qnum], mult: the binned
+ * experiment.  chi, c1, c2 [n] and cross [n][6][qnum] may be NULL. */
+int sxsg_score_exact(const double *rec_xyz, int nrec, const double *lig_xyz, int nlig, const double *vac,
+                     const double *dum, const double *water_w, const double *euler, int64_t n, const double *qvals,
+                     int qnum, int L, const double *a, double mult, double *chi, double *c1, double *c2,
+                     double *cross);
+
 /* Pose ingestion helpers (tools/correlate.c:202-240): grid index of one
  * Euler 6-tuple (z, b1, g1, a2, b2, g2 as written by sxs_ft2euler) at
  * translation slot z_idx. */

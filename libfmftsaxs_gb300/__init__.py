@@ -303,6 +303,28 @@ class Server:
             pass
 
 
+def score_exact(rec_xyz, lig_xyz, vac, dum, water_w, euler, qvals, L, a, mult, cross=False):
+    """Exact per-pose scoring (sxsg_score_exact): the score_ft_naive flow on
+    the GPU.  euler: [n][6] (z, b1, g1, a2, b2, g2)."""
+    rx, lx, v, d = f64(rec_xyz).reshape(-1, 3), f64(lig_xyz).reshape(-1, 3), f64(vac), f64(dum)
+    w = f64(water_w) if water_w is not None else None
+    eu, q, a = f64(euler).reshape(-1, 6), f64(qvals), f64(a)
+    n = len(eu)
+    chi, c1, c2 = np.zeros(n), np.zeros(n), np.zeros(n)
+    cr = np.zeros((n, 6, len(q))) if cross else None
+    lib = load()
+    lib.sxsg_score_exact.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int] + [C.c_void_p] * 4 + \
+        [C.c_int64, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_double] + [C.c_void_p] * 4
+    _check(lib.sxsg_score_exact(rx.ctypes.data, len(rx), lx.ctypes.data, len(lx), v.ctypes.data, d.ctypes.data,
+                                w.ctypes.data if w is not None else None, eu.ctypes.data, n, q.ctypes.data, len(q),
+                                int(L), a.ctypes.data, float(mult), chi.ctypes.data, c1.ctypes.data, c2.ctypes.data,
+                                cr.ctypes.data if cross else None))
+    out = dict(chi=chi, c1=c1, c2=c2)
+    if cross:
+        out["cross"] = cr
+    return out
+
+
 def profile_from_spf(spf, L, qvals, rm, c1, c2):
     """(I[Q], err[Q]) of one molecule (sxs_profile_from_spf on a flat expansion)."""
     q = f64(qvals)

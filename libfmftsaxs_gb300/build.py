@@ -16,7 +16,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU = {"kernels_faithful.cu": ["-fmad=false"], "kernels_contract.cu": [], "kernels_lbfgsb.cu": ["-fmad=false"],
       "kernels_fitdf.cu": ["-fmad=false"]}
-C = ["sxs_host.c", "sxs_api.c", "sxs_tables.c", "sxs_serve.c"]
+C = ["sxs_host.c", "sxs_api.c", "sxs_tables.c", "sxs_serve.c", "sxs_exact.c"]
 
 
 def _cuda_home():

@@ -56,6 +56,10 @@ size_t sxsk_expand_ws_jl(int natoms, int Q, int L);
 /* host-flat [3][Q][K2][2] -> spf_t [3][K2][Q] complex, in float when fp32 */
 int sxsk_spf_transpose(const double *flat, void *spf_t, int Q, int L, int fp32, cudaStream_t s);
 
+/* cross terms of single molecules: spf [nmol][3][Q][K2][2] (host flat
+ * layout) -> cross [nmol][6][Q] */
+int sxsk_self_cross(const double *spf, int nmol, int Q, int L, double *cross, cudaStream_t s);
+
 /* j_p(q z) for p in [0,2L]: bes[nz][Q][N] (faithful series) */
 int sxsk_bessel_z(const double *z, int nz, const double *q, int Q, int L, double *bes, cudaStream_t s);
 

@@ -194,6 +194,40 @@ __global__ void k_tmatrix(const double *__restrict__ bes, const double *__restri
 	tau[((base + l1) * K + l) * SXS_QT + iq % SXS_QT] = v;
 }
 
+/* Cross terms of single molecules (src/min_saxs.c:450-494): for each
+ * molecule and q, sum over lm of |V|^2, |D|^2, |W|^2, Re(V conj D),
+ * Re(V conj W), Re(D conj W) in the reference's order, the three mixed sums
+ * doubled; spf in the host flat layout [mol][3][Q][K2][2], cross
+ * [mol][6][Q] (VV VD VW DD DW WW).  Thread = (molecule, q). */
+__global__ void k_self_cross(const double *__restrict__ spf, int nmol, int Q, int K2, double *__restrict__ cross)
+{
+	long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= (long)nmol * Q) return;
+	int iq = (int)(t % Q);
+	long mol = t / Q;
+	const double *V = spf + (((size_t)mol * 3 + 0) * Q + iq) * K2 * 2;
+	const double *D = spf + (((size_t)mol * 3 + 1) * Q + iq) * K2 * 2;
+	const double *W = spf + (((size_t)mol * 3 + 2) * Q + iq) * K2 * 2;
+	double vv = 0.0, vd = 0.0, vw = 0.0, dd = 0.0, dw = 0.0, ww = 0.0;
+	for (int id = 0; id < K2; id++) {
+		double vr = V[2 * id], vi = V[2 * id + 1], dr = D[2 * id], di = D[2 * id + 1];
+		double wr = W[2 * id], wi = W[2 * id + 1];
+		vv += vr * vr + vi * vi;
+		dd += dr * dr + di * di;
+		ww += wr * wr + wi * wi;
+		vd += vr * dr + vi * di;
+		vw += vr * wr + vi * wi;
+		dw += dr * wr + di * wi;
+	}
+	double *o = cross + (size_t)mol * 6 * Q + iq;
+	o[0] = vv;
+	o[Q] = vd * 2.0;
+	o[2 * Q] = vw * 2.0;
+	o[3 * Q] = dd;
+	o[4 * Q] = dw * 2.0;
+	o[5 * Q] = ww;
+}
+
 /* Self terms of fill_const (src/fftsaxs.c:27-50, 52-85): per channel pair
  * and q, sum over lm of Re(A1 conj A2) then Re(B1 conj B2), interleaved as in
  * comp_const_int, times {1,2,2,1,2,1}.  spf in the host flat layout. */
@@ -246,6 +280,14 @@ int sxsk_bessel_z(const double *z, int nz, const double *q, int Q, int L, double
 	long n = (long)nz * Q * (2 * L + 1);
 	if (n == 0) return 0;
 	k_bessel_z<<<nblk(n, 128), 128, 0, s>>>(z, nz, q, Q, L, bes);
+	return cudaGetLastError();
+}
+
+int sxsk_self_cross(const double *spf, int nmol, int Q, int L, double *cross, cudaStream_t s)
+{
+	long n = (long)nmol * Q;
+	if (n <= 0) return 0;
+	k_self_cross<<<nblk(n, 128), 128, 0, s>>>(spf, nmol, Q, (L + 1) * (L + 1), cross);
 	return cudaGetLastError();
 }
 
