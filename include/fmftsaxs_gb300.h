@@ -341,6 +341,16 @@ int sxsg_score_exact(const double *rec_xyz, int nrec, const double *lig_xyz, int
                      int qnum, int L, const double *a, double mult, double *chi, double *c1, double *c2,
                      double *cross);
 
+/* Accessible fraction per atom on the GPU (Shrake-Rupley: the solvent
+ * sphere of radius + probe sampled at sph[npts][3] unit points, a golden
+ * spiral of npts points when sph is NULL; fraction of points not inside
+ * any neighbour's sphere; 0 for a zero radius).  The reference takes this
+ * input from libmol2's accs (sxs_faccs, src/saxs_utils.c:30-48), which is
+ * not part of it; this is the restatement the synthetic workloads use.
+ * 1 <= npts <= 1024. */
+int sxsg_sasa(const double *xyz, const double *radius, int natoms, double probe, const double *sph, int npts,
+              double *frac);
+
 /* Pose ingestion helpers (tools/correlate.c:202-240): grid index of one
  * Euler 6-tuple (z, b1, g1, a2, b2, g2 as written by sxs_ft2euler) at
  * translation slot z_idx. */

@@ -325,6 +325,19 @@ def score_exact(rec_xyz, lig_xyz, vac, dum, water_w, euler, qvals, L, a, mult, c
     return out
 
 
+def sasa(xyz, radius, probe=1.4, npts=240, sphere=None):
+    """Accessible fraction per atom on the GPU (sxsg_sasa)."""
+    x, r = f64(xyz).reshape(-1, 3), f64(radius)
+    out = np.zeros(len(r))
+    sph = f64(sphere).reshape(-1, 3) if sphere is not None else None
+    lib = load()
+    lib.sxsg_sasa.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p, C.c_int, C.c_void_p]
+    _check(lib.sxsg_sasa(x.ctypes.data, r.ctypes.data, len(r), float(probe),
+                         sph.ctypes.data if sph is not None else None, len(sph) if sph is not None else int(npts),
+                         out.ctypes.data))
+    return out
+
+
 def profile_from_spf(spf, L, qvals, rm, c1, c2):
     """(I[Q], err[Q]) of one molecule (sxs_profile_from_spf on a flat expansion)."""
     q = f64(qvals)

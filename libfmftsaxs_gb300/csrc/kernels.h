@@ -60,6 +60,11 @@ int sxsk_spf_transpose(const double *flat, void *spf_t, int Q, int L, int fp32, 
  * layout) -> cross [nmol][6][Q] */
 int sxsk_self_cross(const double *spf, int nmol, int Q, int L, double *cross, cudaStream_t s);
 
+/* Shrake-Rupley accessible fraction per atom: sphere points sph[npts][3]
+ * (npts <= 1024) */
+int sxsk_sasa(const double *xyz, const double *rad, int n, double probe, const double *sph, int npts, double *frac,
+              cudaStream_t s);
+
 /* j_p(q z) for p in [0,2L]: bes[nz][Q][N] (faithful series) */
 int sxsk_bessel_z(const double *z, int nz, const double *q, int Q, int L, double *bes, cudaStream_t s);
 

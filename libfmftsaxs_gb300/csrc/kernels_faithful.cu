@@ -228,6 +228,77 @@ __global__ void k_self_cross(const double *__restrict__ spf, int nmol, int Q, in
 	o[5 * Q] = ww;
 }
 
+/* Shrake-Rupley accessible fraction (the restatement the workloads use;
+ * the reference takes it from libmol2's accs): block = one atom i; the
+ * block scans the atoms SASA_CAP at a time for neighbours j != i with
+ * |x_i - x_j| < rr_i + rr_j (rr = radius + probe), keeps them in shared
+ * memory, and each thread tests its sphere points p = x_i + rr_i s_k
+ * against them (buried when |p - x_j|^2 < rr_j^2).  fraction = free points
+ * / npts; 0 for a zero radius.  Compiled without contraction: the same
+ * arithmetic as the host restatement, point for point. */
+#define SASA_CAP 512
+#define SASA_PPT 8
+__global__ void __launch_bounds__(128) k_sasa(const double *__restrict__ xyz, const double *__restrict__ rad, int n,
+                                              double probe, const double *__restrict__ sph, int npts,
+                                              double *__restrict__ frac)
+{
+	__shared__ double nb[SASA_CAP][4];
+	__shared__ int cnt;
+	__shared__ int nfree[128];
+	int i = blockIdx.x;
+	double ri = rad[i];
+	if (ri <= 0.0) {
+		if (threadIdx.x == 0) frac[i] = 0.0;
+		return;
+	}
+	double xi = xyz[3 * i], yi = xyz[3 * i + 1], zi = xyz[3 * i + 2];
+	double rri = ri + probe;
+	/* points of this thread: k = threadIdx.x + j blockDim.x, j < SASA_PPT */
+	unsigned freebits = 0;
+	for (int j = 0; j < SASA_PPT; j++)
+		if (threadIdx.x + j * (int)blockDim.x < npts) freebits |= 1u << j;
+	for (int j0 = 0; j0 < n; j0 += SASA_CAP) {
+		__syncthreads();
+		if (threadIdx.x == 0) cnt = 0;
+		__syncthreads();
+		int j1 = min(n, j0 + SASA_CAP);
+		for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+			if (j == i) continue;
+			double rrj = rad[j] + probe;
+			double dx = xyz[3 * j] - xi, dy = xyz[3 * j + 1] - yi, dz = xyz[3 * j + 2] - zi;
+			double d = sqrt(dx * dx + dy * dy + dz * dz);
+			if (d < rri + rrj) {
+				int slot = atomicAdd(&cnt, 1);   /* < SASA_CAP: at most SASA_CAP candidates per pass */
+				nb[slot][0] = xyz[3 * j];
+				nb[slot][1] = xyz[3 * j + 1];
+				nb[slot][2] = xyz[3 * j + 2];
+				nb[slot][3] = rrj * rrj;
+			}
+		}
+		__syncthreads();
+		int m = cnt;
+		for (int pj = 0; pj < SASA_PPT; pj++) {
+			if (!(freebits >> pj & 1u)) continue;
+			int k = threadIdx.x + pj * blockDim.x;
+			double px = xi + rri * sph[3 * k], py = yi + rri * sph[3 * k + 1], pz = zi + rri * sph[3 * k + 2];
+			for (int t = 0; t < m; t++) {
+				double ex = px - nb[t][0], ey = py - nb[t][1], ez = pz - nb[t][2];
+				if (!(ex * ex + ey * ey + ez * ez >= nb[t][3])) {
+					freebits &= ~(1u << pj);
+					break;
+				}
+			}
+		}
+	}
+	nfree[threadIdx.x] = __popc(freebits);
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		int c = 0;
+		for (int t = 0; t < (int)blockDim.x; t++) c += nfree[t];
+		frac[i] = (double)c / (double)npts;
+	}
+}
+
 /* Self terms of fill_const (src/fftsaxs.c:27-50, 52-85): per channel pair
  * and q, sum over lm of Re(A1 conj A2) then Re(B1 conj B2), interleaved as in
  * comp_const_int, times {1,2,2,1,2,1}.  spf in the host flat layout. */
@@ -288,6 +359,15 @@ int sxsk_self_cross(const double *spf, int nmol, int Q, int L, double *cross, cu
 	long n = (long)nmol * Q;
 	if (n <= 0) return 0;
 	k_self_cross<<<nblk(n, 128), 128, 0, s>>>(spf, nmol, Q, (L + 1) * (L + 1), cross);
+	return cudaGetLastError();
+}
+
+int sxsk_sasa(const double *xyz, const double *rad, int n, double probe, const double *sph, int npts, double *frac,
+              cudaStream_t s)
+{
+	if (n <= 0) return 0;
+	if (npts <= 0 || npts > 128 * SASA_PPT) return cudaErrorInvalidValue;
+	k_sasa<<<n, 128, 0, s>>>(xyz, rad, n, probe, sph, npts, frac);
 	return cudaGetLastError();
 }
 

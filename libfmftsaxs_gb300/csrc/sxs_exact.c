@@ -79,7 +79,6 @@ int sxsg_score_exact(const double *rec_xyz, int nrec, const double *lig_xyz, int
 	int B = n < SXS_EXACT_BATCH ? (int)n : SXS_EXACT_BATCH;
 	size_t spf_n = (size_t)3 * Q * K * K * 2;
 	double *h_xyz = malloc(sizeof(double) * 3 * na * (size_t)B);
-	double *h_cross = malloc(sizeof(double) * 6 * Q * (size_t)B);
 	double *wf = calloc(na, sizeof(double));
 	if (water_w) memcpy(wf, water_w, sizeof(double) * na);
 	double *d_xyz = NULL, *d_vac = NULL, *d_dum = NULL, *d_wf = NULL, *d_q = NULL, *d_a = NULL, *d_jl = NULL;
@@ -129,7 +128,52 @@ int sxsg_score_exact(const double *rec_xyz, int nrec, const double *lig_xyz, int
 	cudaFree(d_xyz); cudaFree(d_vac); cudaFree(d_dum); cudaFree(d_wf); cudaFree(d_q); cudaFree(d_a);
 	cudaFree(d_jl); cudaFree(d_ylm); cudaFree(d_spf); cudaFree(d_cross); cudaFree(d_ct);
 	cudaFree(d_chi); cudaFree(d_c1); cudaFree(d_c2);
-	free(h_xyz); free(h_cross); free(wf);
+	free(h_xyz); free(wf);
 	if (e) return sxs_cuda_fail(e, "sxsg_score_exact");
+	return 0;
+}
+
+/* Accessible fraction of every atom (Shrake-Rupley on the sphere points
+ * sph[npts][3], or a golden spiral of npts points when sph is NULL): the
+ * W-channel weights of the expansion, computed on the device. */
+int sxsg_sasa(const double *xyz, const double *radius, int natoms, double probe, const double *sph, int npts,
+              double *frac)
+{
+	if (natoms < 0 || (natoms > 0 && (!xyz || !radius || !frac)) || npts <= 0 || npts > 1024)
+		return sxs_fail(-2, "sxsg_sasa: bad arguments (1 <= npts <= 1024)");
+	if (natoms == 0) return 0;
+	int rc = sxs_ensure_init();
+	if (rc) return rc;
+	cudaStream_t s = sxs_default_stream();
+	double *h_sph = NULL;
+	if (!sph) {
+		h_sph = malloc(sizeof(double) * 3 * npts);
+		for (int k = 0; k < npts; k++) {
+			double kk = k + 0.5;
+			double phi = acos(1.0 - 2.0 * kk / npts);
+			double th = SXS_PI_FULL * (1.0 + sqrt(5.0)) * kk;
+			h_sph[3 * k] = cos(th) * sin(phi);
+			h_sph[3 * k + 1] = sin(th) * sin(phi);
+			h_sph[3 * k + 2] = cos(phi);
+		}
+		sph = h_sph;
+	}
+	double *d_xyz = NULL, *d_rad = NULL, *d_sph = NULL, *d_f = NULL;
+	cudaError_t e = cudaMalloc((void **)&d_xyz, sizeof(double) * 3 * natoms);
+	if (!e) e = cudaMalloc((void **)&d_rad, sizeof(double) * natoms);
+	if (!e) e = cudaMalloc((void **)&d_sph, sizeof(double) * 3 * npts);
+	if (!e) e = cudaMalloc((void **)&d_f, sizeof(double) * natoms);
+	if (!e) e = cudaMemcpyAsync(d_xyz, xyz, sizeof(double) * 3 * natoms, cudaMemcpyHostToDevice, s);
+	if (!e) e = cudaMemcpyAsync(d_rad, radius, sizeof(double) * natoms, cudaMemcpyHostToDevice, s);
+	if (!e) e = cudaMemcpyAsync(d_sph, sph, sizeof(double) * 3 * npts, cudaMemcpyHostToDevice, s);
+	if (!e) {
+		e = (cudaError_t)sxsk_sasa(d_xyz, d_rad, natoms, probe, d_sph, npts, d_f, s);
+		sxs_count_launches(1);
+	}
+	if (!e) e = cudaMemcpyAsync(frac, d_f, sizeof(double) * natoms, cudaMemcpyDeviceToHost, s);
+	if (!e) e = cudaStreamSynchronize(s);
+	cudaFree(d_xyz); cudaFree(d_rad); cudaFree(d_sph); cudaFree(d_f);
+	free(h_sph);
+	if (e) return sxs_cuda_fail(e, "sxsg_sasa");
 	return 0;
 }

@@ -95,11 +95,13 @@ def golden_sphere(npts):
     return np.stack([np.cos(theta) * np.sin(phi), np.sin(theta) * np.sin(phi), np.cos(phi)], axis=1)
 
 
-def sasa_fraction(xyz, radii, probe=1.4, npts=240):
-    """Shrake-Rupley accessible fraction per atom (0 for zero radius)."""
+def sasa_fraction(xyz, radii, probe=1.4, npts=240, sph=None):
+    """Shrake-Rupley accessible fraction per atom (0 for zero radius); the
+    distances are summed x, y, z in that order, as the GPU kernel does."""
     n = len(xyz)
     rr = radii + probe
-    sph = golden_sphere(npts)
+    sph = golden_sphere(npts) if sph is None else np.asarray(sph, dtype=np.float64)
+    npts = len(sph)
     out = np.zeros(n)
     cut = 2.0 * rr.max()
     cell = {}
@@ -119,12 +121,12 @@ def sasa_fraction(xyz, radii, probe=1.4, npts=240):
         p = xyz[i] + rr[i] * sph
         free = np.ones(npts, dtype=bool)
         if len(nb):
-            d = xyz[nb]
-            dist = np.linalg.norm(d - xyz[i], axis=1)
+            d = xyz[nb] - xyz[i]
+            dist = np.sqrt(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2])
             close = nb[dist < rr[i] + rr[nb]]
             for j in close:
                 dd = p - xyz[j]
-                free &= np.einsum("ij,ij->i", dd, dd) >= rr[j] ** 2
+                free &= dd[:, 0] * dd[:, 0] + dd[:, 1] * dd[:, 1] + dd[:, 2] * dd[:, 2] >= rr[j] * rr[j]
         out[i] = free.mean()
     return out
 
