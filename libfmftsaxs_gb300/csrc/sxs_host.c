@@ -75,6 +75,15 @@ int sxsg_init(int device)
 	}
 	e = cudaSetDevice(device);
 	if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking);
+	if (e == cudaSuccess) {
+		/* keep freed plan memory in this process's stream-ordered pool for
+		 * the next plan instead of unmapping it at every synchronisation */
+		cudaMemPool_t pool;
+		if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+			uint64_t thr = UINT64_MAX;
+			cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+		}
+	}
 	if (e != cudaSuccess) {
 		pthread_mutex_unlock(&g_init_lock);
 		return sxs_cuda_fail(e, "device init");
