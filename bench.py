@@ -165,6 +165,7 @@ def time_plan(g, w, precision, args, clocks=None):
     """K timed runs of a resident plan (inputs on the device); returns
     (ms per run from events on the library stream, stage ms, launches, results)."""
     plan = g.Plan(w.A, w.B, w.q, w.z, w.L, w.a, w.mult, w.peak, w.c1g, w.c2g, precision=precision)
+    plan.set_rotation(g.ROT_TC if args.rotation == "tc" else g.ROT_CUDA)
     if args.budget_gb:
         plan.set_budget(int(args.budget_gb * 2 ** 30))
     plan.set_poses(w.index, skip=1)
@@ -434,6 +435,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true", help="no CPU baseline sample")
     ap.add_argument("--skip-e2e", action="store_true", help="no end-to-end timing")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--rotation", default="cuda", choices=["tc", "cuda"],
+                    help="mixed path: rotation tables on the tcgen05 tensor cores or on CUDA cores")
     ap.add_argument("--skip-serve", action="store_true", help="no serving scenario")
     ap.add_argument("--serve-rate", type=float, default=50.0, help="serving: mean arrivals per second")
     ap.add_argument("--serve-window", type=float, default=2.0, help="serving: seconds of arrivals")

@@ -252,6 +252,12 @@ int sxsg_plan_set_poses(sxsg_plan *plan, const int64_t *index, int64_t n, int sk
  * default is half the free memory at plan creation); touched (z, b2, g2)
  * combos are processed in chunks that fit. */
 int sxsg_plan_set_budget(sxsg_plan *plan, size_t bytes);
+/* Rotation engine of a mixed-precision plan: SXSG_ROT_CUDA (CUDA cores,
+ * the default) or SXSG_ROT_TC (tcgen05 tensor cores, 3xTF32 with FP32
+ * accumulation, for 2L + 1 <= 64; larger L stays on CUDA cores).  FP64
+ * plans always rotate on CUDA cores. */
+enum { SXSG_ROT_CUDA = 0, SXSG_ROT_TC = 1 };
+int sxsg_plan_set_rotation(sxsg_plan *plan, int engine);
 /* Run the GPU work for the current pose list (asynchronous until results). */
 int sxsg_plan_run(sxsg_plan *plan, int fit_mode);
 /* Copy results to the host.  Any pointer may be NULL.  chi/c1/c2/cell: [n];

@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(HERE, "libfmftsaxs_gb300.so")
 FIT_NONE, FIT_GRID, FIT_LBFGSB = 0, 1, 2
 FP64 = 0
 MIXED = 1
+ROT_CUDA, ROT_TC = 0, 1
 
 _lib = None
 
@@ -188,6 +189,10 @@ class Plan:
         idx = np.ascontiguousarray(index, dtype=np.int64)
         self.n = len(idx)
         _check(load().sxsg_plan_set_poses(self.h, idx.ctypes.data, self.n, int(skip)))
+
+    def set_rotation(self, engine):
+        load().sxsg_plan_set_rotation.argtypes = [C.c_void_p, C.c_int]
+        _check(load().sxsg_plan_set_rotation(self.h, int(engine)))
 
     def set_budget(self, nbytes):
         load().sxsg_plan_set_budget.argtypes = [C.c_void_p, C.c_size_t]

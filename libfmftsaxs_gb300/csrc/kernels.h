@@ -9,7 +9,7 @@
  *   spf_t [3 ch][K2 lm][Q]                     lm = l(l+1)+m, q fastest (S)
  *   dtab  [K b][K l][N m+L][N m1+L]            Wigner small-d per beta_b = b*pi/L
  *   dsymb [K2 lm][K l1][N p]
- *   bes   [nz][Q][N p]
+ *   bes   [nz][N p][Q]
  *   tau   [NT][nz][K m][K l][K l1][QT]         T^m_{l l1} = i^{l+l1} tau (real)
  *   rot   [NT][K*N (b,g)][NP pair][3 ch][QT]   pair = (m >= 0, l >= m), m-major (S)
  *   trans [NT][ncombo][NP pair][3 ch][QT]      (S)
@@ -65,7 +65,7 @@ int sxsk_self_cross(const double *spf, int nmol, int Q, int L, double *cross, cu
 int sxsk_sasa(const double *xyz, const double *rad, int n, double probe, const double *sph, int npts, double *frac,
               cudaStream_t s);
 
-/* j_p(q z) for p in [0,2L]: bes[nz][Q][N] (faithful series) */
+/* j_p(q z) for p in [0,2L]: bes[nz][N][Q] (faithful series) */
 int sxsk_bessel_z(const double *z, int nz, const double *q, int Q, int L, double *bes, cudaStream_t s);
 
 /* translation matrix T^m_{l l1}(q z) = i^{l+l1} tau -> tau; ll1 lists the
@@ -83,6 +83,17 @@ int sxsk_const_int(const double *A, const double *B, int Q, int L, double *cst, 
  * with C = spf_t, conjugated when conj != 0. */
 int sxsk_rotate(const void *spf_t, const void *dtab, const double2 *tw, int Q, int L, int conj, void *out,
                 int fp32, cudaStream_t s);   /* dtab in float when fp32 */
+
+/* The mixed path's rotation table on the tcgen05 tensor cores (3xTF32,
+ * FP32 accumulation in tensor memory); same output as sxsk_rotate with
+ * fp32; 2L + 1 <= 64.  dtabf: the float Wigner-d table. */
+int sxsk_rotate_tc(const void *spf_t, const float *dtabf, const double2 *tw, int Q, int L, int conj, void *out,
+                   float *amat, cudaStream_t s);
+/* floats of the scratch (amat) that sxsk_rotate_tc needs */
+size_t sxsk_rotate_tc_scratch(int L);
+/* nonzero when a block of sxsk_rotate_tc gave up waiting for its MMAs
+ * since the last call; resets the flag */
+int sxsk_rotate_tc_status(void);
 
 /* translated ligand table for the combos of a run of slices, m >= 0, all q tiles:
  * R[t][c][pair(m,l)][ch][q] = sum_{l1>=m} conj(T[t][zi][m][l][l1][q]) U[t][(b2,g2)][pair(m,l1)][ch][q].

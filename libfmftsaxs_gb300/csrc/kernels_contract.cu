@@ -106,14 +106,14 @@ __device__ __forceinline__ void st2(double2 *p, double2 a, double2 b)
 
 /* Rotation tables in the q-tiled layout:
  *   out[t][b*N+g][pair(m,l)][ch][q] = sum_{m1=-l..l} tw[(m1' g) mod N] d^l_{m m1}(beta_b) C[ch][l,m1][q]
- * (C = spf_t, conjugated when conj != 0).  Block = (b, m, QS q of a tile),
- * thread = (g, q): the block stages its coefficients C[ch][l >= m][m1][QS q],
- * the d row d^l_{m m1}(beta_b) and the twiddles in shared memory once and
- * every gamma thread reuses them; the twiddle index (m1' g) mod N advances
- * by g per m1. */
+ * (C = spf_t, conjugated when conj != 0).  Block = (b, QS q of a tile, group
+ * of m = mg, mg + MG, ...); thread = (g, q).  The block stages the
+ * coefficients C[ch][lm][QS q] of every lm and the twiddles in shared memory
+ * once, then per m the d row d^l_{m m1}(beta_b); every gamma thread reuses
+ * them, and the twiddle index (m1' g) mod N advances by g per m1. */
 template <typename S>
 __global__ void k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const S *__restrict__ dtab,
-                         const double2 *__restrict__ tw, int Q, int L, int conj, int QS,
+                         const double2 *__restrict__ tw, int Q, int L, int conj, int QS, int MG,
                          typename Cx<S>::T *__restrict__ out)
 {
 	typedef typename Cx<S>::T V;
@@ -121,20 +121,19 @@ __global__ void k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const S *_
 	int K = L + 1, N = 2 * L + 1, K2 = K * K, NP = K * (K + 1) / 2, nrow = K * N;
 	int NT = (Q + SXS_QT - 1) / SXS_QT, nsub = SXS_QT / QS;
 	int bid = blockIdx.x;
+	int mg = bid % MG;
+	bid /= MG;
 	int t = bid % (NT * nsub);
-	bid /= NT * nsub;
+	int b = bid / (NT * nsub);
 	int q0 = t * QS;                         /* first q of the block */
 	t = q0 / SXS_QT;
-	int m = bid % K, b = bid / K;
-	int lm0 = m * m;                         /* first lm with l >= m */
-	int nlm = K2 - lm0;
-	V *cs = reinterpret_cast<V *>(rsm_raw);  /* [3][nlm][QS] */
-	V *ws = cs + 3 * nlm * QS;               /* [N] twiddles */
-	S *ds = reinterpret_cast<S *>(ws + N);   /* [nlm] d^l_{m m1}(beta_b), indexed like lm */
+	V *cs = reinterpret_cast<V *>(rsm_raw);  /* [3][K2][QS] */
+	V *ws = cs + 3 * K2 * QS;                /* [N] twiddles */
+	S *ds = reinterpret_cast<S *>(ws + N);   /* [K2] d^l_{m m1}(beta_b) of the current m, indexed like lm */
 	S sg = conj ? (S)-1 : (S)1;
-	for (int k = threadIdx.x; k < 3 * nlm * QS; k += blockDim.x) {
+	for (int k = threadIdx.x; k < 3 * K2 * QS; k += blockDim.x) {
 		int qq = k % QS, r = k / QS;
-		int lm = lm0 + r % nlm, ch = r / nlm;
+		int lm = r % K2, ch = r / K2;
 		int q = q0 + qq;
 		V v = zero2<V>();
 		if (q < Q) {
@@ -144,39 +143,43 @@ __global__ void k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const S *_
 		cs[k] = v;
 	}
 	for (int k = threadIdx.x; k < N; k += blockDim.x) ws[k] = from2<V>(tw[k]);
-	for (int k = threadIdx.x; k < nlm; k += blockDim.x) {
-		int lm = lm0 + k;
-		int l = 0;
-		while ((l + 1) * (l + 1) <= lm) l++;
-		int m1 = lm - l * (l + 1);
-		ds[k] = dtab[(((size_t)b * K + l) * N + m + L) * N + m1 + L];
-	}
-	__syncthreads();
 	int g = threadIdx.x / QS, qq = threadIdx.x % QS;
-	if (g >= N) return;
-	int po = psym(m, K);
-	V *ob = out + (((size_t)t * nrow + b * N + g) * NP + po) * 3 * SXS_QT + q0 % SXS_QT + qq;
-	for (int l = m; l <= L; l++) {
-		V acc0 = zero2<V>(), acc1 = acc0, acc2 = acc0;
-		int r0 = l * l - lm0;                /* lm = l^2 + (m1 + l) */
-		int e = ((N - l) * g) % N;           /* (m1' g) mod N at m1 = -l */
-		for (int j = 0; j < 2 * l + 1; j++) {
-			S dv = ds[r0 + j];
-			V w = ws[e];
-			V f;
-			f.x = w.x * dv;
-			f.y = w.y * dv;
-			const V *c = cs + (size_t)(r0 + j) * QS + qq;
-			cfma(acc0, f, c[0]);
-			cfma(acc1, f, c[(size_t)nlm * QS]);
-			cfma(acc2, f, c[(size_t)2 * nlm * QS]);
-			e += g;
-			if (e >= N) e -= N;
+	bool act = g < N;
+	const S *db = dtab + (size_t)b * K * N * N;
+	for (int m = mg; m <= L; m += MG) {
+		__syncthreads();   /* previous m done with ds (and the staging above) */
+		for (int lm = m * m + threadIdx.x; lm < K2; lm += blockDim.x) {
+			int l = 0;
+			while ((l + 1) * (l + 1) <= lm) l++;
+			int m1 = lm - l * (l + 1);
+			ds[lm] = db[((size_t)l * N + m + L) * N + m1 + L];
 		}
-		V *o = ob + (size_t)(l - m) * 3 * SXS_QT;
-		o[0] = acc0;
-		o[SXS_QT] = acc1;
-		o[2 * SXS_QT] = acc2;
+		__syncthreads();
+		if (!act) continue;
+		int po = psym(m, K);
+		V *ob = out + (((size_t)t * nrow + b * N + g) * NP + po) * 3 * SXS_QT + q0 % SXS_QT + qq;
+		for (int l = m; l <= L; l++) {
+			V acc0 = zero2<V>(), acc1 = acc0, acc2 = acc0;
+			int r0 = l * l;                      /* lm = l^2 + (m1 + l) */
+			int e = ((N - l) * g) % N;           /* (m1' g) mod N at m1 = -l */
+			for (int j = 0; j < 2 * l + 1; j++) {
+				S dv = ds[r0 + j];
+				V w = ws[e];
+				V f;
+				f.x = w.x * dv;
+				f.y = w.y * dv;
+				const V *c = cs + (size_t)(r0 + j) * QS + qq;
+				cfma(acc0, f, c[0]);
+				cfma(acc1, f, c[(size_t)K2 * QS]);
+				cfma(acc2, f, c[(size_t)2 * K2 * QS]);
+				e += g;
+				if (e >= N) e -= N;
+			}
+			V *o = ob + (size_t)(l - m) * 3 * SXS_QT;
+			o[0] = acc0;
+			o[SXS_QT] = acc1;
+			o[2 * SXS_QT] = acc2;
+		}
 	}
 }
 
@@ -707,18 +710,30 @@ int sxsk_rotate(const void *spf_t, const void *dtab, const double2 *tw, int Q, i
                 cudaStream_t s)
 {
 	int K = L + 1, N = 2 * L + 1, NT = (Q + SXS_QT - 1) / SXS_QT;
-	size_t nlm = (size_t)K * K;  /* at m = 0, the largest */
+	size_t K2 = (size_t)K * K;
 	size_t celem = fp32 ? sizeof(float2) : sizeof(double2);
-	/* q per block: the largest of 8, 4, 2, 1 whose staged coefficients fit */
+	int dev = 0, nsm = 0;
+	cudaGetDevice(&dev);
+	cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+	/* q per block: the largest of the tile width, halves, ... whose staged
+	 * coefficients fit; m groups: enough blocks for two waves */
 	int QS = SXS_QT;
 	size_t smem;
 	for (;;) {
-		smem = celem * (3 * nlm * QS + N) + (fp32 ? sizeof(float) : sizeof(double)) * nlm;
+		smem = celem * (3 * K2 * QS + N) + (fp32 ? sizeof(float) : sizeof(double)) * K2;
 		if (smem <= 200 * 1024 || QS == 1) break;
 		QS /= 2;
 	}
 	if (smem > 227 * 1024) return cudaErrorInvalidValue;
-	long nb = (long)K * K * NT * (SXS_QT / QS);
+	long base = (long)K * NT * (SXS_QT / QS);
+	int threads0 = ((N * QS + 31) / 32) * 32;
+	long bps = (long)(227 * 1024) / (long)smem;
+	if (bps > 2048 / threads0) bps = 2048 / threads0;
+	if (bps < 1) bps = 1;
+	/* m groups: at least four waves of resident blocks */
+	int MG = 1;
+	while (MG < 16 && MG < K && base * MG < 4L * nsm * bps) MG *= 2;
+	long nb = base * MG;
 	int threads = ((N * QS + 31) / 32) * 32;
 	if (fp32) {
 		if (smem > 48 * 1024) {
@@ -727,7 +742,7 @@ int sxsk_rotate(const void *spf_t, const void *dtab, const double2 *tw, int Q, i
 			if (e != cudaSuccess) return e;
 		}
 		k_rotate<float><<<(unsigned)nb, threads, smem, s>>>((const float2 *)spf_t, (const float *)dtab, tw, Q, L,
-		                                                    conj, QS, (float2 *)out);
+		                                                    conj, QS, MG, (float2 *)out);
 	} else {
 		if (smem > 48 * 1024) {
 			cudaError_t e = cudaFuncSetAttribute(k_rotate<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -735,7 +750,7 @@ int sxsk_rotate(const void *spf_t, const void *dtab, const double2 *tw, int Q, i
 			if (e != cudaSuccess) return e;
 		}
 		k_rotate<double><<<(unsigned)nb, threads, smem, s>>>((const double2 *)spf_t, (const double *)dtab, tw, Q,
-		                                                     L, conj, QS, (double2 *)out);
+		                                                     L, conj, QS, MG, (double2 *)out);
 	}
 	return cudaGetLastError();
 }

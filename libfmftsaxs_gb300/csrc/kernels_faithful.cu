@@ -142,19 +142,18 @@ __global__ void k_accum(const double2 *__restrict__ ylm, const double *__restric
 	o[2 * chs] = c_r * wr - c_i * wi;     o[2 * chs + 1] = c_r * wi + c_i * wr;
 }
 
-/* bes[iz][q][p] = j_p(z q) (src/fftsaxs.c:110-121). */
+/* bes[iz][p][q] = j_p(z q) (src/fftsaxs.c:110-121), q fastest. */
 __global__ void k_bessel_z(const double *__restrict__ z, int nz, const double *__restrict__ q, int Q, int L,
                            double *__restrict__ bes)
 {
 	int N = 2 * L + 1;
 	long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
 	if (t >= (long)nz * Q * N) return;
-	int p = (int)(t % N);
-	long r2 = t / N;
-	int iq = (int)(r2 % Q), iz = (int)(r2 / Q);
+	int iq = (int)(t % Q);
+	long r2 = t / Q;
+	int p = (int)(r2 % N), iz = (int)(r2 / N);
 	bes[t] = sbessel(p, z[iz] * q[iq]);
 }
-
 /* T^{|m|}_{l l1}(q z) = sum_p (-1)^m i^p j_p d_lm(l1,p) for l <= l1, mirrored
  * (src/fftsaxs.c:182-243).  Thread = (iz, m, l, l1 >= l, q), q fastest.
  * Output in the q-tiled layout of the contraction tables (tiles of SXS_QT q).
@@ -165,8 +164,6 @@ __global__ void k_bessel_z(const double *__restrict__ z, int nz, const double *_
 __global__ void k_tmatrix(const double *__restrict__ bes, const double *__restrict__ ds, int nz, int Q, int L,
                           const int2 *__restrict__ ll1, int nll1, double *__restrict__ tau)
 {
-	const double ipr[4] = {1.0, 0.0, -1.0, 0.0};
-	const double ipi[4] = {0.0, 1.0, 0.0, -1.0};
 	int K = L + 1, N = 2 * L + 1;
 	long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
 	if (t >= (long)nz * (K) * nll1 * Q) return;
@@ -179,21 +176,26 @@ __global__ void k_tmatrix(const double *__restrict__ bes, const double *__restri
 	if (l < m) return;
 	double sgn = (m % 2 == 0) ? 1.0 : -1.0;
 	const double *dp = ds + ((size_t)lm_index(l, m) * K + l1) * N;
-	const double *bp = bes + ((size_t)iz * Q + iq) * N;
-	double re = 0.0, im = 0.0;
-	int p0 = l1 - l;  /* |l - l1| with l <= l1 */
-	for (int p = p0; p <= l + l1; p++) {
-		double v = sgn * dp[p] * bp[p];
-		re += ipr[p % 4] * v;
-		im += ipi[p % 4] * v;
+	const double *bp = bes + (size_t)iz * N * Q + iq;
+	/* the reference sums Re and Im with i^p in {1, i, -1, -i}; for the
+	 * component kept here (Re for even l + l1, Im for odd) the terms with p
+	 * of the other parity add +-0, so summing only p = l + l1 (mod 2), in
+	 * the same order, gives the same value bit for bit */
+	double v = 0.0;
+	int p0 = l1 - l;  /* |l - l1| with l <= l1, same parity as l + l1 */
+	int odd = (l + l1) & 1;
+	for (int p = p0; p <= l + l1; p += 2) {
+		double w = sgn * dp[p] * bp[(size_t)p * Q];
+		/* i^p for even p: +1 (p % 4 == 0), -1 (p % 4 == 2); the imaginary unit
+		 * of i^p for odd p: +1 (p % 4 == 1), -1 (p % 4 == 3) */
+		int neg = odd ? ((p & 3) == 3) : ((p & 3) == 2);
+		v += (neg ? -1.0 : 1.0) * w;
 	}
-	double v = ((l + l1) & 1) ? im : re;
 	/* q-tiled: [tile][iz][m][l][l1][SXS_QT], tile = q / SXS_QT */
 	size_t base = (((size_t)(iq / SXS_QT) * nz + iz) * K + m) * K;
 	tau[((base + l) * K + l1) * SXS_QT + iq % SXS_QT] = v;
 	tau[((base + l1) * K + l) * SXS_QT + iq % SXS_QT] = v;
 }
-
 /* Cross terms of single molecules (src/min_saxs.c:450-494): for each
  * molecule and q, sum over lm of |V|^2, |D|^2, |W|^2, Re(V conj D),
  * Re(V conj W), Re(D conj W) in the reference's order, the three mixed sums

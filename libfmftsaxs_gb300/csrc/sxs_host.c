@@ -193,6 +193,9 @@ struct sxsg_plan {
 	/* rotation tables (depend on the twiddle variant) */
 	void *d_P, *d_U;
 	int ext_tables;             /* P and U belong to the caller (serving cache) */
+	int rot_engine;             /* SXSG_ROT_*: rotation on CUDA cores or tensor cores */
+	int tc_used;                /* the last run rotated on the tensor cores */
+	float *d_amat;              /* twiddle operand of the tensor-core rotation */
 	int P_valid, U_valid;       /* caller tables already hold this run's rows */
 	int tw_variant; /* -1 none, 0 simple_ft, 1 exact */
 	/* poses */
@@ -252,7 +255,7 @@ void sxsg_plan_destroy(sxsg_plan *p)
 	plan_free_poses(p);
 	pfree(p, p->d_A); pfree(p, p->d_B); pfree(p, p->d_q); pfree(p, p->d_fc); pfree(p, p->d_a); pfree(p, p->d_gtab); pfree(p, p->d_gdf);
 	pfree(p, p->d_c1g); pfree(p, p->d_c2g); pfree(p, p->d_cst); pfree(p, p->d_At); pfree(p, p->d_Bt);
-	pfree(p, p->d_tw); pfree(p, p->d_R);
+	pfree(p, p->d_tw); pfree(p, p->d_R); pfree(p, p->d_amat);
 	if (!p->ext_tables) {
 		pfree(p, p->d_P);
 		pfree(p, p->d_U);
@@ -390,6 +393,14 @@ int sxs_plan_create_on(sxsg_plan **out, const double *A, const double *B, const 
 	cudaMemGetInfo(&fr, &tot);
 	p->r_budget = fr / 2;
 	*out = p;
+	return 0;
+}
+
+int sxsg_plan_set_rotation(sxsg_plan *p, int engine)
+{
+	if (!p || (engine != SXSG_ROT_CUDA && engine != SXSG_ROT_TC))
+		return sxs_fail(-2, "sxsg_plan_set_rotation: bad arguments");
+	p->rot_engine = engine;
 	return 0;
 }
 
@@ -558,14 +569,20 @@ static int plan_tables(sxsg_plan *p)
 		free(tw);
 		if (e) return sxs_cuda_fail(e, "twiddle upload");
 		const void *dtab = p->fp32 ? (const void *)p->lt->d_dtabf : (const void *)p->lt->d_dtab;
+		int tc = p->fp32 && p->rot_engine == SXSG_ROT_TC && 2 * N <= 128;
+		if (tc && !p->d_amat)
+			SXS_CU(cudaMallocAsync((void **)&p->d_amat, sizeof(float) * sxsk_rotate_tc_scratch(L), s));
 		if (!p->ext_tables || !p->P_valid) {
-			SXS_K(sxsk_rotate(p->d_At, dtab, p->d_tw, Q, L, 0, p->d_P, p->fp32, s));
+			if (tc) SXS_K(sxsk_rotate_tc(p->d_At, p->lt->d_dtabf, p->d_tw, Q, L, 0, p->d_P, p->d_amat, s));
+			else SXS_K(sxsk_rotate(p->d_At, dtab, p->d_tw, Q, L, 0, p->d_P, p->fp32, s));
 			sxs_count_launches(1);
 		}
 		if (!p->ext_tables || !p->U_valid) {
-			SXS_K(sxsk_rotate(p->d_Bt, dtab, p->d_tw, Q, L, 1, p->d_U, p->fp32, s));
+			if (tc) SXS_K(sxsk_rotate_tc(p->d_Bt, p->lt->d_dtabf, p->d_tw, Q, L, 1, p->d_U, p->d_amat, s));
+			else SXS_K(sxsk_rotate(p->d_Bt, dtab, p->d_tw, Q, L, 1, p->d_U, p->fp32, s));
 			sxs_count_launches(1);
 		}
+		p->tc_used = tc;
 		if (p->ext_tables) p->P_valid = p->U_valid = 1;
 		p->tw_variant = variant;
 	}
@@ -711,6 +728,8 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 	if (!pipe) cudaEventElapsedTime(&t_fit, p->ev[5], end);
 	cudaEventDestroy(end);
 	p->ms[0] = t_tab; p->ms[1] = t_tr; p->ms[2] = t_pc; p->ms[3] = t_fit; p->ms[4] = t_all;
+	if (p->tc_used && sxsk_rotate_tc_status())
+		return sxs_fail(-6, "sxsg_plan_run: the tensor-core rotation did not complete (MMA wait gave up)");
 	return 0;
 }
 
