@@ -6,7 +6,8 @@
  *
  * A double-float is the unevaluated sum hi + lo of two floats with
  * |lo| <= ulp(hi)/2 (Dekker's two-product via fmaf, Knuth's two-sum); each
- * operation below is accurate to about 2^-48 relative.
+ * operation below is accurate to about 2^-48 relative (the lazy forms to a
+ * few units of 2^-48).
  *
  * The fit follows point_score and best_scale of the reference
  * (src/min_saxs.c:261-320, 391-448): for one c1 the model at q_i is
@@ -77,6 +78,27 @@ DF_HD dfl df_twice(dfl a) { return df_mk(2.0f * a.hi, 2.0f * a.lo); }
 DF_HD int df_gt(dfl a, dfl b) { return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo); }
 DF_HD int df_pos(dfl a) { return a.hi > 0.0f || (a.hi == 0.0f && a.lo > 0.0f); }
 
+/* Lazy forms: results are unevaluated sums hi + lo that are not
+ * renormalised (|lo| stays a few ulp of hi unless the operands cancel), so
+ * each saves the final fast-two-sum of df_mul / df_add.  Products drop
+ * only lo*lo; sums keep the two-sum error and add the tails in float. */
+DF_HD dfl lz_mul(dfl a, dfl b)
+{
+	float p = a.hi * b.hi;
+	float e = fmaf(a.hi, b.hi, -p);
+	e = fmaf(a.hi, b.lo, e);
+	e = fmaf(a.lo, b.hi, e);
+	return df_mk(p, e);
+}
+DF_HD dfl lz_add(dfl a, dfl b)
+{
+	dfl s = df_two_sum(a.hi, b.hi);
+	return df_mk(s.hi, s.lo + (a.lo + b.lo));
+}
+DF_HD dfl lz_norm(dfl a) { return df_fast_two_sum(a.hi, a.lo); }
+/* y*x + c, unnormalised */
+DF_HD dfl lz_fma(dfl y, dfl x, dfl c) { return lz_add(lz_mul(y, x), c); }
+
 /* compensated float sum: s + c tracks the exact sum of the added floats */
 typedef struct {
 	float s, c;
@@ -89,17 +111,21 @@ DF_HD void fs_add(fsum *a, float x)
 }
 DF_HD dfl fs_df(fsum a) { return df_fast_two_sum(a.s, a.c); }
 
-/* One pose's channel rows c[8][Q] = VV VD VW DD DW WW F3G P4 (model
- * normalised), constants fs[5][Q] = a3 e f a1 u.  For q = i0, i0+step, ...:
- * F3G = a3 ga (double-float), P4 = {e ga + f D_ga, e D_ga} (two floats,
- * D_ga = ga_i - ga_{i-1}), and the partial sums of the c2^2 coefficients. */
-DF_HD void df_pose_prep(dfl *c, const dfl *fs, int Q, int i0, int step, dfl *u2, dfl *d4)
+/* Per-pose work of one run of n consecutive q.  Channel rows start at c
+ * with row stride ld: VV VD VW DD DW WW F3G P4 (model normalised); c[-1] of
+ * each row is the previous q unless `first` (the run starts at q = 0).
+ * Constants fs[5][ldf] = a3 e f a1 u start at the same q.  For local
+ * k = k0, k0+step, ...: F3G = a3 ga (double-float), P4 = {e ga + f D_ga,
+ * e D_ga} (two floats, D_ga = ga_q - ga_{q-1}), and the partial sums of the
+ * c2^2 coefficients are added to u2, d4. */
+DF_HD void df_pose_prep_run(dfl *c, int ld, const dfl *fs, int ldf, int k0, int n, int step, int first, dfl *u2,
+                            dfl *d4)
 {
-	const dfl *WW = c + 5 * Q, *F3 = fs, *FE = fs + Q, *FF = fs + 2 * Q, *F1 = fs + 3 * Q, *FU = fs + 4 * Q;
-	dfl *F3G = c + 6 * Q, *P4 = c + 7 * Q;
-	dfl su = df_mk(0, 0), sd = df_mk(0, 0);
-	for (int i = i0; i < Q; i += step) {
-		dfl ga = WW[i], dg = i > 0 ? df_sub(ga, WW[i - 1]) : df_mk(0, 0);
+	const dfl *WW = c + 5 * ld, *F3 = fs, *FE = fs + ldf, *FF = fs + 2 * ldf, *F1 = fs + 3 * ldf, *FU = fs + 4 * ldf;
+	dfl *F3G = c + 6 * ld, *P4 = c + 7 * ld;
+	dfl su = *u2, sd = *d4;
+	for (int i = k0; i < n; i += step) {
+		dfl ga = WW[i], dg = (i > 0 || !first) ? df_sub(ga, WW[i - 1]) : df_mk(0, 0);
 		dfl p3 = df_fma(F3[i], ga, df_mul(FE[i], dg));
 		dfl p4 = df_fma(FE[i], ga, df_mul(FF[i], dg));
 		F3G[i] = df_mul(F3[i], ga);
@@ -111,78 +137,133 @@ DF_HD void df_pose_prep(dfl *c, const dfl *fs, int Q, int i0, int step, dfl *u2,
 	*d4 = sd;
 }
 
-/* Coefficients for one c1 (G[i] = c1^3 exp(-mult (c1^2-1) q_i^2)):
- * up = u[0] + c2 u[1] + c2^2 U2, down = d[0] + c2 d[1] + ... + c2^4 D4.
- * The model in_i (al + c2 be + c2^2 ga) and the terms that carry the
- * cancellation of the score, a3 in^2 and a1 in, are double-float; the terms
- * with a difference D_i = in_i - in_{i-1} or a bin offset (e, f, u) are at
- * most a few percent of those and are summed as compensated floats. */
-DF_HD void df_row(const dfl *c, const dfl *fs, const dfl *G, int Q, dfl *u, dfl *d)
+/* All Q at once: rows c[8][Q], constants fs[5][Q], q = i0, i0+step, ... */
+DF_HD void df_pose_prep(dfl *c, const dfl *fs, int Q, int i0, int step, dfl *u2, dfl *d4)
 {
-	const dfl *VV = c, *VD = c + Q, *VW = c + 2 * Q, *DD = c + 3 * Q, *DW = c + 4 * Q, *WW = c + 5 * Q;
-	const dfl *F3G = c + 6 * Q, *P4 = c + 7 * Q;
-	const dfl *F3 = fs, *FE = fs + Q, *FF = fs + 2 * Q, *F1 = fs + 3 * Q, *FU = fs + 4 * Q;
+	*u2 = df_mk(0, 0);
+	*d4 = df_mk(0, 0);
+	df_pose_prep_run(c, Q, fs, Q, i0, Q, step, 1, u2, d4);
+}
+
+/* Running sums of one (pose, c1) over q (df_row below). */
+typedef struct {
+	dfl U0, U1, D0, D1, D2a, D2b, D3, alp, bep;
+	fsum e0, e1, e2, e3, e4, eu0, eu1;
+} df_rowst;
+
+/* model terms at one q: al = VV + g (g DD - VD), be = VW - g DW */
+DF_HD void df_model(const dfl *c, int ld, dfl g, dfl *al, dfl *be)
+{
+	*al = lz_norm(lz_add(c[0], lz_mul(g, lz_add(lz_mul(g, c[3 * ld]), df_neg(c[ld])))));
+	*be = lz_norm(lz_add(c[2 * ld], df_neg(lz_mul(g, c[4 * ld]))));
+}
+
+/* start at q = 0 (c, g: the rows and G there) */
+DF_HD void df_row_init(df_rowst *r, const dfl *c, int ld, dfl g)
+{
 	dfl z = df_mk(0, 0);
-	dfl U0 = z, U1 = z, D0 = z, D1 = z, D2a = z, D2b = z, D3 = z;
-	fsum e0 = {0, 0}, e1 = {0, 0}, e2 = {0, 0}, e3 = {0, 0}, e4 = {0, 0}, eu0 = {0, 0}, eu1 = {0, 0};
-	dfl g = G[0];
-	dfl alp = df_fma(g, df_fma(g, DD[0], df_neg(VD[0])), VV[0]);
-	dfl bep = df_fma(df_neg(g), DW[0], VW[0]);
-	for (int i = 0; i < Q; i++) {
-		g = G[i];
-		dfl al = df_fma(g, df_fma(g, DD[i], df_neg(VD[i])), VV[i]);
-		dfl be = df_fma(df_neg(g), DW[i], VW[i]);
+	fsum f = {0, 0};
+	r->U0 = r->U1 = r->D0 = r->D1 = r->D2a = r->D2b = r->D3 = z;
+	r->e0 = r->e1 = r->e2 = r->e3 = r->e4 = r->eu0 = r->eu1 = f;
+	df_model(c, ld, g, &r->alp, &r->bep);
+}
+
+/* n consecutive q: rows from c (stride ld, F3G and P4 filled), constants
+ * fs (stride ldf) and G from the first of them.
+ * The model in_q (al + c2 be + c2^2 ga) and the terms that carry the
+ * cancellation of the score, a3 in^2 and a1 in, are double-float (lazy
+ * products and sums, renormalised once per q for al and be); the terms with
+ * a difference D_q = in_q - in_{q-1} or a bin offset (e, f, u) are at most a
+ * few percent of those and are summed as compensated floats. */
+DF_HD void df_row_run(df_rowst *r, const dfl *c, int ld, const dfl *fs, int ldf, const dfl *G, int n)
+{
+	const dfl *F3G = c + 6 * ld, *P4 = c + 7 * ld;
+	const dfl *F3 = fs, *FE = fs + ldf, *FF = fs + 2 * ldf, *F1 = fs + 3 * ldf, *FU = fs + 4 * ldf;
+	dfl U0 = r->U0, U1 = r->U1, D0 = r->D0, D1 = r->D1, D2a = r->D2a, D2b = r->D2b, D3 = r->D3;
+	dfl alp = r->alp, bep = r->bep;
+	fsum e0 = r->e0, e1 = r->e1, e2 = r->e2, e3 = r->e3, e4 = r->e4, eu0 = r->eu0, eu1 = r->eu1;
+#ifdef __CUDACC__
+#pragma unroll 2
+#endif
+	for (int i = 0; i < n; i++) {
+		dfl al, be;
+		df_model(c + i, ld, G[i], &al, &be);
 		float d0 = (al.hi - alp.hi) + (al.lo - alp.lo);
 		float d1 = (be.hi - bep.hi) + (be.lo - bep.lo);
 		float a = al.hi, b = be.hi;
 		float fe = FE[i].hi, ff = FF[i].hi;
-		dfl t = df_mul(F3[i], al), v = df_mul(F3[i], be);
-		D0 = df_fma(t, al, D0);                 /* a3 al^2 */
-		D1 = df_fma(t, be, D1);                 /* a3 al be */
-		D2a = df_fma(v, be, D2a);               /* a3 be^2 */
-		D2b = df_fma(al, F3G[i], D2b);          /* a3 al ga */
-		D3 = df_fma(be, F3G[i], D3);            /* a3 be ga */
-		U0 = df_fma(F1[i], al, U0);
-		U1 = df_fma(F1[i], be, U1);
+		dfl t = lz_mul(F3[i], al), v = lz_mul(F3[i], be), f3g = F3G[i], f1 = F1[i];
+		D0 = lz_fma(t, al, D0);                 /* a3 al^2 */
+		D1 = lz_fma(t, be, D1);                 /* a3 al be */
+		D2a = lz_fma(v, be, D2a);               /* a3 be^2 */
+		D2b = lz_fma(al, f3g, D2b);             /* a3 al ga */
+		D3 = lz_fma(be, f3g, D3);               /* a3 be ga */
+		U0 = lz_fma(f1, al, U0);
+		U1 = lz_fma(f1, be, U1);
 		float p4 = P4[i].hi, edg = P4[i].lo;    /* e ga + f D_ga, e D_ga */
-		fs_add(&e0, a * (2.0f * fe * d0) + ff * d0 * d0);
-		fs_add(&e1, fe * (a * d1 + b * d0) + ff * d0 * d1);
-		fs_add(&e2, b * (2.0f * fe * d1) + ff * d1 * d1);
-		fs_add(&e3, a * edg + d0 * p4);
-		fs_add(&e4, b * edg + d1 * p4);
+		float fa = fe * a, fb = fe * b, fd0 = ff * d0;
+		fs_add(&e0, d0 * fmaf(ff, d0, fa + fa));              /* 2 e al D_al + f D_al^2 */
+		fs_add(&e1, fmaf(fa, d1, fmaf(fb, d0, fd0 * d1)));  /* e (al D_be + be D_al) + f D_al D_be */
+		fs_add(&e2, d1 * fmaf(ff, d1, fb + fb));              /* 2 e be D_be + f D_be^2 */
+		fs_add(&e3, fmaf(a, edg, d0 * p4));
+		fs_add(&e4, fmaf(b, edg, d1 * p4));
 		fs_add(&eu0, FU[i].hi * d0);
 		fs_add(&eu1, FU[i].hi * d1);
 		alp = al;
 		bep = be;
 	}
-	u[0] = df_add(U0, fs_df(eu0));
-	u[1] = df_add(U1, fs_df(eu1));
-	d[0] = df_add(D0, fs_df(e0));
-	d[1] = df_twice(df_add(D1, fs_df(e1)));
-	d[2] = df_add(df_add(D2a, fs_df(e2)), df_twice(df_add(D2b, fs_df(e3))));
-	d[3] = df_twice(df_add(D3, fs_df(e4)));
+	r->U0 = U0; r->U1 = U1; r->D0 = D0; r->D1 = D1; r->D2a = D2a; r->D2b = D2b; r->D3 = D3;
+	r->alp = alp; r->bep = bep;
+	r->e0 = e0; r->e1 = e1; r->e2 = e2; r->e3 = e3; r->e4 = e4; r->eu0 = eu0; r->eu1 = eu1;
 }
 
-DF_HD dfl df_up(const dfl *u, dfl U2, dfl c2) { return df_fma(c2, df_fma(c2, U2, u[1]), u[0]); }
+/* up = u[0] + c2 u[1] + c2^2 U2, down = d[0] + c2 d[1] + ... + c2^4 D4 */
+DF_HD void df_row_finish(const df_rowst *r, dfl *u, dfl *d)
+{
+	u[0] = df_add(lz_norm(r->U0), fs_df(r->eu0));
+	u[1] = df_add(lz_norm(r->U1), fs_df(r->eu1));
+	d[0] = df_add(lz_norm(r->D0), fs_df(r->e0));
+	d[1] = df_twice(df_add(lz_norm(r->D1), fs_df(r->e1)));
+	d[2] = df_add(df_add(lz_norm(r->D2a), fs_df(r->e2)), df_twice(df_add(lz_norm(r->D2b), fs_df(r->e3))));
+	d[3] = df_twice(df_add(lz_norm(r->D3), fs_df(r->e4)));
+}
+
+/* Coefficients for one c1 (G[q] = c1^3 exp(-mult (c1^2-1) q^2)) over all
+ * Q: rows c[8][Q] after df_pose_prep, constants fs[5][Q]. */
+DF_HD void df_row(const dfl *c, const dfl *fs, const dfl *G, int Q, dfl *u, dfl *d)
+{
+	df_rowst r;
+	df_row_init(&r, c, Q, G[0]);
+	df_row_run(&r, c, Q, fs, Q, G, Q);
+	df_row_finish(&r, u, d);
+}
+
+DF_HD dfl df_up(const dfl *u, dfl U2, dfl c2) { return lz_norm(lz_fma(c2, lz_fma(c2, U2, u[1]), u[0])); }
 DF_HD dfl df_down(const dfl *d, dfl D4, dfl c2)
 {
-	return df_fma(c2, df_fma(c2, df_fma(c2, df_fma(c2, D4, d[3]), d[2]), d[1]), d[0]);
+	return lz_norm(lz_fma(c2, lz_fma(c2, lz_fma(c2, lz_fma(c2, D4, d[3]), d[2]), d[1]), d[0]));
 }
 
 /* Best c2 cell of one c1 row: the largest up^2/down over cells with
- * down > 0 (lowest index on ties); returns its index or -1. */
+ * down > 0 (lowest index on ties); returns its index or -1.  The test
+ * up^2 xd > xu^2 down is the sign of their lazy difference. */
 DF_HD int df_best_c2(const dfl *u, dfl U2, const dfl *d, dfl D4, const dfl *c2s, int n2, dfl *bu, dfl *bd)
 {
 	int bi = -1;
-	dfl xu = df_mk(0, 0), xd = df_mk(0, 0);
+	dfl xu = df_mk(0, 0), xd = df_mk(0, 0), xuu = df_mk(0, 0);
 	for (int i2 = 0; i2 < n2; i2++) {
 		dfl up = df_up(u, U2, c2s[i2]);
 		dfl down = df_down(d, D4, c2s[i2]);
-		if (df_pos(down) && (bi < 0 || df_gt(df_mul(df_mul(up, up), xd), df_mul(df_mul(xu, xu), down)))) {
-			xu = up;
-			xd = down;
-			bi = i2;
+		if (!df_pos(down)) continue;
+		dfl uu = lz_mul(up, up);
+		if (bi >= 0) {
+			dfl diff = lz_add(lz_mul(uu, xd), df_neg(lz_mul(xuu, down)));
+			if (!(diff.hi + diff.lo > 0.0f)) continue;
 		}
+		xu = up;
+		xd = down;
+		xuu = uu;
+		bi = i2;
 	}
 	*bu = xu;
 	*bd = xd;

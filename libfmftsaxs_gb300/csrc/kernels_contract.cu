@@ -94,6 +94,26 @@ __device__ __forceinline__ Pair2<double> ld2(const double2 *p)
 	r.b = p[1];
 	return r;
 }
+/* L2 eviction policies for streamed (evict_first) and reused (evict_last) rows */
+__device__ __forceinline__ uint64_t l2_policy(bool keep)
+{
+	uint64_t pol;
+	if (keep) asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+	else asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+	return pol;
+}
+__device__ __forceinline__ Pair2<float> ld2_pol(const float2 *p, uint64_t pol)
+{
+	float4 v;
+	asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+	    : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+	    : "l"(p), "l"(pol));
+	Pair2<float> r;
+	r.a = make_float2(v.x, v.y);
+	r.b = make_float2(v.z, v.w);
+	return r;
+}
+__device__ __forceinline__ Pair2<double> ld2_pol(const double2 *p, uint64_t) { return ld2(p); }
 __device__ __forceinline__ void st2(float2 *p, float2 a, float2 b)
 {
 	*reinterpret_cast<float4 *>(p) = make_float4(a.x, a.y, b.x, b.y);
@@ -344,10 +364,12 @@ k_translate_col(const typename Cx<S>::T *__restrict__ U, const S *__restrict__ t
 /* Per-pose cross terms of one chunk, all q tiles.  Thread = (pose, 2
  * adjacent q); block = 32 consecutive poses (sorted by combo, so their R
  * rows repeat and hit in L1) x 4 q pairs of one tile; blocks ordered
- * tile-major.  The pose's phase w_m = tw[(m a2) mod N] (doubled for m > 0)
+ * tile-major.  HINT: P rows (reused by every pose of the same rotation) are
+ * loaded with the L2 evict_last policy, R rows (streamed once per chunk)
+ * with evict_first.  The pose's phase w_m = tw[(m a2) mod N] (doubled for m > 0)
  * is applied to R first, so each channel product needs only its real part:
  *   cross[src][c][q] = cst[c][q] + 2 sum_{m,l} Re(P_a[m,l] (w_m R_b[m,l])). */
-template <typename S>
+template <typename S, bool HINT>
 __global__ void __launch_bounds__(128)
 k_pose_cross(const sxsk_pose *__restrict__ poses, int npose, int combo_base, int ncombo,
              const typename Cx<S>::T *__restrict__ P, const typename Cx<S>::T *__restrict__ R,
@@ -376,6 +398,11 @@ k_pose_cross(const sxsk_pose *__restrict__ poses, int npose, int combo_base, int
 	 * changes where a row of m starts */
 	int m = 0, mend = K, e = 0;
 	S wx = tws[0].x, wy = tws[0].y;
+	uint64_t polP = 0, polR = 0;
+	if (HINT) {
+		polP = l2_policy(true);
+		polR = l2_policy(false);
+	}
 #pragma unroll 2
 	for (int p = 0; p < NP; p++) {
 		if (p == mend) {
@@ -391,8 +418,13 @@ k_pose_cross(const sxsk_pose *__restrict__ poses, int npose, int combo_base, int
 		Pair2<S> cp[3], cr[3];
 #pragma unroll
 		for (int c = 0; c < 3; c++) {
-			cp[c] = ld2(pp + c * SXS_QT);
-			cr[c] = ld2(rr + c * SXS_QT);
+			if (HINT) {
+				cp[c] = ld2_pol(pp + c * SXS_QT, polP);
+				cr[c] = ld2_pol(rr + c * SXS_QT, polR);
+			} else {
+				cp[c] = ld2(pp + c * SXS_QT);
+				cr[c] = ld2(rr + c * SXS_QT);
+			}
 		}
 #pragma unroll
 		for (int k = 0; k < 2; k++) {
@@ -783,10 +815,10 @@ int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, int ncomb
 	long nb = (long)NT * ((npose + PC_PPB - 1) / PC_PPB);
 	if (nb > 0x7fffffffL) return cudaErrorInvalidValue;
 	if (fp32)
-		k_pose_cross<float><<<(unsigned)nb, 128, 0, s>>>(poses, npose, combo_base, ncombo, (const float2 *)P,
+		k_pose_cross<float, true><<<(unsigned)nb, 128, 0, s>>>(poses, npose, combo_base, ncombo, (const float2 *)P,
 		                                                  (const float2 *)R, tw, cst, Q, L, cross);
 	else
-		k_pose_cross<double><<<(unsigned)nb, 128, 0, s>>>(poses, npose, combo_base, ncombo, (const double2 *)P,
+		k_pose_cross<double, false><<<(unsigned)nb, 128, 0, s>>>(poses, npose, combo_base, ncombo, (const double2 *)P,
 		                                                   (const double2 *)R, tw, cst, Q, L, cross);
 	return cudaGetLastError();
 }

@@ -22,19 +22,32 @@ namespace {
 
 #define FITD_THREADS 128
 #define FITD_NFC 5
+/* q per staged chunk at most: the pose rows of a block take
+ * ppb * 8 * (qc + 1) double-floats of shared memory instead of ppb * 8 * Q */
+#define FITD_QC 32
+/* G(c1, q) is staged in shared memory up to this size, else read from global */
+#define FITD_GSMEM (64 * 1024)
 
+/* Block = ppb poses x tp threads; thread (pose, c1 row lt, lt + tp, ...).
+ * Per group of poses the q range runs in chunks of qc: the block stages the
+ * chunk's normalised channel rows (plus the q before it), fills F3G and P4,
+ * and every thread advances the running sums of its (pose, c1) over the
+ * chunk.  After the last chunk a thread has the polynomial coefficients of
+ * its row and scans the c2 cells. */
 __global__ void __launch_bounds__(FITD_THREADS)
 k_fit_grid_df(const double *__restrict__ cross, const sxsk_pose *__restrict__ order, int slot0, int nslot, int Q,
               const double *__restrict__ fc, double a0sum, double peak, const float2 *__restrict__ gdf,
               const double *__restrict__ c1g, int n1, const double *__restrict__ c2g, int n2, int tp, int ppb,
-              double *__restrict__ chi, double *__restrict__ c1o, double *__restrict__ c2o,
+              int qc, int gsm, double *__restrict__ chi, double *__restrict__ c1o, double *__restrict__ c2o,
               int32_t *__restrict__ cello, double *__restrict__ grid, double *__restrict__ scaled)
 {
 	extern __shared__ double sm[];
-	dfl *cs = reinterpret_cast<dfl *>(sm);             /* [ppb][8][Q]: VV VD VW DD DW WW P3 P4 */
-	dfl *fs = cs + (size_t)ppb * 8 * Q;                /* [FITD_NFC][Q] */
+	int ld = qc + 1;                                   /* staged q per row: the previous q + the chunk */
+	dfl *cs = reinterpret_cast<dfl *>(sm);             /* [ppb][8][ld]: VV VD VW DD DW WW F3G P4 */
+	dfl *fs = cs + (size_t)ppb * 8 * ld;               /* [FITD_NFC][Q] */
 	dfl *c2s = fs + (size_t)FITD_NFC * Q;              /* [n2] */
-	double *red = reinterpret_cast<double *>(c2s + n2); /* [ppb*tp][2] */
+	dfl *gs = c2s + n2;                                /* [n1][Q] G(c1, q) when gsm */
+	double *red = reinterpret_cast<double *>(gs + (gsm ? (size_t)n1 * Q : 0)); /* [ppb*tp][2] */
 	int *redc = (int *)(red + 2 * ppb * tp);           /* [ppb*tp] */
 	double *sf = (double *)(redc + ((ppb * tp + 1) & ~1)); /* [ppb][2]: 1/norm, peak/norm */
 	dfl *sfd = reinterpret_cast<dfl *>(sf + 2 * ppb);  /* [ppb][2]: U2, D4 */
@@ -48,7 +61,14 @@ k_fit_grid_df(const double *__restrict__ cross, const sxsk_pose *__restrict__ or
 		fs[k] = df_from(fc[i * FITD_NFC + c] * (c < 3 ? pk2 : peak));
 	}
 	for (int k = tid; k < n2; k += blockDim.x) c2s[k] = df_from(c2g[k]);
+	if (gsm)
+		for (int k = tid; k < n1 * Q; k += blockDim.x) {
+			float2 v = gdf[k];
+			gs[k] = df_mk(v.x, v.y);
+		}
+	const dfl *gtab = gsm ? gs : reinterpret_cast<const dfl *>(gdf);
 	int ngroup = (nslot + ppb - 1) / ppb;
+	int nround = (n1 + tp - 1) / tp;
 	for (int grp = blockIdx.x; grp < ngroup; grp += gridDim.x) {
 		int s0 = grp * ppb;
 		int nhere = min(ppb, nslot - s0);
@@ -62,42 +82,60 @@ k_fit_grid_df(const double *__restrict__ cross, const sxsk_pose *__restrict__ or
 			sf[2 * tid] = 1.0 / sc;
 			sf[2 * tid + 1] = peak / sc;
 		}
-		__syncthreads();
-		for (int k = tid; k < nhere * 6 * Q; k += blockDim.x) {
-			int p = k / (6 * Q), r = k % (6 * Q);
-			double v = cross[(size_t)srcs[p] * 6 * Q + r];
-			cs[(size_t)p * 8 * Q + r] = df_from(v * sf[2 * p]);
-			if (scaled) scaled[(size_t)srcs[p] * 6 * Q + r] = v * sf[2 * p + 1];
-		}
-		__syncthreads();
-		dfl *c = cs + (size_t)lp * 8 * Q;
-		if (live) {
-			dfl u2, d4;
-			df_pose_prep(c, fs, Q, lt, tp, &u2, &d4);
-			red[2 * tid] = df_to(u2);
-			red[2 * tid + 1] = df_to(d4);
-		}
-		__syncthreads();
-		if (live && lt == 0) {
-			/* partial sums added in double: exact enough and order-fixed */
-			double u2 = 0, d4 = 0;
-			for (int t = 0; t < tp; t++) {
-				u2 += red[2 * (tid + t)];
-				d4 += red[2 * (tid + t) + 1];
-			}
-			sfd[2 * lp] = df_from(u2);
-			sfd[2 * lp + 1] = df_from(d4);
-		}
-		__syncthreads();
 		double bscore = __longlong_as_double(0x7ff0000000000000LL);
 		int bcell = -1;
 		int pid = live ? srcs[lp] : 0;
-		if (live) {
-			dfl U2 = sfd[2 * lp], D4 = sfd[2 * lp + 1];
-			for (int j = lt; j < n1; j += tp) {
-				const dfl *G = reinterpret_cast<const dfl *>(gdf) + (size_t)j * Q;
+		dfl *c = cs + (size_t)lp * 8 * ld;
+		for (int round = 0; round < nround; round++) {
+			int j = lt + round * tp;
+			bool row = live && j < n1;
+			const dfl *G = gtab + (size_t)(row ? j : 0) * Q;
+			df_rowst st;
+			dfl u2 = df_mk(0, 0), d4 = df_mk(0, 0);
+			for (int q0 = 0; q0 < Q; q0 += qc) {
+				int n = min(qc, Q - q0);
+				__syncthreads();   /* previous chunk done (and sf written) */
+				int w = n + 1;
+				for (int k = tid; k < nhere * 6 * w; k += blockDim.x) {
+					int p = k / (6 * w), r = k % (6 * w);
+					int ch = r / w, kk = r % w;
+					int q = q0 - 1 + kk;
+					dfl v = df_mk(0, 0);
+					if (q >= 0) {
+						double x = cross[(size_t)srcs[p] * 6 * Q + ch * Q + q];
+						v = df_from(x * sf[2 * p]);
+						if (scaled && kk > 0 && round == 0) scaled[(size_t)srcs[p] * 6 * Q + ch * Q + q] = x * sf[2 * p + 1];
+					}
+					cs[(size_t)p * 8 * ld + ch * ld + kk] = v;
+				}
+				__syncthreads();
+				if (live) df_pose_prep_run(c + 1, ld, fs + q0, Q, lt, n, tp, q0 == 0, &u2, &d4);
+				__syncthreads();
+				if (row) {
+					if (q0 == 0) df_row_init(&st, c + 1, ld, G[0]);
+					df_row_run(&st, c + 1, ld, fs + q0, Q, G + q0, n);
+				}
+			}
+			if (live) {
+				red[2 * tid] = df_to(u2);
+				red[2 * tid + 1] = df_to(d4);
+			}
+			__syncthreads();
+			if (live && lt == 0) {
+				/* partial sums added in double: exact enough and order-fixed */
+				double a = 0, b = 0;
+				for (int t = 0; t < tp; t++) {
+					a += red[2 * (tid + t)];
+					b += red[2 * (tid + t) + 1];
+				}
+				sfd[2 * lp] = df_from(a);
+				sfd[2 * lp + 1] = df_from(b);
+			}
+			__syncthreads();
+			if (row) {
+				dfl U2 = sfd[2 * lp], D4 = sfd[2 * lp + 1];
 				dfl u[2], d[4];
-				df_row(c, fs, G, Q, u, d);
+				df_row_finish(&st, u, d);
 				if (grid) {
 					for (int i2 = 0; i2 < n2; i2++) {
 						double uu = df_to(df_up(u, U2, c2s[i2])), dd = df_to(df_down(d, D4, c2s[i2]));
@@ -118,6 +156,8 @@ k_fit_grid_df(const double *__restrict__ cross, const sxsk_pose *__restrict__ or
 					}
 				}
 			}
+		}
+		if (live) {
 			red[2 * tid] = bscore;
 			redc[tid] = bcell;
 		}
@@ -153,13 +193,16 @@ extern "C" int sxsk_fit_grid_df(const double *cross, const sxsk_pose *order, int
                                 double *c2, int32_t *cell, double *grid, double *scaled, cudaStream_t s)
 {
 	if (nslot <= 0) return 0;
-	if (n1 <= 0 || n2 <= 0) return cudaErrorInvalidValue;
+	if (n1 <= 0 || n2 <= 0 || Q <= 0) return cudaErrorInvalidValue;
 	int tp = n1 < FITD_THREADS ? n1 : FITD_THREADS;
 	int ppb = FITD_THREADS / tp;
+	int nchunk = (Q + FITD_QC - 1) / FITD_QC;
+	int qc = (Q + nchunk - 1) / nchunk;
+	int gsm = sizeof(dfl) * (size_t)n1 * Q <= FITD_GSMEM;
 	size_t smem;
 	for (;;) {
 		size_t nthr = (size_t)ppb * tp;
-		smem = sizeof(dfl) * ((size_t)ppb * 8 * Q + (size_t)FITD_NFC * Q + n2) +
+		smem = sizeof(dfl) * ((size_t)ppb * 8 * (qc + 1) + (size_t)FITD_NFC * Q + n2 + (gsm ? (size_t)n1 * Q : 0)) +
 		       sizeof(double) * (2 * nthr + 2 * ppb) + sizeof(int) * ((nthr + 1) & ~(size_t)1) +
 		       sizeof(dfl) * 2 * ppb + sizeof(int) * ppb;
 		if (smem <= 227 * 1024 || ppb == 1) break;
@@ -173,6 +216,6 @@ extern "C" int sxsk_fit_grid_df(const double *cross, const sxsk_pose *order, int
 	long ngroup = (nslot + ppb - 1) / ppb;
 	int grid_n = (int)(ngroup < (long)max_blocks || max_blocks <= 0 ? ngroup : max_blocks);
 	k_fit_grid_df<<<grid_n, FITD_THREADS, smem, s>>>(cross, order, slot0, nslot, Q, fc, a0sum, peak, gdf, c1g, n1,
-	                                                  c2g, n2, tp, ppb, chi, c1, c2, cell, grid, scaled);
+	                                                  c2g, n2, tp, ppb, qc, gsm, chi, c1, c2, cell, grid, scaled);
 	return cudaGetLastError();
 }

@@ -175,9 +175,8 @@ struct sxsg_plan {
 	int L, K, N, K2, Q, nz, n1, n2, precision;
 	const sxs_ltables *lt;
 	cudaStream_t s;
-	cudaStream_t sf;            /* fit stream, high priority: overlaps the contractions */
 	int nsm;
-	cudaEvent_t *cev;           /* per-chunk events, 5 per chunk */
+	cudaEvent_t *cev;           /* per-chunk events, 3 per chunk */
 	int ncev;
 	double mult, peak, a0sum;
 	/* resident inputs */
@@ -265,7 +264,6 @@ void sxsg_plan_destroy(sxsg_plan *p)
 	for (int i = 0; i < 6; i++) if (p->ev[i]) cudaEventDestroy(p->ev[i]);
 	for (int i = 0; i < p->ncev; i++) cudaEventDestroy(p->cev[i]);
 	free(p->cev);
-	if (p->sf) cudaStreamDestroy(p->sf);
 	free(p->h_z);
 	free(p);
 }
@@ -307,11 +305,6 @@ int sxs_plan_create_on(sxsg_plan **out, const double *A, const double *B, const 
 	size_t spf_n = (size_t)3 * Q * p->K2 * 2;
 	cudaError_t e = cudaSuccess;
 	for (int i = 0; i < 6 && !e; i++) e = cudaEventCreate(&p->ev[i]);
-	if (!e) {
-		int lo = 0, hi = 0;
-		e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
-		if (!e) e = cudaStreamCreateWithPriority(&p->sf, cudaStreamNonBlocking, hi);
-	}
 	if (!e) {
 		int dev = 0;
 		e = cudaGetDevice(&dev);
@@ -611,12 +604,6 @@ static int plan_fit_grid(sxsg_plan *p, const sxsk_pose *order, int slot0, int ns
 	                     p->n1, p->d_c2g, p->n2, max_blocks, chi, c1, c2, cell, grid, scaled, st);
 }
 
-/* Chunks the grid-fit run is split into at least, so that the fit of one
- * chunk (FP64 pipe) overlaps the contractions of the next (HBM / FP32). */
-#define SXS_PIPE_CHUNKS 8
-/* resident fit blocks per SM while it overlaps the contractions */
-#define SXS_FIT_BLOCKS_PER_SM 1
-
 static int plan_events(sxsg_plan *p, int need)
 {
 	if (need <= p->ncev) return 0;
@@ -646,15 +633,10 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 	size_t per_combo = (size_t)p->NP * 3 * SXS_QT * p->NT * p->celem;
 	int64_t chunk = (int64_t)(p->r_budget / (per_combo * SXS_SLICE));   /* slices per chunk */
 	if (chunk < 1) chunk = 1;
-	int pipe = fit_mode == SXSG_FIT_GRID && p->ncombo > 0;
-	if (pipe) {
-		int64_t c = (p->nslice + SXS_PIPE_CHUNKS - 1) / SXS_PIPE_CHUNKS;
-		if (c < chunk) chunk = c;
-	}
 	if (chunk > p->nslice) chunk = p->nslice;
 	int64_t nch = chunk > 0 ? (p->nslice + chunk - 1) / chunk : 0;
-	if (nch > INT32_MAX / 5) return sxs_fail(-2, "sxsg_plan_run: too many chunks");
-	if ((rc = plan_events(p, (int)(5 * nch + 1)))) return rc;
+	if (nch > INT32_MAX / 3) return sxs_fail(-2, "sxsg_plan_run: too many chunks");
+	if ((rc = plan_events(p, (int)(3 * nch)))) return rc;
 	int64_t rcap = chunk * SXS_SLICE;
 	if (rcap > p->ncombo) rcap = p->ncombo;
 	if (rcap > 0 && p->R_combos < rcap) {
@@ -667,7 +649,7 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 	for (int64_t k = 0; k < nch; k++) {
 		int64_t s0 = k * chunk, s1 = s0 + chunk < p->nslice ? s0 + chunk : p->nslice;
 		int64_t c0 = p->h_slices[2 * s0], c1 = p->h_slices[2 * (s1 - 1)] + p->h_slices[2 * (s1 - 1) + 1];
-		cudaEvent_t *e = p->cev + 5 * k;
+		cudaEvent_t *e = p->cev + 3 * k;
 		SXS_CU(cudaEventRecord(e[0], s));
 		SXS_K(sxsk_translate(p->d_U, tau, p->d_combo + 3 * c0, p->d_slices + 2 * s0, (int)(s1 - s0), (int)c0,
 		                     (int)(c1 - c0), p->nzt, Q, L, p->d_R, p->fp32, s));
@@ -678,23 +660,10 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 		                      p->d_cross, p->fp32, s));
 		SXS_CU(cudaEventRecord(e[2], s));
 		sxs_count_launches(2);
-		if (pipe) {
-			SXS_CU(cudaStreamWaitEvent(p->sf, e[2], 0));
-			SXS_CU(cudaEventRecord(e[3], p->sf));
-			SXS_K(plan_fit_grid(p, p->d_poses, (int)p0, (int)(p1 - p0), SXS_FIT_BLOCKS_PER_SM * p->nsm, p->d_chi,
-			                    p->d_c1, p->d_c2, p->d_cell, NULL, p->d_scaled, p->sf));
-			SXS_CU(cudaEventRecord(e[4], p->sf));
-			sxs_count_launches(p1 > p0 ? 1 : 0);
-		}
-	}
-	if (pipe) {
-		cudaEvent_t j = p->cev[5 * nch];
-		SXS_CU(cudaEventRecord(j, p->sf));
-		SXS_CU(cudaStreamWaitEvent(s, j, 0));
 	}
 	SXS_CU(cudaEventRecord(p->ev[5], s));
 	int n = (int)p->npose;
-	if (fit_mode == SXSG_FIT_GRID && !pipe) {
+	if (fit_mode == SXSG_FIT_GRID) {
 		SXS_K(plan_fit_grid(p, NULL, 0, n, 0, p->d_chi, p->d_c1, p->d_c2, p->d_cell, NULL, p->d_scaled, s));
 		sxs_count_launches(n > 0 ? 1 : 0);
 	} else if (fit_mode == SXSG_FIT_LBFGSB) {
@@ -714,18 +683,14 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 	cudaEventElapsedTime(&t_tab, p->ev[0], p->ev[1]);
 	cudaEventElapsedTime(&t_all, p->ev[0], end);
 	for (int64_t k = 0; k < nch; k++) {
-		cudaEvent_t *e = p->cev + 5 * k;
-		float a = 0, b = 0, c = 0;
+		cudaEvent_t *e = p->cev + 3 * k;
+		float a = 0, b = 0;
 		cudaEventElapsedTime(&a, e[0], e[1]);
 		cudaEventElapsedTime(&b, e[1], e[2]);
 		t_tr += a;
 		t_pc += b;
-		if (pipe) {
-			cudaEventElapsedTime(&c, e[3], e[4]);
-			t_fit += c;
-		}
 	}
-	if (!pipe) cudaEventElapsedTime(&t_fit, p->ev[5], end);
+	cudaEventElapsedTime(&t_fit, p->ev[5], end);
 	cudaEventDestroy(end);
 	p->ms[0] = t_tab; p->ms[1] = t_tr; p->ms[2] = t_pc; p->ms[3] = t_fit; p->ms[4] = t_all;
 	if (p->tc_used && sxsk_rotate_tc_status())
