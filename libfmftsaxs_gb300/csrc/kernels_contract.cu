@@ -29,8 +29,6 @@ template <typename S> struct Cx;
 template <> struct Cx<double> { typedef double2 T; };
 template <> struct Cx<float> { typedef float2 T; };
 
-__device__ __forceinline__ int lm_index(int l, int m) { return l * (l + 1) + m; }
-
 /* first pair of row m >= 0 */
 __device__ __forceinline__ int psym(int m, int K) { return m * K - m * (m - 1) / 2; }
 
@@ -40,13 +38,6 @@ __device__ __forceinline__ void cfma(double2 &acc, double2 a, double2 b)
 	acc.x = fma(-a.y, b.y, acc.x);
 	acc.y = fma(a.x, b.y, acc.y);
 	acc.y = fma(a.y, b.x, acc.y);
-}
-__device__ __forceinline__ void cfma(float2 &acc, float2 a, float2 b)
-{
-	acc.x = fmaf(a.x, b.x, acc.x);
-	acc.x = fmaf(-a.y, b.y, acc.x);
-	acc.y = fmaf(a.x, b.y, acc.y);
-	acc.y = fmaf(a.y, b.x, acc.y);
 }
 template <typename V> __device__ __forceinline__ V zero2() { V v; v.x = 0; v.y = 0; return v; }
 template <typename V> __device__ __forceinline__ V from2(double2 a) { V v; v.x = a.x; v.y = a.y; return v; }
@@ -124,81 +115,143 @@ __device__ __forceinline__ void st2(double2 *p, double2 a, double2 b)
 	p[1] = b;
 }
 
+/* Twiddle factors of the paired rotation sum, extended so that index
+ * k + j m1 needs no wrap: entry k holds h+ = (tw[k] + tw[N-k])/2 and
+ * h- = (tw[k] - tw[N-k])/2 (indices mod N).  The FP32 path keeps
+ * (Re tw[k], Im tw[k]): with a conjugate-symmetric table h+ = Re tw and
+ * h- = i Im tw; the reference's twiddles are symmetric to ~1e-11, far below
+ * FP32 rounding.  The FP64 path keeps both complex halves exactly. */
+template <typename S> struct RotTw;
+template <> struct RotTw<float> { float2 cs; };
+template <> struct RotTw<double> { double2 hp, hm; };
+template <typename S> __device__ __forceinline__ RotTw<S> rot_tw(const double2 *tw, int k, int N);
+template <> __device__ __forceinline__ RotTw<float> rot_tw<float>(const double2 *tw, int k, int N)
+{
+	double2 a = tw[k % N];
+	RotTw<float> r;
+	r.cs = make_float2((float)a.x, (float)a.y);
+	return r;
+}
+template <> __device__ __forceinline__ RotTw<double> rot_tw<double>(const double2 *tw, int k, int N)
+{
+	int kk = k % N;
+	double2 a = tw[kk], b = tw[(N - kk) % N];
+	RotTw<double> r;
+	r.hp = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y));
+	r.hm = make_double2(0.5 * (a.x - b.x), 0.5 * (a.y - b.y));
+	return r;
+}
+/* A += h+ S, B += h- D */
+__device__ __forceinline__ void rot_acc(float2 &A, float2 &B, const RotTw<float> &h, float2 S, float2 D)
+{
+	A.x = fmaf(h.cs.x, S.x, A.x);
+	A.y = fmaf(h.cs.x, S.y, A.y);
+	B.x = fmaf(h.cs.y, D.x, B.x);   /* B = sum sin D; h- D = i B */
+	B.y = fmaf(h.cs.y, D.y, B.y);
+}
+__device__ __forceinline__ void rot_acc(double2 &A, double2 &B, const RotTw<double> &h, double2 S, double2 D)
+{
+	cfma(A, h.hp, S);
+	cfma(B, h.hm, D);
+}
+/* X(gamma) = y0 + A + (h- part), X(N - gamma) = y0 + A - (h- part) */
+__device__ __forceinline__ void rot_out(float2 y0, float2 A, float2 B, float2 &xp, float2 &xm)
+{
+	xp = make_float2(y0.x + A.x - B.y, y0.y + A.y + B.x);
+	xm = make_float2(y0.x + A.x + B.y, y0.y + A.y - B.x);
+}
+__device__ __forceinline__ void rot_out(double2 y0, double2 A, double2 B, double2 &xp, double2 &xm)
+{
+	xp = make_double2(y0.x + A.x + B.x, y0.y + A.y + B.y);
+	xm = make_double2(y0.x + A.x - B.x, y0.y + A.y - B.y);
+}
+
+#define ROT_GROUPS 4
+#define ROT_THREADS (ROT_GROUPS * 3 * SXS_QT)
+
 /* Rotation tables in the q-tiled layout:
  *   out[t][b*N+g][pair(m,l)][ch][q] = sum_{m1=-l..l} tw[(m1' g) mod N] d^l_{m m1}(beta_b) C[ch][l,m1][q]
- * (C = spf_t, conjugated when conj != 0).  Block = (b, QS q of a tile, group
- * of m = mg, mg + MG, ...); thread = (g, q).  The block stages the
- * coefficients C[ch][lm][QS q] of every lm and the twiddles in shared memory
- * once, then per m the d row d^l_{m m1}(beta_b); every gamma thread reuses
- * them, and the twiddle index (m1' g) mod N advances by g per m1. */
-template <typename S>
-__global__ void k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const S *__restrict__ dtab,
-                         const double2 *__restrict__ tw, int Q, int L, int conj, int QS, int MG,
-                         typename Cx<S>::T *__restrict__ out)
+ * (C = spf_t, conjugated when conj != 0).  With y(m1) = d^l_{m m1} C[l,m1],
+ * S = y(m1) + y(-m1), D = y(m1) - y(-m1) and k = m1 g mod N, the terms of
+ * m1 and -m1 at gamma g and N - g combine to
+ *   X(g) = y(0) + sum_{m1>0} h+(k) S + h-(k) D,  X(N-g) = y(0) + sum h+(k) S - h-(k) D,
+ * so each (m1 > 0, gamma pair) costs one S and one D product.
+ * Block = (m, beta b, q tile t), blocks ordered m fastest so that the blocks
+ * of one tile read the same coefficients from L1/L2; thread = (group of G
+ * gamma pairs, channel, q): the thread forms S and D once per m1 and
+ * accumulates its G gamma pairs in registers.  The padding q >= Q is written
+ * as zeros. */
+template <typename S, int G>
+__global__ void __launch_bounds__(ROT_THREADS)
+k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const S *__restrict__ dtab, const double2 *__restrict__ tw,
+         int Q, int L, int conj, typename Cx<S>::T *__restrict__ out)
 {
 	typedef typename Cx<S>::T V;
 	extern __shared__ __align__(16) unsigned char rsm_raw[];
+	RotTw<S> *hs = reinterpret_cast<RotTw<S> *>(rsm_raw);   /* [N + (G-1) L] */
 	int K = L + 1, N = 2 * L + 1, K2 = K * K, NP = K * (K + 1) / 2, nrow = K * N;
-	int NT = (Q + SXS_QT - 1) / SXS_QT, nsub = SXS_QT / QS;
 	int bid = blockIdx.x;
-	int mg = bid % MG;
-	bid /= MG;
-	int t = bid % (NT * nsub);
-	int b = bid / (NT * nsub);
-	int q0 = t * QS;                         /* first q of the block */
-	t = q0 / SXS_QT;
-	V *cs = reinterpret_cast<V *>(rsm_raw);  /* [3][K2][QS] */
-	V *ws = cs + 3 * K2 * QS;                /* [N] twiddles */
-	S *ds = reinterpret_cast<S *>(ws + N);   /* [K2] d^l_{m m1}(beta_b) of the current m, indexed like lm */
+	int m = bid % K;
+	bid /= K;
+	int b = bid % K;
+	int t = bid / K;
+	int ne = N + (G - 1) * L;
+	for (int k = threadIdx.x; k < ne; k += blockDim.x) hs[k] = rot_tw<S>(tw, k, N);
+	__syncthreads();
+	int qq = threadIdx.x % SXS_QT, ch = (threadIdx.x / SXS_QT) % 3, gg = threadIdx.x / (3 * SXS_QT);
+	int q = t * SXS_QT + qq;
+	bool qok = q < Q;
+	int g0 = gg * G;
+	if (g0 > L) return;
 	S sg = conj ? (S)-1 : (S)1;
-	for (int k = threadIdx.x; k < 3 * K2 * QS; k += blockDim.x) {
-		int qq = k % QS, r = k / QS;
-		int lm = r % K2, ch = r / K2;
-		int q = q0 + qq;
-		V v = zero2<V>();
-		if (q < Q) {
-			v = spf_t[((size_t)ch * K2 + lm) * Q + q];
-			v.y *= sg;
-		}
-		cs[k] = v;
-	}
-	for (int k = threadIdx.x; k < N; k += blockDim.x) ws[k] = from2<V>(tw[k]);
-	int g = threadIdx.x / QS, qq = threadIdx.x % QS;
-	bool act = g < N;
-	const S *db = dtab + (size_t)b * K * N * N;
-	for (int m = mg; m <= L; m += MG) {
-		__syncthreads();   /* previous m done with ds (and the staging above) */
-		for (int lm = m * m + threadIdx.x; lm < K2; lm += blockDim.x) {
-			int l = 0;
-			while ((l + 1) * (l + 1) <= lm) l++;
-			int m1 = lm - l * (l + 1);
-			ds[lm] = db[((size_t)l * N + m + L) * N + m1 + L];
-		}
-		__syncthreads();
-		if (!act) continue;
-		int po = psym(m, K);
-		V *ob = out + (((size_t)t * nrow + b * N + g) * NP + po) * 3 * SXS_QT + q0 % SXS_QT + qq;
-		for (int l = m; l <= L; l++) {
-			V acc0 = zero2<V>(), acc1 = acc0, acc2 = acc0;
-			int r0 = l * l;                      /* lm = l^2 + (m1 + l) */
-			int e = ((N - l) * g) % N;           /* (m1' g) mod N at m1 = -l */
-			for (int j = 0; j < 2 * l + 1; j++) {
-				S dv = ds[r0 + j];
-				V w = ws[e];
-				V f;
-				f.x = w.x * dv;
-				f.y = w.y * dv;
-				const V *c = cs + (size_t)(r0 + j) * QS + qq;
-				cfma(acc0, f, c[0]);
-				cfma(acc1, f, c[(size_t)K2 * QS]);
-				cfma(acc2, f, c[(size_t)2 * K2 * QS]);
-				e += g;
-				if (e >= N) e -= N;
+	const V *C = spf_t + (size_t)ch * K2 * Q + (qok ? q : 0);
+	const S *db = dtab + ((size_t)b * K * N + m + L) * N + L;   /* d^l_{m m1}(beta_b) at l = 0, m1 = 0 */
+	V *ob = out + (((size_t)t * nrow + (size_t)b * N) * NP + psym(m, K)) * 3 * SXS_QT + ch * SXS_QT + qq;
+	size_t gstride = (size_t)NP * 3 * SXS_QT;
+	for (int l = m; l <= L; l++) {
+		const S *dl = db + (size_t)l * N * N;
+		const V *Cl = C + (size_t)l * (l + 1) * Q;    /* lm of m1 = 0 */
+		V c0 = zero2<V>();
+		if (qok) c0 = Cl[0];
+		S d0 = dl[0];
+		V y0;
+		y0.x = d0 * c0.x;
+		y0.y = d0 * c0.y * sg;
+		V A[G], B[G];
+#pragma unroll
+		for (int j = 0; j < G; j++) A[j] = B[j] = zero2<V>();
+		int base = 0;                                  /* m1 g0 mod N */
+		for (int m1 = 1; m1 <= l; m1++) {
+			base += g0;
+			if (base >= N) base -= N;
+			V cp = zero2<V>(), cm = zero2<V>();
+			if (qok) {
+				cp = Cl[(size_t)m1 * Q];
+				cm = Cl[-(ptrdiff_t)m1 * Q];
 			}
-			V *o = ob + (size_t)(l - m) * 3 * SXS_QT;
-			o[0] = acc0;
-			o[SXS_QT] = acc1;
-			o[2 * SXS_QT] = acc2;
+			S dp = dl[m1], dm = dl[-m1];
+			V yp, Sv, Dv;
+			yp.x = dp * cp.x;
+			yp.y = dp * cp.y * sg;
+			S mx = dm * cm.x, my = dm * cm.y * sg;
+			Sv.x = yp.x + mx; Sv.y = yp.y + my;
+			Dv.x = yp.x - mx; Dv.y = yp.y - my;
+			int k = base;
+#pragma unroll
+			for (int j = 0; j < G; j++) {
+				rot_acc(A[j], B[j], hs[k], Sv, Dv);
+				k += m1;
+			}
+		}
+		V *o = ob + (size_t)(l - m) * 3 * SXS_QT;
+#pragma unroll
+		for (int j = 0; j < G; j++) {
+			int g = g0 + j;
+			if (g > L) break;
+			V xp, xm;
+			rot_out(y0, A[j], B[j], xp, xm);
+			o[(size_t)g * gstride] = xp;
+			if (g > 0) o[(size_t)(N - g) * gstride] = xm;
 		}
 	}
 }
@@ -460,13 +513,6 @@ __global__ void k_to_float(const double *__restrict__ a, float *__restrict__ b, 
 	if (i < n) b[i] = (float)a[i];
 }
 
-__device__ __forceinline__ double warp_sum(double v)
-{
-#pragma unroll
-	for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-	return v;
-}
-
 /* Grid fit (src/min_saxs.c:170-188 peak rescale, 261-320 best scale,
  * 391-448 point_score).  For one pose and one (c1, c2) cell the model at q_i
  * is in_i = al_i + c2 be_i + c2^2 ga_i with G_i = c1^3 exp(-mult (c1^2-1) q_i^2),
@@ -649,7 +695,6 @@ k_fit_grid(const double *__restrict__ cross, const sxsk_pose *__restrict__ order
 }
 
 inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
-inline int qthreads(int Q) { return ((Q + 31) / 32) * 32; }
 
 } // namespace
 
@@ -728,6 +773,39 @@ static int translate_slices(const void *U, const void *tau, const int32_t *combo
 	return cudaGetLastError();
 }
 
+template <typename S, int G>
+static int rotate_launch(const void *spf_t, const void *dtab, const double2 *tw, int Q, int L, int conj, void *out,
+                         cudaStream_t s)
+{
+	typedef typename Cx<S>::T V;
+	int K = L + 1, N = 2 * L + 1, NT = (Q + SXS_QT - 1) / SXS_QT;
+	size_t smem = sizeof(RotTw<S>) * (size_t)(N + (G - 1) * L);
+	if (smem > 48 * 1024) {
+		cudaError_t e = cudaFuncSetAttribute(k_rotate<S, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		if (e != cudaSuccess) return e;
+	}
+	long nb = (long)K * K * NT;
+	if (nb > 0x7fffffffL) return cudaErrorInvalidValue;
+	k_rotate<S, G><<<(unsigned)nb, ROT_THREADS, smem, s>>>((const V *)spf_t, (const S *)dtab, tw, Q, L, conj,
+	                                                      (V *)out);
+	return cudaGetLastError();
+}
+
+template <typename S>
+static int rotate_any(const void *spf_t, const void *dtab, const double2 *tw, int Q, int L, int conj, void *out,
+                      cudaStream_t s)
+{
+	/* gamma pairs per thread: the L + 1 pairs over ROT_GROUPS groups */
+	int need = (L + 1 + ROT_GROUPS - 1) / ROT_GROUPS;
+	if (need <= 2) return rotate_launch<S, 2>(spf_t, dtab, tw, Q, L, conj, out, s);
+	if (need <= 4) return rotate_launch<S, 4>(spf_t, dtab, tw, Q, L, conj, out, s);
+	if (need <= 6) return rotate_launch<S, 6>(spf_t, dtab, tw, Q, L, conj, out, s);
+	if (need <= 8) return rotate_launch<S, 8>(spf_t, dtab, tw, Q, L, conj, out, s);
+	if (need <= 12) return rotate_launch<S, 12>(spf_t, dtab, tw, Q, L, conj, out, s);
+	if (need <= 16) return rotate_launch<S, 16>(spf_t, dtab, tw, Q, L, conj, out, s);
+	return cudaErrorInvalidValue;
+}
+
 extern "C" {
 
 int sxsk_spf_transpose(const double *flat, void *spf_t, int Q, int L, int fp32, cudaStream_t s)
@@ -741,50 +819,9 @@ int sxsk_spf_transpose(const double *flat, void *spf_t, int Q, int L, int fp32, 
 int sxsk_rotate(const void *spf_t, const void *dtab, const double2 *tw, int Q, int L, int conj, void *out, int fp32,
                 cudaStream_t s)
 {
-	int K = L + 1, N = 2 * L + 1, NT = (Q + SXS_QT - 1) / SXS_QT;
-	size_t K2 = (size_t)K * K;
-	size_t celem = fp32 ? sizeof(float2) : sizeof(double2);
-	int dev = 0, nsm = 0;
-	cudaGetDevice(&dev);
-	cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-	/* q per block: the largest of the tile width, halves, ... whose staged
-	 * coefficients fit; m groups: enough blocks for two waves */
-	int QS = SXS_QT;
-	size_t smem;
-	for (;;) {
-		smem = celem * (3 * K2 * QS + N) + (fp32 ? sizeof(float) : sizeof(double)) * K2;
-		if (smem <= 200 * 1024 || QS == 1) break;
-		QS /= 2;
-	}
-	if (smem > 227 * 1024) return cudaErrorInvalidValue;
-	long base = (long)K * NT * (SXS_QT / QS);
-	int threads0 = ((N * QS + 31) / 32) * 32;
-	long bps = (long)(227 * 1024) / (long)smem;
-	if (bps > 2048 / threads0) bps = 2048 / threads0;
-	if (bps < 1) bps = 1;
-	/* m groups: at least four waves of resident blocks */
-	int MG = 1;
-	while (MG < 16 && MG < K && base * MG < 4L * nsm * bps) MG *= 2;
-	long nb = base * MG;
-	int threads = ((N * QS + 31) / 32) * 32;
-	if (fp32) {
-		if (smem > 48 * 1024) {
-			cudaError_t e = cudaFuncSetAttribute(k_rotate<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-			                                     (int)smem);
-			if (e != cudaSuccess) return e;
-		}
-		k_rotate<float><<<(unsigned)nb, threads, smem, s>>>((const float2 *)spf_t, (const float *)dtab, tw, Q, L,
-		                                                    conj, QS, MG, (float2 *)out);
-	} else {
-		if (smem > 48 * 1024) {
-			cudaError_t e = cudaFuncSetAttribute(k_rotate<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-			                                     (int)smem);
-			if (e != cudaSuccess) return e;
-		}
-		k_rotate<double><<<(unsigned)nb, threads, smem, s>>>((const double2 *)spf_t, (const double *)dtab, tw, Q,
-		                                                     L, conj, QS, MG, (double2 *)out);
-	}
-	return cudaGetLastError();
+	if (L < 0 || L + 1 > SXS_LMAX_K || Q <= 0) return cudaErrorInvalidValue;
+	if (fp32) return rotate_any<float>(spf_t, dtab, tw, Q, L, conj, out, s);
+	return rotate_any<double>(spf_t, dtab, tw, Q, L, conj, out, s);
 }
 
 int sxsk_to_float(const double *a, float *b, long n, cudaStream_t s)
