@@ -130,9 +130,10 @@ class Clocks:
 
 # ---------------------------------------------------------------- GPU side
 # DRAM bytes per pose of the dominant kernel from ncu captures of the same
-# kernel on a smaller pose list of this workload (profiles/): the traffic of
-# a launch scales with the poses it processes.
-TRAFFIC_PER_POSE = {("c1", "mixed"): 2.36e5, ("c1", "fp64"): 5.73e5}
+# kernel on the poses of this workload with translation z index < 3 (the
+# same poses per translated row as the whole list, profiles/): the traffic
+# of a launch scales with the poses it processes at that density.
+TRAFFIC_PER_POSE = {("c1", "mixed"): 9.20e4, ("c1", "fp64"): 5.73e5}
 
 
 def pose_flops(L, Q, precision):
@@ -183,8 +184,9 @@ def time_plan(g, w, precision, args, clocks=None):
         ms = g.timer_stop()
     launches = g.launch_count() - l0
     res = plan.results()
+    nchunks = plan.chunks()
     plan.close()
-    return ms / args.steps, stage / args.steps, launches, res
+    return ms / args.steps, stage / args.steps, launches, res, nchunks
 
 
 class _Null:
@@ -312,7 +314,7 @@ def run_ours(args):
             clocks = clk.summary()
         else:
             runs[name] = time_plan(g, w, prec[name], args)
-    ms, stage, launches, res = runs[head]
+    ms, stage, launches, res, nchunks = runs[head]
     value = n / (ms * 1e-3)
 
     # end to end through the one-shot C-ABI call from host buffers
@@ -333,7 +335,6 @@ def run_ours(args):
     achieved = pf / (stage[2] * 1e-3) / 1e12
     peak = fp32_peak if head == "mixed" else fp64_peak
     fref = reference_flops(w)
-    nchunks = 8
     tkey = (args.config, head)
     traffic = TRAFFIC_PER_POSE[tkey] * n / nchunks if tkey in TRAFFIC_PER_POSE else None
     out = {
@@ -354,7 +355,8 @@ def run_ours(args):
                    "precision": head, "skip": 1,
                    "l2": "inputs larger than L2 (rotation tables of ~1 GB and translated tables of several GB per step)"},
         "stages_ms": {"tables": stage[0], "translate": stage[1], "pose": stage[2], "fit": stage[3],
-                      "note": "per-chunk stage times on two streams; the fit of one chunk overlaps the next chunk"},
+                      "note": "stages run in order on the plan stream; translate and pose summed over %d chunk(s)"
+                              % nchunks},
         "fp64": {"value": n / (runs["fp64"][0] * 1e-3), "unit": "poses/s", "ms_per_step": runs["fp64"][0],
                  "stages_ms": dict(zip(("tables", "translate", "pose", "fit"), runs["fp64"][1][:4].tolist()))},
         "reference_flops_per_step": fref,
@@ -364,8 +366,8 @@ def run_ours(args):
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak > 0 else None,
                      "traffic": traffic,
-                     "traffic_source": "ncu DRAM read+write per pose of the same kernel on a smaller pose list, "
-                                       "scaled to the poses of one launch (one of %d chunks)" % nchunks,
+                     "traffic_source": "ncu DRAM read+write per pose of the same kernel on the poses with z index < 3, "
+                                       "scaled to the poses of one launch (%d chunk(s) per run)" % nchunks,
                      "hbm_frac": (traffic * nchunks / (stage[2] * 1e-3) / 1e9 / 6773.5) if traffic else None,
                      "peak_source": "measured in this run: register-resident %s FMA chains on every SM"
                                     % ("FP32" if head == "mixed" else "FP64")},

@@ -265,11 +265,13 @@ int sxsg_plan_run(sxsg_plan *plan, int fit_mode);
  * rescale); grid: chi^2 [n][n1][n2] (grid fit only). */
 int sxsg_plan_results(sxsg_plan *plan, double *chi, double *c1, double *c2, int32_t *cell,
                       double *cross, double *grid);
-/* Stage timings of the last run in ms (CUDA events): [0] tables,
- * [1] translate, [2] per-pose, [3] fit, [4] whole run.  A grid-fit run
- * overlaps the fit of one chunk of poses with the contractions of the next,
- * so [4] can be less than the sum of the stages. */
+/* Stage timings of the last run in ms (CUDA events on the plan stream):
+ * [0] tables, [1] translate, [2] per-pose, [3] fit, [4] whole run. */
 int sxsg_plan_timings(sxsg_plan *plan, double *ms5);
+/* Chunks of the translated table the last run was split into (the pose
+ * list is processed one chunk of whole z slices at a time, sized by the
+ * plan's budget); 0 before the first run. */
+int sxsg_plan_chunks(const sxsg_plan *plan);
 void sxsg_plan_destroy(sxsg_plan *plan);
 
 /* ------------------------------------------------------------ serving

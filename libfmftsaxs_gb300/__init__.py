@@ -216,6 +216,11 @@ class Plan:
             out["grid"] = gr
         return out
 
+    def chunks(self):
+        """Chunks of the translated table the last run used."""
+        load().sxsg_plan_chunks.argtypes = [C.c_void_p]
+        return int(load().sxsg_plan_chunks(self.h))
+
     def timings(self):
         ms = np.zeros(5)
         _check(load().sxsg_plan_timings(self.h, ms.ctypes.data))

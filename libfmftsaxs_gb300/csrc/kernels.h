@@ -100,6 +100,8 @@ int sxsk_rotate_tc_status(void);
  * combo_zbg = the combos of the chunk (cbase = the first one's index),
  * slices[nslice][2] = {first combo, count} runs of <= 16 combos sharing z;
  * R holds ncombo combos; tau is float when fp32; nzt = z count of tau */
+/* kernel launches one sxsk_translate call makes for this L */
+int sxsk_translate_launches(int L);
 int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, const int32_t *slices, int nslice,
                    int cbase, int ncombo, int nzt, int Q, int L, void *R, int fp32, cudaStream_t s);
 

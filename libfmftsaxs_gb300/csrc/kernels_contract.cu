@@ -831,6 +831,21 @@ int sxsk_to_float(const double *a, float *b, long n, cudaStream_t s)
 	return cudaGetLastError();
 }
 
+int sxsk_translate_launches(int L)
+{
+	int K = L + 1;
+	if (K > 32) return 1;
+	int n = 0;
+	for (int nb = 4; nb <= 32; nb += 4) {
+		/* the m range of translate_col_launch<S, nb> */
+		int m_hi = K - (nb - 3), m_lo = K - nb;
+		if (m_hi > L) m_hi = L;
+		if (m_lo < 0) m_lo = 0;
+		n += m_hi >= m_lo;
+	}
+	return n;
+}
+
 int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, const int32_t *slices, int nslice,
                    int cbase, int ncombo, int nzt, int Q, int L, void *R, int fp32, cudaStream_t s)
 {

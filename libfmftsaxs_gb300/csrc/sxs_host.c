@@ -222,6 +222,7 @@ struct sxsg_plan {
 	int *d_iters;
 	size_t out_cap;
 	int last_fit;
+	int last_chunks;
 	int grid_valid;
 	cudaEvent_t ev[6];
 	double ms[5];
@@ -568,12 +569,12 @@ static int plan_tables(sxsg_plan *p)
 		if (!p->ext_tables || !p->P_valid) {
 			if (tc) SXS_K(sxsk_rotate_tc(p->d_At, p->lt->d_dtabf, p->d_tw, Q, L, 0, p->d_P, p->d_amat, s));
 			else SXS_K(sxsk_rotate(p->d_At, dtab, p->d_tw, Q, L, 0, p->d_P, p->fp32, s));
-			sxs_count_launches(1);
+			sxs_count_launches(tc ? 2 : 1);
 		}
 		if (!p->ext_tables || !p->U_valid) {
 			if (tc) SXS_K(sxsk_rotate_tc(p->d_Bt, p->lt->d_dtabf, p->d_tw, Q, L, 1, p->d_U, p->d_amat, s));
 			else SXS_K(sxsk_rotate(p->d_Bt, dtab, p->d_tw, Q, L, 1, p->d_U, p->fp32, s));
-			sxs_count_launches(1);
+			sxs_count_launches(tc ? 2 : 1);
 		}
 		p->tc_used = tc;
 		if (p->ext_tables) p->P_valid = p->U_valid = 1;
@@ -635,6 +636,7 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 	if (chunk < 1) chunk = 1;
 	if (chunk > p->nslice) chunk = p->nslice;
 	int64_t nch = chunk > 0 ? (p->nslice + chunk - 1) / chunk : 0;
+	p->last_chunks = (int)(nch < INT32_MAX ? nch : INT32_MAX);
 	if (nch > INT32_MAX / 3) return sxs_fail(-2, "sxsg_plan_run: too many chunks");
 	if ((rc = plan_events(p, (int)(3 * nch)))) return rc;
 	int64_t rcap = chunk * SXS_SLICE;
@@ -659,7 +661,7 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 		                      p->d_cst, Q, L,
 		                      p->d_cross, p->fp32, s));
 		SXS_CU(cudaEventRecord(e[2], s));
-		sxs_count_launches(2);
+		sxs_count_launches(sxsk_translate_launches(L) + 1);
 	}
 	SXS_CU(cudaEventRecord(p->ev[5], s));
 	int n = (int)p->npose;
@@ -732,6 +734,8 @@ int sxsg_plan_results(sxsg_plan *p, double *chi, double *c1, double *c2, int32_t
 	SXS_CU(cudaStreamSynchronize(s));
 	return 0;
 }
+
+int sxsg_plan_chunks(const sxsg_plan *p) { return p ? p->last_chunks : 0; }
 
 int sxsg_plan_timings(sxsg_plan *p, double *ms5)
 {
