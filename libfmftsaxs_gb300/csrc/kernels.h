@@ -100,6 +100,16 @@ int sxsk_rotate_tc_status(void);
  * combo_zbg = the combos of the chunk (cbase = the first one's index),
  * slices[nslice][2] = {first combo, count} runs of <= 16 combos sharing z;
  * R holds ncombo combos; tau is float when fp32; nzt = z count of tau */
+/* Pose list on the device (src/index.c:3-29 packing, most significant
+ * first: z slot, beta1, beta2, alpha2, gamma1, gamma2).  decode: one thread
+ * per pose writes the decoded pose and its combo key (zi nb + b2) N + g2,
+ * counts keys and touched z slots, and records in err[0] / err[1] the
+ * smallest pose index with a negative index / a z slot >= nz (err preset to
+ * all ones).  scatter: places pose i at pos[key]++ with its combo id. */
+int sxsk_pose_decode(const int64_t *index, int64_t n, int N, int nb, int nz, sxsk_pose *tmp, int32_t *key,
+                     int32_t *cnt, int32_t *zused, unsigned long long *err, cudaStream_t s);
+int sxsk_pose_scatter(const sxsk_pose *tmp, const int32_t *key, int64_t n, int32_t *pos, const int32_t *cid,
+                      sxsk_pose *out, cudaStream_t s);
 /* kernel launches one sxsk_translate call makes for this L */
 int sxsk_translate_launches(int L);
 int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, const int32_t *slices, int nslice,

@@ -507,6 +507,49 @@ k_pose_cross(const sxsk_pose *__restrict__ poses, int npose, int combo_base, int
 	}
 }
 
+__global__ void k_pose_decode(const int64_t *__restrict__ index, int64_t n, int N, int nb, int nz,
+                              sxsk_pose *__restrict__ tmp, int32_t *__restrict__ key, int32_t *__restrict__ cnt,
+                              int32_t *__restrict__ zused, unsigned long long *__restrict__ err)
+{
+	int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	int64_t v = index[i];
+	if (v < 0) {
+		atomicMin(&err[0], (unsigned long long)i);
+		return;
+	}
+	sxsk_pose ps;
+	ps.g2 = (int32_t)(v % N); v /= N;
+	ps.g1 = (int32_t)(v % N); v /= N;
+	ps.a2 = (int32_t)(v % N); v /= N;
+	ps.b2 = (int32_t)(v % nb); v /= nb;
+	ps.b1 = (int32_t)(v % nb); v /= nb;
+	if (v >= nz) {
+		atomicMin(&err[1], (unsigned long long)i);
+		return;
+	}
+	ps.zi = (int32_t)v;
+	ps.src = (int32_t)i;
+	ps.combo = 0;
+	int32_t k = (ps.zi * nb + ps.b2) * N + ps.g2;
+	tmp[i] = ps;
+	key[i] = k;
+	atomicAdd(&cnt[k], 1);
+	zused[ps.zi] = 1;
+}
+
+__global__ void k_pose_scatter(const sxsk_pose *__restrict__ tmp, const int32_t *__restrict__ key, int64_t n,
+                               int32_t *__restrict__ pos, const int32_t *__restrict__ cid,
+                               sxsk_pose *__restrict__ out)
+{
+	int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	int32_t k = key[i];
+	sxsk_pose ps = tmp[i];
+	ps.combo = cid[k];
+	out[atomicAdd(&pos[k], 1)] = ps;
+}
+
 __global__ void k_to_float(const double *__restrict__ a, float *__restrict__ b, long n)
 {
 	long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -828,6 +871,26 @@ int sxsk_to_float(const double *a, float *b, long n, cudaStream_t s)
 {
 	if (n <= 0) return 0;
 	k_to_float<<<nblk(n, 256), 256, 0, s>>>(a, b, n);
+	return cudaGetLastError();
+}
+
+int sxsk_pose_decode(const int64_t *index, int64_t n, int N, int nb, int nz, sxsk_pose *tmp, int32_t *key,
+                     int32_t *cnt, int32_t *zused, unsigned long long *err, cudaStream_t s)
+{
+	if (n <= 0) return 0;
+	long nbk = (n + 255) / 256;
+	if (nbk > 0x7fffffffL) return cudaErrorInvalidValue;
+	k_pose_decode<<<(unsigned)nbk, 256, 0, s>>>(index, n, N, nb, nz, tmp, key, cnt, zused, err);
+	return cudaGetLastError();
+}
+
+int sxsk_pose_scatter(const sxsk_pose *tmp, const int32_t *key, int64_t n, int32_t *pos, const int32_t *cid,
+                      sxsk_pose *out, cudaStream_t s)
+{
+	if (n <= 0) return 0;
+	long nbk = (n + 255) / 256;
+	if (nbk > 0x7fffffffL) return cudaErrorInvalidValue;
+	k_pose_scatter<<<(unsigned)nbk, 256, 0, s>>>(tmp, key, n, pos, cid, out);
 	return cudaGetLastError();
 }
 

@@ -200,7 +200,7 @@ struct sxsg_plan {
 	/* poses */
 	int64_t npose;
 	int skip;
-	sxsk_pose *h_poses, *d_poses;
+	sxsk_pose *d_poses;         /* sorted by combo */
 	int ncombo;
 	int32_t *h_combo, *d_combo; /* [ncombo][3]: tslot, b2, g2 */
 	int64_t *h_cstart;          /* [ncombo+1] first sorted pose of each combo */
@@ -238,12 +238,12 @@ static void pfree(const sxsg_plan *p, void *x)
 
 static void plan_free_poses(sxsg_plan *p)
 {
-	free(p->h_poses); free(p->h_combo); free(p->h_cstart); free(p->h_zt); free(p->h_slices);
+	free(p->h_combo); free(p->h_cstart); free(p->h_zt); free(p->h_slices);
 	pfree(p, p->d_slices);
 	p->h_slices = NULL; p->d_slices = NULL; p->nslice = 0;
 	pfree(p, p->d_poses); pfree(p, p->d_combo); pfree(p, p->d_zt); pfree(p, p->d_bes); pfree(p, p->d_tau);
 	pfree(p, p->d_tauf);
-	p->h_poses = NULL; p->h_combo = NULL; p->h_cstart = NULL; p->h_zt = NULL;
+	p->h_combo = NULL; p->h_cstart = NULL; p->h_zt = NULL;
 	p->d_poses = NULL; p->d_combo = NULL; p->d_zt = NULL; p->d_bes = NULL; p->d_tau = NULL; p->d_tauf = NULL;
 	p->pose_cap = p->combo_cap = p->zt_cap = 0;
 }
@@ -425,105 +425,123 @@ int sxsg_plan_set_poses(sxsg_plan *p, const int64_t *index, int64_t n, int skip)
 	if (!p || n < 0 || (n > 0 && !index)) return sxs_fail(-2, "sxsg_plan_set_poses: bad arguments");
 	if (n > INT32_MAX) return sxs_fail(-2, "sxsg_plan_set_poses: at most 2^31-1 poses per plan");
 	int L = p->L, N = p->N, nb = p->K, nz = p->nz;
+	int64_t nkey = (int64_t)nz * nb * N;
+	if (nkey > INT32_MAX) return sxs_fail(-2, "sxsg_plan_set_poses: znum (L+1) (2L+1) must be below 2^31");
 	plan_free_poses(p);
 	p->npose = n;
 	p->skip = skip;
 	p->grid_valid = 0;
-	int64_t nkey = (int64_t)nz * nb * N;
-	int64_t *cnt = calloc(nkey + 1, sizeof(int64_t));
-	int32_t *key = malloc(sizeof(int32_t) * (n > 0 ? n : 1));
-	sxsk_pose *tmp = malloc(sizeof(sxsk_pose) * (n > 0 ? n : 1));
-	char *zused = calloc(nz, 1);
-	for (int64_t i = 0; i < n; i++) {
-		int64_t v = index[i];
-		if (v < 0) {
-			free(cnt); free(key); free(tmp); free(zused);
-			return sxs_fail(-3, "pose %lld: negative grid index %lld", (long long)i, (long long)v);
-		}
-		sxsk_pose ps;
-		ps.g2 = (int32_t)(v % N); v /= N;
-		ps.g1 = (int32_t)(v % N); v /= N;
-		ps.a2 = (int32_t)(v % N); v /= N;
-		ps.b2 = (int32_t)(v % nb); v /= nb;
-		ps.b1 = (int32_t)(v % nb); v /= nb;
-		if (v >= nz) {
-			free(cnt); free(key); free(tmp); free(zused);
-			return sxs_fail(-3, "pose %lld: translation slot %lld >= znum %d", (long long)i, (long long)v, nz);
-		}
-		ps.zi = (int32_t)v;
-		ps.src = (int32_t)i;
-		ps.combo = 0;
-		tmp[i] = ps;
-		key[i] = (int32_t)(((int64_t)ps.zi * nb + ps.b2) * N + ps.g2);
-		cnt[key[i] + 1]++;
-		zused[ps.zi] = 1;
+	cudaStream_t s = p->s;
+	size_t nn = (size_t)(n > 0 ? n : 1);
+	/* decode and count keys (zi, b2, g2) on the device */
+	int64_t *d_idx = NULL;
+	sxsk_pose *d_tmp = NULL;
+	int32_t *d_key = NULL, *d_cnt = NULL, *d_zu = NULL, *d_cid = NULL;
+	unsigned long long *d_err = NULL, h_err[2] = {0, 0};
+	int32_t *h_cnt = malloc(sizeof(int32_t) * (size_t)(nkey > 0 ? nkey : 1));
+	int32_t *h_zu = malloc(sizeof(int32_t) * (size_t)(nz > 0 ? nz : 1));
+	int32_t *h_cid = malloc(sizeof(int32_t) * (size_t)(nkey > 0 ? nkey : 1));
+	int *zslot = malloc(sizeof(int) * (size_t)(nz > 0 ? nz : 1));
+	int rc = 0;
+	cudaError_t e = (h_cnt && h_zu && h_cid && zslot) ? cudaSuccess : cudaErrorMemoryAllocation;
+	if (!e) e = cudaMallocAsync((void **)&d_idx, sizeof(int64_t) * nn, s);
+	if (!e) e = cudaMallocAsync((void **)&d_tmp, sizeof(sxsk_pose) * nn, s);
+	if (!e) e = cudaMallocAsync((void **)&d_key, sizeof(int32_t) * nn, s);
+	if (!e) e = cudaMallocAsync((void **)&d_cnt, sizeof(int32_t) * (size_t)(nkey > 0 ? nkey : 1), s);
+	if (!e) e = cudaMallocAsync((void **)&d_cid, sizeof(int32_t) * (size_t)(nkey > 0 ? nkey : 1), s);
+	if (!e) e = cudaMallocAsync((void **)&d_zu, sizeof(int32_t) * (size_t)(nz > 0 ? nz : 1), s);
+	if (!e) e = cudaMallocAsync((void **)&d_err, sizeof(h_err), s);
+	if (!e) e = cudaMemsetAsync(d_cnt, 0, sizeof(int32_t) * (size_t)nkey, s);
+	if (!e) e = cudaMemsetAsync(d_zu, 0, sizeof(int32_t) * (size_t)nz, s);
+	if (!e) e = cudaMemsetAsync(d_err, 0xff, sizeof(h_err), s);
+	if (!e && n > 0) e = cudaMemcpyAsync(d_idx, index, sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice, s);
+	if (!e) e = (cudaError_t)sxsk_pose_decode(d_idx, n, N, nb, nz, d_tmp, d_key, d_cnt, d_zu, d_err, s);
+	if (!e) e = cudaMemcpyAsync(h_err, d_err, sizeof(h_err), cudaMemcpyDeviceToHost, s);
+	if (!e) e = cudaMemcpyAsync(h_cnt, d_cnt, sizeof(int32_t) * (size_t)nkey, cudaMemcpyDeviceToHost, s);
+	if (!e) e = cudaMemcpyAsync(h_zu, d_zu, sizeof(int32_t) * (size_t)nz, cudaMemcpyDeviceToHost, s);
+	if (!e) e = cudaStreamSynchronize(s);
+	if (!e) sxs_count_launches(n > 0 ? 1 : 0);
+	if (!e && (h_err[0] != ~0ULL || h_err[1] != ~0ULL)) {
+		/* the first bad pose in list order, with the reference's message */
+		long long i = (long long)(h_err[0] < h_err[1] ? h_err[0] : h_err[1]);
+		if (h_err[0] < h_err[1])
+			rc = sxs_fail(-3, "pose %lld: negative grid index %lld", i, (long long)index[i]);
+		else
+			rc = sxs_fail(-3, "pose %lld: translation slot %lld >= znum %d", i,
+			              (long long)(index[i] / ((int64_t)N * N * N * nb * nb)), nz);
 	}
-	/* touched z -> slot */
-	int *zslot = malloc(sizeof(int) * nz);
-	int nzt = 0;
-	for (int i = 0; i < nz; i++) zslot[i] = zused[i] ? nzt++ : -1;
-	p->nzt = nzt;
-	p->h_zt = malloc(sizeof(double) * (nzt > 0 ? nzt : 1));
-	for (int i = 0; i < nz; i++) if (zslot[i] >= 0) p->h_zt[zslot[i]] = p->h_z[i];
-	/* combos and counting sort */
-	int ncombo = 0;
-	for (int64_t k = 0; k < nkey; k++) if (cnt[k + 1]) ncombo++;
-	p->ncombo = ncombo;
-	p->h_combo = malloc(sizeof(int32_t) * 3 * (ncombo > 0 ? ncombo : 1));
-	p->h_cstart = malloc(sizeof(int64_t) * (ncombo + 1));
-	int32_t *cid = malloc(sizeof(int32_t) * nkey);
-	int c = 0;
-	for (int64_t k = 0; k < nkey; k++) {
-		if (cnt[k + 1]) {
-			cid[k] = c;
-			int g2 = (int)(k % N), b2 = (int)((k / N) % nb), zi = (int)(k / N / nb);
-			p->h_combo[3 * c] = zslot[zi];
-			p->h_combo[3 * c + 1] = b2;
-			p->h_combo[3 * c + 2] = g2;
-			c++;
-		} else {
-			cid[k] = -1;
+	int ncombo = 0, nzt = 0;
+	if (!e && !rc) {
+		/* touched z -> slot */
+		for (int i = 0; i < nz; i++) zslot[i] = h_zu[i] ? nzt++ : -1;
+		p->nzt = nzt;
+		p->h_zt = malloc(sizeof(double) * (nzt > 0 ? nzt : 1));
+		for (int i = 0; i < nz; i++) if (zslot[i] >= 0) p->h_zt[zslot[i]] = p->h_z[i];
+		/* combos in key order; h_cnt becomes the first slot of each key */
+		for (int64_t k = 0; k < nkey; k++) if (h_cnt[k]) ncombo++;
+		p->ncombo = ncombo;
+		p->h_combo = malloc(sizeof(int32_t) * 3 * (ncombo > 0 ? ncombo : 1));
+		p->h_cstart = malloc(sizeof(int64_t) * (ncombo + 1));
+		int c = 0;
+		int32_t run = 0;
+		for (int64_t k = 0; k < nkey; k++) {
+			int32_t m = h_cnt[k];
+			h_cnt[k] = run;
+			if (m) {
+				h_cid[k] = c;
+				int g2 = (int)(k % N), b2 = (int)((k / N) % nb), zi = (int)(k / N / nb);
+				p->h_combo[3 * c] = zslot[zi];
+				p->h_combo[3 * c + 1] = b2;
+				p->h_combo[3 * c + 2] = g2;
+				p->h_cstart[c] = run;
+				c++;
+			} else {
+				h_cid[k] = -1;
+			}
+			run += m;
 		}
-	}
-	for (int64_t k = 0; k < nkey; k++) cnt[k + 1] += cnt[k];
-	int64_t *pos = cnt; /* cnt[k] = first slot of key k */
-	p->h_poses = malloc(sizeof(sxsk_pose) * (n > 0 ? n : 1));
-	c = 0;
-	for (int64_t k = 0; k < nkey; k++)
-		if (cid[k] >= 0) p->h_cstart[c++] = pos[k];
-	p->h_cstart[ncombo] = n;
-	/* slices for the translation kernel */
-	p->h_slices = malloc(sizeof(int32_t) * 2 * (ncombo > 0 ? ncombo : 1));
-	p->nslice = 0;
-	for (int k = 0; k < ncombo; k++) {
-		int ns = p->nslice;
-		if (ns > 0 && p->h_slices[2 * ns - 1] < SXS_SLICE && p->h_combo[3 * (k - 1)] == p->h_combo[3 * k]) {
-			p->h_slices[2 * ns - 1]++;
-		} else {
-			p->h_slices[2 * ns] = k;
-			p->h_slices[2 * ns + 1] = 1;
-			p->nslice++;
+		p->h_cstart[ncombo] = n;
+		/* slices for the translation kernel */
+		p->h_slices = malloc(sizeof(int32_t) * 2 * (ncombo > 0 ? ncombo : 1));
+		p->nslice = 0;
+		for (int k = 0; k < ncombo; k++) {
+			int ns = p->nslice;
+			if (ns > 0 && p->h_slices[2 * ns - 1] < SXS_SLICE && p->h_combo[3 * (k - 1)] == p->h_combo[3 * k]) {
+				p->h_slices[2 * ns - 1]++;
+			} else {
+				p->h_slices[2 * ns] = k;
+				p->h_slices[2 * ns + 1] = 1;
+				p->nslice++;
+			}
 		}
+		/* sorted by combo on the device (order inside a combo is free: each
+		 * pose's result depends only on its own rows) */
+		e = cudaMallocAsync((void **)&p->d_poses, sizeof(sxsk_pose) * nn, s);
+		if (!e) e = cudaMemcpyAsync(d_cnt, h_cnt, sizeof(int32_t) * (size_t)nkey, cudaMemcpyHostToDevice, s);
+		if (!e) e = cudaMemcpyAsync(d_cid, h_cid, sizeof(int32_t) * (size_t)nkey, cudaMemcpyHostToDevice, s);
+		if (!e) e = (cudaError_t)sxsk_pose_scatter(d_tmp, d_key, n, d_cnt, d_cid, p->d_poses, s);
+		if (!e) sxs_count_launches(n > 0 ? 1 : 0);
+		/* the host arrays above are read by the copies: wait before freeing */
+		if (!e) e = cudaStreamSynchronize(s);
 	}
-	for (int64_t i = 0; i < n; i++) {
-		int64_t dst = pos[key[i]]++;
-		sxsk_pose ps = tmp[i];
-		ps.combo = cid[key[i]];
-		p->h_poses[dst] = ps;
+	pfree(p, d_idx); pfree(p, d_tmp); pfree(p, d_key); pfree(p, d_cnt);
+	pfree(p, d_cid); pfree(p, d_zu); pfree(p, d_err);
+	free(h_cnt); free(h_zu); free(h_cid); free(zslot);
+	if (e || rc) {
+		plan_free_poses(p);
+		p->npose = 0;
+		p->ncombo = p->nzt = 0;
+		return e ? sxs_cuda_fail(e, "sxsg_plan_set_poses") : rc;
 	}
-	free(cnt); free(key); free(tmp); free(zused); free(zslot); free(cid);
 
 	/* upload */
-	size_t nn = (size_t)(n > 0 ? n : 1);
-	int rc = 0;
-	cudaError_t e = cudaMallocAsync((void **)&p->d_poses, sizeof(sxsk_pose) * nn, p->s);
+	e = cudaSuccess;
 	if (!e) e = cudaMallocAsync((void **)&p->d_combo, sizeof(int32_t) * 3 * (ncombo > 0 ? ncombo : 1), p->s);
 	if (!e) e = cudaMallocAsync((void **)&p->d_zt, sizeof(double) * (nzt > 0 ? nzt : 1), p->s);
 	if (!e && nzt > 0) e = cudaMallocAsync((void **)&p->d_bes, sizeof(double) * (size_t)nzt * p->Q * N, p->s);
 	size_t tau_n = (size_t)p->NT * nzt * p->K * p->K * p->K * SXS_QT;
 	if (!e && nzt > 0) e = cudaMallocAsync((void **)&p->d_tau, sizeof(double) * tau_n, p->s);
 	if (!e && nzt > 0 && p->fp32) e = cudaMallocAsync((void **)&p->d_tauf, sizeof(float) * tau_n, p->s);
-	if (!e && n > 0) e = cudaMemcpyAsync(p->d_poses, p->h_poses, sizeof(sxsk_pose) * n, cudaMemcpyHostToDevice, p->s);
 	if (!e && ncombo > 0) e = cudaMemcpyAsync(p->d_combo, p->h_combo, sizeof(int32_t) * 3 * ncombo, cudaMemcpyHostToDevice, p->s);
 	if (!e) e = cudaMallocAsync((void **)&p->d_slices, sizeof(int32_t) * 2 * (p->nslice > 0 ? p->nslice : 1), p->s);
 	if (!e && p->nslice > 0)

@@ -203,6 +203,13 @@ def test_invalid_pose_indices_are_rejected(gpu):
         p.set_poses(np.array([5, -1]), skip=1)
     with pytest.raises(gpu.SxsError, match="znum"):
         p.set_poses(np.array([len(g["z"]) * nb * nb * N ** 3]), skip=1)
+    # the first bad pose in list order is the one reported, as in the
+    # reference's sequential check
+    far = len(g["z"]) * nb * nb * N ** 3
+    with pytest.raises(gpu.SxsError, match=r"pose 2: negative grid index -7"):
+        p.set_poses(np.array([5, 6, -7, far, -1]), skip=1)
+    with pytest.raises(gpu.SxsError, match=r"pose 1: translation slot %d >= znum" % len(g["z"])):
+        p.set_poses(np.array([5, far, -7, far + 3]), skip=1)
     # the plan is still usable after a rejected list
     p.set_poses(g["index"][:5], skip=1)
     p.run(gpu.FIT_GRID)
