@@ -116,9 +116,16 @@ int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, con
                    int cbase, int ncombo, int nzt, int Q, int L, void *R, int fp32, cudaStream_t s);
 
 /* per-pose raw cross terms: cross[p][c][q] = cst[c][q] + 2 Re sum_m tw(m' a2) sum_l P R,
- * the m < 0 half folded in by symmetry; R holds the ncombo combos from combo_base */
+ * the m < 0 half folded in by symmetry; R holds the ncombo combos from combo_base.
+ * FP64 path: cst and cross are double.  FP32 path: cst and cross are
+ * double-float pairs {hi, lo} (float2), so that neither this kernel nor the
+ * fit that reads the terms touches the FP64 pipe. */
 int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, int ncombo, const void *P, const void *R,
-                    const double2 *tw, const double *cst, int Q, int L, double *cross, int fp32, cudaStream_t s);
+                    const double2 *tw, const void *cst, int Q, int L, void *cross, int fp32, cudaStream_t s);
+/* double -> double-float pairs {hi, lo} */
+int sxsk_to_df(const double *a, float2 *b, long n, cudaStream_t s);
+/* double-float pairs -> double (hi + lo), in place allowed */
+int sxsk_df_to_double(const float2 *a, double *b, long n, cudaStream_t s);
 
 /* grid fit: per pose, peak rescale then chi^2 at every (c1, c2) cell; best cell.
  * Scores the poses at slots [slot0, slot0 + nslot) of order (order[i].src
@@ -128,16 +135,16 @@ int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, int ncomb
  * max_blocks resident blocks (persistent loop; <= 0: one block per group). */
 int sxsk_fit_grid(const double *cross, const sxsk_pose *order, int slot0, int nslot, int Q, const double *fc,
                   double a0sum, double peak, const double *gtab, const double *c1g, int n1, const double *c2g, int n2,
-                  int max_blocks, double *chi, double *c1, double *c2, int32_t *cell, double *grid, double *scaled,
-                  cudaStream_t s);
+                  int max_blocks, double *chi, double *c1, double *c2, int32_t *cell, double *grid, cudaStream_t s);
 
 /* the grid fit of the mixed path in double-float arithmetic (FP32 pipe);
- * same arguments as sxsk_fit_grid, with gdf[n1][Q] = gtab split into
+ * same arguments as sxsk_fit_grid, with the cross terms as double-float
+ * pairs (sxsk_pose_cross, FP32 path) and gdf[n1][Q] = gtab split into
  * {hi, lo} floats */
-int sxsk_fit_grid_df(const double *cross, const sxsk_pose *order, int slot0, int nslot, int Q, const double *fc,
+int sxsk_fit_grid_df(const float2 *cross, const sxsk_pose *order, int slot0, int nslot, int Q, const double *fc,
                      double a0sum, double peak, const float2 *gdf, const double *c1g, int n1, const double *c2g,
                      int n2, int max_blocks, double *chi, double *c1, double *c2, int32_t *cell, double *grid,
-                     double *scaled, cudaStream_t s);
+                     cudaStream_t s);
 
 #ifdef __cplusplus
 }

@@ -414,6 +414,29 @@ k_translate_col(const typename Cx<S>::T *__restrict__ U, const S *__restrict__ t
 	}
 }
 
+/* Storage of the per-pose cross terms: double on the FP64 path; on the FP32
+ * path a double-float pair {hi, lo} = cst + 2 f formed with an error-free
+ * sum (explicit round-to-nearest adds, never contracted), so that the fit
+ * reads it without the FP64 pipe. */
+template <typename S> struct CrossT;
+template <> struct CrossT<double> { typedef double T; };
+template <> struct CrossT<float> { typedef float2 T; };
+__device__ __forceinline__ void cross_store(double *o, const double *cst, size_t i, double f)
+{
+	o[i] = cst[i] + 2.0 * f;
+}
+__device__ __forceinline__ void cross_store(float2 *o, const float2 *cst, size_t i, float f)
+{
+	float2 c = cst[i];
+	float t = 2.0f * f;                       /* exact */
+	float s = __fadd_rn(c.x, t);
+	float bb = __fsub_rn(s, c.x);
+	float e = __fadd_rn(__fsub_rn(c.x, __fsub_rn(s, bb)), __fsub_rn(t, bb));
+	e = __fadd_rn(e, c.y);
+	float h = __fadd_rn(s, e);
+	o[i] = make_float2(h, __fsub_rn(e, __fsub_rn(h, s)));
+}
+
 /* Per-pose cross terms of one chunk, all q tiles.  Thread = (pose, 2
  * adjacent q); block = 32 consecutive poses (sorted by combo, so their R
  * rows repeat and hit in L1) x 4 q pairs of one tile; blocks ordered
@@ -426,7 +449,8 @@ template <typename S, bool HINT>
 __global__ void __launch_bounds__(128)
 k_pose_cross(const sxsk_pose *__restrict__ poses, int npose, int combo_base, int ncombo,
              const typename Cx<S>::T *__restrict__ P, const typename Cx<S>::T *__restrict__ R,
-             const double2 *__restrict__ tw, const double *__restrict__ cst, int Q, int L, double *__restrict__ cross)
+             const double2 *__restrict__ tw, const typename CrossT<S>::T *__restrict__ cst, int Q, int L,
+             typename CrossT<S>::T *__restrict__ cross)
 {
 	typedef typename Cx<S>::T V;
 	__shared__ V tws[2 * SXS_LMAX_K - 1];
@@ -496,13 +520,13 @@ k_pose_cross(const sxsk_pose *__restrict__ poses, int npose, int combo_base, int
 			f[k][5] += a2.x * s2.x - a2.y * s2.y;
 		}
 	}
-	double *o = cross + (size_t)ps.src * 6 * Q;
+	typename CrossT<S>::T *o = cross + (size_t)ps.src * 6 * Q;
 #pragma unroll
 	for (int k = 0; k < 2; k++) {
 		int q = q0 + k;
 		if (q < Q) {
 #pragma unroll
-			for (int c = 0; c < 6; c++) o[c * Q + q] = cst[c * Q + q] + 2.0 * (double)f[k][c];
+			for (int c = 0; c < 6; c++) cross_store(o, cst, (size_t)c * Q + q, f[k][c]);
 		}
 	}
 }
@@ -584,7 +608,7 @@ k_fit_grid(const double *__restrict__ cross, const sxsk_pose *__restrict__ order
            const double *__restrict__ fc, double a0sum, double peak, const double *__restrict__ gtab,
            const double *__restrict__ c1g, int n1, const double *__restrict__ c2g, int n2, int tp, int ppb,
            double *__restrict__ chi, double *__restrict__ c1o, double *__restrict__ c2o, int32_t *__restrict__ cello,
-           double *__restrict__ grid, double *__restrict__ scaled)
+           double *__restrict__ grid)
 {
 	extern __shared__ double sm[];
 	double *cs = sm;                                   /* [ppb][8][Q]: VV VD VW DD DW WW P3 P4 */
@@ -622,9 +646,7 @@ k_fit_grid(const double *__restrict__ cross, const sxsk_pose *__restrict__ order
 		__syncthreads();
 		for (int k = tid; k < nhere * 6 * Q; k += blockDim.x) {
 			int p = k / (6 * Q), r = k % (6 * Q);
-			double v = cs[(size_t)p * 8 * Q + r] * sf[3 * p];
-			cs[(size_t)p * 8 * Q + r] = v;
-			if (scaled) scaled[(size_t)srcs[p] * 6 * Q + r] = v;
+			cs[(size_t)p * 8 * Q + r] *= sf[3 * p];
 		}
 		__syncthreads();
 		double *c = cs + (size_t)lp * 8 * Q;
@@ -923,7 +945,7 @@ int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, con
 }
 
 int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, int ncombo, const void *P, const void *R,
-                    const double2 *tw, const double *cst, int Q, int L, double *cross, int fp32, cudaStream_t s)
+                    const double2 *tw, const void *cst, int Q, int L, void *cross, int fp32, cudaStream_t s)
 {
 	if (npose <= 0) return 0;
 	int NT = (Q + SXS_QT - 1) / SXS_QT;
@@ -931,17 +953,18 @@ int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, int ncomb
 	if (nb > 0x7fffffffL) return cudaErrorInvalidValue;
 	if (fp32)
 		k_pose_cross<float, true><<<(unsigned)nb, 128, 0, s>>>(poses, npose, combo_base, ncombo, (const float2 *)P,
-		                                                  (const float2 *)R, tw, cst, Q, L, cross);
+		                                                  (const float2 *)R, tw, (const float2 *)cst, Q, L,
+		                                                  (float2 *)cross);
 	else
 		k_pose_cross<double, false><<<(unsigned)nb, 128, 0, s>>>(poses, npose, combo_base, ncombo, (const double2 *)P,
-		                                                   (const double2 *)R, tw, cst, Q, L, cross);
+		                                                   (const double2 *)R, tw, (const double *)cst, Q, L,
+		                                                   (double *)cross);
 	return cudaGetLastError();
 }
 
 int sxsk_fit_grid(const double *cross, const sxsk_pose *order, int slot0, int nslot, int Q, const double *fc,
                   double a0sum, double peak, const double *gtab, const double *c1g, int n1, const double *c2g, int n2,
-                  int max_blocks, double *chi, double *c1, double *c2, int32_t *cell, double *grid, double *scaled,
-                  cudaStream_t s)
+                  int max_blocks, double *chi, double *c1, double *c2, int32_t *cell, double *grid, cudaStream_t s)
 {
 	if (nslot <= 0) return 0;
 	if (n1 <= 0 || n2 <= 0) return cudaErrorInvalidValue;
@@ -963,7 +986,7 @@ int sxsk_fit_grid(const double *cross, const sxsk_pose *order, int slot0, int ns
 	long ngroup = (nslot + ppb - 1) / ppb;
 	int grid_n = (int)(ngroup < (long)max_blocks || max_blocks <= 0 ? ngroup : max_blocks);
 	k_fit_grid<<<grid_n, FIT_THREADS, smem, s>>>(cross, order, slot0, nslot, Q, fc, a0sum, peak, gtab, c1g, n1, c2g,
-	                                              n2, tp, ppb, chi, c1, c2, cell, grid, scaled);
+	                                              n2, tp, ppb, chi, c1, c2, cell, grid);
 	return cudaGetLastError();
 }
 

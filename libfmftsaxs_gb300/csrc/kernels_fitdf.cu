@@ -10,7 +10,9 @@
  * (point_score of src/min_saxs.c:391-448 with the per-q constants folded on
  * the host); the model is normalised to 1 at q_0 instead of to the peak, and
  * the constants are scaled by peak (a1, u) and peak^2 (a3, e, f), which
- * leaves up and down unchanged and keeps every intermediate near 1.
+ * leaves up and down unchanged and keeps every intermediate near 1.  The
+ * cross terms arrive as double-float pairs (the FP32 per-pose kernel), so the
+ * FP64 pipe sees one division per pose.
  *
  * Compiled with -fmad=false: the error-free transformations of
  * fitdf_core.h must not be contracted.
@@ -35,11 +37,11 @@ namespace {
  * chunk.  After the last chunk a thread has the polynomial coefficients of
  * its row and scans the c2 cells. */
 __global__ void __launch_bounds__(FITD_THREADS)
-k_fit_grid_df(const double *__restrict__ cross, const sxsk_pose *__restrict__ order, int slot0, int nslot, int Q,
+k_fit_grid_df(const float2 *__restrict__ cross, const sxsk_pose *__restrict__ order, int slot0, int nslot, int Q,
               const double *__restrict__ fc, double a0sum, double peak, const float2 *__restrict__ gdf,
               const double *__restrict__ c1g, int n1, const double *__restrict__ c2g, int n2, int tp, int ppb,
               int qc, int gsm, double *__restrict__ chi, double *__restrict__ c1o, double *__restrict__ c2o,
-              int32_t *__restrict__ cello, double *__restrict__ grid, double *__restrict__ scaled)
+              int32_t *__restrict__ cello, double *__restrict__ grid)
 {
 	extern __shared__ double sm[];
 	int ld = qc + 1;                                   /* staged q per row: the previous q + the chunk */
@@ -49,8 +51,8 @@ k_fit_grid_df(const double *__restrict__ cross, const sxsk_pose *__restrict__ or
 	dfl *gs = c2s + n2;                                /* [n1][Q] G(c1, q) when gsm */
 	double *red = reinterpret_cast<double *>(gs + (gsm ? (size_t)n1 * Q : 0)); /* [ppb*tp][2] */
 	int *redc = (int *)(red + 2 * ppb * tp);           /* [ppb*tp] */
-	double *sf = (double *)(redc + ((ppb * tp + 1) & ~1)); /* [ppb][2]: 1/norm, peak/norm */
-	dfl *sfd = reinterpret_cast<dfl *>(sf + 2 * ppb);  /* [ppb][2]: U2, D4 */
+	dfl *sf = reinterpret_cast<dfl *>(redc + ((ppb * tp + 1) & ~1)); /* [ppb]: 1/norm */
+	dfl *sfd = sf + ppb;                               /* [ppb][2]: U2, D4 */
 	int *srcs = (int *)(sfd + 2 * ppb);                /* [ppb] */
 	int tid = threadIdx.x;
 	int nthr = ppb * tp;
@@ -77,10 +79,11 @@ k_fit_grid_df(const double *__restrict__ cross, const sxsk_pose *__restrict__ or
 		if (tid < nhere) srcs[tid] = order ? order[slot0 + s0 + tid].src : slot0 + s0 + tid;
 		__syncthreads();
 		if (tid < nhere) {
-			const double *c = cross + (size_t)srcs[tid] * 6 * Q;
-			double sc = c[0] + c[3 * Q] + c[5 * Q] + c[2 * Q] - c[Q] - c[4 * Q];
-			sf[2 * tid] = 1.0 / sc;
-			sf[2 * tid + 1] = peak / sc;
+			/* norm = VV + DD + WW + VW - VD - DW at q_0 (the model at q_0 with
+			 * c1 = 1, c2 = 1), in double-float; its inverse once in double */
+			const dfl *c = reinterpret_cast<const dfl *>(cross) + (size_t)srcs[tid] * 6 * Q;
+			dfl sc = df_add(df_add(df_add(c[0], c[3 * Q]), df_add(c[5 * Q], c[2 * Q])), df_neg(df_add(c[Q], c[4 * Q])));
+			sf[tid] = df_from(1.0 / df_to(sc));
 		}
 		double bscore = __longlong_as_double(0x7ff0000000000000LL);
 		int bcell = -1;
@@ -102,9 +105,8 @@ k_fit_grid_df(const double *__restrict__ cross, const sxsk_pose *__restrict__ or
 					int q = q0 - 1 + kk;
 					dfl v = df_mk(0, 0);
 					if (q >= 0) {
-						double x = cross[(size_t)srcs[p] * 6 * Q + ch * Q + q];
-						v = df_from(x * sf[2 * p]);
-						if (scaled && kk > 0 && round == 0) scaled[(size_t)srcs[p] * 6 * Q + ch * Q + q] = x * sf[2 * p + 1];
+						float2 x = cross[(size_t)srcs[p] * 6 * Q + ch * Q + q];
+						v = df_mul(df_mk(x.x, x.y), sf[p]);
 					}
 					cs[(size_t)p * 8 * ld + ch * ld + kk] = v;
 				}
@@ -187,10 +189,10 @@ k_fit_grid_df(const double *__restrict__ cross, const sxsk_pose *__restrict__ or
 
 } // namespace
 
-extern "C" int sxsk_fit_grid_df(const double *cross, const sxsk_pose *order, int slot0, int nslot, int Q,
+extern "C" int sxsk_fit_grid_df(const float2 *cross, const sxsk_pose *order, int slot0, int nslot, int Q,
                                 const double *fc, double a0sum, double peak, const float2 *gdf, const double *c1g,
                                 int n1, const double *c2g, int n2, int max_blocks, double *chi, double *c1,
-                                double *c2, int32_t *cell, double *grid, double *scaled, cudaStream_t s)
+                                double *c2, int32_t *cell, double *grid, cudaStream_t s)
 {
 	if (nslot <= 0) return 0;
 	if (n1 <= 0 || n2 <= 0 || Q <= 0) return cudaErrorInvalidValue;
@@ -203,8 +205,8 @@ extern "C" int sxsk_fit_grid_df(const double *cross, const sxsk_pose *order, int
 	for (;;) {
 		size_t nthr = (size_t)ppb * tp;
 		smem = sizeof(dfl) * ((size_t)ppb * 8 * (qc + 1) + (size_t)FITD_NFC * Q + n2 + (gsm ? (size_t)n1 * Q : 0)) +
-		       sizeof(double) * (2 * nthr + 2 * ppb) + sizeof(int) * ((nthr + 1) & ~(size_t)1) +
-		       sizeof(dfl) * 2 * ppb + sizeof(int) * ppb;
+		       sizeof(double) * 2 * nthr + sizeof(int) * ((nthr + 1) & ~(size_t)1) + sizeof(dfl) * 3 * ppb +
+		       sizeof(int) * ppb;
 		if (smem <= 227 * 1024 || ppb == 1) break;
 		ppb = (ppb + 1) / 2;
 	}
@@ -216,6 +218,41 @@ extern "C" int sxsk_fit_grid_df(const double *cross, const sxsk_pose *order, int
 	long ngroup = (nslot + ppb - 1) / ppb;
 	int grid_n = (int)(ngroup < (long)max_blocks || max_blocks <= 0 ? ngroup : max_blocks);
 	k_fit_grid_df<<<grid_n, FITD_THREADS, smem, s>>>(cross, order, slot0, nslot, Q, fc, a0sum, peak, gdf, c1g, n1,
-	                                                  c2g, n2, tp, ppb, qc, gsm, chi, c1, c2, cell, grid, scaled);
+	                                                  c2g, n2, tp, ppb, qc, gsm, chi, c1, c2, cell, grid);
+	return cudaGetLastError();
+}
+
+namespace {
+__global__ void k_to_df(const double *__restrict__ a, float2 *__restrict__ b, long n)
+{
+	long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) {
+		dfl v = df_from(a[i]);
+		b[i] = make_float2(v.hi, v.lo);
+	}
+}
+__global__ void k_df_to_double(const float2 *a, double *b, long n)
+{
+	long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) {
+		float2 v = a[i];             /* read before the write: a and b may alias */
+		b[i] = (double)v.x + (double)v.y;
+	}
+}
+} // namespace
+
+extern "C" int sxsk_to_df(const double *a, float2 *b, long n, cudaStream_t s)
+{
+	if (n <= 0) return 0;
+	if ((n + 255) / 256 > 0x7fffffffL) return cudaErrorInvalidValue;
+	k_to_df<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, b, n);
+	return cudaGetLastError();
+}
+
+extern "C" int sxsk_df_to_double(const float2 *a, double *b, long n, cudaStream_t s)
+{
+	if (n <= 0) return 0;
+	if ((n + 255) / 256 > 0x7fffffffL) return cudaErrorInvalidValue;
+	k_df_to_double<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, b, n);
 	return cudaGetLastError();
 }

@@ -11,17 +11,22 @@ namespace {
 
 /* raw [pose][6][Q] -> transposed [6*Q][pose], with the peak rescale of
  * src/min_saxs.c:170-188 when rescale != 0 */
-__global__ void k_rescale_transpose(const double *__restrict__ cross, double *__restrict__ ct, int npose, int Q,
+__device__ __forceinline__ double cross_at(const double *c, size_t i) { return c[i]; }
+__device__ __forceinline__ double cross_at(const float2 *c, size_t i) { return (double)c[i].x + (double)c[i].y; }
+
+template <typename T>
+__global__ void k_rescale_transpose(const T *__restrict__ cross, double *__restrict__ ct, int npose, int Q,
                                     double peak, int rescale)
 {
 	long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= (long)npose * 6 * Q) return;
 	int p = (int)(i % npose);
 	int cq = (int)(i / npose);
-	const double *src = cross + (size_t)p * 6 * Q;
-	double v = src[cq];
+	size_t b = (size_t)p * 6 * Q;
+	double v = cross_at(cross, b + cq);
 	if (rescale) {
-		double s = src[0] + src[3 * Q] + src[5 * Q] + src[2 * Q] - src[Q] - src[4 * Q];
+		double s = cross_at(cross, b) + cross_at(cross, b + 3 * Q) + cross_at(cross, b + 5 * Q) +
+		           cross_at(cross, b + 2 * Q) - cross_at(cross, b + Q) - cross_at(cross, b + 4 * Q);
 		s = peak / s;
 		v *= s;
 	}
@@ -55,13 +60,18 @@ __global__ void k_lbfgsb(const double *__restrict__ ct, int npose, int Q, const 
 
 /* cross: [npose][6][Q] (raw when rescale != 0, already rescaled otherwise);
  * ct: workspace of npose*6*Q doubles that receives the transposed terms. */
-extern "C" int sxs_fit_lbfgsb_launch(const double *cross, double *ct, int npose, int Q, const double *q,
+extern "C" int sxs_fit_lbfgsb_launch(const void *cross, int cross_df, double *ct, int npose, int Q, const double *q,
                                      const double *a, double mult, double peak, int rescale, double *chi, double *c1,
                                      double *c2, double *scale, int *nevals, cudaStream_t s)
 {
 	if (npose <= 0) return 0;
 	long n = (long)npose * 6 * Q;
-	k_rescale_transpose<<<(int)((n + 255) / 256), 256, 0, s>>>(cross, ct, npose, Q, peak, rescale);
+	if (cross_df)
+		k_rescale_transpose<float2><<<(int)((n + 255) / 256), 256, 0, s>>>((const float2 *)cross, ct, npose, Q, peak,
+		                                                                 rescale);
+	else
+		k_rescale_transpose<double><<<(int)((n + 255) / 256), 256, 0, s>>>((const double *)cross, ct, npose, Q, peak,
+		                                                                 rescale);
 	k_lbfgsb<<<(npose + 63) / 64, 64, 0, s>>>(ct, npose, Q, q, a, mult, 100000, chi, c1, c2, scale, nevals);
 	return (int)cudaGetLastError();
 }

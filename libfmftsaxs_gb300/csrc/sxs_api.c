@@ -501,7 +501,7 @@ static int fit_profiles_gpu(struct sxs_profile **profiles, const int *sel, int n
 	if (!e) e = cudaMemcpyAsync(d_q, profiles[sel[0]]->qvals, sizeof(double) * Q, cudaMemcpyHostToDevice, s);
 	if (!e) e = cudaMemcpyAsync(d_a, params->a, sizeof(double) * 6 * Q, cudaMemcpyHostToDevice, s);
 	if (!e) {
-		e = (cudaError_t)sxs_fit_lbfgsb_launch(d_c, d_t, n, Q, d_q, d_a, params->mult, params->peak, 0, d_o, d_o + n,
+		e = (cudaError_t)sxs_fit_lbfgsb_launch(d_c, 0, d_t, n, Q, d_q, d_a, params->mult, params->peak, 0, d_o, d_o + n,
 		                                       d_o + 2 * n, d_o + 3 * n, d_it, s);
 		sxs_count_launches(2);
 	}

@@ -114,7 +114,7 @@ int sxsg_score_exact(const double *rec_xyz, int nrec, const double *lig_xyz, int
 			                             d_ylm, d_jl, d_spf + spf_n * k, s);
 		if (!e) e = (cudaError_t)sxsk_self_cross(d_spf, nb, Q, L, d_cross, s);
 		if (!e)
-			e = (cudaError_t)sxs_fit_lbfgsb_launch(d_cross, d_ct, nb, Q, d_q, d_a, mult, 1.0, 0, d_chi, d_c1, d_c2, NULL,
+			e = (cudaError_t)sxs_fit_lbfgsb_launch(d_cross, 0, d_ct, nb, Q, d_q, d_a, mult, 1.0, 0, d_chi, d_c1, d_c2, NULL,
 			                                       NULL, s);
 		sxs_count_launches(3 * nb + 3);
 		if (!e && chi) e = cudaMemcpyAsync(chi + p0, d_chi, sizeof(double) * nb, cudaMemcpyDeviceToHost, s);

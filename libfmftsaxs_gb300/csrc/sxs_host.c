@@ -181,6 +181,7 @@ struct sxsg_plan {
 	double mult, peak, a0sum;
 	/* resident inputs */
 	double *d_A, *d_B, *d_q, *d_fc, *d_a, *d_gtab, *d_c1g, *d_c2g, *d_cst;
+	float2 *d_cstf;             /* cst as double-float pairs (mixed path) */
 	float2 *d_gdf;              /* gtab as {hi, lo} floats (mixed path fit) */
 	double2 *d_tw;
 	void *d_At, *d_Bt;          /* transposed coefficients, table precision */
@@ -217,6 +218,9 @@ struct sxsg_plan {
 	int64_t R_combos;
 	size_t r_budget;
 	/* outputs */
+	/* cross terms [npose][6][Q]: double on the FP64 path, double-float
+	 * pairs {hi, lo} (same size) on the mixed path; d_scaled is the
+	 * L-BFGS-B fit's rescaled, transposed copy */
 	double *d_cross, *d_chi, *d_c1, *d_c2, *d_grid, *d_scaled, *d_scale;
 	int32_t *d_cell;
 	int *d_iters;
@@ -254,7 +258,7 @@ void sxsg_plan_destroy(sxsg_plan *p)
 	cudaStreamSynchronize(p->s);
 	plan_free_poses(p);
 	pfree(p, p->d_A); pfree(p, p->d_B); pfree(p, p->d_q); pfree(p, p->d_fc); pfree(p, p->d_a); pfree(p, p->d_gtab); pfree(p, p->d_gdf);
-	pfree(p, p->d_c1g); pfree(p, p->d_c2g); pfree(p, p->d_cst); pfree(p, p->d_At); pfree(p, p->d_Bt);
+	pfree(p, p->d_c1g); pfree(p, p->d_c2g); pfree(p, p->d_cst); pfree(p, p->d_cstf); pfree(p, p->d_At); pfree(p, p->d_Bt);
 	pfree(p, p->d_tw); pfree(p, p->d_R); pfree(p, p->d_amat);
 	if (!p->ext_tables) {
 		pfree(p, p->d_P);
@@ -319,6 +323,7 @@ int sxs_plan_create_on(sxsg_plan **out, const double *A, const double *B, const 
 	if (!e) e = cudaMallocAsync((void **)&p->d_fc, sizeof(double) * 5 * Q, p->s);
 	if (!e) e = cudaMallocAsync((void **)&p->d_a, sizeof(double) * 6 * Q, p->s);
 	if (!e) e = cudaMallocAsync((void **)&p->d_cst, sizeof(double) * 6 * Q, p->s);
+	if (!e && p->fp32) e = cudaMallocAsync((void **)&p->d_cstf, sizeof(float2) * 6 * Q, p->s);
 	if (!e) e = cudaMallocAsync((void **)&p->d_tw, sizeof(double2) * p->N, p->s);
 	if (!e && n1 > 0) e = cudaMallocAsync((void **)&p->d_gtab, sizeof(double) * n1 * Q, p->s);
 	if (!e && n1 > 0) e = cudaMallocAsync((void **)&p->d_c1g, sizeof(double) * n1, p->s);
@@ -377,6 +382,10 @@ int sxs_plan_create_on(sxsg_plan **out, const double *A, const double *B, const 
 		if (!e) e = (cudaError_t)sxsk_spf_transpose(p->d_B, p->d_Bt, Q, L, p->fp32, s);
 		if (!e) e = (cudaError_t)sxsk_const_int(p->d_A, p->d_B, Q, L, p->d_cst, s);
 		sxs_count_launches(3);
+		if (!e && p->fp32) {
+			e = (cudaError_t)sxsk_to_df(p->d_cst, p->d_cstf, 6L * Q, s);
+			sxs_count_launches(1);
+		}
 	}
 	if (!e) e = cudaStreamSynchronize(s);
 	if (e) {
@@ -612,15 +621,16 @@ static int plan_tables(sxsg_plan *p)
 
 /* grid fit of slots [slot0, slot0 + nslot) of order (all poses in list
  * order when order is NULL) in the plan's precision: FP64 on the plain path,
- * double-float on the FP32 pipe on the mixed path */
+ * double-float on the FP32 pipe on the mixed path (whose cross terms are
+ * double-float pairs) */
 static int plan_fit_grid(sxsg_plan *p, const sxsk_pose *order, int slot0, int nslot, int max_blocks, double *chi,
-                         double *c1, double *c2, int32_t *cell, double *grid, double *scaled, cudaStream_t st)
+                         double *c1, double *c2, int32_t *cell, double *grid, cudaStream_t st)
 {
 	if (p->fp32)
-		return sxsk_fit_grid_df(p->d_cross, order, slot0, nslot, p->Q, p->d_fc, p->a0sum, p->peak, p->d_gdf,
-		                        p->d_c1g, p->n1, p->d_c2g, p->n2, max_blocks, chi, c1, c2, cell, grid, scaled, st);
+		return sxsk_fit_grid_df((const float2 *)p->d_cross, order, slot0, nslot, p->Q, p->d_fc, p->a0sum, p->peak,
+		                        p->d_gdf, p->d_c1g, p->n1, p->d_c2g, p->n2, max_blocks, chi, c1, c2, cell, grid, st);
 	return sxsk_fit_grid(p->d_cross, order, slot0, nslot, p->Q, p->d_fc, p->a0sum, p->peak, p->d_gtab, p->d_c1g,
-	                     p->n1, p->d_c2g, p->n2, max_blocks, chi, c1, c2, cell, grid, scaled, st);
+	                     p->n1, p->d_c2g, p->n2, max_blocks, chi, c1, c2, cell, grid, st);
 }
 
 static int plan_events(sxsg_plan *p, int need)
@@ -676,7 +686,7 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 		SXS_CU(cudaEventRecord(e[1], s));
 		int64_t p0 = p->h_cstart[c0], p1 = p->h_cstart[c1];
 		SXS_K(sxsk_pose_cross(p->d_poses + p0, (int)(p1 - p0), (int)c0, (int)(c1 - c0), p->d_P, p->d_R, p->d_tw,
-		                      p->d_cst, Q, L,
+		                      p->fp32 ? (const void *)p->d_cstf : (const void *)p->d_cst, Q, L,
 		                      p->d_cross, p->fp32, s));
 		SXS_CU(cudaEventRecord(e[2], s));
 		sxs_count_launches(sxsk_translate_launches(L) + 1);
@@ -684,10 +694,10 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 	SXS_CU(cudaEventRecord(p->ev[5], s));
 	int n = (int)p->npose;
 	if (fit_mode == SXSG_FIT_GRID) {
-		SXS_K(plan_fit_grid(p, NULL, 0, n, 0, p->d_chi, p->d_c1, p->d_c2, p->d_cell, NULL, p->d_scaled, s));
+		SXS_K(plan_fit_grid(p, NULL, 0, n, 0, p->d_chi, p->d_c1, p->d_c2, p->d_cell, NULL, s));
 		sxs_count_launches(n > 0 ? 1 : 0);
 	} else if (fit_mode == SXSG_FIT_LBFGSB) {
-		SXS_K(sxs_fit_lbfgsb_launch(p->d_cross, p->d_scaled, n, Q, p->d_q, p->d_a, p->mult, p->peak, 1, p->d_chi,
+		SXS_K(sxs_fit_lbfgsb_launch(p->d_cross, p->fp32, p->d_scaled, n, Q, p->d_q, p->d_a, p->mult, p->peak, 1, p->d_chi,
 		                            p->d_c1, p->d_c2, p->d_scale, p->d_iters, s));
 		sxs_count_launches(n > 0 ? 2 : 0);
 		if (n > 0) SXS_CU(cudaMemsetAsync(p->d_cell, 0xff, sizeof(int32_t) * n, s));
@@ -728,7 +738,19 @@ int sxsg_plan_results(sxsg_plan *p, double *chi, double *c1, double *c2, int32_t
 	if (c1) SXS_CU(cudaMemcpyAsync(c1, p->d_c1, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
 	if (c2) SXS_CU(cudaMemcpyAsync(c2, p->d_c2, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
 	if (cell) SXS_CU(cudaMemcpyAsync(cell, p->d_cell, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
-	if (cross) SXS_CU(cudaMemcpyAsync(cross, p->d_cross, sizeof(double) * n * 6 * p->Q, cudaMemcpyDeviceToHost, s));
+	if (cross) {
+		/* the mixed path keeps double-float pairs: same size, widened here */
+		SXS_CU(cudaMemcpyAsync(cross, p->d_cross, sizeof(double) * n * 6 * p->Q, cudaMemcpyDeviceToHost, s));
+		if (p->fp32) {
+			SXS_CU(cudaStreamSynchronize(s));
+			size_t m = n * 6 * (size_t)p->Q;
+			for (size_t i = 0; i < m; i++) {
+				float v[2];
+				memcpy(v, cross + i, sizeof(v));
+				cross[i] = (double)v[0] + (double)v[1];
+			}
+		}
+	}
 	if (grid) {
 		if (p->n1 <= 0 || p->n2 <= 0) return sxs_fail(-2, "no fit grid in this plan");
 		size_t gn = n * p->n1 * p->n2;
@@ -741,7 +763,7 @@ int sxsg_plan_results(sxsg_plan *p, double *chi, double *c1, double *c2, int32_t
 		if (!e) e = cudaMallocAsync((void **)&t2, sizeof(double) * n, p->s);
 		if (!e) e = cudaMallocAsync((void **)&tcell, sizeof(int32_t) * n, p->s);
 		if (!e) {
-			e = (cudaError_t)plan_fit_grid(p, NULL, 0, (int)n, 0, tc, t1, t2, tcell, d_g, NULL, s);
+			e = (cudaError_t)plan_fit_grid(p, NULL, 0, (int)n, 0, tc, t1, t2, tcell, d_g, s);
 			sxs_count_launches(1);
 		}
 		if (!e) e = cudaMemcpyAsync(grid, d_g, sizeof(double) * gn, cudaMemcpyDeviceToHost, s);

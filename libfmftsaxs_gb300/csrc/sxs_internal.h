@@ -80,8 +80,10 @@ void sxs_fit_constants(const double *q, const double *a, int Q, double *fc);
 /* device L-BFGS-B over (c1, c2) for a batch of poses: cross [n][6][Q]
  * (rescaled here by peak when rescale != 0), ct a workspace of n*6*Q
  * doubles; two kernel launches */
-int sxs_fit_lbfgsb_launch(const double *cross, double *ct, int npose, int Q, const double *q, const double *a,
-                          double mult, double peak, int rescale, double *chi, double *c1, double *c2, double *scale,
-                          int *nevals, cudaStream_t s);
+/* cross: double, or double-float pairs {hi, lo} when cross_df (the mixed
+ * path's per-pose terms) */
+int sxs_fit_lbfgsb_launch(const void *cross, int cross_df, double *ct, int npose, int Q, const double *q,
+                          const double *a, double mult, double peak, int rescale, double *chi, double *c1, double *c2,
+                          double *scale, int *nevals, cudaStream_t s);
 
 #endif
