@@ -356,8 +356,33 @@ __device__ __forceinline__ void ld4(const double *p, double *v)
  * SXS_QT q x 3 ch x SXS_SLICE combos = 384 threads; tau rows are read as float4/double2 chunks that
  * lanes of the same q share.  One launch per NB covers the m with
  * n in (NB - 4, NB]. */
+/* one output row of the column form: sum_k tau[k] x (U[k] for even i + k,
+ * -i U[k] for odd), with the parity of the row i given as PAR */
+template <int PAR, typename S, typename V, int NB>
+__device__ __forceinline__ V tcol_row(const S *row, const V *u)
+{
+	V acc = zero2<V>();
+#pragma unroll
+	for (int k4 = 0; k4 < NB; k4 += 4) {
+		S tv[4];
+		ld4(row + k4, tv);
+#pragma unroll
+		for (int kk = 0; kk < 4; kk++) {
+			int k = k4 + kk;
+			if ((k & 1) == PAR) {
+				acc.x += tv[kk] * u[k].x;
+				acc.y += tv[kk] * u[k].y;
+			} else {
+				acc.x += tv[kk] * u[k].y;
+				acc.y -= tv[kk] * u[k].x;
+			}
+		}
+	}
+	return acc;
+}
+
 template <typename S, int NB>
-__global__ void __launch_bounds__(384)
+__global__ void __launch_bounds__(384, sizeof(S) == 4 ? (NB <= 20 ? 3 : 2) : 1)
 k_translate_col(const typename Cx<S>::T *__restrict__ U, const S *__restrict__ tau,
                 const int32_t *__restrict__ combo_zbg, const int32_t *__restrict__ slices, int nslice, int cbase,
                 int ncombo, int L, int nzt, int m_lo, int nm, typename Cx<S>::T *__restrict__ R)
@@ -394,23 +419,11 @@ k_translate_col(const typename Cx<S>::T *__restrict__ U, const S *__restrict__ t
 	for (int k = 0; k < NB; k++) u[k] = k < n ? Ub[(size_t)k * 3 * SXS_QT] : zero2<V>();
 	const S *tq = ts + q * qstride;
 	V *Rb = R + (((size_t)t * ncombo + c) * NP + po) * 3 * SXS_QT + ch * SXS_QT + q;
-	for (int i = 0; i < n; i++) {
-		const S *row = tq + i * NB;
-		V acc = zero2<V>();
-		int par = i & 1;
-#pragma unroll
-		for (int k4 = 0; k4 < NB; k4 += 4) {
-			S tv[4];
-			ld4(row + k4, tv);
-#pragma unroll
-			for (int kk = 0; kk < 4; kk++) {
-				int k = k4 + kk;
-				/* even i + k: tau U; odd: tau (-i U) */
-				if ((kk & 1) == par) { acc.x += tv[kk] * u[k].x; acc.y += tv[kk] * u[k].y; }
-				else { acc.x += tv[kk] * u[k].y; acc.y -= tv[kk] * u[k].x; }
-			}
-		}
-		Rb[(size_t)i * 3 * SXS_QT] = acc;
+	/* rows in even/odd pairs so that the parity of i + k is known at
+	 * compile time: every k is two FMAs */
+	for (int i = 0; i < n; i += 2) {
+		Rb[(size_t)i * 3 * SXS_QT] = tcol_row<0, S, V, NB>(tq + i * NB, u);
+		if (i + 1 < n) Rb[(size_t)(i + 1) * 3 * SXS_QT] = tcol_row<1, S, V, NB>(tq + (i + 1) * NB, u);
 	}
 }
 
