@@ -307,31 +307,46 @@ k_translate(const typename Cx<S>::T *__restrict__ U, const S *__restrict__ tau, 
 	for (int c = cfirst; c < cfirst + nc; c++) {
 		int b2 = combo_zbg[3 * c + 1], g2 = combo_zbg[3 * c + 2];
 		const V *Ub = U + (((size_t)t * nrow + b2 * N + g2) * NP + po) * 3 * SXS_QT + j2;
-		V acc[3][2];
+		/* sums over l1 = m, m+2, ... (e) and m+1, m+3, ... (o): the terms of
+		 * the class with l + l1 even add tau U, the other tau (-i U), so the
+		 * loop needs no per-thread branch */
+		V ae[3][2], ao[3][2];
 #pragma unroll
-		for (int ch = 0; ch < 3; ch++) acc[ch][0] = acc[ch][1] = zero2<V>();
-		for (int l1 = m; l1 <= L; l1++) {
-			S t0 = tp[l1 * SXS_QT], t1 = tp[l1 * SXS_QT + 1];
+		for (int ch = 0; ch < 3; ch++) ae[ch][0] = ae[ch][1] = ao[ch][0] = ao[ch][1] = zero2<V>();
+		for (int l1 = m; l1 <= L; l1 += 2) {
 			const V *u = Ub + (size_t)(l1 - m) * 3 * SXS_QT;
-			if (((l + l1) & 1) == 0) {
+			S t0 = tp[l1 * SXS_QT], t1 = tp[l1 * SXS_QT + 1];
+#pragma unroll
+			for (int ch = 0; ch < 3; ch++) {
+				Pair2<S> uv = ld2(u + ch * SXS_QT);
+				ae[ch][0].x += t0 * uv.a.x; ae[ch][0].y += t0 * uv.a.y;
+				ae[ch][1].x += t1 * uv.b.x; ae[ch][1].y += t1 * uv.b.y;
+			}
+			if (l1 + 1 <= L) {
+				u += 3 * SXS_QT;
+				t0 = tp[(l1 + 1) * SXS_QT];
+				t1 = tp[(l1 + 1) * SXS_QT + 1];
 #pragma unroll
 				for (int ch = 0; ch < 3; ch++) {
 					Pair2<S> uv = ld2(u + ch * SXS_QT);
-					acc[ch][0].x += t0 * uv.a.x; acc[ch][0].y += t0 * uv.a.y;
-					acc[ch][1].x += t1 * uv.b.x; acc[ch][1].y += t1 * uv.b.y;
-				}
-			} else {
-#pragma unroll
-				for (int ch = 0; ch < 3; ch++) {
-					Pair2<S> uv = ld2(u + ch * SXS_QT);
-					acc[ch][0].x += t0 * uv.a.y; acc[ch][0].y -= t0 * uv.a.x;
-					acc[ch][1].x += t1 * uv.b.y; acc[ch][1].y -= t1 * uv.b.x;
+					ao[ch][0].x += t0 * uv.a.x; ao[ch][0].y += t0 * uv.a.y;
+					ao[ch][1].x += t1 * uv.b.x; ao[ch][1].y += t1 * uv.b.y;
 				}
 			}
 		}
+		bool even = ((l + m) & 1) == 0;   /* class e has l + l1 even */
 		V *o = R + (((size_t)t * ncombo + c) * NP + pr) * 3 * SXS_QT + j2;
 #pragma unroll
-		for (int ch = 0; ch < 3; ch++) st2(o + ch * SXS_QT, acc[ch][0], acc[ch][1]);
+		for (int ch = 0; ch < 3; ch++) {
+			V r[2];
+#pragma unroll
+			for (int k = 0; k < 2; k++) {
+				V a = even ? ae[ch][k] : ao[ch][k], b = even ? ao[ch][k] : ae[ch][k];
+				r[k].x = a.x + b.y;        /* a + (-i) b */
+				r[k].y = a.y - b.x;
+			}
+			st2(o + ch * SXS_QT, r[0], r[1]);
+		}
 	}
 }
 

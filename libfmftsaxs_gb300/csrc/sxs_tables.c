@@ -25,13 +25,27 @@ typedef long double quad_t_;
 #error "no binary128 type known for this host"
 #endif
 
+/* Newton refinement of the double estimate.  The 3j prefactors pass the
+ * double range from L = 32 on (64!^6 ~ 1e530), so a is first brought into
+ * it by an even power of two and the root scaled back by the half power:
+ * both exact, and the steps commute with them, so values inside the double
+ * range are unchanged. */
 static quad_t_ quad_sqrt(quad_t_ a)
 {
 	if (a <= 0) return 0;
+	quad_t_ s = 1;
+	while (a > (quad_t_)0x1p1000) {
+		a *= (quad_t_)0x1p-1000;
+		s *= (quad_t_)0x1p500;
+	}
+	while (a < (quad_t_)0x1p-1000) {
+		a *= (quad_t_)0x1p1000;
+		s *= (quad_t_)0x1p-500;
+	}
 	quad_t_ y = (quad_t_)sqrt((double)a);
 	y = (y + a / y) * (quad_t_)0.5;
 	y = (y + a / y) * (quad_t_)0.5;
-	return y;
+	return y * s;
 }
 
 /* towards zero, the rounding of GMP's mpf_get_d used by the reference */

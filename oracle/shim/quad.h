@@ -18,13 +18,26 @@ typedef long double sxs_quad;
 #error "binary128 type not known for this host"
 #endif
 
+/* Arguments outside the double range (the 3j prefactors from L = 32 on)
+ * are first scaled by an even power of two, exactly, and the root by the
+ * half power, so the double estimate stays finite; inside the double range
+ * the result is unchanged. */
 static inline sxs_quad sxs_quad_sqrt(sxs_quad a)
 {
 	if (a <= 0) return 0;
+	sxs_quad s = 1;
+	while (a > (sxs_quad)0x1p1000) {
+		a *= (sxs_quad)0x1p-1000;
+		s *= (sxs_quad)0x1p500;
+	}
+	while (a < (sxs_quad)0x1p-1000) {
+		a *= (sxs_quad)0x1p1000;
+		s *= (sxs_quad)0x1p-500;
+	}
 	sxs_quad y = (sxs_quad)sqrt((double)a);
 	y = (y + a / y) * (sxs_quad)0.5;
 	y = (y + a / y) * (sxs_quad)0.5;
-	return y;
+	return y * s;
 }
 
 /* Round a quad to double towards zero (the rounding GMP's mpf_get_d uses). */

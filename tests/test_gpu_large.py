@@ -1,8 +1,10 @@
 """The large-expansion configuration (L = 30, q on [0, 0.6]): the widest
-kernels (31 x 31 translation blocks, FP64 rotation with split q tiles)
-against the oracle at Q = 9 (the oracle's cost per (z, beta1, beta2)
-triple grows with Q; L drives the kernels' shapes), and the mixed path
-against the FP64 path at Q = 201 (26 q tiles) on 3,000 poses."""
+kernels (31 x 31 translation blocks) against the oracle at Q = 9 (the
+oracle's cost per (z, beta1, beta2) triple grows with Q; L drives the
+kernels' shapes), and the mixed path against the FP64 path at Q = 201 (26 q
+tiles) on 3,000 poses.  Beyond L = 31 the translation runs the slice kernel
+and the rotation 12 gamma pairs per thread: L = 34 against the oracle at
+Q = 5, L = 40 mixed against FP64."""
 import numpy as np
 import pytest
 
@@ -12,10 +14,9 @@ from test_gpu_parity import TOL, chan_err
 pytestmark = pytest.mark.gpu
 
 
-def _make(oracle, Q, npose):
+def _make(oracle, Q, npose, L=30):
     import libfmftsaxs_gb300 as g
     from libfmftsaxs_gb300 import synth
-    L = 30
     rec = synth.make_molecule(400, 14.0, 31).with_sasa()
     lig = synth.make_molecule(300, 12.0, 32).with_sasa()
     rec = rec.translated(-rec.center_of_extrema())
@@ -52,12 +53,13 @@ def _run(gpu, c, idx, prec):
     return r
 
 
-def test_lmax30_fp64_matches_oracle(gpu, oracle):
+@pytest.mark.parametrize("L,Q", [(30, 9), (34, 5)])
+def test_large_l_fp64_matches_oracle(gpu, oracle, L, Q):
     from libfmftsaxs_gb300 import synth
     from libfmftsaxs_gb300.workload import decode
-    c = _make(oracle, 9, 400)
+    c = _make(oracle, Q, 400, L=L)
     z, b1, b2 = decode(c["index"], c["L"])[:3]
-    key = (z * 31 + b1) * 31 + b2
+    key = (z * (L + 1) + b1) * (L + 1) + b2
     idx = c["index"][key == key[0]][:4].astype(np.int32)   # poses of one triple
     raw, scl, grid, br = oracle.score(c["A"], c["B"], c["q"], c["z"], c["L"], idx, 1, c["peak"], c["a"], c["mult"],
                                       synth.C1_GRID, synth.C2_GRID)
@@ -69,6 +71,15 @@ def test_lmax30_fp64_matches_oracle(gpu, oracle):
 def test_lmax30_mixed_matches_fp64(gpu, case):
     ref = _run(gpu, case, case["index"], gpu.FP64)
     mix = _run(gpu, case, case["index"], gpu.MIXED)
+    assert chan_err(mix["cross"], ref["cross"]) <= CROSS_TOL
+    check_grid(mix, ref["grid"])
+    assert np.max(np.abs(mix["chi"] - ref["chi"]) / ref["chi"]) <= CHI_TOL
+
+
+def test_lmax40_mixed_matches_fp64(gpu, oracle):
+    c = _make(oracle, 51, 1000, L=40)
+    ref = _run(gpu, c, c["index"], gpu.FP64)
+    mix = _run(gpu, c, c["index"], gpu.MIXED)
     assert chan_err(mix["cross"], ref["cross"]) <= CROSS_TOL
     check_grid(mix, ref["grid"])
     assert np.max(np.abs(mix["chi"] - ref["chi"]) / ref["chi"]) <= CHI_TOL

@@ -154,3 +154,46 @@ def test_index_helpers(lib, oracle):
     eu = np.array([12.0, 0.61, 5.9, 6.2, 2.9, 0.05])
     for L in (5, 15, 20):
         assert lib.assemble_index(eu, 3, L) == oracle.assemble_index(eu, 3, L)
+
+
+def _w3j_exact(j1, j2, j3, m1, m2, m3):
+    """3j symbol by the Racah sum in exact rationals, square root in 60-digit
+    decimals."""
+    from decimal import Decimal, getcontext
+    from fractions import Fraction
+    from math import factorial as f
+    getcontext().prec = 60
+    if m1 + m2 + m3:
+        return Decimal(0)
+    t1, t2, t3, t4, t5 = j2 - m1 - j3, j1 + m2 - j3, j1 + j2 - j3, j1 - m1, j2 + m2
+    s = sum(Fraction((-1) ** t, f(t) * f(t - t1) * f(t - t2) * f(t3 - t) * f(t4 - t) * f(t5 - t))
+            for t in range(max(0, t1, t2), min(t3, t4, t5) + 1))
+    pre = Fraction(f(j1 + j2 - j3) * f(j1 - j2 + j3) * f(-j1 + j2 + j3), f(j1 + j2 + j3 + 1)) \
+        * f(j1 + m1) * f(j1 - m1) * f(j2 + m2) * f(j2 - m2) * f(j3 + m3) * f(j3 - m3)
+    v = Decimal(s.numerator) / Decimal(s.denominator) * (Decimal(pre.numerator) / Decimal(pre.denominator)).sqrt()
+    return v if (j1 - j2 - m3) % 2 == 0 else -v
+
+
+def test_dsymb_table_matches_oracle_and_exact_values(lib, oracle):
+    """The d_lm(l1, p) table of src/fftsaxs.c:138-174 (products of 3j symbols,
+    binary128 Racah sums on the host): equal to the restatement bit for bit,
+    and finite and within double rounding of exact 3j values from L = 32 on,
+    where the factorial prefactors (64!^6 ~ 1e530) leave the double range."""
+    from decimal import Decimal
+    f = lib.load().sxs_dsymb_cached
+    f.restype = C.POINTER(C.c_double)
+    f.argtypes = [C.c_int]
+    rng = np.random.default_rng(3)
+    for L in (10, 31, 32, 40):
+        n = (L + 1) ** 3 * (2 * L + 1)
+        tab = np.ctypeslib.as_array(f(L), shape=(n,)).copy()
+        np.testing.assert_array_equal(tab, oracle.dsymb(L))
+        assert np.isfinite(tab).all()
+        for _ in range(12):
+            l, l1 = int(rng.integers(0, L + 1)), int(rng.integers(0, L + 1))
+            p = abs(l - l1) + 2 * int(rng.integers(0, min(l, l1) + 1))
+            m = int(rng.integers(-min(l, l1), min(l, l1) + 1))
+            ex = float(Decimal(2 * p + 1) * Decimal((2 * l1 + 1) * (2 * l + 1)).sqrt()
+                       * _w3j_exact(l, p, l1, 0, 0, 0) * _w3j_exact(l, p, l1, -m, 0, m))
+            got = tab[((l * (l + 1) + m) * (L + 1) + l1) * (2 * L + 1) + p]
+            assert abs(got - ex) <= 2e-15 * abs(ex) + 1e-300, (L, l, m, l1, p, got, ex)
