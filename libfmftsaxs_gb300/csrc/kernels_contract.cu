@@ -361,22 +361,14 @@ __device__ __forceinline__ void ld4(const double *p, double *v)
 	v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
 }
 
-/* Column form of the translation, for L < 32: thread = one column
- * (combo c, channel ch, q) of one m; it holds U[c][pair(m, m+k)][ch][q],
- * k < n = L + 1 - m, in registers (NB = n rounded up to 4, unrolled) and
- * applies the n x n matrix tau^m(q z) staged in shared memory:
- *   R[c][pair(m, m+i)][ch][q] = sum_k tau[i][k] (U[k] or -i U[k] by the
- *   parity of i + k).
- * Block = (tile, slice of <= SXS_SLICE combos sharing z, m) with
- * SXS_QT q x 3 ch x SXS_SLICE combos = 384 threads; tau rows are read as float4/double2 chunks that
- * lanes of the same q share.  One launch per NB covers the m with
- * n in (NB - 4, NB]. */
-/* one output row of the column form: sum_k tau[k] x (U[k] for even i + k,
- * -i U[k] for odd), with the parity of the row i given as PAR */
-template <int PAR, typename S, typename V, int NB>
-__device__ __forceinline__ V tcol_row(const S *row, const V *u)
+/* one output row of the column form for CH channels: sum_k tau[k] x
+ * (U[k] for even i + k, -i U[k] for odd), with the parity of the row i
+ * given as PAR; one tau load serves the CH channels */
+template <int PAR, int CH, typename S, typename V, int NB>
+__device__ __forceinline__ void tcol_row(const S *row, const V (&u)[CH][NB], V (&acc)[CH])
 {
-	V acc = zero2<V>();
+#pragma unroll
+	for (int j = 0; j < CH; j++) acc[j] = zero2<V>();
 #pragma unroll
 	for (int k4 = 0; k4 < NB; k4 += 4) {
 		S tv[4];
@@ -384,20 +376,39 @@ __device__ __forceinline__ V tcol_row(const S *row, const V *u)
 #pragma unroll
 		for (int kk = 0; kk < 4; kk++) {
 			int k = k4 + kk;
-			if ((k & 1) == PAR) {
-				acc.x += tv[kk] * u[k].x;
-				acc.y += tv[kk] * u[k].y;
-			} else {
-				acc.x += tv[kk] * u[k].y;
-				acc.y -= tv[kk] * u[k].x;
+#pragma unroll
+			for (int j = 0; j < CH; j++) {
+				if ((k & 1) == PAR) {
+					acc[j].x += tv[kk] * u[j][k].x;
+					acc[j].y += tv[kk] * u[j][k].y;
+				} else {
+					acc[j].x += tv[kk] * u[j][k].y;
+					acc[j].y -= tv[kk] * u[j][k].x;
+				}
 			}
 		}
 	}
-	return acc;
 }
 
-template <typename S, int NB>
-__global__ void __launch_bounds__(384, sizeof(S) == 4 ? (NB <= 20 ? 3 : 2) : 1)
+/* threads of the column kernel: SXS_SLICE combos x 3/CH channel groups x q */
+#define TCOL_THREADS(CH) (SXS_SLICE * (3 / (CH)) * SXS_QT)
+
+/* Column form of the translation, for L < 32: a thread owns the columns
+ * (combo c, CH channels from ch0, q) of one m; it holds
+ * U[c][pair(m, m+k)][ch][q], k < n = L + 1 - m, in registers (NB = n
+ * rounded up to 4, unrolled) and applies the n x n matrix tau^m(q z) staged
+ * in shared memory:
+ *   R[c][pair(m, m+i)][ch][q] = sum_k tau[i][k] (U[k] or -i U[k] by the
+ *   parity of i + k).
+ * Block = (tile, slice of <= SXS_SLICE combos sharing z, m); tau rows are
+ * padded so the 8 q start on distinct banks and read as float4/double2
+ * chunks that lanes of the same q share.  A 128-bit shared load costs four
+ * wavefronts even as a broadcast, so CH = 3 (one tau load for three
+ * channels) keeps the L1 data pipe below the FMA rate; CH = 1 where three
+ * NB-long columns would not fit the registers.  One launch per NB covers
+ * the m with n in (NB - 4, NB]. */
+template <typename S, int NB, int CH>
+__global__ void __launch_bounds__(TCOL_THREADS(CH), CH == 3 ? 1 : (sizeof(S) == 4 ? (NB <= 20 ? 3 : 2) : 1))
 k_translate_col(const typename Cx<S>::T *__restrict__ U, const S *__restrict__ tau,
                 const int32_t *__restrict__ combo_zbg, const int32_t *__restrict__ slices, int nslice, int cbase,
                 int ncombo, int L, int nzt, int m_lo, int nm, typename Cx<S>::T *__restrict__ R)
@@ -423,22 +434,33 @@ k_translate_col(const typename Cx<S>::T *__restrict__ U, const S *__restrict__ t
 		ts[q * qstride + i * NB + kk] = v;
 	}
 	__syncthreads();
-	int q = threadIdx.x % SXS_QT, ch = (threadIdx.x / SXS_QT) % 3, cl = threadIdx.x / (3 * SXS_QT);
+	int q = threadIdx.x % SXS_QT;
+	int ch0 = CH == 3 ? 0 : (threadIdx.x / SXS_QT) % 3;
+	int cl = threadIdx.x / (SXS_QT * (3 / CH));
 	if (cl >= nc) return;
 	int c = cfirst + cl;
 	int b2 = combo_zbg[3 * c + 1], g2 = combo_zbg[3 * c + 2];
 	int po = psym(m, K);
-	const V *Ub = U + (((size_t)t * nrow + b2 * N + g2) * NP + po) * 3 * SXS_QT + ch * SXS_QT + q;
-	V u[NB];
+	const V *Ub = U + (((size_t)t * nrow + b2 * N + g2) * NP + po) * 3 * SXS_QT + ch0 * SXS_QT + q;
+	V u[CH][NB];
 #pragma unroll
-	for (int k = 0; k < NB; k++) u[k] = k < n ? Ub[(size_t)k * 3 * SXS_QT] : zero2<V>();
+	for (int j = 0; j < CH; j++)
+#pragma unroll
+		for (int k = 0; k < NB; k++) u[j][k] = k < n ? Ub[(size_t)k * 3 * SXS_QT + j * SXS_QT] : zero2<V>();
 	const S *tq = ts + q * qstride;
-	V *Rb = R + (((size_t)t * ncombo + c) * NP + po) * 3 * SXS_QT + ch * SXS_QT + q;
+	V *Rb = R + (((size_t)t * ncombo + c) * NP + po) * 3 * SXS_QT + ch0 * SXS_QT + q;
 	/* rows in even/odd pairs so that the parity of i + k is known at
-	 * compile time: every k is two FMAs */
+	 * compile time: every (k, channel) is two FMAs */
 	for (int i = 0; i < n; i += 2) {
-		Rb[(size_t)i * 3 * SXS_QT] = tcol_row<0, S, V, NB>(tq + i * NB, u);
-		if (i + 1 < n) Rb[(size_t)(i + 1) * 3 * SXS_QT] = tcol_row<1, S, V, NB>(tq + (i + 1) * NB, u);
+		V a[CH];
+		tcol_row<0, CH, S, V, NB>(tq + i * NB, u, a);
+#pragma unroll
+		for (int j = 0; j < CH; j++) Rb[(size_t)i * 3 * SXS_QT + j * SXS_QT] = a[j];
+		if (i + 1 < n) {
+			tcol_row<1, CH, S, V, NB>(tq + (i + 1) * NB, u, a);
+#pragma unroll
+			for (int j = 0; j < CH; j++) Rb[(size_t)(i + 1) * 3 * SXS_QT + j * SXS_QT] = a[j];
+		}
 	}
 }
 
@@ -807,13 +829,15 @@ static cudaError_t translate_col_launch(const void *U, const void *tau, const in
 	long nb = (long)NT * nslice * nm;
 	if (nb > 0x7fffffffL) return cudaErrorInvalidValue;
 	size_t smem = sizeof(S) * SXS_QT * (NB * NB + 4);
+	/* three channels per thread where their columns fit the registers */
+	const int CH = (sizeof(S) == 4 && NB <= 20) ? 3 : 1;
+	auto kern = k_translate_col<S, NB, CH>;
 	if (smem > 48 * 1024) {
-		cudaError_t e = cudaFuncSetAttribute(k_translate_col<S, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                                     (int)smem);
+		cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 		if (e != cudaSuccess) return e;
 	}
-	k_translate_col<S, NB><<<(unsigned)nb, 384, smem, s>>>((const V *)U, (const S *)tau, combo_zbg, slices, nslice,
-	                                                        cbase, ncombo, L, nzt, m_lo, nm, (V *)R);
+	kern<<<(unsigned)nb, TCOL_THREADS(CH), smem, s>>>((const V *)U, (const S *)tau, combo_zbg, slices, nslice, cbase,
+	                                                  ncombo, L, nzt, m_lo, nm, (V *)R);
 	return cudaGetLastError();
 }
 
