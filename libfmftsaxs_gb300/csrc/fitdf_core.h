@@ -99,17 +99,19 @@ DF_HD dfl lz_norm(dfl a) { return df_fast_two_sum(a.hi, a.lo); }
 /* y*x + c, unnormalised */
 DF_HD dfl lz_fma(dfl y, dfl x, dfl c) { return lz_add(lz_mul(y, x), c); }
 
-/* compensated float sum: s + c tracks the exact sum of the added floats */
+/* Kahan-compensated float sum: s - c is the sum of the added floats to
+ * within 2u sum |x| (u = 2^-24), c holding the part lost from s */
 typedef struct {
 	float s, c;
 } fsum;
 DF_HD void fs_add(fsum *a, float x)
 {
-	dfl t = df_two_sum(a->s, x);
-	a->s = t.hi;
-	a->c += t.lo;
+	float y = x - a->c;
+	float t = a->s + y;
+	a->c = (t - a->s) - y;
+	a->s = t;
 }
-DF_HD dfl fs_df(fsum a) { return df_fast_two_sum(a.s, a.c); }
+DF_HD dfl fs_df(fsum a) { return df_two_sum(a.s, -a.c); }
 
 /* Per-pose work of one run of n consecutive q.  Channel rows start at c
  * with row stride ld: VV VD VW DD DW WW F3G P4 (model normalised); c[-1] of
