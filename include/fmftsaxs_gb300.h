@@ -375,6 +375,17 @@ int64_t sxsg_assemble_index(const double *euler6, int z_idx, int L);
 int64_t sxsg_poses_to_indices(const double *rot, const double *tr, int64_t n, const double *ref_lig,
                               const double *zvals, int znum, int L, int64_t *index, uint8_t *keep);
 
+/* Options of the _ex forms.  SXSG_WRAP_ANGLES: the alpha/gamma grid digits
+ * are taken mod N.  The reference rounds them without wrapping
+ * (tools/correlate.c:233-240), so an angle within half a step of 2 pi
+ * (alpha2' = 2 pi - alpha2 for alpha2 < pi/N, about 1/N of random poses)
+ * gets digit N, which carries into the next digit of the packed index and
+ * scores a different cell; the plain forms keep that for bit-exact parity. */
+enum { SXSG_WRAP_ANGLES = 1 };
+int64_t sxsg_assemble_index_ex(const double *euler6, int z_idx, int L, int flags);
+int64_t sxsg_poses_to_indices_ex(const double *rot, const double *tr, int64_t n, const double *ref_lig,
+                                 const double *zvals, int znum, int L, int64_t *index, uint8_t *keep, int flags);
+
 /* Timing on the library's stream: start records an event; stop records a
  * second one, waits for it and returns the elapsed milliseconds. */
 int sxsg_timer_start(void);

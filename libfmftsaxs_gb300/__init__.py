@@ -357,9 +357,13 @@ def profile_from_spf(spf, L, qvals, rm, c1, c2):
     return i, e
 
 
-def poses_to_indices(rot, tr, zvals, L, ref_lig=(0.0, 0.0, 0.0)):
+WRAP_ANGLES = 1
+
+
+def poses_to_indices(rot, tr, zvals, L, ref_lig=(0.0, 0.0, 0.0), wrap=False):
     """Batch pose ingestion (ft2euler, 3-decimal round trip, index assembly).
-    Returns (index[int64] of kept poses, keep mask)."""
+    Returns (index[int64] of kept poses, keep mask).  wrap=True takes the
+    alpha/gamma digits mod N (the reference does not wrap them)."""
     rot = f64(rot).reshape(-1, 9)
     tr = f64(tr).reshape(-1, 3)
     n = len(rot)
@@ -367,8 +371,9 @@ def poses_to_indices(rot, tr, zvals, L, ref_lig=(0.0, 0.0, 0.0)):
     keep = np.zeros(n, dtype=np.uint8)
     ref = f64(ref_lig)
     z = f64(zvals)
-    k = load().sxsg_poses_to_indices(_p(rot), _p(tr), C.c_int64(n), _p(ref), _p(z), C.c_int(len(z)), C.c_int(L),
-                                     idx.ctypes.data_as(C.POINTER(C.c_int64)), keep.ctypes.data_as(C.POINTER(C.c_uint8)))
+    k = load().sxsg_poses_to_indices_ex(_p(rot), _p(tr), C.c_int64(n), _p(ref), _p(z), C.c_int(len(z)), C.c_int(L),
+                                        idx.ctypes.data_as(C.POINTER(C.c_int64)),
+                                        keep.ctypes.data_as(C.POINTER(C.c_uint8)), C.c_int(WRAP_ANGLES if wrap else 0))
     if k < 0:
         raise SxsError(last_error())
     return idx[keep.astype(bool)], keep.astype(bool)

@@ -647,20 +647,28 @@ void sxs_ft2euler(struct sxs_euler *eu, struct mol_vector3 *tv, struct mol_matri
 /* correlate's grid index of one Euler line (tools/correlate.c:222-240):
  * alpha_lig and gamma_lig are flipped to 2 pi - angle, every angle is
  * rounded to its grid step, with no wrap-around. */
-int64_t sxsg_assemble_index(const double *eu, int z_idx, int L)
+int64_t sxsg_assemble_index_ex(const double *eu, int z_idx, int L, int flags)
 {
 	int nb = L + 1, N = 2 * L + 1;
 	double a2 = 2 * SXS_PI - eu[3];
 	double g2 = 2 * SXS_PI - eu[5];
 	double bs = SXS_PI / L, as = 2.0 * SXS_PI / (2 * L + 1);
+	int da = (int)round(a2 / as), dg1 = (int)round(eu[2] / as), dg2 = (int)round(g2 / as);
+	if (flags & SXSG_WRAP_ANGLES) {
+		da = ((da % N) + N) % N;
+		dg1 = ((dg1 % N) + N) % N;
+		dg2 = ((dg2 % N) + N) % N;
+	}
 	int64_t id = (int64_t)z_idx * nb;
 	id = (id + (int)round(eu[1] / bs)) * nb;
 	id = (id + (int)round(eu[4] / bs)) * N;
-	id = (id + (int)round(a2 / as)) * N;
-	id = (id + (int)round(eu[2] / as)) * N;
-	id = id + (int)round(g2 / as);
+	id = (id + da) * N;
+	id = (id + dg1) * N;
+	id = id + dg2;
 	return id;
 }
+
+int64_t sxsg_assemble_index(const double *eu, int z_idx, int L) { return sxsg_assemble_index_ex(eu, z_idx, L, 0); }
 
 double sxs_sbessel(int order, double x) { return sxs_sbessel_host(order, x); }
 
@@ -789,6 +797,12 @@ void sxs_compute_saxs_scores(double *scores, double *c1, double *c2, int *index_
 int64_t sxsg_poses_to_indices(const double *rot, const double *tr, int64_t n, const double *ref, const double *zvals,
                               int znum, int L, int64_t *index, uint8_t *keep)
 {
+	return sxsg_poses_to_indices_ex(rot, tr, n, ref, zvals, znum, L, index, keep, 0);
+}
+
+int64_t sxsg_poses_to_indices_ex(const double *rot, const double *tr, int64_t n, const double *ref,
+                                 const double *zvals, int znum, int L, int64_t *index, uint8_t *keep, int flags)
+{
 	if (n < 0 || (n > 0 && (!rot || !tr || !ref || !zvals || !index || !keep)) || L < 1)
 		return sxs_fail(-2, "sxsg_poses_to_indices: bad arguments");
 	int64_t kept = 0;
@@ -813,7 +827,7 @@ int64_t sxsg_poses_to_indices(const double *rot, const double *tr, int64_t n, co
 			continue;
 		}
 		keep[i] = 1;
-		index[i] = sxsg_assemble_index(v, zi, L);
+		index[i] = sxsg_assemble_index_ex(v, zi, L, flags);
 		kept++;
 	}
 	return kept;

@@ -212,7 +212,6 @@ struct sxsg_plan {
 	double *d_bes;
 	double *d_tau;              /* [nzt][K][K][K][Q] */
 	float *d_tauf;              /* float copy (mixed path) */
-	size_t pose_cap, combo_cap, zt_cap;
 	/* per-chunk translated table */
 	void *d_R;
 	int64_t R_combos;
@@ -249,7 +248,6 @@ static void plan_free_poses(sxsg_plan *p)
 	pfree(p, p->d_tauf);
 	p->h_combo = NULL; p->h_cstart = NULL; p->h_zt = NULL;
 	p->d_poses = NULL; p->d_combo = NULL; p->d_zt = NULL; p->d_bes = NULL; p->d_tau = NULL; p->d_tauf = NULL;
-	p->pose_cap = p->combo_cap = p->zt_cap = 0;
 }
 
 void sxsg_plan_destroy(sxsg_plan *p)
@@ -619,18 +617,17 @@ static int plan_tables(sxsg_plan *p)
 	return 0;
 }
 
-/* grid fit of slots [slot0, slot0 + nslot) of order (all poses in list
- * order when order is NULL) in the plan's precision: FP64 on the plain path,
- * double-float on the FP32 pipe on the mixed path (whose cross terms are
- * double-float pairs) */
-static int plan_fit_grid(sxsg_plan *p, const sxsk_pose *order, int slot0, int nslot, int max_blocks, double *chi,
-                         double *c1, double *c2, int32_t *cell, double *grid, cudaStream_t st)
+/* grid fit of all n poses (list order) in the plan's precision: FP64 on
+ * the plain path, double-float on the FP32 pipe on the mixed path (whose
+ * cross terms are double-float pairs); one block per group of poses */
+static int plan_fit_grid(sxsg_plan *p, int n, double *chi, double *c1, double *c2, int32_t *cell, double *grid,
+                         cudaStream_t st)
 {
 	if (p->fp32)
-		return sxsk_fit_grid_df((const float2 *)p->d_cross, order, slot0, nslot, p->Q, p->d_fc, p->a0sum, p->peak,
-		                        p->d_gdf, p->d_c1g, p->n1, p->d_c2g, p->n2, max_blocks, chi, c1, c2, cell, grid, st);
-	return sxsk_fit_grid(p->d_cross, order, slot0, nslot, p->Q, p->d_fc, p->a0sum, p->peak, p->d_gtab, p->d_c1g,
-	                     p->n1, p->d_c2g, p->n2, max_blocks, chi, c1, c2, cell, grid, st);
+		return sxsk_fit_grid_df((const float2 *)p->d_cross, NULL, 0, n, p->Q, p->d_fc, p->a0sum, p->peak, p->d_gdf,
+		                        p->d_c1g, p->n1, p->d_c2g, p->n2, 0, chi, c1, c2, cell, grid, st);
+	return sxsk_fit_grid(p->d_cross, NULL, 0, n, p->Q, p->d_fc, p->a0sum, p->peak, p->d_gtab, p->d_c1g, p->n1,
+	                     p->d_c2g, p->n2, 0, chi, c1, c2, cell, grid, st);
 }
 
 static int plan_events(sxsg_plan *p, int need)
@@ -694,7 +691,7 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 	SXS_CU(cudaEventRecord(p->ev[5], s));
 	int n = (int)p->npose;
 	if (fit_mode == SXSG_FIT_GRID) {
-		SXS_K(plan_fit_grid(p, NULL, 0, n, 0, p->d_chi, p->d_c1, p->d_c2, p->d_cell, NULL, s));
+		SXS_K(plan_fit_grid(p, n, p->d_chi, p->d_c1, p->d_c2, p->d_cell, NULL, s));
 		sxs_count_launches(n > 0 ? 1 : 0);
 	} else if (fit_mode == SXSG_FIT_LBFGSB) {
 		SXS_K(sxs_fit_lbfgsb_launch(p->d_cross, p->fp32, p->d_scaled, n, Q, p->d_q, p->d_a, p->mult, p->peak, 1, p->d_chi,
@@ -763,7 +760,7 @@ int sxsg_plan_results(sxsg_plan *p, double *chi, double *c1, double *c2, int32_t
 		if (!e) e = cudaMallocAsync((void **)&t2, sizeof(double) * n, p->s);
 		if (!e) e = cudaMallocAsync((void **)&tcell, sizeof(int32_t) * n, p->s);
 		if (!e) {
-			e = (cudaError_t)plan_fit_grid(p, NULL, 0, (int)n, 0, tc, t1, t2, tcell, d_g, s);
+			e = (cudaError_t)plan_fit_grid(p, (int)n, tc, t1, t2, tcell, d_g, s);
 			sxs_count_launches(1);
 		}
 		if (!e) e = cudaMemcpyAsync(grid, d_g, sizeof(double) * gn, cudaMemcpyDeviceToHost, s);

@@ -197,3 +197,27 @@ def test_dsymb_table_matches_oracle_and_exact_values(lib, oracle):
                        * _w3j_exact(l, p, l1, 0, 0, 0) * _w3j_exact(l, p, l1, -m, 0, m))
             got = tab[((l * (l + 1) + m) * (L + 1) + l1) * (2 * L + 1) + p]
             assert abs(got - ex) <= 2e-15 * abs(ex) + 1e-300, (L, l, m, l1, p, got, ex)
+
+
+def test_pose_ingestion_wrap_option(lib):
+    """SXSG_WRAP_ANGLES (opt-in) takes the alpha/gamma digits mod N; the
+    default keeps the reference's unwrapped rounding, whose digit N carries
+    into the next digit of the packed index."""
+    from libfmftsaxs_gb300 import synth
+    from libfmftsaxs_gb300.workload import decode
+    rng = np.random.default_rng(12)
+    R = synth.random_rotations(20000, rng)
+    T = synth.random_translations(20000, 9.5, 30.5, rng)
+    z = np.arange(10.0, 31.0)
+    L, N = 10, 21
+    raw, keep = lib.poses_to_indices(R, T, z, L)
+    wrapped, keep_w = lib.poses_to_indices(R, T, z, L, wrap=True)
+    np.testing.assert_array_equal(keep, keep_w)
+    diff = raw != wrapped
+    assert 0.01 < diff.mean() < 0.2         # alpha2 within half a step of 0 (and the like)
+    for col in decode(wrapped, L)[3:]:
+        assert col.min() >= 0 and col.max() < N
+    # an unwrapped digit N carried into the next digit: raw - wrapped is a
+    # sum of N (gamma2), N^2 (gamma1) and N^3 (alpha2)
+    d = raw[diff] - wrapped[diff]
+    assert np.all(d > 0) and np.all(d % N == 0)
