@@ -39,6 +39,8 @@ __device__ __forceinline__ void cfma(double2 &acc, double2 a, double2 b)
 	acc.y = fma(a.x, b.y, acc.y);
 	acc.y = fma(a.y, b.x, acc.y);
 }
+__device__ __forceinline__ float fma_s(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fma_s(double a, double b, double c) { return fma(a, b, c); }
 template <typename V> __device__ __forceinline__ V zero2() { V v; v.x = 0; v.y = 0; return v; }
 template <typename V> __device__ __forceinline__ V from2(double2 a) { V v; v.x = a.x; v.y = a.y; return v; }
 
@@ -93,18 +95,26 @@ __device__ __forceinline__ uint64_t l2_policy(bool keep)
 	else asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
 	return pol;
 }
+/* 16-byte load at p + OFF bytes with an L2 policy; the offset is an
+ * immediate of the instruction, so loads off one base need no address
+ * arithmetic of their own */
+template <int OFF>
 __device__ __forceinline__ Pair2<float> ld2_pol(const float2 *p, uint64_t pol)
 {
 	float4 v;
-	asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+	asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4+%6], %5;"
 	    : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
-	    : "l"(p), "l"(pol));
+	    : "l"(p), "l"(pol), "n"(OFF));
 	Pair2<float> r;
 	r.a = make_float2(v.x, v.y);
 	r.b = make_float2(v.z, v.w);
 	return r;
 }
-__device__ __forceinline__ Pair2<double> ld2_pol(const double2 *p, uint64_t) { return ld2(p); }
+template <int OFF>
+__device__ __forceinline__ Pair2<double> ld2_pol(const double2 *p, uint64_t)
+{
+	return ld2(reinterpret_cast<const double2 *>(reinterpret_cast<const char *>(p) + OFF));
+}
 __device__ __forceinline__ void st2(float2 *p, float2 a, float2 b)
 {
 	*reinterpret_cast<float4 *>(p) = make_float4(a.x, a.y, b.x, b.y);
@@ -543,12 +553,17 @@ k_pose_cross(const sxsk_pose *__restrict__ poses, int npose, int combo_base, int
 		const V *pp = Pr + (size_t)p * 3 * SXS_QT;
 		const V *rr = Rr + (size_t)p * 3 * SXS_QT;
 		Pair2<S> cp[3], cr[3];
+		if (HINT) {
+			constexpr int CB = SXS_QT * (int)sizeof(V);   /* bytes between channels */
+			cp[0] = ld2_pol<0>(pp, polP);
+			cp[1] = ld2_pol<CB>(pp, polP);
+			cp[2] = ld2_pol<2 * CB>(pp, polP);
+			cr[0] = ld2_pol<0>(rr, polR);
+			cr[1] = ld2_pol<CB>(rr, polR);
+			cr[2] = ld2_pol<2 * CB>(rr, polR);
+		} else {
 #pragma unroll
-		for (int c = 0; c < 3; c++) {
-			if (HINT) {
-				cp[c] = ld2_pol(pp + c * SXS_QT, polP);
-				cr[c] = ld2_pol(rr + c * SXS_QT, polR);
-			} else {
+			for (int c = 0; c < 3; c++) {
 				cp[c] = ld2(pp + c * SXS_QT);
 				cr[c] = ld2(rr + c * SXS_QT);
 			}
@@ -562,12 +577,30 @@ k_pose_cross(const sxsk_pose *__restrict__ poses, int npose, int combo_base, int
 			s0.x = wx * r0.x - wy * r0.y; s0.y = wx * r0.y + wy * r0.x;
 			s1.x = wx * r1.x - wy * r1.y; s1.y = wx * r1.y + wy * r1.x;
 			s2.x = wx * r2.x - wy * r2.y; s2.y = wx * r2.y + wy * r2.x;
-			f[k][0] += a0.x * s0.x - a0.y * s0.y;
-			f[k][1] += a0.x * s1.x - a0.y * s1.y + a1.x * s0.x - a1.y * s0.y;
-			f[k][2] += a0.x * s2.x - a0.y * s2.y + a2.x * s0.x - a2.y * s0.y;
-			f[k][3] += a1.x * s1.x - a1.y * s1.y;
-			f[k][4] += a1.x * s2.x - a1.y * s2.y + a2.x * s1.x - a2.y * s1.y;
-			f[k][5] += a2.x * s2.x - a2.y * s2.y;
+			S *F = f[k];
+			if (sizeof(S) == 8) {
+				/* FP64 (bound by the FP64 pipe): the Re(a s) terms as FMA
+				 * chains straight into the accumulators, 18 operations per q
+				 * instead of 24 for sums of products added to F */
+				F[0] = fma_s(a0.x, s0.x, F[0]); F[0] = fma_s(-a0.y, s0.y, F[0]);
+				F[1] = fma_s(a0.x, s1.x, F[1]); F[1] = fma_s(-a0.y, s1.y, F[1]);
+				F[1] = fma_s(a1.x, s0.x, F[1]); F[1] = fma_s(-a1.y, s0.y, F[1]);
+				F[2] = fma_s(a0.x, s2.x, F[2]); F[2] = fma_s(-a0.y, s2.y, F[2]);
+				F[2] = fma_s(a2.x, s0.x, F[2]); F[2] = fma_s(-a2.y, s0.y, F[2]);
+				F[3] = fma_s(a1.x, s1.x, F[3]); F[3] = fma_s(-a1.y, s1.y, F[3]);
+				F[4] = fma_s(a1.x, s2.x, F[4]); F[4] = fma_s(-a1.y, s2.y, F[4]);
+				F[4] = fma_s(a2.x, s1.x, F[4]); F[4] = fma_s(-a2.y, s1.y, F[4]);
+				F[5] = fma_s(a2.x, s2.x, F[5]); F[5] = fma_s(-a2.y, s2.y, F[5]);
+			} else {
+				/* FP32 (bound by the L1 data path): sums of products, whose
+				 * short dependence on F keeps more loads in flight */
+				F[0] += a0.x * s0.x - a0.y * s0.y;
+				F[1] += a0.x * s1.x - a0.y * s1.y + a1.x * s0.x - a1.y * s0.y;
+				F[2] += a0.x * s2.x - a0.y * s2.y + a2.x * s0.x - a2.y * s0.y;
+				F[3] += a1.x * s1.x - a1.y * s1.y;
+				F[4] += a1.x * s2.x - a1.y * s2.y + a2.x * s1.x - a2.y * s1.y;
+				F[5] += a2.x * s2.x - a2.y * s2.y;
+			}
 		}
 	}
 	typename CrossT<S>::T *o = cross + (size_t)ps.src * 6 * Q;
