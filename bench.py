@@ -340,7 +340,7 @@ def run_ours(args):
     tkey = (args.config, head)
     traffic = TRAFFIC_PER_POSE[tkey] * n / nchunks if tkey in TRAFFIC_PER_POSE else None
     out = {
-        "metric": "poses/s @lmax=20 (%s GPU path, grid fit)" % ("mixed-precision" if head == "mixed" else "FP64 plain"),
+        "metric": "poses/s @lmax=%d (%s GPU path, grid fit)" % (w.L, "mixed-precision" if head == "mixed" else "FP64 plain"),
         "value": value,
         "unit": "poses/s",
         "n_gpus": 1,
@@ -411,8 +411,8 @@ def run_reference(args):
         rates.append(r); ns.append(n); walls.append(wall)
     value = sum(ns) / sum(walls)
     out = {"impl": "reference",
-           "metric": "poses/s @lmax=20 (%s GPU path, grid fit)"
-                     % ("mixed-precision" if args.precision == "mixed" else "FP64 plain"),
+           "metric": "poses/s @lmax=%d (%s GPU path, grid fit)"
+                     % (w.L, "mixed-precision" if args.precision == "mixed" else "FP64 plain"),
            "value": value, "unit": "poses/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": 1e3 * float(np.mean(walls)), "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random-walk dimers, poses and noisy experiment)",
