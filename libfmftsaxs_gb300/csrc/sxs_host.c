@@ -219,7 +219,7 @@ struct sxsg_plan {
 	/* outputs */
 	/* cross terms [npose][6][Q]: double on the FP64 path, double-float
 	 * pairs {hi, lo} (same size) on the mixed path; d_scaled is the
-	 * L-BFGS-B fit's rescaled, transposed copy */
+	 * L-BFGS-B fit's rescaled, transposed copy, allocated on its first use */
 	double *d_cross, *d_chi, *d_c1, *d_c2, *d_grid, *d_scaled, *d_scale;
 	int32_t *d_cell;
 	int *d_iters;
@@ -568,7 +568,6 @@ int sxsg_plan_set_poses(sxsg_plan *p, const int64_t *index, int64_t n, int skip)
 	if (!e) e = cudaMallocAsync((void **)&p->d_cell, sizeof(int32_t) * nn, p->s);
 	if (!e) e = cudaMallocAsync((void **)&p->d_scale, sizeof(double) * nn, p->s);
 	if (!e) e = cudaMallocAsync((void **)&p->d_iters, sizeof(int) * nn, p->s);
-	if (!e) e = cudaMallocAsync((void **)&p->d_scaled, sizeof(double) * nn * 6 * p->Q, p->s);
 	if (e) return sxs_cuda_fail(e, "sxsg_plan_set_poses outputs");
 	(void)L;
 	return 0;
@@ -694,6 +693,8 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 		SXS_K(plan_fit_grid(p, n, p->d_chi, p->d_c1, p->d_c2, p->d_cell, NULL, s));
 		sxs_count_launches(n > 0 ? 1 : 0);
 	} else if (fit_mode == SXSG_FIT_LBFGSB) {
+		if (!p->d_scaled && n > 0)
+			SXS_CU(cudaMallocAsync((void **)&p->d_scaled, sizeof(double) * (size_t)n * 6 * Q, s));
 		SXS_K(sxs_fit_lbfgsb_launch(p->d_cross, p->fp32, p->d_scaled, n, Q, p->d_q, p->d_a, p->mult, p->peak, 1, p->d_chi,
 		                            p->d_c1, p->d_c2, p->d_scale, p->d_iters, s));
 		sxs_count_launches(n > 0 ? 2 : 0);
@@ -815,7 +816,7 @@ size_t sxs_plan_table_bytes(int L, int Q, int precision)
 
 /* Device bytes of a plan besides its rotation tables and translated-table
  * chunk: molecules, per-z tables for nzt touched z, pose lists and outputs. */
-size_t sxs_plan_base_bytes(int L, int Q, int nzt, int64_t npose, int n1, int precision)
+size_t sxs_plan_base_bytes(int L, int Q, int nzt, int64_t npose, int n1, int precision, int fit_mode)
 {
 	size_t K = L + 1, N = 2 * L + 1, NT = (Q + SXS_QT - 1) / SXS_QT, K2 = K * K;
 	size_t celem = precision == SXSG_MIXED ? 8 : 16;
@@ -823,7 +824,8 @@ size_t sxs_plan_base_bytes(int L, int Q, int nzt, int64_t npose, int n1, int pre
 	size_t b = spf * (16 * 2 + celem * 2);                       /* A, B, At, Bt */
 	b += (size_t)nzt * Q * N * 8;                                /* Bessel */
 	b += NT * nzt * K * K * K * SXS_QT * (precision == SXSG_MIXED ? 12 : 8); /* tau */
-	b += (size_t)npose * (sizeof(sxsk_pose) + 12 * Q * 8 + 40);  /* poses, cross, scaled, outputs */
+	b += (size_t)npose * (sizeof(sxsk_pose) + 6 * Q * 8 + 40);   /* poses, cross, outputs */
+	if (fit_mode == SXSG_FIT_LBFGSB) b += (size_t)npose * 6 * Q * 8; /* its rescaled copy */
 	b += (size_t)n1 * Q * 16 + (size_t)64 * Q + (1 << 20);
 	return b;
 }

@@ -71,7 +71,7 @@ int sxs_plan_create_on(sxsg_plan **out, const double *A, const double *B, const 
                        const double *c2g, int n2, int precision, cudaStream_t stream, int ext_tables);
 void sxs_plan_set_tables(sxsg_plan *p, void *P, int P_valid, void *U, int U_valid);
 size_t sxs_plan_table_bytes(int L, int Q, int precision);
-size_t sxs_plan_base_bytes(int L, int Q, int nzt, int64_t npose, int n1, int precision);
+size_t sxs_plan_base_bytes(int L, int Q, int nzt, int64_t npose, int n1, int precision, int fit_mode);
 size_t sxs_plan_combo_bytes(int L, int Q, int precision);
 
 /* per-q constants of the grid fit: fc[Q][5] */

@@ -363,7 +363,7 @@ int64_t sxsg_server_submit(sxsg_server *s, const sxsg_request *r)
 	if (j->rbudget < sxs_plan_combo_bytes(L, Q, r->precision) * 16)
 		j->rbudget = sxs_plan_combo_bytes(L, Q, r->precision) * 16;
 	j->tbytes = sxs_plan_table_bytes(L, Q, r->precision);
-	j->bytes = sxs_plan_base_bytes(L, Q, nzt, r->n, r->n1, r->precision) + j->rbudget;
+	j->bytes = sxs_plan_base_bytes(L, Q, nzt, r->n, r->n1, r->precision, r->fit_mode) + j->rbudget;
 	j->t_submit = now_ms();
 	pthread_mutex_lock(&s->mu);
 	if (s->stop) {
