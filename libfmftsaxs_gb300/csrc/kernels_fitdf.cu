@@ -36,7 +36,7 @@ namespace {
  * and every thread advances the running sums of its (pose, c1) over the
  * chunk.  After the last chunk a thread has the polynomial coefficients of
  * its row and scans the c2 cells. */
-__global__ void __launch_bounds__(FITD_THREADS)
+__global__ void __launch_bounds__(FITD_THREADS, 5)
 k_fit_grid_df(const float2 *__restrict__ cross, const sxsk_pose *__restrict__ order, int slot0, int nslot, int Q,
               const double *__restrict__ fc, double a0sum, double peak, const float2 *__restrict__ gdf,
               const double *__restrict__ c1g, int n1, const double *__restrict__ c2g, int n2, int tp, int ppb,
