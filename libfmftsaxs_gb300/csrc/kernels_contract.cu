@@ -177,7 +177,8 @@ __device__ __forceinline__ void rot_out(double2 y0, double2 A, double2 B, double
 }
 
 #define ROT_GROUPS 4
-#define ROT_THREADS (ROT_GROUPS * 3 * SXS_QT)
+/* threads of a rotation block: ROT_GROUPS gamma groups x 3/CH channel groups x q */
+#define ROT_THREADS(CH) (ROT_GROUPS * (3 / (CH)) * SXS_QT)
 
 /* Rotation tables in the q-tiled layout:
  *   out[t][b*N+g][pair(m,l)][ch][q] = sum_{m1=-l..l} tw[(m1' g) mod N] d^l_{m m1}(beta_b) C[ch][l,m1][q]
@@ -188,11 +189,12 @@ __device__ __forceinline__ void rot_out(double2 y0, double2 A, double2 B, double
  * so each (m1 > 0, gamma pair) costs one S and one D product.
  * Block = (m, beta b, q tile t), blocks ordered m fastest so that the blocks
  * of one tile read the same coefficients from L1/L2; thread = (group of G
- * gamma pairs, channel, q): the thread forms S and D once per m1 and
- * accumulates its G gamma pairs in registers.  The padding q >= Q is written
- * as zeros. */
-template <typename S, int G>
-__global__ void __launch_bounds__(ROT_THREADS)
+ * gamma pairs, CH channels, q): the thread forms S and D once per m1 and
+ * channel and accumulates its G gamma pairs in registers; with CH = 3 one
+ * twiddle load and index step serve the three channels.  The padding
+ * q >= Q is written as zeros. */
+template <typename S, int G, int CH>
+__global__ void __launch_bounds__(ROT_THREADS(CH))
 k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const S *__restrict__ dtab, const double2 *__restrict__ tw,
          int Q, int L, int conj, typename Cx<S>::T *__restrict__ out)
 {
@@ -208,48 +210,62 @@ k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const S *__restrict__ dtab
 	int ne = N + (G - 1) * L;
 	for (int k = threadIdx.x; k < ne; k += blockDim.x) hs[k] = rot_tw<S>(tw, k, N);
 	__syncthreads();
-	int qq = threadIdx.x % SXS_QT, ch = (threadIdx.x / SXS_QT) % 3, gg = threadIdx.x / (3 * SXS_QT);
+	int qq = threadIdx.x % SXS_QT;
+	int ch0 = CH == 3 ? 0 : (threadIdx.x / SXS_QT) % 3;
+	int gg = threadIdx.x / ((3 / CH) * SXS_QT);
 	int q = t * SXS_QT + qq;
 	bool qok = q < Q;
 	int g0 = gg * G;
 	if (g0 > L) return;
 	S sg = conj ? (S)-1 : (S)1;
-	const V *C = spf_t + (size_t)ch * K2 * Q + (qok ? q : 0);
+	const V *C = spf_t + (size_t)ch0 * K2 * Q + (qok ? q : 0);
 	const S *db = dtab + ((size_t)b * K * N + m + L) * N + L;   /* d^l_{m m1}(beta_b) at l = 0, m1 = 0 */
-	V *ob = out + (((size_t)t * nrow + (size_t)b * N) * NP + psym(m, K)) * 3 * SXS_QT + ch * SXS_QT + qq;
+	V *ob = out + (((size_t)t * nrow + (size_t)b * N) * NP + psym(m, K)) * 3 * SXS_QT + ch0 * SXS_QT + qq;
 	size_t gstride = (size_t)NP * 3 * SXS_QT;
+	size_t cstride = (size_t)K2 * Q;                     /* between channels of C */
 	for (int l = m; l <= L; l++) {
 		const S *dl = db + (size_t)l * N * N;
 		const V *Cl = C + (size_t)l * (l + 1) * Q;    /* lm of m1 = 0 */
-		V c0 = zero2<V>();
-		if (qok) c0 = Cl[0];
 		S d0 = dl[0];
-		V y0;
-		y0.x = d0 * c0.x;
-		y0.y = d0 * c0.y * sg;
-		V A[G], B[G];
+		V y0[CH];
 #pragma unroll
-		for (int j = 0; j < G; j++) A[j] = B[j] = zero2<V>();
+		for (int c = 0; c < CH; c++) {
+			V c0 = zero2<V>();
+			if (qok) c0 = Cl[c * cstride];
+			y0[c].x = d0 * c0.x;
+			y0[c].y = d0 * c0.y * sg;
+		}
+		V A[G][CH], B[G][CH];
+#pragma unroll
+		for (int j = 0; j < G; j++)
+#pragma unroll
+			for (int c = 0; c < CH; c++) A[j][c] = B[j][c] = zero2<V>();
 		int base = 0;                                  /* m1 g0 mod N */
 		for (int m1 = 1; m1 <= l; m1++) {
 			base += g0;
 			if (base >= N) base -= N;
-			V cp = zero2<V>(), cm = zero2<V>();
-			if (qok) {
-				cp = Cl[(size_t)m1 * Q];
-				cm = Cl[-(ptrdiff_t)m1 * Q];
-			}
 			S dp = dl[m1], dm = dl[-m1];
-			V yp, Sv, Dv;
-			yp.x = dp * cp.x;
-			yp.y = dp * cp.y * sg;
-			S mx = dm * cm.x, my = dm * cm.y * sg;
-			Sv.x = yp.x + mx; Sv.y = yp.y + my;
-			Dv.x = yp.x - mx; Dv.y = yp.y - my;
+			V Sv[CH], Dv[CH];
+#pragma unroll
+			for (int c = 0; c < CH; c++) {
+				V cp = zero2<V>(), cm = zero2<V>();
+				if (qok) {
+					cp = Cl[c * cstride + (size_t)m1 * Q];
+					cm = Cl[c * cstride - (ptrdiff_t)m1 * Q];
+				}
+				V yp;
+				yp.x = dp * cp.x;
+				yp.y = dp * cp.y * sg;
+				S mx = dm * cm.x, my = dm * cm.y * sg;
+				Sv[c].x = yp.x + mx; Sv[c].y = yp.y + my;
+				Dv[c].x = yp.x - mx; Dv[c].y = yp.y - my;
+			}
 			int k = base;
 #pragma unroll
 			for (int j = 0; j < G; j++) {
-				rot_acc(A[j], B[j], hs[k], Sv, Dv);
+				RotTw<S> h = hs[k];
+#pragma unroll
+				for (int c = 0; c < CH; c++) rot_acc(A[j][c], B[j][c], h, Sv[c], Dv[c]);
 				k += m1;
 			}
 		}
@@ -258,10 +274,13 @@ k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const S *__restrict__ dtab
 		for (int j = 0; j < G; j++) {
 			int g = g0 + j;
 			if (g > L) break;
-			V xp, xm;
-			rot_out(y0, A[j], B[j], xp, xm);
-			o[(size_t)g * gstride] = xp;
-			if (g > 0) o[(size_t)(N - g) * gstride] = xm;
+#pragma unroll
+			for (int c = 0; c < CH; c++) {
+				V xp, xm;
+				rot_out(y0[c], A[j][c], B[j][c], xp, xm);
+				o[(size_t)g * gstride + c * SXS_QT] = xp;
+				if (g > 0) o[(size_t)(N - g) * gstride + c * SXS_QT] = xm;
+			}
 		}
 	}
 }
@@ -928,16 +947,21 @@ static int rotate_launch(const void *spf_t, const void *dtab, const double2 *tw,
                          cudaStream_t s)
 {
 	typedef typename Cx<S>::T V;
+	/* three channels per thread in FP32 (one twiddle load for three) while
+	 * their 12 G accumulators leave room for warps (G <= 6, L <= 23: measured
+	 * 1.10 -> 1.04 ms at L = 20, slower from G = 8 on); FP64 is bound by its
+	 * arithmetic pipe and keeps one */
+	constexpr int CH = (sizeof(S) == 4 && G <= 6) ? 3 : 1;
 	int K = L + 1, N = 2 * L + 1, NT = (Q + SXS_QT - 1) / SXS_QT;
 	size_t smem = sizeof(RotTw<S>) * (size_t)(N + (G - 1) * L);
+	auto kern = k_rotate<S, G, CH>;
 	if (smem > 48 * 1024) {
-		cudaError_t e = cudaFuncSetAttribute(k_rotate<S, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 		if (e != cudaSuccess) return e;
 	}
 	long nb = (long)K * K * NT;
 	if (nb > 0x7fffffffL) return cudaErrorInvalidValue;
-	k_rotate<S, G><<<(unsigned)nb, ROT_THREADS, smem, s>>>((const V *)spf_t, (const S *)dtab, tw, Q, L, conj,
-	                                                      (V *)out);
+	kern<<<(unsigned)nb, ROT_THREADS(CH), smem, s>>>((const V *)spf_t, (const S *)dtab, tw, Q, L, conj, (V *)out);
 	return cudaGetLastError();
 }
 
