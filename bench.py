@@ -134,6 +134,10 @@ class Clocks:
 # same poses per translated row as the whole list, profiles/): the traffic
 # of a launch scales with the poses it processes at that density.
 TRAFFIC_PER_POSE = {("c1", "mixed"): 9.13e4, ("c1", "fp64"): 4.47e5}
+# L2-to-SM bytes per pose of the FP32 per-pose kernel (ncu
+# l1tex__m_xbar2l1tex_read_sectors on the same capture): the P row of every
+# pose (no block shares one) and the R rows, which the poses of a warp share.
+L2_TO_SM_PER_POSE = {("c1", "mixed"): 6.18e5}
 
 
 def pose_flops(L, Q, precision):
@@ -306,6 +310,7 @@ def run_ours(args):
 
     fp64_peak = max(g.fp64_fma_tflops() for _ in range(3))
     fp32_peak = max(g.fp32_fma_tflops() for _ in range(3))
+    l2_peak = max(g.l2_read_gbs() for _ in range(3))
     head = args.precision
     prec = {"mixed": g.MIXED, "fp64": g.FP64}
     runs = {}
@@ -381,6 +386,18 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "clocks": clocks,
     }
+    l2key = (args.config, head)
+    if l2key in L2_TO_SM_PER_POSE and not args.zsub and not args.poses:
+        # the FP32 per-pose kernel is bound by moving P and R rows from L2
+        # into the SMs (L1 data path 88 % busy, FMA pipe 48 %): that is its roofline
+        rl = out["roofline"]
+        l2_ach = L2_TO_SM_PER_POSE[l2key] * n / (stage[2] * 1e-3) / 1e9
+        rl["fp32"] = {"achieved": rl["achieved"], "peak": rl["peak"], "unit": "TFLOP/s", "frac": rl["frac"]}
+        rl.update({"bound": "l2", "achieved": l2_ach, "peak": l2_peak, "unit": "GB/s",
+                   "frac": l2_ach / l2_peak if l2_peak > 0 else None,
+                   "l2_source": "ncu L2-to-SM read bytes per pose (618 KB) x poses / kernel time",
+                   "peak_source": "measured in this run: 16-byte L2-only loads by every SM over a 32 MiB "
+                                  "L2-resident buffer"})
     if head == "mixed":
         out["accuracy"] = accuracy(res, runs["fp64"][3])
     if not args.skip_serve:

@@ -396,6 +396,9 @@ double sxsg_timer_stop(void);
 double sxsg_fp64_fma_tflops(void);
 /* Dense FP32 multiply-add rate of this GPU (TFLOP/s), measured the same way. */
 double sxsg_fp32_fma_tflops(void);
+/* L2-to-SM read bandwidth of this GPU (GB/s): 16-byte L2-only loads by every
+ * SM over a 32 MiB L2-resident buffer. */
+double sxsg_l2_read_gbs(void);
 
 #ifdef __cplusplus
 }

@@ -428,3 +428,9 @@ def fp32_fma_tflops():
     lib = load()
     lib.sxsg_fp32_fma_tflops.restype = C.c_double
     return lib.sxsg_fp32_fma_tflops()
+
+
+def l2_read_gbs():
+    lib = load()
+    lib.sxsg_l2_read_gbs.restype = C.c_double
+    return lib.sxsg_l2_read_gbs()

@@ -1132,6 +1132,57 @@ __global__ void k_fp32_probe(float *out, int iters)
 }
 } // namespace
 
+namespace {
+/* every thread streams 16-byte L2-only loads over an L2-resident buffer */
+__global__ void k_l2_probe(const float4 *__restrict__ buf, long n4, int passes, float *out)
+{
+	float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+	long stride = (long)gridDim.x * blockDim.x;
+	for (int pass = 0; pass < passes; pass++)
+		for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
+			float4 v = __ldcg(buf + i);
+			acc.x += v.x; acc.y += v.y; acc.z += v.z; acc.w += v.w;
+		}
+	float s = acc.x + acc.y + acc.z + acc.w;
+	if (s == 12345.678f) out[threadIdx.x] = s;
+}
+} // namespace
+
+/* L2-to-SM read bandwidth (GB/s): a 32 MiB buffer, warm in L2, read 200
+ * times by every SM with L2-only 16-byte loads */
+extern "C" double sxsk_l2_probe(cudaStream_t s)
+{
+	int dev = 0, nsm = 0;
+	cudaGetDevice(&dev);
+	cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+	const long n4 = (32L << 20) / 16;
+	const int passes = 200;
+	float4 *buf = NULL;
+	float *out = NULL;
+	if (cudaMalloc((void **)&buf, n4 * 16) != cudaSuccess) return -1.0;
+	if (cudaMalloc((void **)&out, 1024 * sizeof(float)) != cudaSuccess) {
+		cudaFree(buf);
+		return -1.0;
+	}
+	cudaMemsetAsync(buf, 0, n4 * 16, s);
+	int blocks = nsm * 8, threads = 256;
+	k_l2_probe<<<blocks, threads, 0, s>>>(buf, n4, 2, out);
+	cudaEvent_t e0, e1;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	cudaEventRecord(e0, s);
+	k_l2_probe<<<blocks, threads, 0, s>>>(buf, n4, passes, out);
+	cudaEventRecord(e1, s);
+	cudaEventSynchronize(e1);
+	float ms = 0;
+	cudaEventElapsedTime(&ms, e0, e1);
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	cudaFree(buf);
+	cudaFree(out);
+	return ms > 0 ? (double)n4 * 16 * passes / (ms * 1e-3) / 1e9 : -1.0;
+}
+
 extern "C" double sxsk_fp32_probe(cudaStream_t s)
 {
 	int dev = 0, nsm = 0;

@@ -872,6 +872,14 @@ double sxsg_fp32_fma_tflops(void)
 	return sxsk_fp32_probe(g_stream);
 }
 
+double sxsg_l2_read_gbs(void)
+{
+	if (sxs_ensure_init()) return -1.0;
+	extern double sxsk_l2_probe(cudaStream_t s);
+	sxs_count_launches(2);
+	return sxsk_l2_probe(g_stream);
+}
+
 double sxsg_fp64_fma_tflops(void)
 {
 	if (sxs_ensure_init()) return -1.0;
