@@ -91,3 +91,25 @@ def test_mixed_matches_fp64_at_lmax20(gpu):
     ref, mix = out[gpu.FP64], out[gpu.MIXED]
     assert chan_err(mix["cross"], ref["cross"]) <= CROSS_TOL
     check_grid(mix, ref["grid"])
+
+
+def test_wide_c1_grid_mixed_matches_fp64(gpu):
+    """More c1 values than a fit block has threads (150 > 128) and a G table
+    too large for shared memory at Q = 101 (150 x 101 double-floats): the
+    double-float fit runs its c1 rows in rounds and reads G from global
+    memory; its grid and best cells against the FP64 fit."""
+    from libfmftsaxs_gb300 import workload
+    w = workload.build("c1", seed=4, lib=gpu, overrides=dict(rec=(400, 11.0), lig=(250, 9.0), lists=(400,),
+                                                             t=(18.0, 30.0)))
+    c1g = np.linspace(0.95, 1.05, 150)
+    c2g = np.linspace(0.0, 4.0, 9)
+    out = {}
+    for prec in (gpu.FP64, gpu.MIXED):
+        p = gpu.Plan(w.A, w.B, w.q, w.z, w.L, w.a, w.mult, w.peak, c1g, c2g, precision=prec)
+        p.set_poses(w.index, skip=1)
+        p.run(gpu.FIT_GRID)
+        out[prec] = p.results(grid=True)
+        p.close()
+    check_grid(out[gpu.MIXED], out[gpu.FP64]["grid"])
+    g = out[gpu.FP64]["grid"].reshape(len(w.index), -1)
+    np.testing.assert_allclose(out[gpu.FP64]["chi"], np.sqrt(g.min(axis=1)), rtol=1e-12, atol=0)
