@@ -239,6 +239,11 @@ __global__ void __launch_bounds__(TC_BLOCK) k_rotate_tc(const float2 *__restrict
 		phase ^= 1u;
 		done = __syncthreads_and(done);
 		if (!done) {
+			/* a second bounded wait for the MMAs in flight before the
+			 * accumulator's TMEM is freed below */
+			for (int it = 0; it < TC_WAIT_LIMIT; it++)
+				if (mbar_try_wait(mbar, phase ^ 1u)) break;
+			__syncthreads();
 			if (tid == 0) atomicExch(&g_tc_status, 1);
 			ok_all = 0;
 			break;
