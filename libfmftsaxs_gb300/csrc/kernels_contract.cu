@@ -493,6 +493,113 @@ k_translate_col(const typename Cx<S>::T *__restrict__ U, const S *__restrict__ t
 	}
 }
 
+/* 16-byte asynchronous global-to-shared copies (completion by wait_group,
+ * a hardware wait on the thread's own copies) */
+__device__ __forceinline__ void cp_async16(void *sdst, const void *gsrc)
+{
+	unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+	asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+/* slices per block of the pipelined column kernel */
+#define TP_SB 8
+
+/* shared bytes of k_translate_pipe<NB>: tau^m [8 q][NB NB + 4] and the U
+ * columns of one slice [SXS_SLICE combos][NB pairs][3 ch][8 q] */
+#define TP_SMEM(NB) (sizeof(float) * SXS_QT * ((NB) * (NB) + 4) + sizeof(float2) * SXS_SLICE * (NB) * 3 * SXS_QT)
+
+/* The FP32 column form with three channels per thread (NB <= 20), pipelined
+ * over slices: block = (tile, run of TP_SB consecutive slices, m); while the
+ * threads apply tau^m to one slice's U columns (held in registers), the U
+ * columns of the next slice stream into shared memory with cp.async, so the
+ * global-load latency that one slice per block leaves exposed at three
+ * blocks per SM overlaps the arithmetic.  tau^m(q z) is restaged only where
+ * z changes between slices (slices are z-major).  Same sums, same order and
+ * same rows as k_translate_col<float, NB, 3>. */
+template <int NB>
+__global__ void __launch_bounds__(TCOL_THREADS(3), NB <= 8 ? 5 : (NB <= 12 ? 4 : 3))
+k_translate_pipe(const float2 *__restrict__ U, const float *__restrict__ tau, const int32_t *__restrict__ combo_zbg,
+                 const int32_t *__restrict__ slices, int nslice, int cbase, int ncombo, int L, int nzt, int m_lo,
+                 int nm, float2 *__restrict__ R)
+{
+	extern __shared__ __align__(16) unsigned char tps_raw[];
+	const int qstride = NB * NB + 4, rowf = 3 * SXS_QT;   /* float2 per pair of one combo */
+	float *ts = reinterpret_cast<float *>(tps_raw);
+	float2 *us = reinterpret_cast<float2 *>(tps_raw + sizeof(float) * SXS_QT * qstride);
+	int K = L + 1, N = 2 * L + 1, NP = K * (K + 1) / 2, nrow = K * N;
+	int ng = (nslice + TP_SB - 1) / TP_SB;
+	int bid = blockIdx.x;
+	int mi = bid % nm;
+	bid /= nm;
+	int gi = bid % ng, t = bid / ng;
+	int m = m_lo + mi, n = K - m, po = psym(m, K);
+	int s0 = gi * TP_SB, s1 = s0 + TP_SB < nslice ? s0 + TP_SB : nslice;
+	int q = threadIdx.x % SXS_QT, cl = threadIdx.x / SXS_QT;
+	/* 16-byte chunks of one combo's n pairs: n x 3 x 8 float2 = 12 n; the
+	 * 8 threads of combo cl copy its chunks in 128-byte rows */
+	const int per = n * rowf / 2;
+	auto issue = [&](int s) {
+		int cf = slices[2 * s] - cbase, nc = slices[2 * s + 1];
+		if (cl < nc) {
+			int cc = cf + cl;
+			int b2 = combo_zbg[3 * cc + 1], g2 = combo_zbg[3 * cc + 2];
+			const float2 *src = U + (((size_t)t * nrow + b2 * N + g2) * NP + po) * rowf;
+			float2 *dst = us + (size_t)cl * NB * rowf;
+			for (int r = q; r < per; r += SXS_QT) cp_async16(dst + 2 * r, src + 2 * r);
+		}
+		cp_async_commit();
+	};
+	int zcur = -1;
+	if (s0 < s1) issue(s0);
+	for (int s = s0; s < s1; s++) {
+		int cf = slices[2 * s] - cbase, nc = slices[2 * s + 1];
+		int zi = combo_zbg[3 * cf];
+		if (zi != zcur) {
+			__syncthreads();   /* no thread still reads the previous tau */
+			const float *tz = tau + ((((size_t)t * nzt + zi) * K + m) * K) * K * SXS_QT;
+			for (int k = threadIdx.x; k < SXS_QT * NB * NB; k += blockDim.x) {
+				int qq = k % SXS_QT, r = k / SXS_QT;
+				int i = r / NB, kk = r % NB;
+				float v = 0;
+				if (i < n && kk < n) v = tz[((size_t)(m + i) * K + m + kk) * SXS_QT + qq];
+				ts[qq * qstride + i * NB + kk] = v;
+			}
+			zcur = zi;
+		}
+		cp_async_wait_all();
+		__syncthreads();   /* this slice's U columns and tau visible to all */
+		bool act = cl < nc;
+		float2 u[3][NB];
+		if (act) {
+			const float2 *uc = us + (size_t)cl * NB * rowf + q;
+#pragma unroll
+			for (int j = 0; j < 3; j++)
+#pragma unroll
+				for (int k = 0; k < NB; k++) u[j][k] = k < n ? uc[k * rowf + j * SXS_QT] : zero2<float2>();
+		}
+		__syncthreads();   /* the buffer is free for the next slice */
+		if (s + 1 < s1) issue(s + 1);
+		if (act) {
+			int c = cf + cl;
+			const float *tq = ts + q * qstride;
+			float2 *Rb = R + (((size_t)t * ncombo + c) * NP + po) * rowf + q;
+			for (int i = 0; i < n; i += 2) {
+				float2 a[3];
+				tcol_row<0, 3, float, float2, NB>(tq + i * NB, u, a);
+#pragma unroll
+				for (int j = 0; j < 3; j++) Rb[(size_t)i * rowf + j * SXS_QT] = a[j];
+				if (i + 1 < n) {
+					tcol_row<1, 3, float, float2, NB>(tq + (i + 1) * NB, u, a);
+#pragma unroll
+					for (int j = 0; j < 3; j++) Rb[(size_t)(i + 1) * rowf + j * SXS_QT] = a[j];
+				}
+			}
+		}
+	}
+}
+
 /* Storage of the per-pose cross terms: double on the FP64 path; on the FP32
  * path a double-float pair {hi, lo} = cst + 2 f formed with an error-free
  * sum (explicit round-to-nearest adds, never contracted), so that the fit
@@ -878,11 +985,29 @@ static cudaError_t translate_col_launch(const void *U, const void *tau, const in
 	if (m_lo < 0) m_lo = 0;
 	if (m_hi < m_lo) return cudaSuccess;
 	int nm = m_hi - m_lo + 1;
+	if constexpr (sizeof(S) == 4 && NB <= 20) {
+		/* three channels per thread, pipelined over runs of slices */
+		long nb = (long)NT * ((nslice + TP_SB - 1) / TP_SB) * nm;
+		if (nb > 0x7fffffffL) return cudaErrorInvalidValue;
+		size_t smem = TP_SMEM(NB);
+		auto kern = k_translate_pipe<NB>;
+		if (smem > 48 * 1024) {
+			cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+			if (e != cudaSuccess) return e;
+		}
+		/* three blocks of ~74 KB per SM at NB = 20 need the largest carveout */
+		cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+		                                     (int)cudaSharedmemCarveoutMaxShared);
+		if (e != cudaSuccess) return e;
+		kern<<<(unsigned)nb, TCOL_THREADS(3), smem, s>>>((const float2 *)U, (const float *)tau, combo_zbg, slices,
+		                                                 nslice, cbase, ncombo, L, nzt, m_lo, nm, (float2 *)R);
+		return cudaGetLastError();
+	}
 	long nb = (long)NT * nslice * nm;
 	if (nb > 0x7fffffffL) return cudaErrorInvalidValue;
 	size_t smem = sizeof(S) * SXS_QT * (NB * NB + 4);
-	/* three channels per thread where their columns fit the registers */
-	const int CH = (sizeof(S) == 4 && NB <= 20) ? 3 : 1;
+	/* one channel per thread where three columns would not fit the registers */
+	const int CH = 1;
 	auto kern = k_translate_col<S, NB, CH>;
 	if (smem > 48 * 1024) {
 		cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
