@@ -175,6 +175,7 @@ struct sxsg_plan {
 	int L, K, N, K2, Q, nz, n1, n2, precision;
 	const sxs_ltables *lt;
 	cudaStream_t s;
+	cudaStream_t s2;            /* per-z tables beside the rotations (ev[2], ev[3]) */
 	int nsm;
 	cudaEvent_t *cev;           /* per-chunk events, 3 per chunk */
 	int ncev;
@@ -241,6 +242,9 @@ static void pfree(const sxsg_plan *p, void *x)
 
 static void plan_free_poses(sxsg_plan *p)
 {
+	/* the side stream's last per-z tables are done before their buffers
+	 * return to the pool (an unrecorded event is complete) */
+	if (p->s2) cudaStreamWaitEvent(p->s, p->ev[3], 0);
 	free(p->h_combo); free(p->h_cstart); free(p->h_zt); free(p->h_slices);
 	pfree(p, p->d_slices);
 	p->h_slices = NULL; p->d_slices = NULL; p->nslice = 0;
@@ -253,6 +257,7 @@ static void plan_free_poses(sxsg_plan *p)
 void sxsg_plan_destroy(sxsg_plan *p)
 {
 	if (!p) return;
+	if (p->s2) cudaStreamSynchronize(p->s2);
 	cudaStreamSynchronize(p->s);
 	plan_free_poses(p);
 	pfree(p, p->d_A); pfree(p, p->d_B); pfree(p, p->d_q); pfree(p, p->d_fc); pfree(p, p->d_a); pfree(p, p->d_gtab); pfree(p, p->d_gdf);
@@ -265,6 +270,7 @@ void sxsg_plan_destroy(sxsg_plan *p)
 	pfree(p, p->d_cross); pfree(p, p->d_chi); pfree(p, p->d_c1); pfree(p, p->d_c2); pfree(p, p->d_grid);
 	pfree(p, p->d_scaled); pfree(p, p->d_scale); pfree(p, p->d_cell); pfree(p, p->d_iters);
 	for (int i = 0; i < 6; i++) if (p->ev[i]) cudaEventDestroy(p->ev[i]);
+	if (p->s2) cudaStreamDestroy(p->s2);
 	for (int i = 0; i < p->ncev; i++) cudaEventDestroy(p->cev[i]);
 	free(p->cev);
 	free(p->h_z);
@@ -308,6 +314,7 @@ int sxs_plan_create_on(sxsg_plan **out, const double *A, const double *B, const 
 	size_t spf_n = (size_t)3 * Q * p->K2 * 2;
 	cudaError_t e = cudaSuccess;
 	for (int i = 0; i < 6 && !e; i++) e = cudaEventCreate(&p->ev[i]);
+	if (!e) e = cudaStreamCreateWithFlags(&p->s2, cudaStreamNonBlocking);
 	if (!e) {
 		int dev = 0;
 		e = cudaGetDevice(&dev);
@@ -573,7 +580,47 @@ int sxsg_plan_set_poses(sxsg_plan *p, const int64_t *index, int64_t n, int skip)
 	return 0;
 }
 
+/* per-z tables: Bessel values and translation matrices (FP64), with their
+ * float copy on the mixed path */
+static int plan_ztables(sxsg_plan *p, cudaStream_t s)
+{
+	int L = p->L, Q = p->Q;
+	SXS_K(sxsk_bessel_z(p->d_zt, p->nzt, p->d_q, Q, L, p->d_bes, s));
+	SXS_K(sxsk_tmatrix(p->d_bes, p->lt->d_dsymb, p->nzt, Q, L, p->lt->d_ll1, p->lt->nll1, p->d_tau, s));
+	sxs_count_launches(2);
+	if (p->fp32) {
+		SXS_K(sxsk_to_float(p->d_tau, p->d_tauf, (long)p->NT * p->nzt * p->K * p->K * p->K * SXS_QT, s));
+		sxs_count_launches(1);
+	}
+	return 0;
+}
+
+static int plan_rotations(sxsg_plan *p);
+
+/* The per-z tables (FP64 pipe) run on the side stream beside the
+ * rotations (FP32 pipe); the plan stream waits for them before it goes on,
+ * also when a rotation launch failed, so no later work of the plan stream
+ * overtakes them. */
 static int plan_tables(sxsg_plan *p)
+{
+	cudaStream_t s = p->s;
+	int side = p->nzt > 0 && p->s2, rc = 0;
+	if (!side) {
+		rc = plan_rotations(p);
+		if (!rc && p->nzt > 0) rc = plan_ztables(p, s);
+		return rc;
+	}
+	SXS_CU(cudaEventRecord(p->ev[2], s));
+	SXS_CU(cudaStreamWaitEvent(p->s2, p->ev[2], 0));
+	rc = plan_ztables(p, p->s2);
+	cudaError_t e = cudaEventRecord(p->ev[3], p->s2);
+	if (!rc && !e) rc = plan_rotations(p);
+	if (!e) e = cudaStreamWaitEvent(s, p->ev[3], 0);
+	if (e) return sxs_cuda_fail(e, "side stream of the per-z tables");
+	return rc;
+}
+
+static int plan_rotations(sxsg_plan *p)
 {
 	int L = p->L, Q = p->Q, N = p->N;
 	cudaStream_t s = p->s;
@@ -603,15 +650,6 @@ static int plan_tables(sxsg_plan *p)
 		p->tc_used = tc;
 		if (p->ext_tables) p->P_valid = p->U_valid = 1;
 		p->tw_variant = variant;
-	}
-	if (p->nzt > 0) {
-		SXS_K(sxsk_bessel_z(p->d_zt, p->nzt, p->d_q, Q, L, p->d_bes, s));
-		SXS_K(sxsk_tmatrix(p->d_bes, p->lt->d_dsymb, p->nzt, Q, L, p->lt->d_ll1, p->lt->nll1, p->d_tau, s));
-		sxs_count_launches(2);
-		if (p->fp32) {
-			SXS_K(sxsk_to_float(p->d_tau, p->d_tauf, (long)p->NT * p->nzt * p->K * p->K * p->K * SXS_QT, s));
-			sxs_count_launches(1);
-		}
 	}
 	return 0;
 }
