@@ -519,7 +519,7 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
  * z changes between slices (slices are z-major).  Same sums, same order and
  * same rows as k_translate_col<float, NB, 3>. */
 template <int NB>
-__global__ void __launch_bounds__(TCOL_THREADS(3), NB <= 8 ? 5 : (NB <= 12 ? 4 : 3))
+__global__ void __launch_bounds__(TCOL_THREADS(3), NB <= 8 ? 5 : (NB <= 12 ? 4 : (NB <= 20 ? 3 : 2)))
 k_translate_pipe(const float2 *__restrict__ U, const float *__restrict__ tau, const int32_t *__restrict__ combo_zbg,
                  const int32_t *__restrict__ slices, int nslice, int cbase, int ncombo, int L, int nzt, int m_lo,
                  int nm, float2 *__restrict__ R)
@@ -985,7 +985,7 @@ static cudaError_t translate_col_launch(const void *U, const void *tau, const in
 	if (m_lo < 0) m_lo = 0;
 	if (m_hi < m_lo) return cudaSuccess;
 	int nm = m_hi - m_lo + 1;
-	if constexpr (sizeof(S) == 4 && NB <= 20) {
+	if constexpr (sizeof(S) == 4 && NB <= 24) {
 		/* three channels per thread, pipelined over runs of slices */
 		long nb = (long)NT * ((nslice + TP_SB - 1) / TP_SB) * nm;
 		if (nb > 0x7fffffffL) return cudaErrorInvalidValue;
