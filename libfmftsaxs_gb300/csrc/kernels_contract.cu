@@ -431,13 +431,13 @@ __device__ __forceinline__ void tcol_row(const S *row, const V (&u)[CH][NB], V (
  *   parity of i + k).
  * Block = (tile, slice of <= SXS_SLICE combos sharing z, m); tau rows are
  * padded so the 8 q start on distinct banks and read as float4/double2
- * chunks that lanes of the same q share.  A 128-bit shared load costs four
- * wavefronts even as a broadcast, so CH = 3 (one tau load for three
- * channels) keeps the L1 data pipe below the FMA rate; CH = 1 where three
- * NB-long columns would not fit the registers.  One launch per NB covers
- * the m with n in (NB - 4, NB]. */
+ * chunks that lanes of the same q share.  One launch per NB covers the m
+ * with n in (NB - 4, NB].  The FP64 path runs it with CH = 1 (bound by the
+ * FP64 pipe); FP32 runs the pipelined three-channel form below, since a
+ * 128-bit shared load costs four wavefronts even as a broadcast and one
+ * channel per tau load leaves the L1 data pipe ahead of the FMA rate. */
 template <typename S, int NB, int CH>
-__global__ void __launch_bounds__(TCOL_THREADS(CH), CH == 3 ? 1 : (sizeof(S) == 4 ? (NB <= 20 ? 3 : 2) : 1))
+__global__ void __launch_bounds__(TCOL_THREADS(CH), 1)
 k_translate_col(const typename Cx<S>::T *__restrict__ U, const S *__restrict__ tau,
                 const int32_t *__restrict__ combo_zbg, const int32_t *__restrict__ slices, int nslice, int cbase,
                 int ncombo, int L, int nzt, int m_lo, int nm, typename Cx<S>::T *__restrict__ R)
@@ -510,16 +510,17 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
  * columns of one slice [SXS_SLICE combos][NB pairs][3 ch][8 q] */
 #define TP_SMEM(NB) (sizeof(float) * SXS_QT * ((NB) * (NB) + 4) + sizeof(float2) * SXS_SLICE * (NB) * 3 * SXS_QT)
 
-/* The FP32 column form with three channels per thread (NB <= 20), pipelined
- * over slices: block = (tile, run of TP_SB consecutive slices, m); while the
- * threads apply tau^m to one slice's U columns (held in registers), the U
- * columns of the next slice stream into shared memory with cp.async, so the
- * global-load latency that one slice per block leaves exposed at three
- * blocks per SM overlaps the arithmetic.  tau^m(q z) is restaged only where
- * z changes between slices (slices are z-major).  Same sums, same order and
- * same rows as k_translate_col<float, NB, 3>. */
+/* The FP32 column form with three channels per thread, pipelined over
+ * slices: block = (tile, run of TP_SB consecutive slices, m); while the
+ * threads apply tau^m to one slice's U columns (held in registers: 6 NB
+ * floats), the U columns of the next slice stream into shared memory with
+ * cp.async, so the global-load latency of the low occupancy that these
+ * registers allow (1-5 blocks of 4 warps per SM by NB) overlaps the
+ * arithmetic.  tau^m(q z) is restaged only where z changes between slices
+ * (slices are z-major).  The sums are those of k_translate_col with CH = 3:
+ * rows in even/odd pairs, one tau load for three channels. */
 template <int NB>
-__global__ void __launch_bounds__(TCOL_THREADS(3), NB <= 8 ? 5 : (NB <= 12 ? 4 : (NB <= 20 ? 3 : 2)))
+__global__ void __launch_bounds__(TCOL_THREADS(3), NB <= 8 ? 5 : (NB <= 12 ? 4 : (NB <= 20 ? 3 : (NB <= 28 ? 2 : 1))))
 k_translate_pipe(const float2 *__restrict__ U, const float *__restrict__ tau, const int32_t *__restrict__ combo_zbg,
                  const int32_t *__restrict__ slices, int nslice, int cbase, int ncombo, int L, int nzt, int m_lo,
                  int nm, float2 *__restrict__ R)
@@ -985,8 +986,8 @@ static cudaError_t translate_col_launch(const void *U, const void *tau, const in
 	if (m_lo < 0) m_lo = 0;
 	if (m_hi < m_lo) return cudaSuccess;
 	int nm = m_hi - m_lo + 1;
-	if constexpr (sizeof(S) == 4 && NB <= 24) {
-		/* three channels per thread, pipelined over runs of slices */
+	if constexpr (sizeof(S) == 4) {
+		/* FP32: three channels per thread, pipelined over runs of slices */
 		long nb = (long)NT * ((nslice + TP_SB - 1) / TP_SB) * nm;
 		if (nb > 0x7fffffffL) return cudaErrorInvalidValue;
 		size_t smem = TP_SMEM(NB);
@@ -995,27 +996,27 @@ static cudaError_t translate_col_launch(const void *U, const void *tau, const in
 			cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 			if (e != cudaSuccess) return e;
 		}
-		/* three blocks of ~74 KB per SM at NB = 20 need the largest carveout */
+		/* blocks of 75-131 KB (NB 20-32) need the largest carveout */
 		cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
 		                                     (int)cudaSharedmemCarveoutMaxShared);
 		if (e != cudaSuccess) return e;
 		kern<<<(unsigned)nb, TCOL_THREADS(3), smem, s>>>((const float2 *)U, (const float *)tau, combo_zbg, slices,
 		                                                 nslice, cbase, ncombo, L, nzt, m_lo, nm, (float2 *)R);
 		return cudaGetLastError();
+	} else {
+		/* FP64 (bound by its pipe): one channel per thread */
+		long nb = (long)NT * nslice * nm;
+		if (nb > 0x7fffffffL) return cudaErrorInvalidValue;
+		size_t smem = sizeof(S) * SXS_QT * (NB * NB + 4);
+		auto kern = k_translate_col<S, NB, 1>;
+		if (smem > 48 * 1024) {
+			cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+			if (e != cudaSuccess) return e;
+		}
+		kern<<<(unsigned)nb, TCOL_THREADS(1), smem, s>>>((const V *)U, (const S *)tau, combo_zbg, slices, nslice,
+		                                                 cbase, ncombo, L, nzt, m_lo, nm, (V *)R);
+		return cudaGetLastError();
 	}
-	long nb = (long)NT * nslice * nm;
-	if (nb > 0x7fffffffL) return cudaErrorInvalidValue;
-	size_t smem = sizeof(S) * SXS_QT * (NB * NB + 4);
-	/* one channel per thread where three columns would not fit the registers */
-	const int CH = 1;
-	auto kern = k_translate_col<S, NB, CH>;
-	if (smem > 48 * 1024) {
-		cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-		if (e != cudaSuccess) return e;
-	}
-	kern<<<(unsigned)nb, TCOL_THREADS(CH), smem, s>>>((const V *)U, (const S *)tau, combo_zbg, slices, nslice, cbase,
-	                                                  ncombo, L, nzt, m_lo, nm, (V *)R);
-	return cudaGetLastError();
 }
 
 template <typename S>
