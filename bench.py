@@ -76,7 +76,7 @@ def cpu_sample(w, kind, workers, triples_per_worker=1, seed=11):
 
 def cpu_kind():
     from oracle import bind
-    if os.path.isdir(bind.REF_SRC):
+    if bind.have_ref():
         try:
             bind.build_ref()
             return "reference"

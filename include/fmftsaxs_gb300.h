@@ -206,17 +206,19 @@ int sxsg_profile_from_flat(const double *spf, int L, int qnum, double rm, const 
  * Every pointer is a DEVICE pointer the caller owns: xyz[3 natoms],
  * vacuum_ff, dummy_ff, water_w[natoms] (water form factor x accessible
  * fraction per atom; NULL for no hydration shell), qvals[qnum], spf_out in
- * the flat layout [3][qnum][(L+1)^2][2].  Work buffers live in one static
- * device array of 64 MiB (8 Mi doubles) that every GPU loading this library
- * keeps until exit; a call needs about natoms (2 (L+1)^2 + qnum (L+1))
- * doubles of it, L <= 40, and a larger request returns -3 without touching
- * the GPU.  Work is queued on `stream` (a cudaStream_t; NULL for the
- * default stream); the call returns once the Y_lm norm table is on the
- * device.  The first call on each device looks up the array's device
- * address, so make that first call before any stream capture.  All calls
- * share the array: calls that overlap on the GPU race with each other.
- * Returns 0, -2 (bad argument), -3 (too large for the static array), -4
- * (no current device) or a CUDA error code. */
+ * the flat layout [3][qnum][(L+1)^2][2].  Work buffers (the Y_lm norm
+ * table, Y_lm and j_l per atom) live in one static device array of 64 MiB
+ * (8 Mi doubles) that every GPU loading this library keeps until exit; a
+ * call needs about natoms (2 (L+1)^2 + qnum (L+1)) doubles of it, L <= 40,
+ * and a larger request returns -3 without touching the GPU.  Work is queued
+ * on `stream` (a cudaStream_t; NULL for the default stream) and the call
+ * returns without waiting for it.  The first call on each device looks up
+ * the array's device address (cudaGetSymbolAddress), so make that first
+ * call before any stream capture; like the library's other per-device
+ * state, the address is not looked up again after a cudaDeviceReset.  All
+ * calls share the array: calls that overlap on the GPU race with each
+ * other.  Returns 0, -2 (bad argument), -3 (too large for the static
+ * array), -4 (no current device) or a CUDA error code. */
 int sxsg_expand_noalloc(const double *xyz, const double *vacuum_ff, const double *dummy_ff, const double *water_w,
                         int natoms, const double *qvals, int qnum, int L, double *spf_out, void *stream);
 
@@ -255,7 +257,11 @@ int sxsg_plan_set_budget(sxsg_plan *plan, size_t bytes);
 /* Rotation engine of a mixed-precision plan: SXSG_ROT_CUDA (CUDA cores,
  * the default) or SXSG_ROT_TC (tcgen05 tensor cores, 3xTF32 with FP32
  * accumulation, for 2L + 1 <= 64; larger L stays on CUDA cores).  FP64
- * plans always rotate on CUDA cores. */
+ * plans always rotate on CUDA cores.  The tensor-core kernel's waits for its
+ * MMAs are bounded: sxsg_plan_run returns -6 when a wait gave up (the run's
+ * results are invalid) and -7 when the MMAs did not finish in a second
+ * bounded wait either (tensor memory was left allocated: treat the CUDA
+ * context as unusable). */
 enum { SXSG_ROT_CUDA = 0, SXSG_ROT_TC = 1 };
 int sxsg_plan_set_rotation(sxsg_plan *plan, int engine);
 /* Run the GPU work for the current pose list (asynchronous until results). */
@@ -280,12 +286,17 @@ void sxsg_plan_destroy(sxsg_plan *plan);
  * each).  Jobs are admitted in arrival order as device memory frees up under
  * an HBM cap, run concurrently on separate streams, and their results are
  * bitwise those of the same job run alone.  Rotation tables of molecules
- * with a nonzero key are cached on the device across jobs. */
+ * with a nonzero key are cached on the device across jobs; a table is shared
+ * once the job that filled it has finished, and a job whose table is still
+ * being filled by another one fills its own copy. */
 typedef struct sxsg_server sxsg_server;
 
 typedef struct {
 	const double *A, *B;          /* flat expansions [3][qnum][(L+1)^2][2] */
-	uint64_t keyA, keyB;          /* molecule keys for the table cache; 0 = not cached */
+	uint64_t keyA, keyB;          /* nonzero: cache this molecule's rotation table on the
+	                               * device (the key is combined with a digest of the
+	                               * coefficients, so a reused key never returns another
+	                               * molecule's table); 0 = not cached */
 	const double *qvals;
 	int qnum;
 	const double *zvals;

@@ -88,12 +88,14 @@ int sxsk_rotate(const void *spf_t, const void *dtab, const double2 *tw, int Q, i
  * FP32 accumulation in tensor memory); same output as sxsk_rotate with
  * fp32; 2L + 1 <= 64.  dtabf: the float Wigner-d table. */
 int sxsk_rotate_tc(const void *spf_t, const float *dtabf, const double2 *tw, int Q, int L, int conj, void *out,
-                   float *amat, cudaStream_t s);
+                   float *amat, int *status, cudaStream_t s);
 /* floats of the scratch (amat) that sxsk_rotate_tc needs */
 size_t sxsk_rotate_tc_scratch(int L);
-/* nonzero when a block of sxsk_rotate_tc gave up waiting for its MMAs
- * since the last call; resets the flag */
-int sxsk_rotate_tc_status(void);
+/* *status (device int, zeroed by the caller) after sxsk_rotate_tc: the
+ * largest of 0 (every block saw its MMAs finish), 1 (a block gave up
+ * waiting, its MMAs then finished: output invalid) and 2 (a block's MMAs
+ * did not finish in either bounded wait: output invalid, its tensor memory
+ * was not freed and the context must be considered unusable). */
 
 /* translated ligand table for the combos of a run of slices, m >= 0, all q tiles:
  * R[t][c][pair(m,l)][ch][q] = sum_{l1>=m} conj(T[t][zi][m][l][l1][q]) U[t][(b2,g2)][pair(m,l1)][ch][q].

@@ -410,8 +410,32 @@ int sxsk_const_int(const double *A, const double *B, int Q, int L, double *cst, 
 
 static __device__ __align__(256) double g_noalloc_scratch[SXS_NOALLOC_DOUBLES];
 
-extern "C" void sxs_ynorm_host(int L, double *y);
 extern "C" void sxs_count_launches(int n);
+
+/* The Y_lm normalisation table y[l][m + L] = sqrt((2l+1)/(4 pi) (l-m)!/(l+m)!),
+ * times (-1)^m for -m, zero for |m| > l: the arithmetic of sxs_ynorm_host
+ * (src/borrowed.c:19-38) in the same order with IEEE division and square
+ * root, so both give the same bits.  One thread per l. */
+__global__ void k_ynorm(int L, double *__restrict__ y)
+{
+	int l = blockIdx.x * blockDim.x + threadIdx.x;
+	if (l > L) return;
+	int N = 2 * L + 1;
+	double *row = y + (size_t)l * N;
+	for (int m = l + 1; m <= L; m++) {
+		row[m + L] = 0.0;
+		row[-m + L] = 0.0;
+	}
+	double fact = 1.;
+	double tmp0 = __ddiv_rn(2 * l + 1., 4. * SXS_PI);
+	for (int m = 0; m <= l; m++) {
+		if (m > 0) fact = __dmul_rn(fact, (double)((l - m + 1) * (l + m)));
+		double tmp = __dsqrt_rn(__ddiv_rn(tmp0, fact));
+		double sgn = (m % 2 == 0) ? 1 : -1;
+		row[m + L] = tmp;
+		row[-m + L] = __dmul_rn(sgn, tmp);
+	}
+}
 
 namespace {
 std::mutex g_noalloc_lock;
@@ -445,13 +469,12 @@ extern "C" int sxsg_expand_noalloc(const double *xyz, const double *vac, const d
 		base = g_noalloc_ptr[dev];
 	}
 	cudaStream_t s = (cudaStream_t)stream;
-	double yn[(SXS_NOALLOC_LMAX + 1) * (2 * SXS_NOALLOC_LMAX + 1)];
-	sxs_ynorm_host(L, yn);
-	cudaError_t e = cudaMemcpyAsync(base, yn, sizeof(double) * K * N, cudaMemcpyHostToDevice, s);
+	/* every call rewrites the norm table: a call with another L may have
+	 * left other values there */
+	k_ynorm<<<1, 64, 0, s>>>(L, base);
+	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess) return (int)e;
-	/* the copy above reads a stack buffer: finish it before returning */
-	e = cudaStreamSynchronize(s);
-	if (e != cudaSuccess) return (int)e;
+	sxs_count_launches(1);
 	const double *w = water_w;
 	if (!w && natoms > 0) {
 		/* no hydration shell: the weights must start at zero on every call */

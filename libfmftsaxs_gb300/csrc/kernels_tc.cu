@@ -19,8 +19,13 @@
  * a_hi b_hi + a_hi b_lo + a_lo b_hi are accumulated (three MMAs per K step),
  * which keeps the result at FP32 level.
  *
- * The mbarrier wait is bounded; a block that gives up records the failure in
- * a device flag (sxsk_rotate_tc_status) and still frees its tensor memory.
+ * The mbarrier wait is bounded.  A block that gives up records it in the
+ * caller's status word and waits (bounded again) for the MMAs it issued:
+ * status 1 means they then finished and the block freed its tensor memory
+ * as usual; status 2 means the second wait gave up too, and the block
+ * returns without freeing tensor memory that an MMA may still be writing.
+ * The tables of a launch with a nonzero status are not valid; after
+ * status 2 the CUDA context itself must be considered unusable.
  */
 #include "kernels.h"
 
@@ -31,8 +36,6 @@ namespace {
 #define TC_THREADS 128
 #define TC_M 128
 #define TC_WAIT_LIMIT (1 << 20)
-
-__device__ int g_tc_status;
 
 __device__ __forceinline__ int psym_tc(int m, int K) { return m * K - m * (m - 1) / 2; }
 
@@ -134,7 +137,8 @@ __global__ void __launch_bounds__(TC_BLOCK) k_rotate_tc(const float2 *__restrict
                                                         const float *__restrict__ dtab,
                                                         const float *__restrict__ ahi_g,
                                                         const float *__restrict__ alo_g, int Q, int L, int conj,
-                                                        int KP, int NTILE, float2 *__restrict__ out)
+                                                        int KP, int NTILE, float2 *__restrict__ out,
+                                                        int *__restrict__ status)
 {
 	extern __shared__ __align__(1024) unsigned char tsm[];
 	int K = L + 1, N = 2 * L + 1, K2 = K * K, NP = K * (K + 1) / 2, nrow = K * N;
@@ -174,7 +178,7 @@ __global__ void __launch_bounds__(TC_BLOCK) k_rotate_tc(const float2 *__restrict
 	uint32_t sbo = (uint32_t)(KP >> 2) * 128;
 	float sg = conj ? -1.0f : 1.0f;
 	float *Out = reinterpret_cast<float *>(Bhi);
-	int ok_all = 1;
+	int mma_live = 0;   /* both bounded waits gave up: an MMA may still run */
 	unsigned phase = 0;
 	for (int item = blockIdx.x; item < nitem; item += gridDim.x) {
 		int j = item % nchunk, bt = item / nchunk;
@@ -241,11 +245,15 @@ __global__ void __launch_bounds__(TC_BLOCK) k_rotate_tc(const float2 *__restrict
 		if (!done) {
 			/* a second bounded wait for the MMAs in flight before the
 			 * accumulator's TMEM is freed below */
+			bool drained = false;
 			for (int it = 0; it < TC_WAIT_LIMIT; it++)
-				if (mbar_try_wait(mbar, phase ^ 1u)) break;
-			__syncthreads();
-			if (tid == 0) atomicExch(&g_tc_status, 1);
-			ok_all = 0;
+				if (mbar_try_wait(mbar, phase ^ 1u)) {
+					drained = true;
+					break;
+				}
+			drained = __syncthreads_and(drained);
+			if (tid == 0) atomicMax(status, drained ? 1 : 2);
+			mma_live = !drained;
 			break;
 		}
 		asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -270,7 +278,7 @@ __global__ void __launch_bounds__(TC_BLOCK) k_rotate_tc(const float2 *__restrict
 		}
 		__syncthreads();   /* Out is the next item's B */
 	}
-	(void)ok_all;
+	if (mma_live) return;   /* never free TMEM under a live MMA (status 2) */
 	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 	__syncthreads();
 	if (warp == 0)
@@ -280,7 +288,7 @@ __global__ void __launch_bounds__(TC_BLOCK) k_rotate_tc(const float2 *__restrict
 } // namespace
 
 extern "C" int sxsk_rotate_tc(const void *spf_t, const float *dtabf, const double2 *tw, int Q, int L, int conj,
-                              void *out, float *amat, cudaStream_t s)
+                              void *out, float *amat, int *status, cudaStream_t s)
 {
 	int K = L + 1, N = 2 * L + 1;
 	if (2 * N > TC_M) return cudaErrorInvalidValue;
@@ -308,7 +316,7 @@ extern "C" int sxsk_rotate_tc(const void *spf_t, const float *dtabf, const doubl
 	long nitem = (long)K * NT * nchunk;
 	int grid = (int)(nitem < nsm ? nitem : nsm);
 	k_rotate_tc<<<grid, TC_BLOCK, smem, s>>>((const float2 *)spf_t, dtabf, amat, amat + ae, Q, L, conj, KP, NTILE,
-	                                         (float2 *)out);
+	                                         (float2 *)out, status);
 	return cudaGetLastError();
 }
 
@@ -317,14 +325,4 @@ extern "C" size_t sxsk_rotate_tc_scratch(int L)
 {
 	int N = 2 * L + 1, KP = ((2 * N + 7) / 8) * 8;
 	return (size_t)2 * TC_M * KP;
-}
-
-/* 0 when every block of the tensor-core rotation saw its MMAs finish;
- * resets the flag */
-extern "C" int sxsk_rotate_tc_status(void)
-{
-	int v = 0, z = 0;
-	cudaMemcpyFromSymbol(&v, g_tc_status, sizeof(int));
-	cudaMemcpyToSymbol(g_tc_status, &z, sizeof(int));
-	return v;
 }

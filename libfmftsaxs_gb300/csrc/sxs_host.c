@@ -197,6 +197,7 @@ struct sxsg_plan {
 	int rot_engine;             /* SXSG_ROT_*: rotation on CUDA cores or tensor cores */
 	int tc_used;                /* the last run rotated on the tensor cores */
 	float *d_amat;              /* twiddle operand of the tensor-core rotation */
+	int *d_tcstat;              /* its status word (kernels.h, sxsk_rotate_tc) */
 	int P_valid, U_valid;       /* caller tables already hold this run's rows */
 	int tw_variant; /* -1 none, 0 simple_ft, 1 exact */
 	/* poses */
@@ -262,7 +263,7 @@ void sxsg_plan_destroy(sxsg_plan *p)
 	plan_free_poses(p);
 	pfree(p, p->d_A); pfree(p, p->d_B); pfree(p, p->d_q); pfree(p, p->d_fc); pfree(p, p->d_a); pfree(p, p->d_gtab); pfree(p, p->d_gdf);
 	pfree(p, p->d_c1g); pfree(p, p->d_c2g); pfree(p, p->d_cst); pfree(p, p->d_cstf); pfree(p, p->d_At); pfree(p, p->d_Bt);
-	pfree(p, p->d_tw); pfree(p, p->d_R); pfree(p, p->d_amat);
+	pfree(p, p->d_tw); pfree(p, p->d_R); pfree(p, p->d_amat); pfree(p, p->d_tcstat);
 	if (!p->ext_tables) {
 		pfree(p, p->d_P);
 		pfree(p, p->d_U);
@@ -637,13 +638,15 @@ static int plan_rotations(sxsg_plan *p)
 		int tc = p->fp32 && p->rot_engine == SXSG_ROT_TC && 2 * N <= 128;
 		if (tc && !p->d_amat)
 			SXS_CU(cudaMallocAsync((void **)&p->d_amat, sizeof(float) * sxsk_rotate_tc_scratch(L), s));
+		if (tc && !p->d_tcstat) SXS_CU(cudaMallocAsync((void **)&p->d_tcstat, sizeof(int), s));
+		if (tc) SXS_CU(cudaMemsetAsync(p->d_tcstat, 0, sizeof(int), s));
 		if (!p->ext_tables || !p->P_valid) {
-			if (tc) SXS_K(sxsk_rotate_tc(p->d_At, p->lt->d_dtabf, p->d_tw, Q, L, 0, p->d_P, p->d_amat, s));
+			if (tc) SXS_K(sxsk_rotate_tc(p->d_At, p->lt->d_dtabf, p->d_tw, Q, L, 0, p->d_P, p->d_amat, p->d_tcstat, s));
 			else SXS_K(sxsk_rotate(p->d_At, dtab, p->d_tw, Q, L, 0, p->d_P, p->fp32, s));
 			sxs_count_launches(tc ? 2 : 1);
 		}
 		if (!p->ext_tables || !p->U_valid) {
-			if (tc) SXS_K(sxsk_rotate_tc(p->d_Bt, p->lt->d_dtabf, p->d_tw, Q, L, 1, p->d_U, p->d_amat, s));
+			if (tc) SXS_K(sxsk_rotate_tc(p->d_Bt, p->lt->d_dtabf, p->d_tw, Q, L, 1, p->d_U, p->d_amat, p->d_tcstat, s));
 			else SXS_K(sxsk_rotate(p->d_Bt, dtab, p->d_tw, Q, L, 1, p->d_U, p->fp32, s));
 			sxs_count_launches(tc ? 2 : 1);
 		}
@@ -759,8 +762,16 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 	cudaEventElapsedTime(&t_fit, p->ev[5], end);
 	cudaEventDestroy(end);
 	p->ms[0] = t_tab; p->ms[1] = t_tr; p->ms[2] = t_pc; p->ms[3] = t_fit; p->ms[4] = t_all;
-	if (p->tc_used && sxsk_rotate_tc_status())
-		return sxs_fail(-6, "sxsg_plan_run: the tensor-core rotation did not complete (MMA wait gave up)");
+	if (p->tc_used) {
+		int st = 0;
+		SXS_CU(cudaMemcpyAsync(&st, p->d_tcstat, sizeof(int), cudaMemcpyDeviceToHost, s));
+		SXS_CU(cudaStreamSynchronize(s));
+		if (st == 1)
+			return sxs_fail(-6, "sxsg_plan_run: the tensor-core rotation did not complete (MMA wait gave up)");
+		if (st)
+			return sxs_fail(-7, "sxsg_plan_run: the tensor-core rotation's MMAs did not finish; the CUDA context "
+			                    "is unusable");
+	}
 	return 0;
 }
 

@@ -12,13 +12,19 @@
  *    started as soon as a worker and memory are free, and its kernels
  *    interleave with theirs).  Plans allocate stream-ordered, so one job's
  *    frees never stall another's kernels.
- *  - Rotation tables (receptor P, ligand U) are cached on the device, keyed
- *    by the caller's molecule key, L, the q grid, the twiddle variant and
- *    the precision; a job whose receptor (or ligand) is cached skips that
- *    rotation.  Unreferenced entries are evicted least recently used when
- *    admission needs the memory.
+ *  - Rotation tables (receptor P, ligand U) of molecules with a nonzero
+ *    caller key are cached on the device, keyed by a hash of the
+ *    coefficients themselves, the caller's key, L, the q grid, the twiddle
+ *    variant and the precision; a job whose receptor (or ligand) table is
+ *    cached and complete skips that rotation.  A table is shared only once
+ *    the job that filled it has finished on the device (its stream was
+ *    synchronised before the entry is marked valid); a job that finds its
+ *    table still being filled by another running job fills a private copy.
+ *    Unreferenced entries are evicted least recently used when admission
+ *    needs the memory.
  *  - Results are bitwise those of the same job run alone: every kernel is
- *    deterministic and jobs share no mutable device state.
+ *    deterministic, and the only device state jobs share is complete
+ *    rotation tables that they read and never write.
  */
 #define _XOPEN_SOURCE 700
 #include <pthread.h>
@@ -36,7 +42,7 @@ typedef struct sxs_job {
 	int64_t n;
 	double mult, peak;
 	uint64_t keyA, keyB;
-	uint64_t kP, kU;            /* rotation-table cache keys */
+	uint64_t kP, kU;            /* rotation-table cache keys (0: not cached) */
 	size_t bytes, rbudget, tbytes;
 	double t_submit, t_start, t_end;
 	double *chi, *c1, *c2;
@@ -50,7 +56,8 @@ typedef struct sxs_tentry {
 	uint64_t key;
 	void *d;
 	size_t bytes;
-	int valid, refs, priv;
+	int valid;                  /* filled by a job that has finished on the device */
+	int refs, priv;
 	uint64_t stamp;
 	struct sxs_tentry *next;
 } sxs_tentry;
@@ -93,21 +100,50 @@ static uint64_t fnv(uint64_t h, const void *p, size_t n)
 	return h;
 }
 
-static uint64_t table_key(uint64_t mol, int role, const sxs_job *j)
+/* 64-bit digest of n doubles, word by word (multiply-xorshift mixing) */
+static uint64_t digest(const double *x, size_t n)
 {
+	uint64_t h = 0x243f6a8885a308d3ull ^ (uint64_t)n;
+	for (size_t i = 0; i < n; i++) {
+		uint64_t w;
+		memcpy(&w, x + i, sizeof(w));
+		h ^= w;
+		h *= 0x9e3779b97f4a7c15ull;
+		h ^= h >> 29;
+	}
+	return h;
+}
+
+/* Cache key of a rotation table: the coefficients' digest (so a reused
+ * caller key with other coefficients never aliases), the caller's key, the
+ * role (P or U) and everything else the table depends on.  0 = not cached. */
+static uint64_t table_key(uint64_t mol, int role, const sxs_job *j, const double *coef)
+{
+	if (!mol) return 0;
+	int K = j->L + 1;
 	uint64_t h = 1469598103934665603ull;
 	int v[5] = {role, j->L, j->Q, j->skip == 1, j->precision};
+	uint64_t d = digest(coef, (size_t)3 * j->Q * K * K * 2);
 	h = fnv(h, &mol, sizeof(mol));
+	h = fnv(h, &d, sizeof(d));
 	h = fnv(h, v, sizeof(v));
 	h = fnv(h, j->q, sizeof(double) * j->Q);
 	return h ? h : 1;
 }
 
+/* a shared entry of this key, complete or still being filled */
 static sxs_tentry *cache_find(sxsg_server *s, uint64_t key)
 {
 	for (sxs_tentry *e = s->cache; e; e = e->next)
 		if (e->key == key && !e->priv) return e;
 	return NULL;
+}
+
+/* a shared entry of this key that a job may read */
+static sxs_tentry *cache_find_valid(sxsg_server *s, uint64_t key)
+{
+	sxs_tentry *e = key ? cache_find(s, key) : NULL;
+	return e && e->valid ? e : NULL;
 }
 
 /* free unreferenced entries, least recently used first, until `need` more
@@ -130,28 +166,34 @@ static int cache_make_room(sxsg_server *s, size_t need, cudaStream_t st)
 	return 1;
 }
 
-/* bytes a job adds beyond its own footprint: its cache misses */
+/* bytes a job adds beyond its own footprint: the tables it must fill */
 static size_t job_table_need(sxsg_server *s, const sxs_job *j)
 {
 	size_t need = 0;
-	if (!j->keyA || !cache_find(s, j->kP)) need += j->tbytes;
-	if (!j->keyB || !cache_find(s, j->kU)) need += j->tbytes;
+	if (!cache_find_valid(s, j->kP)) need += j->tbytes;
+	if (!cache_find_valid(s, j->kU)) need += j->tbytes;
 	return need;
 }
 
-static sxs_tentry *cache_acquire(sxsg_server *s, uint64_t mol, uint64_t key, size_t bytes, cudaStream_t st, int *err)
+/* A table for a job: a complete shared entry (read only), else a new one
+ * that this job fills.  The new entry is shared (others find it once it is
+ * valid) unless the key is 0 or a shared entry of the key is already being
+ * filled by another running job, whose rotation may still be in flight on
+ * its own stream: then the new entry is private to this job. */
+static sxs_tentry *cache_acquire(sxsg_server *s, uint64_t key, size_t bytes, cudaStream_t st, int *err)
 {
-	sxs_tentry *e = mol ? cache_find(s, key) : NULL;
+	sxs_tentry *e = cache_find_valid(s, key);
 	if (e) {
 		e->refs++;
 		e->stamp = ++s->clock;
 		s->hits++;
 		return e;
 	}
+	int priv = key == 0 || cache_find(s, key) != NULL;
 	s->misses++;
 	e = calloc(1, sizeof(*e));
-	e->key = mol ? key : ++s->priv_key;
-	e->priv = mol == 0;
+	e->key = priv ? ++s->priv_key : key;
+	e->priv = priv;
 	e->bytes = bytes;
 	e->refs = 1;
 	e->stamp = ++s->clock;
@@ -168,6 +210,9 @@ static sxs_tentry *cache_acquire(sxsg_server *s, uint64_t mol, uint64_t key, siz
 	return e;
 }
 
+/* Called after the job's stream was synchronised: a table it filled is
+ * complete on the device, so marking it valid lets jobs on other streams
+ * read it without further ordering. */
 static void cache_release(sxsg_server *s, sxs_tentry *e, int valid, cudaStream_t st)
 {
 	if (!e) return;
@@ -237,8 +282,8 @@ static void *worker(void *arg)
 		j->status = 1;
 		j->t_start = now_ms();
 		int err = 0;
-		sxs_tentry *tp = cache_acquire(s, j->keyA, j->kP, j->tbytes, st, &err);
-		sxs_tentry *tu = tp ? cache_acquire(s, j->keyB, j->kU, j->tbytes, st, &err) : NULL;
+		sxs_tentry *tp = cache_acquire(s, j->kP, j->tbytes, st, &err);
+		sxs_tentry *tu = tp ? cache_acquire(s, j->kU, j->tbytes, st, &err) : NULL;
 		pthread_mutex_unlock(&s->mu);
 		int P_ok = 0, U_ok = 0;
 		if (tp && tu) {
@@ -335,8 +380,8 @@ int64_t sxsg_server_submit(sxsg_server *s, const sxsg_request *r)
 	j->fit_mode = r->fit_mode; j->precision = r->precision; j->n = r->n; j->mult = r->mult; j->peak = r->peak;
 	j->keyA = r->keyA;
 	j->keyB = r->keyB;
-	j->kP = table_key(r->keyA, 0, j);
-	j->kU = table_key(r->keyB, 1, j);
+	j->kP = table_key(r->keyA, 0, j, j->A);
+	j->kU = table_key(r->keyB, 1, j, j->B);
 	size_t n = r->n > 0 ? (size_t)r->n : 1;
 	j->chi = malloc(sizeof(double) * n);
 	j->c1 = malloc(sizeof(double) * n);

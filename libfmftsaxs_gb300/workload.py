@@ -39,6 +39,55 @@ class Workload:
     pass
 
 
+def config(name="c1", overrides=None):
+    """The configuration dict of a named workload, with optional changes."""
+    cfg = dict(CONFIGS[name])
+    if overrides:
+        cfg.update(overrides)
+    return cfg
+
+
+def molecules(cfg, seed=2026):
+    """Receptor (centred at its centre of extrema) and ligand (centred at its
+    centroid) of a configuration, with their accessible fractions."""
+    rec = synth.make_molecule(cfg["rec"][0], cfg["rec"][1], seed)
+    lig = synth.make_molecule(cfg["lig"][0], cfg["lig"][1], seed + 1)
+    rec = rec.translated(-rec.center_of_extrema()).with_sasa()
+    lig = lig.translated(-lig.centroid()).with_sasa()
+    return rec, lig
+
+
+def native_complex(rec, lig, cfg, seed=2026):
+    """The seeded native pose of the joined complex (centred at its centroid,
+    with accessible fractions) and the generator that then draws the
+    experiment's noise."""
+    rng = np.random.default_rng(seed + 7)
+    Rn = synth.random_rotations(1, rng)[0]
+    Tn = synth.random_translations(1, cfg["t"][0], cfg["t"][1], rng)[0]
+    native = synth.join(rec, synth.Molecule(lig.xyz @ Rn.T + Tn, lig.elements))
+    native = native.translated(-native.centroid()).with_sasa()
+    return native, rng
+
+
+def zvals(cfg):
+    """Translation grid: integer z covering the configuration's |t| range."""
+    t = cfg["t"]
+    return np.arange(np.floor(t[0]), np.ceil(t[1]) + 1.0)
+
+
+def pose_lists(cfg, seed, to_indices, z, L):
+    """Packed grid indices of the configuration's seeded pose lists, in list
+    order; to_indices(R, T, z, L) -> (index, keep) converts one list."""
+    idx = []
+    for k, n in enumerate(cfg["lists"]):
+        r = np.random.default_rng(seed + 100 + k)
+        R = synth.random_rotations(n, r)
+        T = synth.random_translations(n, cfg["t"][0], cfg["t"][1], r)
+        ii, keep = to_indices(R, T, z, L)
+        idx.append(np.asarray(ii, dtype=np.int64))
+    return np.concatenate(idx)
+
+
 def build(name="c1", seed=2026, lib=None, expand=None, profile=None, to_indices=None, overrides=None):
     """Assemble a workload.  `lib` is the libfmftsaxs_gb300 module; the
     callables default to it (expansion on the GPU, profile and pose
@@ -46,9 +95,7 @@ def build(name="c1", seed=2026, lib=None, expand=None, profile=None, to_indices=
     if lib is None:
         import importlib
         lib = importlib.import_module(__package__)
-    cfg = dict(CONFIGS[name])
-    if overrides:
-        cfg.update(overrides)
+    cfg = config(name, overrides)
     expand = expand or lib.expand
     profile = profile or lib.profile_from_spf
     to_indices = to_indices or (lambda R, T, z, L: lib.poses_to_indices(R, T, z, L))
@@ -56,10 +103,7 @@ def build(name="c1", seed=2026, lib=None, expand=None, profile=None, to_indices=
     w = Workload()
     w.name, w.L, w.Q = name, L, Q
     w.q = lib.mkarray(0.0, cfg["qmax"], Q)
-    rec = synth.make_molecule(cfg["rec"][0], cfg["rec"][1], seed)
-    lig = synth.make_molecule(cfg["lig"][0], cfg["lig"][1], seed + 1)
-    rec = rec.translated(-rec.center_of_extrema()).with_sasa()
-    lig = lig.translated(-lig.centroid()).with_sasa()
+    rec, lig = molecules(cfg, seed)
     water = lib.ff_water()
     vr, dr = form_factors(lib, rec)
     vl, dl = form_factors(lib, lig)
@@ -68,12 +112,8 @@ def build(name="c1", seed=2026, lib=None, expand=None, profile=None, to_indices=
     w.rmA, w.rmB = float(np.mean(rec.radius)), float(np.mean(lig.radius))
     w.rm = (w.rmA * rec.natoms + w.rmB * lig.natoms) / (rec.natoms + lig.natoms)
     w.rec, w.lig = rec, lig
-    rng = np.random.default_rng(seed + 7)
     # native pose and its noisy single-molecule profile
-    Rn = synth.random_rotations(1, rng)[0]
-    Tn = synth.random_translations(1, cfg["t"][0], cfg["t"][1], rng)[0]
-    native = synth.join(rec, synth.Molecule(lig.xyz @ Rn.T + Tn, lig.elements))
-    native = native.translated(-native.centroid()).with_sasa()
+    native, rng = native_complex(rec, lig, cfg, seed)
     vn, dn = form_factors(lib, native)
     C = expand(native.xyz, vn, dn, native.sasa, water, w.q, L)
     rmC = float(np.mean(native.radius))
@@ -81,15 +121,8 @@ def build(name="c1", seed=2026, lib=None, expand=None, profile=None, to_indices=
     w.exp = synth.noisy_experiment(w.q, I, 0.01, rng)
     w.a, w.mult, w.peak = lib.bin_experiment(w.exp[0], w.exp[1], w.exp[2], w.q, w.rm)
     # poses
-    w.z = np.arange(np.floor(cfg["t"][0]), np.ceil(cfg["t"][1]) + 1.0)
-    idx = []
-    for k, n in enumerate(cfg["lists"]):
-        r = np.random.default_rng(seed + 100 + k)
-        R = synth.random_rotations(n, r)
-        T = synth.random_translations(n, cfg["t"][0], cfg["t"][1], r)
-        ii, keep = to_indices(R, T, w.z, L)
-        idx.append(np.asarray(ii, dtype=np.int64))
-    w.index = np.concatenate(idx)
+    w.z = zvals(cfg)
+    w.index = pose_lists(cfg, seed, to_indices, w.z, L)
     w.c1g, w.c2g = synth.C1_GRID, synth.C2_GRID
     return w
 

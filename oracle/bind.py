@@ -15,7 +15,21 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libsxsref.so")
-REF_SRC = "/root/reference"
+# Root of the reference project's source tree (read-only), given by the
+# environment; without it the checker library is only loaded if an earlier
+# build left it in oracle/_ref/.
+REF_SRC = os.environ.get("FMFTSAXS_REFERENCE_SRC", "")
+
+
+def have_ref_src():
+    """Whether the reference sources are available to build the checker."""
+    return bool(REF_SRC) and os.path.isdir(os.path.join(REF_SRC, "src"))
+
+
+def have_ref():
+    """Whether the checker library exists or can be built."""
+    return have_ref_src() or os.path.exists(REF_SO)
+
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
@@ -31,9 +45,10 @@ def build_oracle(force=False):
 
 
 def build_ref():
-    """Compile the reference's own sources with the shims (needs the reference tree)."""
-    if not os.path.isdir(REF_SRC):
-        return None
+    """Compile the reference's own sources with the shims (needs the
+    reference tree); without it, return an earlier build if there is one."""
+    if not have_ref_src():
+        return REF_SO if os.path.exists(REF_SO) else None
     subprocess.check_call(["make", "-s", "-f", "Makefile.ref", "REF=" + REF_SRC], cwd=HERE)
     return REF_SO
 
@@ -184,7 +199,8 @@ class Oracle:
 
 class Ref:
     """The reference's own code (checker build).  Available only where the
-    reference tree exists (this container), never on the GPU host."""
+    reference sources were given (FMFTSAXS_REFERENCE_SRC) or an earlier build
+    of them is present; the GPU test machines have neither."""
 
     def __init__(self):
         so = build_ref()

@@ -2,7 +2,7 @@
  * CPU oracle for the libfmftsaxs FFT-correlation scoring path.
  * TEST INFRASTRUCTURE ONLY (see oracle.h): the checker, never the product.
  *
- * Build: oracle/build_oracle.py (gcc -std=c11 -O2 -ffp-contract=off).
+ * Build: oracle/bind.py, build_oracle() (gcc -std=c11 -O2 -ffp-contract=off).
  */
 #include "oracle.h"
 

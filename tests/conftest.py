@@ -37,7 +37,7 @@ def gpu(lib):
 
 @pytest.fixture(scope="session")
 def ref():
-    from oracle.bind import Ref, REF_SRC
-    if not os.path.isdir(REF_SRC):
-        pytest.skip("reference sources not present on this host")
+    from oracle.bind import Ref, have_ref
+    if not have_ref():
+        pytest.skip("no reference build: set FMFTSAXS_REFERENCE_SRC to the reference source tree")
     return Ref()

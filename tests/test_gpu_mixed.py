@@ -22,7 +22,7 @@ from test_gpu_parity import _random_case, chan_err, load
 
 pytestmark = pytest.mark.gpu
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "dimer_*.npz")))
 CHI_TOL = 1e-4
 CROSS_TOL = 1e-5
 

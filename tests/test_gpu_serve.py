@@ -13,7 +13,7 @@ from test_gpu_parity import _random_case, load
 
 pytestmark = pytest.mark.gpu
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "dimer_*.npz")))
 
 
 def _jobs(oracle):
@@ -97,3 +97,55 @@ def test_failing_job_is_isolated(gpu, oracle):
     good = srv.wait(tg)
     srv.close()
     np.testing.assert_array_equal(good["chi"], _alone(gpu, jobs[1])["chi"])
+
+
+def _same_molecule_base(g, keyA, keyB, precision):
+    return dict(A=g["A"], B=g["B"], qvals=g["q"], zvals=g["z"], L=int(g["L"]), a=g["a"], mult=float(g["mult"]),
+                peak=float(g["peak"]), c1grid=g["c1g"], c2grid=g["c2g"], skip=1, precision=precision, keyA=keyA,
+                keyB=keyB)
+
+
+def test_same_molecule_jobs_at_once_match_alone(gpu, oracle):
+    """Jobs with the same receptor and ligand submitted together, three on
+    the device at once: the first fills the shared tables while the others,
+    finding them still being filled, fill private copies; jobs admitted
+    later read the completed tables.  Every result is bitwise the job run
+    alone, over repeated rounds and both precisions."""
+    g = load(GOLDEN[-1])
+    idx = g["index"]
+    subsets = [idx, idx[::2], idx[1::3], idx[::-1].copy(), idx[5:], idx[:40]]
+    jobs = [dict(_same_molecule_base(g, 21, 22, prec), index=s) for prec in (1, 0) for s in subsets]
+    alone = [_alone(gpu, j)["chi"] for j in jobs]
+    srv = gpu.Server(max_active=3)
+    for _ in range(3):
+        tickets = [srv.submit(**j) for j in jobs]
+        for t, a in zip(tickets, alone):
+            np.testing.assert_array_equal(srv.wait(t)["chi"], a)
+    st = srv.stats()
+    srv.close()
+    # two tables per precision are shared; later rounds hit them
+    assert st["cache_entries"] == 4
+    assert st["cache_hits"] >= 2 * len(jobs)
+
+
+def test_reused_key_with_other_coefficients_does_not_alias(gpu, oracle):
+    """A caller key reused for a different molecule (same L and q grid)
+    gets that molecule's own tables: the cache key covers the coefficients."""
+    g = load(GOLDEN[-1])
+    base = _same_molecule_base(g, 41, 42, 1)
+    other = dict(base, A=g["A"] * 0.75, B=g["B"][::-1].copy())
+    j1, j2 = dict(base, index=g["index"]), dict(other, index=g["index"])
+    a1, a2 = _alone(gpu, j1)["chi"], _alone(gpu, j2)["chi"]
+    assert not np.array_equal(a1, a2)
+    srv = gpu.Server(max_active=2)
+    r1 = srv.wait(srv.submit(**j1))
+    r2 = srv.wait(srv.submit(**j2))
+    t = [srv.submit(**j) for j in (j1, j2, j2, j1)]
+    rr = [srv.wait(x)["chi"] for x in t]
+    st = srv.stats()
+    srv.close()
+    np.testing.assert_array_equal(r1["chi"], a1)
+    np.testing.assert_array_equal(r2["chi"], a2)
+    for got, want in zip(rr, (a1, a2, a2, a1)):
+        np.testing.assert_array_equal(got, want)
+    assert st["cache_entries"] == 4

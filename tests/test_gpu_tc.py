@@ -12,7 +12,7 @@ from test_gpu_parity import _random_case, chan_err, load
 
 pytestmark = pytest.mark.gpu
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "dimer_*.npz")))
 
 
 def _both(gpu, A, B, q, z, L, a, mult, peak, idx, skip=1):

@@ -8,7 +8,7 @@ import os
 import numpy as np
 import pytest
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "dimer_*.npz")))
 
 
 def load(path):
@@ -79,24 +79,21 @@ def test_profile_from_spf_matches_oracle(lib, oracle, path):
         np.testing.assert_array_equal(e1, e2)
 
 
-def test_form_factor_constants(lib, ref):
-    names = ["C", "N", "O", "S", "CH", "CH2", "CH3", "NH", "NH2", "NH3", "OH", "SH", "P", "H"]
-    mp = os.path.join("/root/reference/prms", "pdb_formfactor_mapping_clean.prm")
-    # residue/atom pairs of the mapping file that resolve to each type
-    pairs = {"C": ("ALA", "C"), "N": ("ALA", "N"), "O": ("ALA", "O"), "S": ("MET", "SD"), "CH": ("ALA", "CA"),
-             "CH3": ("ALA", "CB"), "CH2": ("ARG", "CB"), "H": ("ALA", "H")}
-    for t, (r, a) in pairs.items():
-        v, d, h2o, bad = ref.ff_lookup(mp, [r], [a])
-        assert bad == 0
-        assert lib.ff_type(t) == (v[0], d[0])
-        assert lib.ff_water() == h2o
-    v, d, missing = lib.ff_lookup(mp, [p[0] for p in pairs.values()] + ["XXX"], [p[1] for p in pairs.values()] + ["Q"])
-    assert missing == 1 and np.isnan(v[-1])
-    for k, t in enumerate(pairs):
-        assert (v[k], d[k]) == lib.ff_type(t)
+def test_form_factor_constants(lib):
+    """Per-type constants against the reference's get_ff on its own mapping
+    file (captured in tests/golden/ref_4g9s.npz by make_refdata.py)."""
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_4g9s.npz"), allow_pickle=False))
+
+    def names(a):
+        return [bytes(r).rstrip(b"\0").decode() for r in a]
+
+    types, res, atom = names(g["ff_types"]), names(g["ff_res"]), names(g["ff_atom"])
+    for k, t in enumerate(types):
+        assert lib.ff_type(t) == (g["ff_vac"][k], g["ff_dum"][k])
+    assert lib.ff_water() == float(g["h2o"])
     with pytest.raises(KeyError):
         lib.ff_type("UNOBTAINIUM")
-    assert len(names) > 0
+    assert len(res) == len(atom) == len(types)
 
 
 def test_ff_lookup_with_written_mapping(lib, tmp_path):

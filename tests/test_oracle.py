@@ -8,7 +8,7 @@ import os
 import numpy as np
 import pytest
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "dimer_*.npz")))
 
 
 def load(path):
@@ -130,52 +130,28 @@ def test_pose_conversion_bit_exact_vs_reference(oracle, ref):
 
 
 # ------------------------------------------------------- the reference's own tests
-REF_DATA = "/root/reference/tests/data"
+def ref_4g9s():
+    """The reference's test data (tests/golden/make_refdata.py)."""
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_4g9s.npz"), allow_pickle=False))
+    L, Q = int(g["spf_L"]), int(g["spf_Q"])
+    vals = g["spf_mant"].astype(np.float64) * 10.0 ** g["spf_exp"].astype(np.float64)
+    g["ref_spf"] = vals.reshape(Q, (L + 1) ** 2, 6)
+    return g
 
 
-def _read_pdb(path):
-    xyz, res, atom = [], [], []
-    with open(path) as f:
-        for line in f:
-            if line.startswith(("ATOM", "HETATM")):
-                atom.append(line[12:16].strip())
-                res.append(line[17:21].strip())
-                xyz.append([float(line[30:38]), float(line[38:46]), float(line[46:54])])
-    return np.array(xyz), res, atom
-
-
-def _read_prm_radii(path):
-    rad = {}
-    with open(path) as f:
-        for line in f:
-            p = line.split()
-            if len(p) >= 7 and p[0] == "atom":
-                rad[(p[2], p[3])] = float(p[5])
-    return rad
-
-
-@pytest.mark.skipif(not os.path.isdir(REF_DATA), reason="reference test data not present")
-def test_expansion_pinned_to_reference_ref_spf(oracle, ref):
+def test_expansion_pinned_to_reference_ref_spf(oracle):
     """The reference's test_pdb2spf (tests/saxs_test.c:59-127): A_lm of the
     4g9s receptor, L = 15, 50 q, against tests/data/ref_spf at 1e-3
     relative.  The V and D channels depend only on coordinates, radii and
     form factors; W also needs libmol2's accessible areas (absent here), so
     the W channel is not pinned by this file."""
-    xyz, res, atom = _read_pdb(os.path.join(REF_DATA, "4g9s_r_native.pdb"))
-    rad = _read_prm_radii(os.path.join(REF_DATA, "atoms.0.0.6.prm.ms.3cap+0.5ace.Hr0rec"))
-    vdw = np.array([rad.get((r, a), np.nan) for r, a in zip(res, atom)])
-    xyz = xyz - 0.5 * (xyz.min(0) + xyz.max(0))
-    vac, dum, h2o, bad = ref.ff_lookup(os.path.join(REF_DATA, "pdb_formfactor_mapping_clean.prm"), res, atom)
-    assert bad == 0
-    q = oracle.mkarray(0.0, 0.5, 50)
-    L = 15
-    A = oracle.expand(xyz, vac, dum, None, h2o, q, L).reshape(3, 50, (L + 1) ** 2, 2)
-    with open(os.path.join(REF_DATA, "ref_spf")) as f:
-        hdr = f.readline().split()
-        gold = np.loadtxt(f).reshape(50, (L + 1) ** 2, 6)
-    assert int(hdr[0]) == L and int(hdr[1]) == 50
-    assert np.isfinite(vdw).all()
-    assert round(oracle.average_radius(vdw), 4) == pytest.approx(float(hdr[2]), abs=1e-4)
+    g = ref_4g9s()
+    L, Q = int(g["spf_L"]), int(g["spf_Q"])
+    q = oracle.mkarray(0.0, 0.5, Q)
+    A = oracle.expand(g["rec_xyz"], g["rec_vac"], g["rec_dum"], None, float(g["h2o"]), q, L)
+    A = A.reshape(3, Q, (L + 1) ** 2, 2)
+    gold = g["ref_spf"]
+    assert round(oracle.average_radius(g["rec_vdw"]), 4) == pytest.approx(float(g["spf_rm_text"]), abs=1e-4)
     for ch in (0, 1):
         for part in (0, 1):
             got = A[ch, :, :, part]
@@ -186,3 +162,27 @@ def test_expansion_pinned_to_reference_ref_spf(oracle, ref):
             # "% .4e" rounding alone is up to 5e-5
             assert rel.max() <= 1e-4
             assert np.all(np.abs(got[~both] - want[~both]) <= 1e-6)
+
+
+# ------------------------------------------- fixtures at the benchmark shapes
+@pytest.mark.parametrize("name", ["c0_shape", "c1_shape"])
+def test_oracle_matches_reference_at_benchmark_shape(oracle, name):
+    """The restatement against the reference's outputs at the benchmark
+    shapes (tests/golden/make_golden.py): expansion of the stored atoms
+    against the sampled A_lm, B_lm, and the scoring of the detail poses (the
+    fixture's first three triples, which the reference scores on its
+    simple_ft branch) against their raw cross terms and chi^2 grids."""
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"), allow_pickle=False))
+    L, q, h2o = int(g["L"]), g["q"], float(g["h2o"])
+    A = oracle.expand(g["rec_xyz"], g["rec_vac"], g["rec_dum"], g["rec_sasa"], h2o, q, L)
+    B = oracle.expand(g["lig_xyz"], g["lig_vac"], g["lig_dum"], g["lig_sasa"], h2o, q, L)
+    for full, at, want in ((A, g["A_at"], g["A_val"]), (B, g["B_at"], g["B_val"])):
+        np.testing.assert_allclose(full[at], want, rtol=1e-12, atol=1e-12 * np.abs(want).max())
+    d = g["detail"]
+    assert not g["branch"][d].any()
+    raw, scl, grid, br = oracle.score(A, B, q, g["z"], L, g["index"][d], 1, float(g["peak"]), g["a"],
+                                      float(g["mult"]), g["c1g"], g["c2g"])
+    assert chan_err(raw, g["raw"]) <= 1e-13
+    np.testing.assert_allclose(grid, g["grid"], rtol=1e-10, atol=0)
+    cell = grid.reshape(len(d), -1).argmin(axis=1)
+    np.testing.assert_array_equal(cell, g["cell"][d])

@@ -66,6 +66,15 @@ def test_noalloc_expansion_matches_regular_entry_twice(gpu):
         assert chan_err(got, want, Q) <= TOL
         if not with_water:
             assert np.all(got.reshape(3, -1)[2] == 0.0)
+    # another L next: every call rewrites the norm table it shares
+    L2, Q2 = 7, 9
+    q2 = gpu.mkarray(0.0, 0.4, Q2)
+    mol = mols[0][0]
+    ff = np.array([gpu.ff_type(e) for e in mol.elements])
+    want = gpu.expand(mol.xyz, ff[:, 0], ff[:, 1], mol.sasa, water, q2, L2)
+    rc, got = _call_noalloc(gpu, torch, mol.xyz, ff[:, 0], ff[:, 1], water * mol.sasa, q2, L2)
+    assert rc == 0
+    assert chan_err(got, want, Q2) <= TOL
 
 
 def test_noalloc_rejects_requests_beyond_the_static_array(gpu):
