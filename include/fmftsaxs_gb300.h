@@ -179,6 +179,31 @@ double sxsg_ff_water(void);
 int sxsg_ff_lookup(const char *mapping_path, const char *res8, const char *atom8, int n,
                    double *vacuum_ff, double *dummy_ff);
 
+/* Zero-angle form factors (zero_ff, vacuum_ff, dummy_ff; any may be NULL)
+ * of form-factor type `type`, the index of the reference's enum
+ * saxs_ff_type (0 = H ... 41 = s_OH2, 42 = SH; src/form_factor_table.h:27-37,
+ * values src/form_factor_table.c:8-49).  Returns 0, or -2 for a type
+ * outside [0, 43). */
+int sxsg_ff_constants(int type, double *zero_ff, double *vacuum_ff, double *dummy_ff);
+/* The mapping-file name of a type ("C", "CH2", "SOD+", ...), NULL for types
+ * that no mapping line can select (ff_type_to_string,
+ * src/form_factor_table.c:109-136). */
+const char *sxsg_ff_name(int type);
+
+/* A (residue, atom) -> form-factor type map read from a mapping file in the
+ * reference's format (default_ff_table, src/form_factor_table.c:138-188):
+ * '#' and blank lines skipped, "residue atom type" per line, a later line
+ * for the same pair replacing an earlier one.  NULL on error
+ * (sxsg_last_error). */
+typedef struct sxsg_ff_map sxsg_ff_map;
+#define SXSG_FF_UNKNOWN 99   /* s_UNK: the line names a type the reference does not know */
+sxsg_ff_map *sxsg_ff_map_load(const char *mapping_path);
+/* Type of one atom: the names are trimmed as get_ff does (leading blanks
+ * skipped, up to the next blank, at most 7 characters); returns the type
+ * index, SXSG_FF_UNKNOWN, or -1 when the pair has no mapping line. */
+int sxsg_ff_map_type(const sxsg_ff_map *map, const char *residue, const char *atom);
+void sxsg_ff_map_free(sxsg_ff_map *map);
+
 /* A_lm(q) of one molecule on the GPU (atom_grp2spf_inplace, src/pdb2spf.c:24-152)
  * from arrays: coordinates xyz[3n] (already centred), per-atom vacuum and
  * excluded-volume form factors, per-atom accessible fraction sasa (NULL:

@@ -674,84 +674,204 @@ double sxs_sbessel(int order, double x) { return sxs_sbessel_host(order, x); }
 
 /* ====================================================== form factors */
 
-/* Zero-angle form factors of the types the reference's mapping file can
- * name (src/form_factor_table.c:8-49 for the values, 76-107 for the names):
- * vacuum and excluded-volume ("dummy") factors. */
-static const struct { const char *name; double vacuum, dummy; } k_ff[] = {
-	{"H", 0.999953, 1.7201},   {"HE", 0.999872, 1.7201}, {"C", 5.9992, 5.49096},   {"N", 6.9946, 0.83166},
-	{"O", 7.9994, 3.04942},    {"NE", 9.999, 3.006},     {"SOD+", 10.9924, 3.006}, {"MG2+", 11.9865, 3.006},
-	{"P", 14.9993, 1.91382},   {"S", 15.9998, 6.63324},  {"K", 18.99, 3.006},      {"CAL2+", 18.0025, 3.006},
-	{"FE2+", 24.0006, 3.006},  {"ZN2+", 27.9996, 3.006}, {"SE", 33.99, 3.006},     {"AU", 78.9572, 6.63324},
-	{"CH", 6.99915, 7.21106},  {"CH2", 7.99911, 8.93116}, {"CH3", 8.99906, 10.6513}, {"NH", 7.99455, 2.55176},
-	{"NH2", 8.99451, 4.27186}, {"NH3", 9.99446, 5.99196}, {"OH", 8.99935, 4.76952}, {"SH", 16.9998, 8.35334},
+/* Zero-angle form factors of the reference's 43 form-factor types, by the
+ * index of its enum saxs_ff_type (src/form_factor_table.h:27-37; values
+ * src/form_factor_table.c:8-49): zero_ff, vacuum_ff and excluded-volume
+ * ("dummy") factor, with the name that the mapping file uses for the type
+ * (src/form_factor_table.c:76-107; NULL for types no mapping line can
+ * select). */
+static const struct { const char *name; double zero, vacuum, dummy; } k_ff[SXS_FF_NTYPES] = {
+	{"H", -0.720147, 0.999953, 1.7201},     {"HE", -0.720228, 0.999872, 1.7201},
+	{NULL, 1.591, 2.99, 1.399},             {NULL, 2.591, 3.99, 1.399},
+	{NULL, 3.591, 4.99, 1.399},             {"C", 0.50824, 5.9992, 5.49096},
+	{"N", 6.16294, 6.9946, 0.83166},        {"O", 4.94998, 7.9994, 3.04942},
+	{NULL, 7.591, 8.99, 1.399},             {"NE", 6.993, 9.999, 3.006},
+	{"SOD+", 7.9864, 10.9924, 3.006},       {"MG2+", 8.9805, 11.9865, 3.006},
+	{NULL, 9.984, 12.99, 3.006},            {NULL, 10.984, 13.99, 3.006},
+	{"P", 13.0855, 14.9993, 1.91382},       {"S", 9.36656, 15.9998, 6.63324},
+	{NULL, 13.984, 16.99, 3.006},           {NULL, 16.591, 17.99, 1.399},
+	{"K", 15.984, 18.99, 3.006},            {"CAL2+", 14.9965, 18.0025, 3.006},
+	{NULL, 20.984, 23.99, 3.006},           {NULL, 21.984, 24.99, 3.006},
+	{"FE2+", 20.9946, 24.0006, 3.006},      {NULL, 23.984, 26.99, 3.006},
+	{NULL, 24.984, 27.99, 3.006},           {NULL, 25.984, 28.99, 3.006},
+	{"ZN2+", 24.9936, 27.9996, 3.006},      {"SE", 30.9825, 33.99, 3.006},
+	{NULL, 31.984, 34.99, 3.006},           {NULL, 49.16, 52.99, 3.83},
+	{NULL, 70.35676, 76.99, 6.63324},       {NULL, 71.35676, 77.99, 6.63324},
+	{"AU", 72.324, 78.9572, 6.63324},       {NULL, 73.35676, 79.99, 6.63324},
+	{"CH", -0.211907, 6.99915, 7.21106},    {"CH2", -0.932054, 7.99911, 8.93116},
+	{"CH3", -1.6522, 8.99906, 10.6513},     {"NH", 5.44279, 7.99455, 2.55176},
+	{"NH2", 4.72265, 8.99451, 4.27186},     {"NH3", 4.0025, 9.99446, 5.99196},
+	{"OH", 4.22983, 8.99935, 4.76952},      {NULL, 3.50968, 9.9993, 6.48962},
+	{"SH", 8.64641, 16.9998, 8.35334},
 };
-/* zero_ff of OH2, the hydration-shell weight (src/pdb2spf.c:41-43) */
-#define SXS_WATER_FF 3.50968
+/* the hydration-shell weight: zero_ff of OH2 (src/pdb2spf.c:41-43) */
+#define SXS_FF_OH2 41
 
-double sxsg_ff_water(void) { return SXS_WATER_FF; }
+double sxsg_ff_water(void) { return k_ff[SXS_FF_OH2].zero; }
+
+/* type index of a mapping file's type name, SXSG_FF_UNKNOWN for other names
+ * (string_to_ff_type compares the name as written: case-sensitive) */
+static int ff_type_index(const char *name)
+{
+	for (int i = 0; i < SXS_FF_NTYPES; i++)
+		if (k_ff[i].name && !strcmp(name, k_ff[i].name)) return i;
+	return SXSG_FF_UNKNOWN;
+}
+
+int sxsg_ff_constants(int type, double *zero_ff, double *vacuum_ff, double *dummy_ff)
+{
+	if (type < 0 || type >= SXS_FF_NTYPES) return sxs_fail(-2, "sxsg_ff_constants: type %d out of range", type);
+	if (zero_ff) *zero_ff = k_ff[type].zero;
+	if (vacuum_ff) *vacuum_ff = k_ff[type].vacuum;
+	if (dummy_ff) *dummy_ff = k_ff[type].dummy;
+	return 0;
+}
+
+const char *sxsg_ff_name(int type)
+{
+	return type >= 0 && type < SXS_FF_NTYPES ? k_ff[type].name : NULL;
+}
 
 int sxsg_ff_type(const char *name, double *vac, double *dum)
 {
 	if (!name) return -1;
-	for (size_t i = 0; i < sizeof(k_ff) / sizeof(k_ff[0]); i++)
-		if (!strcmp(name, k_ff[i].name)) {
-			if (vac) *vac = k_ff[i].vacuum;
-			if (dum) *dum = k_ff[i].dummy;
-			return 0;
-		}
-	return -1;
+	int t = ff_type_index(name);
+	if (t == SXSG_FF_UNKNOWN) return -1;
+	if (vac) *vac = k_ff[t].vacuum;
+	if (dum) *dum = k_ff[t].dummy;
+	return 0;
 }
 
-typedef struct { char res[8], atom[8]; int type; } ff_entry;
+/* ------------------------------------------- (residue, atom) -> type map
+ * Open-addressing hash of the mapping file's lines; a later line for the
+ * same key replaces an earlier one (kh_put then kh_value). */
+typedef struct { char res[8], atom[8]; int type; int used; } ff_slot;
+struct sxsg_ff_map {
+	ff_slot *slot;
+	size_t cap, count;
+};
 
+static uint64_t ff_hash(const char *res, const char *atom)
+{
+	uint64_t h = 1469598103934665603ull;
+	for (const char *c = res; *c; c++) h = (h ^ (unsigned char)*c) * 1099511628211ull;
+	h = (h ^ 0xff) * 1099511628211ull;
+	for (const char *c = atom; *c; c++) h = (h ^ (unsigned char)*c) * 1099511628211ull;
+	return h;
+}
+
+static ff_slot *ff_find(const sxsg_ff_map *m, const char *res, const char *atom)
+{
+	size_t i = ff_hash(res, atom) & (m->cap - 1);
+	while (m->slot[i].used) {
+		if (!strcmp(m->slot[i].res, res) && !strcmp(m->slot[i].atom, atom)) return &m->slot[i];
+		i = (i + 1) & (m->cap - 1);
+	}
+	return &m->slot[i];
+}
+
+static int ff_put(sxsg_ff_map *m, const char *res, const char *atom, int type)
+{
+	if (2 * (m->count + 1) > m->cap) {
+		size_t oc = m->cap;
+		ff_slot *old = m->slot;
+		m->cap = oc ? 2 * oc : 256;
+		m->slot = calloc(m->cap, sizeof(ff_slot));
+		if (!m->slot) return -1;
+		for (size_t i = 0; i < oc; i++)
+			if (old[i].used) *ff_find(m, old[i].res, old[i].atom) = old[i];
+		free(old);
+	}
+	ff_slot *sl = ff_find(m, res, atom);
+	if (!sl->used) {
+		sl->used = 1;
+		strcpy(sl->res, res);
+		strcpy(sl->atom, atom);
+		m->count++;
+	}
+	sl->type = type;
+	return 0;
+}
+
+sxsg_ff_map *sxsg_ff_map_load(const char *path)
+{
+	if (!path) {
+		sxs_fail(-2, "sxsg_ff_map_load: no path");
+		return NULL;
+	}
+	FILE *f = fopen(path, "r");
+	if (!f) {
+		sxs_fail(-2, "Could not open file %s", path);
+		return NULL;
+	}
+	sxsg_ff_map *m = calloc(1, sizeof(*m));
+	char line[1024];
+	int bad = !m;
+	/* default_ff_table's loop (src/form_factor_table.c:164-183): skip '#'
+	 * and blank lines, read "residue atom type" tokens of at most 7, 7 and
+	 * 15 characters into buffers kept across lines (a line with fewer
+	 * tokens keeps the previous line's remaining fields, as there) */
+	char r[8] = {0}, a[8] = {0}, t[16] = {0};
+	while (!bad && fgets(line, sizeof(line), f)) {
+		int blank = 1;
+		for (char *c = line; *c; c++)
+			if (!isspace((unsigned char)*c)) {
+				blank = 0;
+				break;
+			}
+		if (line[0] == '#' || blank) continue;
+		if (sscanf(line, "%7s %7s %15s", r, a, t) < 1) continue;
+		bad = ff_put(m, r, a, ff_type_index(t)) != 0;
+	}
+	fclose(f);
+	if (bad) {
+		sxsg_ff_map_free(m);
+		sxs_fail(-5, "sxsg_ff_map_load: out of host memory");
+		return NULL;
+	}
+	return m;
+}
+
+void sxsg_ff_map_free(sxsg_ff_map *m)
+{
+	if (!m) return;
+	free(m->slot);
+	free(m);
+}
+
+/* get_ff's key (src/form_factor_table.c:98-121): skip leading blanks, copy
+ * up to the next blank, at most 7 characters */
 static void trim_token(const char *src, char *dst)
 {
-	/* get_ff's key: skip leading blanks, copy up to the next blank
-	 * (src/form_factor_table.c:98-121), at most 7 characters */
 	int n = 0;
 	while (*src == ' ') src++;
 	while (*src && *src != ' ' && n < 7) dst[n++] = *src++;
 	dst[n] = 0;
 }
 
+int sxsg_ff_map_type(const sxsg_ff_map *m, const char *res, const char *atom)
+{
+	if (!m || !res || !atom) return -1;
+	char r[8], a[8];
+	trim_token(res, r);
+	trim_token(atom, a);
+	if (!m->cap) return -1;
+	const ff_slot *sl = ff_find(m, r, a);
+	return sl->used ? sl->type : -1;
+}
+
 int sxsg_ff_lookup(const char *path, const char *res8, const char *atom8, int n, double *vac, double *dum)
 {
 	if (!path || n < 0 || (n > 0 && (!res8 || !atom8 || !vac || !dum))) return sxs_fail(-2, "sxsg_ff_lookup: bad arguments");
-	FILE *f = fopen(path, "r");
-	if (!f) return sxs_fail(-2, "cannot open mapping file %s", path);
-	size_t cap = 256, cnt = 0;
-	ff_entry *tab = malloc(sizeof(ff_entry) * cap);
-	char line[512];
-	while (fgets(line, sizeof(line), f)) {
-		int blank = 1;
-		for (char *c = line; *c; c++) if (!isspace((unsigned char)*c)) { blank = 0; break; }
-		if (line[0] == '#' || blank) continue;
-		char r[8] = {0}, a[8] = {0}, t[16] = {0};
-		if (sscanf(line, "%7s %7s %15s", r, a, t) != 3) continue;
-		int type = -1;
-		for (size_t i = 0; i < sizeof(k_ff) / sizeof(k_ff[0]); i++) if (!strcmp(t, k_ff[i].name)) type = (int)i;
-		size_t k;
-		for (k = 0; k < cnt; k++) if (!strcmp(tab[k].res, r) && !strcmp(tab[k].atom, a)) break;
-		if (k == cnt) {
-			if (cnt == cap) tab = realloc(tab, sizeof(ff_entry) * (cap *= 2));
-			cnt++;
-			strcpy(tab[k].res, r);
-			strcpy(tab[k].atom, a);
-		}
-		tab[k].type = type; /* later lines overwrite earlier ones, like kh_put */
-	}
-	fclose(f);
+	sxsg_ff_map *m = sxsg_ff_map_load(path);
+	if (!m) return -2;
 	int missing = 0;
 	for (int i = 0; i < n; i++) {
-		char r[8], a[8], rs[9], as[9];
+		char rs[9], as[9];
 		memcpy(rs, res8 + 8 * i, 8); rs[8] = 0;
 		memcpy(as, atom8 + 8 * i, 8); as[8] = 0;
-		trim_token(rs, r);
-		trim_token(as, a);
-		int type = -1;
-		for (size_t k = 0; k < cnt; k++)
-			if (!strcmp(tab[k].res, r) && !strcmp(tab[k].atom, a)) { type = tab[k].type; break; }
-		if (type < 0) {
+		int type = sxsg_ff_map_type(m, rs, as);
+		if (type < 0 || type >= SXS_FF_NTYPES) {
 			vac[i] = dum[i] = NAN;
 			missing++;
 		} else {
@@ -759,7 +879,7 @@ int sxsg_ff_lookup(const char *path, const char *res8, const char *atom8, int n,
 			dum[i] = k_ff[type].dummy;
 		}
 	}
-	free(tab);
+	sxsg_ff_map_free(m);
 	return missing;
 }
 

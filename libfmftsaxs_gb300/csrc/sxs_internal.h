@@ -24,6 +24,7 @@
 #define SXS_C1_DEFAULT 1.0
 #define SXS_C2_DEFAULT 0.0
 #define SXS_LMAX 60
+#define SXS_FF_NTYPES 43   /* HEAVY_ATOM_SIZE, src/form_factor_table.h:35 */
 
 /* error state (thread-local message) */
 int sxs_fail(int code, const char *fmt, ...);

@@ -12,6 +12,8 @@ it run where the reference tree is absent.
                   exponent
   form factors    (vacuum, excluded volume) of the mapping's types C, N, O, S,
                   CH, CH2, CH3, H and of water, from the reference's get_ff
+  mapping         the (residue, atom, type) lines of the mapping file, so a
+                  test can write the same file for the drop-in default_ff_table
 
 Usage: FMFTSAXS_REFERENCE_SRC=<reference tree> python tests/golden/make_refdata.py
 """
@@ -92,12 +94,22 @@ def main():
     L, Q = int(hdr[0]), int(hdr[1])
     assert len(toks) == Q * (L + 1) ** 2 * 6
     m, e = decimal_parts(toks)
+    mres, matom, mtype = [], [], []
+    with open(mapping) as f:
+        for line in f:
+            if line.startswith("#") or not line.strip():
+                continue
+            p = line.split()
+            mres.append(p[0])
+            matom.append(p[1])
+            mtype.append(p[2] if len(p) > 2 else "")
     ff_types = list(FF_PAIRS)
     ffv, ffd, _, _ = r.ff_lookup(mapping, [FF_PAIRS[t][0] for t in ff_types], [FF_PAIRS[t][1] for t in ff_types])
     out = dict(rec_xyz=xyz, rec_res=names8(res), rec_atom=names8(atom), rec_vdw=vdw, rec_vac=vac, rec_dum=dum,
                h2o=h2o, spf_L=L, spf_Q=Q, spf_rm_text=float(hdr[2]), spf_mant=m, spf_exp=e,
                ff_types=names8(ff_types), ff_res=names8([FF_PAIRS[t][0] for t in ff_types]),
-               ff_atom=names8([FF_PAIRS[t][1] for t in ff_types]), ff_vac=ffv, ff_dum=ffd)
+               ff_atom=names8([FF_PAIRS[t][1] for t in ff_types]), ff_vac=ffv, ff_dum=ffd,
+               map_res=names8(mres), map_atom=names8(matom), map_type=names8(mtype))
     path = os.path.join(HERE, "ref_4g9s.npz")
     np.savez_compressed(path, **out)
     print(path, os.path.getsize(path), "bytes,", len(vdw), "atoms")
