@@ -84,12 +84,14 @@ int main(int argc, char *argv[])
 	/* Euler file -> grid indices (no wrap of the angle digits) */
 	FILE *euler_file = fopen(eul_path, "r");
 	CHECK_PTR(euler_file);
-	int ft_id, ft_num = 0;
+	int ft_id, ft_num = 0, nread;
 	double z, line[5];
-	while (fscanf(euler_file, "%d %lf %lf %lf %lf %lf %lf", &ft_id, &z, &line[0], &line[1], &line[2], &line[3],
-	              &line[4]) != EOF)
+	while ((nread = fscanf(euler_file, "%d %lf %lf %lf %lf %lf %lf", &ft_id, &z, &line[0], &line[1], &line[2],
+	                       &line[3], &line[4])) != EOF) {
+		if (nread != 7) ERROR_MSG("Wrong Euler file format.");
 		for (int j = 0; j < znum; j++)
 			if (zvals[j] > z - 0.001 && zvals[j] < z + 0.001) ft_num++;
+	}
 	rewind(euler_file);
 	int *saxs_index = calloc(ft_num, sizeof(int));
 	int *ft_index = calloc(ft_num, sizeof(int));
@@ -100,8 +102,9 @@ int main(int argc, char *argv[])
 	double a_step = 2.0 * M_PI / (2 * L + 1);
 	struct sxs_euler euler;
 	int counter = 0;
-	while (fscanf(euler_file, "%d %lf %lf %lf %lf %lf %lf", &ft_id, &euler.z, &euler.b1, &euler.g1, &euler.a2,
-	              &euler.b2, &euler.g2) != EOF) {
+	while ((nread = fscanf(euler_file, "%d %lf %lf %lf %lf %lf %lf", &ft_id, &euler.z, &euler.b1, &euler.g1,
+	                       &euler.a2, &euler.b2, &euler.g2)) != EOF) {
+		if (nread != 7) ERROR_MSG("Wrong Euler file format.");
 		for (int j = 0; j < znum; j++) {
 			if (zvals[j] > euler.z - 0.001 && zvals[j] < euler.z + 0.001) {
 				euler.a2 = 2 * M_PI - euler.a2;

@@ -82,7 +82,7 @@ def test_reference_style_caller_matches_reference(gpu, tmp_path, path):
     exe = _build(gpu, tmp_path)
     inp, out = str(tmp_path / "in.bin"), str(tmp_path / "out.txt")
     _write_input(inp, g)
-    r = subprocess.run([exe, inp, out], capture_output=True, text=True, timeout=600)
+    r = subprocess.run([exe, inp, out], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stderr
     res = np.loadtxt(out, ndmin=2)
     assert res.shape == (len(g["index"]), 3)

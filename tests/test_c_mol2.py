@@ -185,7 +185,7 @@ def test_dropin_atom_grp2spf_matches_reference_ref_spf(gpu, oracle, tmp_path):
     out = str(tmp_path / "spf.txt")
     L, Q = int(g["spf_L"]), int(g["spf_Q"])
     r = subprocess.run([exe, "expand", mp, prm, pdb, out, str(L), str(Q), "0"], capture_output=True, text=True,
-                       timeout=300)
+                       timeout=120)
     assert r.returncode == 0, r.stderr
     with open(out) as f:
         hdr = f.readline().split()
@@ -244,8 +244,8 @@ def test_correlate_style_caller_matches_reference_fixture(gpu, tmp_path):
     bs, ast = np.pi / L, 2 * np.pi / N
     with open(files["euler.txt"], "w") as f:
         for k in range(len(v)):
-            f.write("%d %r %r %r %r %r %r\n" % (k, float(z[zi[k]]), b1[k] * bs, g1[k] * ast,
-                                                2 * np.pi - a2[k] * ast, b2[k] * bs, 2 * np.pi - g2[k] * ast))
+            e = (z[zi[k]], b1[k] * bs, g1[k] * ast, 2 * np.pi - a2[k] * ast, b2[k] * bs, 2 * np.pi - g2[k] * ast)
+            f.write("%d " % k + " ".join(repr(float(x)) for x in e) + "\n")
     exe = build(gpu, tmp_path, "correlate_caller")
     out = files["out.txt"]
     cmd = [exe, files["mapping.prm"], files["atoms.prm"], files["rec.pdb"], files["lig.pdb"], files["exp.dat"],
@@ -255,7 +255,7 @@ def test_correlate_style_caller_matches_reference_fixture(gpu, tmp_path):
     with open(both, "w") as f:
         f.write(open(files["areas_rec"]).read() + open(files["areas_lig"]).read())
     env = dict(os.environ, SXS_TEST_ACCS=both)
-    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, env=env)
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=120, env=env)
     assert r.returncode == 0, r.stderr
     res = np.loadtxt(out, ndmin=2)
     assert res.shape == (len(g["index"]), 4)
