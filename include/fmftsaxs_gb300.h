@@ -296,6 +296,14 @@ int sxsg_plan_run(sxsg_plan *plan, int fit_mode);
  * rescale); grid: chi^2 [n][n1][n2] (grid fit only). */
 int sxsg_plan_results(sxsg_plan *plan, double *chi, double *c1, double *c2, int32_t *cell,
                       double *cross, double *grid);
+/* The k best poses of the last fitted run (grid or L-BFGS-B), selected on
+ * the device: pose[i] = position in the plan's pose list, with its chi, c1,
+ * c2 (any output may be NULL), in ascending chi, ties in list order, NaN
+ * last (the order of a stable argsort).  k <= 16384; a k above the number of
+ * poses returns every pose.  Returns the number written, or a negative
+ * error.  It has no counterpart in the reference, which writes every pose's
+ * score (tools/correlate.c:362-375). */
+int sxsg_plan_topk(sxsg_plan *plan, int k, int64_t *pose, double *chi, double *c1, double *c2);
 /* Stage timings of the last run in ms (CUDA events on the plan stream):
  * [0] tables, [1] translate, [2] per-pose, [3] fit, [4] whole run. */
 int sxsg_plan_timings(sxsg_plan *plan, double *ms5);

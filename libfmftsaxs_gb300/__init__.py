@@ -216,6 +216,19 @@ class Plan:
             out["grid"] = gr
         return out
 
+    def topk(self, k):
+        """The k best poses of the last fitted run, selected on the device
+        (sxsg_plan_topk): dict(pose=list positions, chi, c1, c2), ascending
+        chi, ties in list order."""
+        lib = load()
+        lib.sxsg_plan_topk.argtypes = [C.c_void_p, C.c_int] + [C.c_void_p] * 4
+        m = min(int(k), self.n)
+        pose, chi, c1, c2 = np.zeros(m, dtype=np.int64), np.zeros(m), np.zeros(m), np.zeros(m)
+        got = lib.sxsg_plan_topk(self.h, int(k), pose.ctypes.data, chi.ctypes.data, c1.ctypes.data, c2.ctypes.data)
+        if got < 0:
+            raise SxsError(last_error())
+        return dict(pose=pose[:got], chi=chi[:got], c1=c1[:got], c2=c2[:got])
+
     def chunks(self):
         """Chunks of the translated table the last run used."""
         load().sxsg_plan_chunks.argtypes = [C.c_void_p]

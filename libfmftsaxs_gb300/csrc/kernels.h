@@ -148,6 +148,17 @@ int sxsk_fit_grid_df(const float2 *cross, const sxsk_pose *order, int slot0, int
                      int n2, int max_blocks, double *chi, double *c1, double *c2, int32_t *cell, double *grid,
                      cudaStream_t s);
 
+/* device top-k (kernels_topk.cu): the k smallest chi[0, n) in ascending
+ * order, ties in list order, NaN last (a stable argsort); 1 <= k <=
+ * min(n, SXSK_TOPK_MAX); outputs list positions and the chi, c1, c2 of
+ * them (any output may be NULL; c1, c2 are read only for their outputs);
+ * scratch: device memory of sxsk_topk_scratch(n, k) bytes */
+#define SXSK_TOPK_MAX 16384
+size_t sxsk_topk_scratch(long n, int k);
+int sxsk_topk_launches(void);
+int sxsk_topk(const double *chi, const double *c1, const double *c2, long n, int k, void *scratch, int64_t *out_pos,
+              double *out_chi, double *out_c1, double *out_c2, cudaStream_t s);
+
 #ifdef __cplusplus
 }
 #endif

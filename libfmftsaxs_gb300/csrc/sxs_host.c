@@ -822,6 +822,39 @@ int sxsg_plan_results(sxsg_plan *p, double *chi, double *c1, double *c2, int32_t
 	return 0;
 }
 
+int sxsg_plan_topk(sxsg_plan *p, int k, int64_t *pose, double *chi, double *c1, double *c2)
+{
+	if (!p || k < 0) return sxs_fail(-2, "sxsg_plan_topk: bad arguments");
+	if (p->last_fit != SXSG_FIT_GRID && p->last_fit != SXSG_FIT_LBFGSB)
+		return sxs_fail(-2, "sxsg_plan_topk: no fitted run");
+	int64_t n = p->npose;
+	if (k > n) k = (int)n;
+	if (k == 0) return 0;
+	if (k > SXSK_TOPK_MAX) return sxs_fail(-2, "sxsg_plan_topk: k above %d", SXSK_TOPK_MAX);
+	cudaStream_t s = p->s;
+	void *ws = NULL;
+	int64_t *d_pos = NULL;
+	double *d_out = NULL;
+	cudaError_t e = cudaMallocAsync(&ws, sxsk_topk_scratch((long)n, k), s);
+	if (!e) e = cudaMallocAsync((void **)&d_pos, sizeof(int64_t) * k, s);
+	if (!e) e = cudaMallocAsync((void **)&d_out, sizeof(double) * 3 * (size_t)k, s);
+	if (!e) {
+		e = (cudaError_t)sxsk_topk(p->d_chi, p->d_c1, p->d_c2, (long)n, k, ws, d_pos, d_out, c1 ? d_out + k : NULL,
+		                           c2 ? d_out + 2 * (size_t)k : NULL, s);
+		sxs_count_launches(sxsk_topk_launches());
+	}
+	if (!e && pose) e = cudaMemcpyAsync(pose, d_pos, sizeof(int64_t) * k, cudaMemcpyDeviceToHost, s);
+	if (!e && chi) e = cudaMemcpyAsync(chi, d_out, sizeof(double) * k, cudaMemcpyDeviceToHost, s);
+	if (!e && c1) e = cudaMemcpyAsync(c1, d_out + k, sizeof(double) * k, cudaMemcpyDeviceToHost, s);
+	if (!e && c2) e = cudaMemcpyAsync(c2, d_out + 2 * (size_t)k, sizeof(double) * k, cudaMemcpyDeviceToHost, s);
+	if (!e) e = cudaStreamSynchronize(s);
+	pfree(p, ws);
+	pfree(p, d_pos);
+	pfree(p, d_out);
+	if (e) return sxs_cuda_fail(e, "sxsg_plan_topk");
+	return k;
+}
+
 int sxsg_plan_chunks(const sxsg_plan *p) { return p ? p->last_chunks : 0; }
 
 int sxsg_plan_timings(sxsg_plan *p, double *ms5)
