@@ -33,45 +33,101 @@ sys.path.insert(0, HERE)
 
 # ---------------------------------------------------------------- CPU side
 def _cpu_worker(args):
-    """Score one sample of poses with a CPU implementation; returns (n, s)."""
-    kind, A, B, q, z, L, idx, a, mult, peak, c1g, c2g, exp, rms = args
+    """Three calls of a CPU implementation on one z slice: no pose (the
+    per-call setup), the poses of the first triple, the poses of all the
+    worker's triples (per-z setup shared, as in a full run).  Returns
+    (poses of the last call, [seconds of the three calls])."""
+    kind, A, B, q, z, L, idx1, idx, a, mult, peak, c1g, c2g, exp, rms = args
     from oracle import bind
     if kind == "reference":
         r = bind.Ref()
-        r.score(A, B, rms[0], rms[1], rms[2], exp, q, z, L, idx[:1], 1, c1g[:1], c2g[:1])  # warm the tables
-        t = time.perf_counter()
-        r.score(A, B, rms[0], rms[1], rms[2], exp, q, z, L, idx, 1, c1g, c2g)
+
+        def call(ix):
+            r.score(A, B, rms[0], rms[1], rms[2], exp, q, z, L, ix, 1, c1g, c2g)
     else:
         o = bind.Oracle()
-        o.score(A, B, q, z, L, idx[:1], 1, peak, a, mult, c1g[:1], c2g[:1])  # build the 3j table once
+
+        def call(ix):
+            o.score(A, B, q, z, L, ix, 1, peak, a, mult, c1g, c2g)
+    times = []
+    for ix in (idx[:0], idx1, idx):
         t = time.perf_counter()
-        o.score(A, B, q, z, L, idx, 1, peak, a, mult, c1g, c2g)
-    return len(idx), time.perf_counter() - t
+        call(ix)
+        times.append(time.perf_counter() - t)
+    return len(idx), times
 
 
-def cpu_sample(w, kind, workers, triples_per_worker=1, seed=11):
-    """Each worker scores all listed poses of `triples_per_worker` distinct
-    (z, beta1, beta2) triples drawn from the workload (the unit of work of
-    the reference loop).  Rate = poses scored / slowest worker's time."""
-    from libfmftsaxs_gb300.workload import decode, triple_counts
+def cpu_sample(w, kind, workers, triples_per_worker=4, seed=11):
+    """CPU throughput on a bounded sample: each worker takes one touched z
+    slice (slices drawn at random, seeded) and scores every listed pose of
+    `triples_per_worker` of that slice's (z, beta1, beta2) triples in one
+    call, so the per-z work (Bessel values, T matrix, ligand sums) is shared
+    by its triples as in a full run.  Returns the measured rate (poses / the
+    slowest worker's time) and the costs that extrapolate to the whole list
+    (per call, per touched z, per touched triple; means over workers)."""
+    from libfmftsaxs_gb300.workload import decode
     L = w.L
-    keys, counts = triple_counts(w.index, L)
+    K = L + 1
+    zi, b1, b2 = decode(w.index, L)[:3]
+    key = (zi * K + b1) * K + b2
     rng = np.random.default_rng(seed)
-    pick = rng.choice(len(keys), size=workers * triples_per_worker, replace=False)
-    z, b1, b2 = decode(w.index, L)[:3]
-    key = (z * (L + 1) + b1) * (L + 1) + b2
-    jobs = []
+    zt = np.unique(zi)
+    zpick = rng.choice(zt, size=workers, replace=workers > len(zt))
+    jobs, ntrip = [], []
     for k in range(workers):
-        sel = keys[pick[k * triples_per_worker:(k + 1) * triples_per_worker]]
+        trip = np.unique(key[zi == zpick[k]])
+        sel = rng.choice(trip, size=min(triples_per_worker, len(trip)), replace=False)
+        ntrip.append(len(sel))
         idx = w.index[np.isin(key, sel)].astype(np.int32)
-        jobs.append((kind, w.A, w.B, w.q, w.z, L, idx, w.a, w.mult, w.peak, w.c1g, w.c2g, w.exp,
+        idx1 = w.index[key == sel[0]].astype(np.int32)
+        jobs.append((kind, w.A, w.B, w.q, w.z, L, idx1, idx, w.a, w.mult, w.peak, w.c1g, w.c2g, w.exp,
                      (w.rmA, w.rmB, w.rm)))
     ctx = mp.get_context("spawn")
     with ctx.Pool(workers) as pool:
         res = pool.map(_cpu_worker, jobs)
     n = sum(r[0] for r in res)
-    wall = max(r[1] for r in res)
-    return n / wall, n, wall
+    wall = max(r[1][2] for r in res)
+    per_call = float(np.mean([r[1][0] for r in res]))
+    multi = [(r[1][2] - r[1][1]) / (nt - 1) for r, nt in zip(res, ntrip) if nt > 1]
+    per_trip = float(np.mean(multi)) if multi else float(np.mean([r[1][1] - r[1][0] for r in res]))
+    per_z = float(np.mean([r[1][1] - r[1][0] for r in res])) - per_trip
+    return dict(rate=n / wall, poses=n, wall=wall, per_call_s=per_call, per_z_s=max(per_z, 0.0),
+                per_triple_s=per_trip, workers=workers, triples_per_worker=triples_per_worker)
+
+
+def cpu_extrapolate(w, cs, ranks=8):
+    """Whole-list CPU time from the sample's costs, serial and as correlate
+    runs it on `ranks` MPI processes (z values dealt round-robin,
+    tools/correlate.c:142-147; wall = the slowest rank, whose only exchange
+    is the final gather)."""
+    from libfmftsaxs_gb300.workload import decode
+    L = w.L
+    K = L + 1
+    zi, b1, b2 = decode(w.index, L)[:3]
+    trips = {}
+    for z, t in zip(zi.tolist(), ((zi * K + b1) * K + b2).tolist()):
+        trips.setdefault(z, set()).add(t)
+    cost = {z: cs["per_z_s"] + len(t) * cs["per_triple_s"] for z, t in trips.items()}
+    serial = cs["per_call_s"] + sum(cost.values())
+    rank_s = [cs["per_call_s"] + sum(c for z, c in cost.items() if z % ranks == r) for r in range(ranks)]
+    n = len(w.index)
+    return {"serial": {"poses_per_s": n / serial, "seconds": serial, "cores": 1},
+            "mpi_emulated": {"poses_per_s": n / max(rank_s), "seconds": max(rank_s), "cores": ranks,
+                             "ranks": ranks},
+            "touched_triples": int(sum(len(t) for t in trips.values())), "touched_z": len(trips),
+            "label": "extrapolated from the sample's per-call, per-z and per-triple costs"}
+
+
+def metric_name(w):
+    return "poses/s @lmax=%d, grid fit %dx%d (c1 x c2)" % (w.L, len(w.c1g), len(w.c2g))
+
+
+def cpu_baseline_entry(w, cs, kind):
+    return {"value": cs["rate"], "unit": "poses/s", "cores": cs["workers"], "kind": kind,
+            "sample": "%d poses: %d processes, each every listed pose of %d (z, beta1, beta2) triples of one z slice "
+                      "in one call (per-z setup shared), grid fit; %.2f s per touched triple, %.2f s per call"
+                      % (cs["poses"], cs["workers"], cs["triples_per_worker"], cs["per_triple_s"], cs["per_call_s"]),
+            "whole_list": cpu_extrapolate(w, cs)}
 
 
 def cpu_kind():
@@ -201,13 +257,70 @@ class _Null:
         pass
 
 
-def accuracy(mix, ref, k=100):
+def model_intensity(cross, q, mult, c1, c2):
+    """point_score's model I(q) (src/min_saxs.c:391-448) of raw cross terms
+    [n][6][Q] at per-pose (c1, c2); the peak rescale is a common factor and
+    leaves relative errors unchanged."""
+    c1 = np.asarray(c1)[:, None]
+    c2 = np.asarray(c2)[:, None]
+    G = c1 ** 3 * np.exp(-mult * (c1 * c1 - 1.0) * q[None, :] ** 2)
+    VV, VD, VW, DD, DW, WW = (cross[:, c, :] for c in range(6))
+    return VV - G * VD + c2 * VW + G * G * DD - G * c2 * DW + c2 * c2 * WW
+
+
+def iq_accuracy(g, w, n=4000):
+    """I(q) of the mixed path against the FP64 path on the first n poses, at
+    the FP64 path's best (c1, c2) cell of each pose."""
+    idx = w.index[:n]
+    out = {}
+    for prec in (g.FP64, g.MIXED):
+        p = g.Plan(w.A, w.B, w.q, w.z, w.L, w.a, w.mult, w.peak, w.c1g, w.c2g, precision=prec)
+        p.set_poses(idx, skip=1)
+        p.run(g.FIT_GRID)
+        out[prec] = p.results(cross=True)
+        p.close()
+    ref = out[g.FP64]
+    i_ref = model_intensity(ref["cross"], w.q, w.mult, ref["c1"], ref["c2"])
+    i_mix = model_intensity(out[g.MIXED]["cross"], w.q, w.mult, ref["c1"], ref["c2"])
+    rel = np.abs(i_mix - i_ref) / np.abs(i_ref)
+    return {"iq_rel_max": float(rel.max()), "iq_rel_median": float(np.median(rel)), "iq_poses": len(idx)}
+
+
+def accuracy(mix, ref, k=100, topk=None):
     rel = np.abs(mix["chi"] - ref["chi"]) / ref["chi"]
     top_m = set(np.argsort(mix["chi"], kind="stable")[:k].tolist())
     top_r = set(np.argsort(ref["chi"], kind="stable")[:k].tolist())
-    return {"vs": "FP64 GPU path (pinned to the reference at 1e-10)", "dchi_rel_max": float(rel.max()),
-            "dchi_rel_median": float(np.median(rel)), "bound": 1e-4, "top%d_overlap" % k: len(top_m & top_r) / k,
-            "same_cell": float(np.mean(mix["cell"] == ref["cell"]))}
+    out = {"vs": "FP64 GPU path (within 1e-10 of the reference build on the C0/C1-shape fixtures)",
+           "dchi_rel_max": float(rel.max()), "dchi_rel_median": float(np.median(rel)), "bound": 1e-4,
+           "top%d_overlap" % k: len(top_m & top_r) / k, "same_cell": float(np.mean(mix["cell"] == ref["cell"]))}
+    if topk is not None:
+        out["top%d_device" % k] = {
+            "mixed_equals_argsort": bool(np.array_equal(topk["mixed"], np.argsort(mix["chi"], kind="stable")[:k])),
+            "fp64_equals_argsort": bool(np.array_equal(topk["fp64"], np.argsort(ref["chi"], kind="stable")[:k])),
+            "overlap": len(set(topk["mixed"].tolist()) & set(topk["fp64"].tolist())) / k}
+    return out
+
+
+def expansion_timing(g, w, fp64_peak):
+    """The A_lm expansion per molecule (sxsg_expand, with its transfers of a
+    few MB) and its FP64 rate over the accumulation's 12 FLOPs per atom, q
+    and (l, m) (3 channels of complex-by-real multiply-adds)."""
+    out = {}
+    water = g.ff_water()
+    for name, m in (("receptor", w.rec), ("ligand", w.lig)):
+        v = np.array([g.ff_type(e)[0] for e in m.elements])
+        d = np.array([g.ff_type(e)[1] for e in m.elements])
+        g.expand(m.xyz, v, d, m.sasa, water, w.q, w.L)
+        ts = []
+        for _ in range(3):
+            g.timer_start()
+            g.expand(m.xyz, v, d, m.sasa, water, w.q, w.L)
+            ts.append(g.timer_stop())
+        ms = float(np.median(ts))
+        tf = 12.0 * m.natoms * w.Q * (w.L + 1) ** 2 / (ms * 1e-3) / 1e12
+        out[name] = {"atoms": m.natoms, "ms": ms, "fp64_tflops": tf,
+                     "fp64_frac": tf / fp64_peak if fp64_peak > 0 else None}
+    return out
 
 
 def run_serving(g, args):
@@ -306,7 +419,7 @@ def run_ours(args):
 
     # CPU baseline sample first (spawned processes, no GPU use)
     workers = max(1, min(os.cpu_count() or 1, 16))
-    cpu_rate, cpu_n, cpu_wall = cpu_sample(w, kind, workers) if not args.skip_cpu else (None, 0, 0)
+    cs = cpu_sample(w, kind, workers) if not args.skip_cpu else None
 
     fp64_peak = max(g.fp64_fma_tflops() for _ in range(3))
     fp32_peak = max(g.fp32_fma_tflops() for _ in range(3))
@@ -345,7 +458,7 @@ def run_ours(args):
     tkey = (args.config, head)
     traffic = TRAFFIC_PER_POSE[tkey] * n / nchunks if tkey in TRAFFIC_PER_POSE else None
     out = {
-        "metric": "poses/s @lmax=%d (%s GPU path, grid fit)" % (w.L, "mixed-precision" if head == "mixed" else "FP64 plain"),
+        "metric": metric_name(w),
         "value": value,
         "unit": "poses/s",
         "n_gpus": 1,
@@ -379,9 +492,7 @@ def run_ours(args):
                      "hbm_frac": (traffic * nchunks / (stage[2] * 1e-3) / 1e9 / 6773.5) if traffic else None,
                      "peak_source": "measured in this run: register-resident %s FMA chains on every SM"
                                     % ("FP32" if head == "mixed" else "FP64")},
-        "cpu_baseline": {"value": cpu_rate, "unit": "poses/s", "cores": workers, "kind": kind,
-                         "sample": "%d poses of %d (z,beta1,beta2) triples, one triple per process, grid fit"
-                                   % (cpu_n, workers)},
+        "cpu_baseline": cpu_baseline_entry(w, cs, kind) if cs else None,
         "e2e": {"value": n / e2e_s, "unit": "poses/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
         "clocks": clocks,
@@ -399,47 +510,56 @@ def run_ours(args):
                    "peak_source": "measured in this run: 16-byte L2-only loads by every SM over a 32 MiB "
                                   "L2-resident buffer"})
     if head == "mixed":
-        out["accuracy"] = accuracy(res, runs["fp64"][3])
+        tk = None
+        if n >= 100:
+            tk = {}
+            for name in ("fp64", "mixed"):
+                p = g.Plan(w.A, w.B, w.q, w.z, w.L, w.a, w.mult, w.peak, w.c1g, w.c2g, precision=prec[name])
+                p.set_poses(w.index, skip=1)
+                p.run(g.FIT_GRID)
+                tk[name] = p.topk(100)["pose"]
+                p.close()
+        out["accuracy"] = accuracy(res, runs["fp64"][3], topk=tk)
+        out["accuracy"].update(iq_accuracy(g, w))
+    out["expansion"] = expansion_timing(g, w, fp64_peak)
     if not args.skip_serve:
         out["serving"] = run_serving(g, args)
     print(json.dumps(out))
 
 
 def run_reference(args):
+    """The reference algorithm on the host cores: the reference's own code
+    (oracle/_ref) where it was built, else the C restatement, on the same
+    workload, whose inputs the oracle builds (no GPU, no product library)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import libfmftsaxs_gb300 as g
-    from libfmftsaxs_gb300 import build as libbuild
     from libfmftsaxs_gb300 import workload as wl
+    from oracle.bind import OracleWorkload
     kind = cpu_kind()
-    if not os.path.exists(g.LIB_PATH):
-        libbuild.build()
-    # the workload's inputs (expansions, experiment) come from the GPU library;
-    # the timed work is the CPU implementation only
-    g.init(0)
-    w = wl.build(args.config, seed=args.seed)
+    w = wl.build(args.config, seed=args.seed, lib=OracleWorkload())
     workers = max(1, min(os.cpu_count() or 1, 16))
-    for _ in range(args.warmup):
-        cpu_sample(w, kind, workers, seed=1000 + _)
-    rates, ns, walls = [], [], []
-    for k in range(args.steps):
-        r, n, wall = cpu_sample(w, kind, workers, seed=k)
-        rates.append(r); ns.append(n); walls.append(wall)
-    value = sum(ns) / sum(walls)
-    out = {"impl": "reference",
-           "metric": "poses/s @lmax=%d (%s GPU path, grid fit)"
-                     % (w.L, "mixed-precision" if args.precision == "mixed" else "FP64 plain"),
-           "value": value, "unit": "poses/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-           "ms_per_step": 1e3 * float(np.mean(walls)), "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random-walk dimers, poses and noisy experiment)",
+    tpw = 4 if args.steps + args.warmup <= 8 else 2
+    cpu_sample(w, kind, workers, triples_per_worker=1, seed=1000)   # warm-up: start-up and caches
+    samples = [cpu_sample(w, kind, workers, triples_per_worker=tpw, seed=k) for k in range(args.steps)]
+    n = sum(c["poses"] for c in samples)
+    wall = sum(c["wall"] for c in samples)
+    value = n / wall
+    agg = dict(samples[0], rate=value, poses=n, wall=wall,
+               per_call_s=float(np.mean([c["per_call_s"] for c in samples])),
+               per_z_s=float(np.mean([c["per_z_s"] for c in samples])),
+               per_triple_s=float(np.mean([c["per_triple_s"] for c in samples])))
+    out = {"impl": "reference", "metric": metric_name(w), "value": value, "unit": "poses/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded random-walk dimers, poses and noisy experiment)",
            "config": {"workload": "%s: receptor %d / ligand %d atoms, L=%d, Q=%d, %d poses, fit grid %dx%d"
                                   % (args.config, w.rec.natoms, w.lig.natoms, w.L, w.Q, len(w.index), len(w.c1g),
                                      len(w.c2g)),
                       "precision": "fp64 (the reference's CPU arithmetic)", "skip": 1,
-                      "sample": "each step: one (z,beta1,beta2) triple of the pose list per host process"},
-           "cpu_baseline": {"value": value, "unit": "poses/s", "cores": workers, "kind": kind,
-                            "sample": "%d processes x 1 triple per step" % workers},
+                      "sample": "each step: %d processes, each the listed poses of %d triples of one z slice"
+                                % (workers, tpw)},
+           "cpu_baseline": cpu_baseline_entry(w, agg, kind),
            "e2e": {"value": value, "unit": "poses/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 

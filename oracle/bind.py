@@ -323,3 +323,40 @@ class Ref:
         out = np.zeros(6)
         self.lib.refh_ft2euler(_p(tv), _p(rm9), _p(ref_lig), _p(out))
         return out
+
+
+class OracleWorkload:
+    """The calls libfmftsaxs_gb300.workload.build makes on the product
+    library, answered by the oracle on the CPU, so that a CPU baseline can
+    build its inputs without loading the product.  Form factors: the
+    zero-angle constants of the four types the synthetic molecules use and
+    of water (src/form_factor_table.c:8-49)."""
+
+    FF = {"C": (5.9992, 5.49096), "N": (6.9946, 0.83166), "O": (7.9994, 3.04942), "S": (15.9998, 6.63324)}
+    WATER = 3.50968
+
+    def __init__(self):
+        self.o = Oracle()
+
+    def mkarray(self, b, e, n):
+        return self.o.mkarray(b, e, n)
+
+    def ff_type(self, name):
+        return self.FF[name]
+
+    def ff_water(self):
+        return self.WATER
+
+    def expand(self, xyz, vac, dum, sasa, water, q, L):
+        return self.o.expand(xyz, vac, dum, sasa, water, q, L)
+
+    def profile_from_spf(self, spf, L, q, rm, c1, c2):
+        return self.o.profile_from_spf(spf, L, q, rm, c1, c2)
+
+    def bin_experiment(self, eq, ei, ee, q, rm):
+        return self.o.opt_params(eq, ei, ee, q, rm)
+
+    def poses_to_indices(self, R, T, z, L):
+        from libfmftsaxs_gb300 import synth
+        idx, keep = synth.poses_to_indices(R, T, np.zeros(3), z, L, self.o.ft2euler, self.o.assemble_index)
+        return idx.astype(np.int64), keep

@@ -186,3 +186,19 @@ def test_oracle_matches_reference_at_benchmark_shape(oracle, name):
     np.testing.assert_allclose(grid, g["grid"], rtol=1e-10, atol=0)
     cell = grid.reshape(len(d), -1).argmin(axis=1)
     np.testing.assert_array_equal(cell, g["cell"][d])
+
+
+def test_oracle_workload_matches_the_product_host_code(lib):
+    """The oracle-built workload that the CPU baseline uses has the pose
+    indices and experiment binning of the product's host code (C0 list)."""
+    from libfmftsaxs_gb300 import workload
+    from oracle.bind import OracleWorkload
+    ow = OracleWorkload()
+    cfg = workload.config("c0")
+    z = workload.zvals(cfg)
+    a = workload.pose_lists(cfg, 2026, ow.poses_to_indices, z, cfg["L"])
+    b = workload.pose_lists(cfg, 2026, lambda R, T, zz, L: lib.poses_to_indices(R, T, zz, L), z, cfg["L"])
+    np.testing.assert_array_equal(a, b)
+    for name in ow.FF:
+        assert ow.ff_type(name) == lib.ff_type(name)
+    assert ow.ff_water() == lib.ff_water()
