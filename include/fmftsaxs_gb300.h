@@ -430,6 +430,17 @@ int64_t sxsg_assemble_index_ex(const double *euler6, int z_idx, int L, int flags
 int64_t sxsg_poses_to_indices_ex(const double *rot, const double *tr, int64_t n, const double *ref_lig,
                                  const double *zvals, int znum, int L, int64_t *index, uint8_t *keep, int flags);
 
+/* sxsg_poses_to_indices_ex on the GPU, with the same results: the device
+ * converts every pose (a thread each), and the few poses whose result could
+ * depend on the last bits of acos, sin or cos (a value within a few ulps of
+ * a "% .3f" rounding boundary, or an ill-conditioned angle: acos argument
+ * near +-1, sin beta near 0, a tested sign of a near-zero entry) are redone
+ * by the host path; *host_poses (may be NULL) gives their number.  Host
+ * buffers in and out, processed in device batches of 2^20 poses. */
+int64_t sxsg_poses_to_indices_gpu(const double *rot, const double *tr, int64_t n, const double *ref_lig,
+                                  const double *zvals, int znum, int L, int64_t *index, uint8_t *keep, int flags,
+                                  int64_t *host_poses);
+
 /* Timing on the library's stream: start records an event; stop records a
  * second one, waits for it and returns the elapsed milliseconds. */
 int sxsg_timer_start(void);

@@ -392,6 +392,30 @@ def poses_to_indices(rot, tr, zvals, L, ref_lig=(0.0, 0.0, 0.0), wrap=False):
     return idx[keep.astype(bool)], keep.astype(bool)
 
 
+def poses_to_indices_gpu(rot, tr, zvals, L, ref_lig=(0.0, 0.0, 0.0), wrap=False, full=False):
+    """poses_to_indices on the GPU (sxsg_poses_to_indices_gpu), same results.
+    Returns (index of kept poses, keep mask, poses the host redid); with
+    full=True the index array covers every pose (-1 where not kept)."""
+    lib = load()
+    lib.sxsg_poses_to_indices_gpu.restype = C.c_int64
+    rot = f64(rot).reshape(-1, 9)
+    tr = f64(tr).reshape(-1, 3)
+    n = len(rot)
+    idx = np.zeros(n, dtype=np.int64)
+    keep = np.zeros(n, dtype=np.uint8)
+    ref = f64(ref_lig)
+    z = f64(zvals)
+    nh = C.c_int64(0)
+    k = lib.sxsg_poses_to_indices_gpu(_p(rot), _p(tr), C.c_int64(n), _p(ref), _p(z), C.c_int(len(z)), C.c_int(L),
+                                      idx.ctypes.data_as(C.POINTER(C.c_int64)),
+                                      keep.ctypes.data_as(C.POINTER(C.c_uint8)), C.c_int(WRAP_ANGLES if wrap else 0),
+                                      C.byref(nh))
+    if k < 0:
+        raise SxsError(last_error())
+    kb = keep.astype(bool)
+    return (idx if full else idx[kb]), kb, nh.value
+
+
 def score_flat(A, B, qvals, zvals, L, index, a, mult, peak, skip=1, fit=FIT_GRID, c1grid=None, c2grid=None,
                cross=False, precision=FP64):
     """One-shot scoring from host buffers (sxsg_score_flat)."""

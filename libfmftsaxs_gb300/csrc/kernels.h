@@ -159,6 +159,14 @@ int sxsk_topk_launches(void);
 int sxsk_topk(const double *chi, const double *c1, const double *c2, long n, int k, void *scratch, int64_t *out_pos,
               double *out_chi, double *out_c1, double *out_c2, cudaStream_t s);
 
+/* pose ingestion (kernels_ingest.cu): rot[9n] row-major, tr[3n], ref (host
+ * pointer, 3 values) -> index[n] (-1 when z is off the grid), keep[n];
+ * poses the host must recompute are appended to flagged[] (n slots), their
+ * count in *nflag (zeroed by the caller) */
+int sxsk_pose_ingest(const double *rot, const double *tr, long n, const double *ref, const double *zvals, int znum,
+                     int L, int wrap, long long *index, unsigned char *keep, unsigned int *nflag, long long *flagged,
+                     cudaStream_t s);
+
 #ifdef __cplusplus
 }
 #endif

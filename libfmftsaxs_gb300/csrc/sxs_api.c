@@ -920,36 +920,109 @@ int64_t sxsg_poses_to_indices(const double *rot, const double *tr, int64_t n, co
 	return sxsg_poses_to_indices_ex(rot, tr, n, ref, zvals, znum, L, index, keep, 0);
 }
 
+/* one pose the host way: ft2euler, the "% .3f" round trip, z slot, index;
+ * returns 1 if kept */
+static int ingest_one(const double *rot9, const double *tr3, const double *ref, const double *zvals, int znum, int L,
+                      int flags, int64_t *index)
+{
+	char buf[64];
+	struct mol_vector3 t = {tr3[0], tr3[1], tr3[2]}, r = {ref[0], ref[1], ref[2]};
+	const double *m = rot9;
+	struct mol_matrix3 mm = {m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8]};
+	struct sxs_euler e;
+	sxs_ft2euler(&e, &t, &mm, &r);
+	double v[6] = {e.z, e.b1, e.g1, e.a2, e.b2, e.g2};
+	for (int k = 0; k < 6; k++) {
+		snprintf(buf, sizeof(buf), "% .3f", v[k]);
+		v[k] = strtod(buf, NULL);
+	}
+	int zi = -1;
+	for (int j = 0; j < znum; j++)
+		if (zvals[j] > v[0] - 0.001 && zvals[j] < v[0] + 0.001) {
+			zi = j;
+			break;
+		}
+	if (zi < 0) {
+		*index = -1;
+		return 0;
+	}
+	*index = sxsg_assemble_index_ex(v, zi, L, flags);
+	return 1;
+}
+
 int64_t sxsg_poses_to_indices_ex(const double *rot, const double *tr, int64_t n, const double *ref,
                                  const double *zvals, int znum, int L, int64_t *index, uint8_t *keep, int flags)
 {
 	if (n < 0 || (n > 0 && (!rot || !tr || !ref || !zvals || !index || !keep)) || L < 1)
 		return sxs_fail(-2, "sxsg_poses_to_indices: bad arguments");
 	int64_t kept = 0;
-	char buf[64];
 	for (int64_t i = 0; i < n; i++) {
-		struct mol_vector3 t = {tr[3 * i], tr[3 * i + 1], tr[3 * i + 2]}, r = {ref[0], ref[1], ref[2]};
-		const double *m = rot + 9 * i;
-		struct mol_matrix3 mm = {m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8]};
-		struct sxs_euler e;
-		sxs_ft2euler(&e, &t, &mm, &r);
-		double v[6] = {e.z, e.b1, e.g1, e.a2, e.b2, e.g2};
-		for (int k = 0; k < 6; k++) {
-			snprintf(buf, sizeof(buf), "% .3f", v[k]);
-			v[k] = strtod(buf, NULL);
-		}
-		int zi = -1;
-		for (int j = 0; j < znum; j++)
-			if (zvals[j] > v[0] - 0.001 && zvals[j] < v[0] + 0.001) { zi = j; break; }
-		if (zi < 0) {
-			keep[i] = 0;
-			index[i] = -1;
-			continue;
-		}
-		keep[i] = 1;
-		index[i] = sxsg_assemble_index_ex(v, zi, L, flags);
-		kept++;
+		keep[i] = (uint8_t)ingest_one(rot + 9 * i, tr + 3 * i, ref, zvals, znum, L, flags, index + i);
+		kept += keep[i];
 	}
+	return kept;
+}
+
+/* Device batches of at most this many poses (about 120 MB of device memory) */
+#define SXS_INGEST_BATCH ((int64_t)1 << 20)
+
+int64_t sxsg_poses_to_indices_gpu(const double *rot, const double *tr, int64_t n, const double *ref,
+                                  const double *zvals, int znum, int L, int64_t *index, uint8_t *keep, int flags,
+                                  int64_t *host_poses)
+{
+	if (n < 0 || (n > 0 && (!rot || !tr || !ref || !zvals || !index || !keep)) || L < 1 || znum < 0)
+		return sxs_fail(-2, "sxsg_poses_to_indices_gpu: bad arguments");
+	if (host_poses) *host_poses = 0;
+	if (n == 0) return 0;
+	int rc = sxs_ensure_init();
+	if (rc) return rc;
+	cudaStream_t s = sxs_default_stream();
+	int64_t nb = n < SXS_INGEST_BATCH ? n : SXS_INGEST_BATCH;
+	double *d_rot = NULL, *d_tr = NULL, *d_z = NULL;
+	long long *d_idx = NULL, *d_fl = NULL;
+	unsigned char *d_keep = NULL;
+	unsigned int *d_nf = NULL;
+	long long *h_fl = malloc(sizeof(long long) * (size_t)nb);
+	cudaError_t e = h_fl ? cudaSuccess : cudaErrorMemoryAllocation;
+	if (!e) e = cudaMallocAsync((void **)&d_rot, sizeof(double) * 9 * nb, s);
+	if (!e) e = cudaMallocAsync((void **)&d_tr, sizeof(double) * 3 * nb, s);
+	if (!e) e = cudaMallocAsync((void **)&d_z, sizeof(double) * (znum > 0 ? znum : 1), s);
+	if (!e) e = cudaMallocAsync((void **)&d_idx, sizeof(long long) * nb, s);
+	if (!e) e = cudaMallocAsync((void **)&d_fl, sizeof(long long) * nb, s);
+	if (!e) e = cudaMallocAsync((void **)&d_keep, nb, s);
+	if (!e) e = cudaMallocAsync((void **)&d_nf, sizeof(unsigned int), s);
+	if (!e && znum > 0) e = cudaMemcpyAsync(d_z, zvals, sizeof(double) * znum, cudaMemcpyHostToDevice, s);
+	int64_t kept = 0, nhost = 0;
+	for (int64_t b0 = 0; !e && b0 < n; b0 += nb) {
+		int64_t m = n - b0 < nb ? n - b0 : nb;
+		unsigned int nf = 0;
+		e = cudaMemcpyAsync(d_rot, rot + 9 * b0, sizeof(double) * 9 * m, cudaMemcpyHostToDevice, s);
+		if (!e) e = cudaMemcpyAsync(d_tr, tr + 3 * b0, sizeof(double) * 3 * m, cudaMemcpyHostToDevice, s);
+		if (!e) e = cudaMemsetAsync(d_nf, 0, sizeof(unsigned int), s);
+		if (!e) {
+			e = (cudaError_t)sxsk_pose_ingest(d_rot, d_tr, (long)m, ref, d_z, znum, L, (flags & SXSG_WRAP_ANGLES) != 0,
+			                                  d_idx, d_keep, d_nf, d_fl, s);
+			sxs_count_launches(1);
+		}
+		if (!e) e = cudaMemcpyAsync(index + b0, d_idx, sizeof(int64_t) * m, cudaMemcpyDeviceToHost, s);
+		if (!e) e = cudaMemcpyAsync(keep + b0, d_keep, m, cudaMemcpyDeviceToHost, s);
+		if (!e) e = cudaMemcpyAsync(&nf, d_nf, sizeof(unsigned int), cudaMemcpyDeviceToHost, s);
+		if (!e) e = cudaStreamSynchronize(s);
+		if (!e && nf > 0) e = cudaMemcpy(h_fl, d_fl, sizeof(long long) * nf, cudaMemcpyDeviceToHost);
+		if (e) break;
+		/* flagged poses: the host path decides (see kernels_ingest.cu) */
+		for (unsigned int k = 0; k < nf; k++) {
+			int64_t i = b0 + h_fl[k];
+			keep[i] = (uint8_t)ingest_one(rot + 9 * i, tr + 3 * i, ref, zvals, znum, L, flags, index + i);
+		}
+		nhost += nf;
+		for (int64_t i = b0; i < b0 + m; i++) kept += keep[i];
+	}
+	cudaFreeAsync(d_rot, s); cudaFreeAsync(d_tr, s); cudaFreeAsync(d_z, s); cudaFreeAsync(d_idx, s);
+	cudaFreeAsync(d_fl, s); cudaFreeAsync(d_keep, s); cudaFreeAsync(d_nf, s);
+	free(h_fl);
+	if (e) return sxs_cuda_fail(e, "sxsg_poses_to_indices_gpu");
+	if (host_poses) *host_poses = nhost;
 	return kept;
 }
 
