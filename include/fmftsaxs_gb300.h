@@ -232,9 +232,9 @@ int sxsg_profile_from_flat(const double *spf, int L, int qnum, double rm, const 
  * vacuum_ff, dummy_ff, water_w[natoms] (water form factor x accessible
  * fraction per atom; NULL for no hydration shell), qvals[qnum], spf_out in
  * the flat layout [3][qnum][(L+1)^2][2].  Work buffers (the Y_lm norm
- * table, Y_lm and j_l per atom) live in one static device array of 64 MiB
- * (8 Mi doubles) that every GPU loading this library keeps until exit; a
- * call needs about natoms (2 (L+1)^2 + qnum (L+1)) doubles of it, L <= 40,
+ * table, Y_lm and the radius of each atom) live in one static device array
+ * of 64 MiB (8 Mi doubles) that every GPU loading this library keeps until
+ * exit; a call needs about natoms (2 (L+1)^2 + 2) doubles of it, L <= 40,
  * and a larger request returns -3 without touching the GPU.  Work is queued
  * on `stream` (a cudaStream_t; NULL for the default stream) and the call
  * returns without waiting for it.  The first call on each device looks up

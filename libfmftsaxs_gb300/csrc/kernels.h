@@ -44,14 +44,16 @@ typedef struct {
 	int32_t src;     /* position in the caller's list */
 } sxsk_pose;
 
-/* A_lm expansion (faithful FP64): per-atom Y_lm, per (atom,q,l) Bessel series,
- * accumulation, 4 pi i^l phase.  spf_out uses the host flat layout
- * [3][Q][K2][2]. */
+/* A_lm expansion (FP64, the reference's j_l series and Legendre recurrence):
+ * per-atom Y_lm and radius into ylm_ws / rad_ws, then one block per (q, l)
+ * with the atoms staged through shared memory (series, accumulation, 4 pi
+ * i^l phase).  spf_out uses the host flat layout [3][Q][K2][2]. */
 int sxsk_expand(const double *xyz, const double *vac, const double *dum, const double *wfac,
                 int natoms, const double *q, int Q, int L, const double *ynorm,
-                double2 *ylm_ws, double *jl_ws, double *spf_out, cudaStream_t s);
+                double2 *ylm_ws, double *rad_ws, double *spf_out, cudaStream_t s);
 size_t sxsk_expand_ws_ylm(int natoms, int L);
-size_t sxsk_expand_ws_jl(int natoms, int Q, int L);
+size_t sxsk_expand_ws_rad(int natoms);
+int sxsk_expand_launches(void);
 
 /* host-flat [3][Q][K2][2] -> spf_t [3][K2][Q] complex, in float when fp32 */
 int sxsk_spf_transpose(const double *flat, void *spf_t, int Q, int L, int fp32, cudaStream_t s);

@@ -50,7 +50,7 @@ __device__ double sbessel(int l, double x)
  * src/borrowed.c:40-65 (N = L+1), times the Y norm, times e^{-i m phi}
  * (src/pdb2spf.c:76-84), written for +m and -m. */
 __global__ void k_ylm(const double *__restrict__ xyz, int natoms, int L, const double *__restrict__ ynorm,
-                      double2 *__restrict__ ylm)
+                      double2 *__restrict__ ylm, double *__restrict__ rad)
 {
 	int K = L + 1, K2 = K * K;
 	long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -58,6 +58,7 @@ __global__ void k_ylm(const double *__restrict__ xyz, int natoms, int L, const d
 	int a = (int)(t / K), m = (int)(t % K);
 	double x = xyz[3 * a], y = xyz[3 * a + 1], z = xyz[3 * a + 2];
 	double r = sqrt(x * x + y * y + z * z);
+	if (m == 0 && rad) rad[a] = r;
 	double th = acos(z / r);
 	double ph;
 	if (y > 0.0) ph = acos(x / sqrt(x * x + y * y));
@@ -94,52 +95,103 @@ __global__ void k_ylm(const double *__restrict__ xyz, int natoms, int L, const d
 	}
 }
 
-/* j_l(q r_a): jl[a][q][l]. */
-__global__ void k_jl(const double *__restrict__ xyz, int natoms, const double *__restrict__ q, int Q, int L,
-                     double *__restrict__ jl)
+/* j_l(x) with the series of sbessel and the same value: the same terms in
+ * the same order, with two changes that leave the rounded series alone.
+ * The stop test fabs(term / sum) > 1e-5 is decided by comparing |term|
+ * with |sum| 1e-5 (1 +- 1e-10), whose rounding errors are far below that
+ * margin; only a quotient within the margin is divided out.  x^l is a
+ * chain of products instead of pow (a few ulps, outside the cancelling
+ * sum).  term0 = 1 / (2l+1)!! is the block's. */
+__device__ __forceinline__ double sbessel_fast(int l, double x, double term0)
 {
-	int K = L + 1;
-	long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-	if (t >= (long)natoms * Q * K) return;
-	int l = (int)(t % K);
-	long r2 = t / K;
-	int iq = (int)(r2 % Q), a = (int)(r2 / Q);
-	double x = xyz[3 * a], y = xyz[3 * a + 1], z = xyz[3 * a + 2];
-	double r = sqrt(x * x + y * y + z * z);
-	jl[t] = sbessel(l, q[iq] * r);
+	if (x > 0.0) {
+		double tl1 = 2.0 * (double)l + 1.0;
+		double num = (-1.0) * x * x;
+		double term = term0, sum = term0;
+		const double c = 0.00001, hi = c * (1.0 + 1e-10), lo = c * (1.0 - 1e-10);
+		for (int k = 1; k < 100000; k++) {
+			double at = fabs(term), as = fabs(sum);
+			bool go;
+			if (at > as * hi) go = true;
+			else if (at < as * lo) go = false;
+			else go = fabs(term / sum) > c;
+			if (!go) break;
+			double ratio = num / ((2.0 * (double)k) * (2.0 * (double)k + tl1));
+			term = term * ratio;
+			sum = sum + term;
+		}
+		double xl = 1.0;
+		for (int i = 0; i < l; i++) xl = xl * x;
+		return sum * xl;
+	}
+	return l == 0 ? 1.0 : 0.0;
 }
 
-/* A[ch][q][lm] = 4 pi i^l sum_a f_ch(a) (j_l(q r_a) Y*_lm(a)), atoms in
- * order, each term f*(j*Y) as src/pdb2spf.c:104-112, then the phase of
- * lines 118-147.  Output in the host flat layout [3][Q][K2][2]. */
-__global__ void k_accum(const double2 *__restrict__ ylm, const double *__restrict__ jl,
-                        const double *__restrict__ vac, const double *__restrict__ dum, const double *__restrict__ wfac,
-                        int natoms, int Q, int L, double *__restrict__ spf)
+#define EXP_THREADS 128
+
+/* A[ch][q][l m] for one (q, l) per block: atoms in tiles of EXP_THREADS,
+ * staged through shared memory as w_ch = f_ch(a) j_l(q r_a) (one series
+ * per thread), then accumulated against Y*_lm(a) by (m, slice) threads,
+ * each slice a fixed residue class of the tile's atoms; the slices are
+ * summed in order and the 4 pi i^l phase applied (src/pdb2spf.c:104-147).
+ * Deterministic: the same partition and order on every run. */
+__global__ void __launch_bounds__(EXP_THREADS) k_expand_ql(const double2 *__restrict__ ylm,
+                                                            const double *__restrict__ rad,
+                                                            const double *__restrict__ vac,
+                                                            const double *__restrict__ dum,
+                                                            const double *__restrict__ wfac, int natoms,
+                                                            const double *__restrict__ q, int Q, int L,
+                                                            double *__restrict__ spf)
 {
+	__shared__ double w[3][EXP_THREADS];
+	__shared__ double red[EXP_THREADS][6];
 	int K = L + 1, K2 = K * K;
-	long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-	if (t >= (long)Q * K2) return;
-	int lm = (int)(t % K2), iq = (int)(t / K2);
-	int l = 0;
-	while ((l + 1) * (l + 1) <= lm) l++;
-	double vr = 0.0, vi = 0.0, dr = 0.0, di = 0.0, wr = 0.0, wi = 0.0;
-	for (int a = 0; a < natoms; a++) {
-		double b = jl[((size_t)a * Q + iq) * K + l];
-		double2 h = ylm[(size_t)a * K2 + lm];
-		double xr = b * h.x, xi = b * h.y;
-		double fv = vac[a], fd = dum[a], fw = wfac[a];
-		vr += fv * xr; vi += fv * xi;
-		dr += fd * xr; di += fd * xi;
-		wr += fw * xr; wi += fw * xi;
+	int iq = blockIdx.x / K, l = blockIdx.x % K;
+	int nm = 2 * l + 1, nslice = EXP_THREADS / nm;
+	int t = threadIdx.x;
+	int mi = t % nm, sl = t / nm;
+	bool acc_thread = sl < nslice;
+	double qv = q[iq];
+	double term0 = 1.0 / odd_factorial(2 * l + 1);
+	double a6[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+	const double2 *yl = ylm + l * l;   /* this l's first (l, m) of every atom row */
+	for (int a0 = 0; a0 < natoms; a0 += EXP_THREADS) {
+		int a = a0 + t;
+		if (a < natoms) {
+			double j = sbessel_fast(l, qv * rad[a], term0);
+			w[0][t] = vac[a] * j;
+			w[1][t] = dum[a] * j;
+			w[2][t] = wfac[a] * j;
+		}
+		__syncthreads();
+		if (acc_thread) {
+			int na = min(EXP_THREADS, natoms - a0);
+			for (int k = sl; k < na; k += nslice) {
+				double2 y = yl[(size_t)(a0 + k) * K2 + mi];
+				double wv = w[0][k], wd = w[1][k], ww = w[2][k];
+				a6[0] = fma(wv, y.x, a6[0]); a6[1] = fma(wv, y.y, a6[1]);
+				a6[2] = fma(wd, y.x, a6[2]); a6[3] = fma(wd, y.y, a6[3]);
+				a6[4] = fma(ww, y.x, a6[4]); a6[5] = fma(ww, y.y, a6[5]);
+			}
+		}
+		__syncthreads();
 	}
-	const double fp = 4.0 * SXS_PI;
-	double cre[4] = {fp, 0.0, -fp, 0.0}, cim[4] = {0.0, fp, 0.0, -fp};
-	double c_r = cre[l % 4], c_i = cim[l % 4];
-	size_t chs = (size_t)Q * K2 * 2;
-	double *o = spf + ((size_t)iq * K2 + lm) * 2;
-	o[0] = c_r * vr - c_i * vi;           o[1] = c_r * vi + c_i * vr;
-	o[chs] = c_r * dr - c_i * di;         o[chs + 1] = c_r * di + c_i * dr;
-	o[2 * chs] = c_r * wr - c_i * wi;     o[2 * chs + 1] = c_r * wi + c_i * wr;
+	if (acc_thread)
+		for (int c = 0; c < 6; c++) red[t][c] = a6[c];
+	__syncthreads();
+	if (t < nm) {
+		double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+		for (int sidx = 0; sidx < nslice; sidx++)
+			for (int c = 0; c < 6; c++) v[c] = v[c] + red[sidx * nm + t][c];
+		const double fp = 4.0 * SXS_PI;
+		double cre[4] = {fp, 0.0, -fp, 0.0}, cim[4] = {0.0, fp, 0.0, -fp};
+		double c_r = cre[l % 4], c_i = cim[l % 4];
+		size_t chs = (size_t)Q * K2 * 2;
+		double *o = spf + ((size_t)iq * K2 + l * l + t) * 2;
+		o[0] = c_r * v[0] - c_i * v[1];           o[1] = c_r * v[1] + c_i * v[0];
+		o[chs] = c_r * v[2] - c_i * v[3];         o[chs + 1] = c_r * v[3] + c_i * v[2];
+		o[2 * chs] = c_r * v[4] - c_i * v[5];     o[2 * chs + 1] = c_r * v[5] + c_i * v[4];
+	}
 }
 
 /* bes[iz][p][q] = j_p(z q) (src/fftsaxs.c:110-121), q fastest. */
@@ -331,10 +383,10 @@ inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 extern "C" {
 
 size_t sxsk_expand_ws_ylm(int natoms, int L) { return (size_t)natoms * (L + 1) * (L + 1) * sizeof(double2); }
-size_t sxsk_expand_ws_jl(int natoms, int Q, int L) { return (size_t)natoms * Q * (L + 1) * sizeof(double); }
+size_t sxsk_expand_ws_rad(int natoms) { return (size_t)natoms * sizeof(double); }
 
 int sxsk_expand(const double *xyz, const double *vac, const double *dum, const double *wfac, int natoms,
-                 const double *q, int Q, int L, const double *ynorm, double2 *ylm_ws, double *jl_ws,
+                 const double *q, int Q, int L, const double *ynorm, double2 *ylm_ws, double *rad_ws,
                  double *spf_out, cudaStream_t s)
 {
 	int K = L + 1;
@@ -342,11 +394,14 @@ int sxsk_expand(const double *xyz, const double *vac, const double *dum, const d
 		cudaMemsetAsync(spf_out, 0, (size_t)3 * Q * K * K * 2 * sizeof(double), s);
 		return cudaGetLastError();
 	}
-	k_ylm<<<nblk((long)natoms * K, 128), 128, 0, s>>>(xyz, natoms, L, ynorm, ylm_ws);
-	k_jl<<<nblk((long)natoms * Q * K, 128), 128, 0, s>>>(xyz, natoms, q, Q, L, jl_ws);
-	k_accum<<<nblk((long)Q * K * K, 128), 128, 0, s>>>(ylm_ws, jl_ws, vac, dum, wfac, natoms, Q, L, spf_out);
+	if ((long)Q * K > 0x7fffffffL) return cudaErrorInvalidValue;
+	k_ylm<<<nblk((long)natoms * K, 128), 128, 0, s>>>(xyz, natoms, L, ynorm, ylm_ws, rad_ws);
+	k_expand_ql<<<Q * K, EXP_THREADS, 0, s>>>(ylm_ws, rad_ws, vac, dum, wfac, natoms, q, Q, L, spf_out);
 	return cudaGetLastError();
 }
+
+/* kernel launches of one sxsk_expand call with atoms */
+int sxsk_expand_launches(void) { return 2; }
 
 int sxsk_bessel_z(const double *z, int nz, const double *q, int Q, int L, double *bes, cudaStream_t s)
 {
@@ -449,10 +504,10 @@ extern "C" int sxsg_expand_noalloc(const double *xyz, const double *vac, const d
 	    (natoms > 0 && (!xyz || !vac || !dum)))
 		return -2;
 	int K = L + 1, N = 2 * L + 1, K2 = K * K;
-	/* layout in doubles: ynorm | Y_lm (complex) | j_l | zero water weights */
+	/* layout in doubles: ynorm | Y_lm (complex) | radii | zero water weights */
 	size_t off_y = ((size_t)K * N + 31) / 32 * 32;
-	size_t off_j = off_y + ((size_t)natoms * K2 * 2 + 31) / 32 * 32;
-	size_t off_w = off_j + ((size_t)natoms * Q * K + 31) / 32 * 32;
+	size_t off_r = off_y + ((size_t)natoms * K2 * 2 + 31) / 32 * 32;
+	size_t off_w = off_r + ((size_t)natoms + 31) / 32 * 32;
 	size_t need = off_w + (water_w ? 0 : (size_t)natoms);
 	if (need > SXS_NOALLOC_DOUBLES) return -3;
 	int dev = 0;
@@ -482,7 +537,7 @@ extern "C" int sxsg_expand_noalloc(const double *xyz, const double *vac, const d
 		if (e != cudaSuccess) return (int)e;
 		w = base + off_w;
 	}
-	int rc = sxsk_expand(xyz, vac, dum, w, natoms, q, Q, L, base, (double2 *)(base + off_y), base + off_j, spf_out, s);
-	sxs_count_launches(natoms > 0 ? 3 : 0);
+	int rc = sxsk_expand(xyz, vac, dum, w, natoms, q, Q, L, base, (double2 *)(base + off_y), base + off_r, spf_out, s);
+	sxs_count_launches(natoms > 0 ? sxsk_expand_launches() : 0);
 	return rc;
 }

@@ -81,7 +81,7 @@ int sxsg_score_exact(const double *rec_xyz, int nrec, const double *lig_xyz, int
 	double *h_xyz = malloc(sizeof(double) * 3 * na * (size_t)B);
 	double *wf = calloc(na, sizeof(double));
 	if (water_w) memcpy(wf, water_w, sizeof(double) * na);
-	double *d_xyz = NULL, *d_vac = NULL, *d_dum = NULL, *d_wf = NULL, *d_q = NULL, *d_a = NULL, *d_jl = NULL;
+	double *d_xyz = NULL, *d_vac = NULL, *d_dum = NULL, *d_wf = NULL, *d_q = NULL, *d_a = NULL, *d_rad = NULL;
 	double *d_spf = NULL, *d_cross = NULL, *d_ct = NULL, *d_chi = NULL, *d_c1 = NULL, *d_c2 = NULL;
 	double2 *d_ylm = NULL;
 	cudaError_t e = cudaSuccess;
@@ -91,7 +91,7 @@ int sxsg_score_exact(const double *rec_xyz, int nrec, const double *lig_xyz, int
 	if (!e) e = cudaMalloc((void **)&d_wf, sizeof(double) * na);
 	if (!e) e = cudaMalloc((void **)&d_q, sizeof(double) * Q);
 	if (!e) e = cudaMalloc((void **)&d_a, sizeof(double) * 6 * Q);
-	if (!e) e = cudaMalloc((void **)&d_jl, sxsk_expand_ws_jl(na, Q, L));
+	if (!e) e = cudaMalloc((void **)&d_rad, sxsk_expand_ws_rad(na));
 	if (!e) e = cudaMalloc((void **)&d_ylm, sxsk_expand_ws_ylm(na, L));
 	if (!e) e = cudaMalloc((void **)&d_spf, sizeof(double) * spf_n * B);
 	if (!e) e = cudaMalloc((void **)&d_cross, sizeof(double) * 6 * Q * (size_t)B);
@@ -111,12 +111,12 @@ int sxsg_score_exact(const double *rec_xyz, int nrec, const double *lig_xyz, int
 		e = cudaMemcpyAsync(d_xyz, h_xyz, sizeof(double) * 3 * na * (size_t)nb, cudaMemcpyHostToDevice, s);
 		for (int k = 0; k < nb && !e; k++)
 			e = (cudaError_t)sxsk_expand(d_xyz + 3 * (size_t)na * k, d_vac, d_dum, d_wf, na, d_q, Q, L, lt->d_ynorm,
-			                             d_ylm, d_jl, d_spf + spf_n * k, s);
+			                             d_ylm, d_rad, d_spf + spf_n * k, s);
 		if (!e) e = (cudaError_t)sxsk_self_cross(d_spf, nb, Q, L, d_cross, s);
 		if (!e)
 			e = (cudaError_t)sxs_fit_lbfgsb_launch(d_cross, 0, d_ct, nb, Q, d_q, d_a, mult, 1.0, 0, d_chi, d_c1, d_c2, NULL,
 			                                       NULL, s);
-		sxs_count_launches(3 * nb + 3);
+		sxs_count_launches(sxsk_expand_launches() * nb + 3);
 		if (!e && chi) e = cudaMemcpyAsync(chi + p0, d_chi, sizeof(double) * nb, cudaMemcpyDeviceToHost, s);
 		if (!e && c1) e = cudaMemcpyAsync(c1 + p0, d_c1, sizeof(double) * nb, cudaMemcpyDeviceToHost, s);
 		if (!e && c2) e = cudaMemcpyAsync(c2 + p0, d_c2, sizeof(double) * nb, cudaMemcpyDeviceToHost, s);
@@ -126,7 +126,7 @@ int sxsg_score_exact(const double *rec_xyz, int nrec, const double *lig_xyz, int
 		if (!e) e = cudaStreamSynchronize(s);
 	}
 	cudaFree(d_xyz); cudaFree(d_vac); cudaFree(d_dum); cudaFree(d_wf); cudaFree(d_q); cudaFree(d_a);
-	cudaFree(d_jl); cudaFree(d_ylm); cudaFree(d_spf); cudaFree(d_cross); cudaFree(d_ct);
+	cudaFree(d_rad); cudaFree(d_ylm); cudaFree(d_spf); cudaFree(d_cross); cudaFree(d_ct);
 	cudaFree(d_chi); cudaFree(d_c1); cudaFree(d_c2);
 	free(h_xyz); free(wf);
 	if (e) return sxs_cuda_fail(e, "sxsg_score_exact");

@@ -119,7 +119,7 @@ int sxsg_expand(const double *xyz, const double *vac, const double *dum, const d
 	size_t spf_n = (size_t)3 * Q * K * K * 2;
 	double *wf = malloc(sizeof(double) * (natoms > 0 ? natoms : 1));
 	for (int i = 0; i < natoms; i++) wf[i] = sasa ? water_ff * sasa[i] : 0.0;
-	double *d_xyz = NULL, *d_vac = NULL, *d_dum = NULL, *d_wf = NULL, *d_q = NULL, *d_jl = NULL, *d_out = NULL;
+	double *d_xyz = NULL, *d_vac = NULL, *d_dum = NULL, *d_wf = NULL, *d_q = NULL, *d_rad = NULL, *d_out = NULL;
 	double2 *d_ylm = NULL;
 	int na = natoms > 0 ? natoms : 1;
 	cudaError_t e = cudaSuccess;
@@ -128,7 +128,7 @@ int sxsg_expand(const double *xyz, const double *vac, const double *dum, const d
 	if (!e) e = cudaMalloc((void **)&d_dum, sizeof(double) * na);
 	if (!e) e = cudaMalloc((void **)&d_wf, sizeof(double) * na);
 	if (!e) e = cudaMalloc((void **)&d_q, sizeof(double) * Q);
-	if (!e) e = cudaMalloc((void **)&d_jl, sxsk_expand_ws_jl(na, Q, L));
+	if (!e) e = cudaMalloc((void **)&d_rad, sxsk_expand_ws_rad(na));
 	if (!e) e = cudaMalloc((void **)&d_ylm, sxsk_expand_ws_ylm(na, L));
 	if (!e) e = cudaMalloc((void **)&d_out, sizeof(double) * spf_n);
 	if (!e && natoms > 0) {
@@ -139,13 +139,13 @@ int sxsg_expand(const double *xyz, const double *vac, const double *dum, const d
 	}
 	if (!e) e = cudaMemcpyAsync(d_q, q, sizeof(double) * Q, cudaMemcpyHostToDevice, s);
 	if (!e) {
-		e = (cudaError_t)sxsk_expand(d_xyz, d_vac, d_dum, d_wf, natoms, d_q, Q, L, lt->d_ynorm, d_ylm, d_jl, d_out, s);
-		sxs_count_launches(natoms > 0 ? 3 : 0);
+		e = (cudaError_t)sxsk_expand(d_xyz, d_vac, d_dum, d_wf, natoms, d_q, Q, L, lt->d_ynorm, d_ylm, d_rad, d_out, s);
+		sxs_count_launches(natoms > 0 ? sxsk_expand_launches() : 0);
 	}
 	if (!e) e = cudaMemcpyAsync(spf_out, d_out, sizeof(double) * spf_n, cudaMemcpyDeviceToHost, s);
 	if (!e) e = cudaStreamSynchronize(s);
 	cudaFree(d_xyz); cudaFree(d_vac); cudaFree(d_dum); cudaFree(d_wf); cudaFree(d_q);
-	cudaFree(d_jl); cudaFree(d_ylm); cudaFree(d_out);
+	cudaFree(d_rad); cudaFree(d_ylm); cudaFree(d_out);
 	free(wf);
 	if (e) return sxs_cuda_fail(e, "sxsg_expand");
 	return 0;

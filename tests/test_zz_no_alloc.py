@@ -80,7 +80,7 @@ def test_noalloc_expansion_matches_regular_entry_twice(gpu):
 def test_noalloc_rejects_requests_beyond_the_static_array(gpu):
     torch = pytest.importorskip("torch")
     L, Q = 30, 201
-    n = 2000  # needs about 2000 * (2*961 + 201*31) doubles > 8 Mi
+    n = 5000  # needs about 5000 * (2*961 + 2) doubles > 8 Mi
     xyz = np.random.default_rng(0).normal(size=(n, 3)) * 10
     rc, _ = _call_noalloc(gpu, torch, xyz, np.ones(n), np.ones(n), None, gpu.mkarray(0.0, 0.5, Q), L)
     assert rc == -3
