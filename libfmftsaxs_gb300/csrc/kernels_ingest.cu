@@ -28,16 +28,20 @@
 
 namespace {
 
-/* margins of the host fallback: acos arguments within ING_EDGE of +-1 (the
- * slope 1/sqrt(1 - x^2) reaches 700 there), sin beta below ING_SIN, matrix
- * entries whose sign is tested below ING_SIGN, values whose 1000-fold
- * fractional part is within ING_HALF of 1/2 */
+/* margins of the host fallback: acos arguments within ING_EDGE of +-1 on
+ * either side (inside, the slope 1/sqrt(1 - x^2) passes 700; just outside,
+ * the value is clamped, and both machines must land on the same side),
+ * sin beta below ING_SIN, matrix entries whose sign is tested below
+ * ING_SIGN, values whose 1000-fold fractional part is within ING_HALF of
+ * 1/2.  Arguments further outside [-1, 1] clamp to exactly +-1 on both. */
 #define ING_EDGE 1e-6
 #define ING_SIN 1e-3
 #define ING_SIGN 1e-9
 #define ING_HALF 1e-5
 
 __device__ __forceinline__ double clamp1(double a) { return a < -1.0 ? -1.0 : (a > 1.0 ? 1.0 : a); }
+
+__device__ __forceinline__ bool near_one(double x) { return fabs(fabs(x) - 1.0) < ING_EDGE; }
 
 __device__ __forceinline__ bool near_half(double v)
 {
@@ -75,12 +79,12 @@ __global__ void k_pose_ingest(const double *__restrict__ rot, const double *__re
 	double z = round(sqrt(vx * vx + vy * vy + vz * vz));
 	bool flag = false;
 	double x = vz / z;
-	flag |= fabs(x) > 1.0 - ING_EDGE;
+	flag |= near_one(x);
 	double b1 = acos(clamp1(x));
 	double sb1 = sin(b1);
 	flag |= sb1 < ING_SIN;
 	x = -vx / (z * sb1);
-	flag |= fabs(x) > 1.0 - ING_EDGE;
+	flag |= near_one(x);
 	double g1 = acos(clamp1(x));
 	if (vy / (z * sb1) < 0.0) g1 = 2 * SXS_PI - g1;
 	/* receptor rotation R(0, b1, g1) (sxs_fill_active_rotation_matrix with
@@ -94,17 +98,17 @@ __global__ void k_pose_ingest(const double *__restrict__ rot, const double *__re
 	double l31 = a31 * m[0] + a32 * m[3] + a33 * m[6];
 	double l32 = a31 * m[1] + a32 * m[4] + a33 * m[7];
 	double l33 = a31 * m[2] + a32 * m[5] + a33 * m[8];
-	flag |= fabs(l33) > 1.0 - ING_EDGE;
+	flag |= near_one(l33);
 	double b2 = acos(clamp1(l33));
 	double sb2 = sin(b2);
 	flag |= sb2 < ING_SIN;
 	x = l13 / sb2;
-	flag |= fabs(x) > 1.0 - ING_EDGE;
+	flag |= near_one(x);
 	double a2 = acos(clamp1(x));
 	flag |= fabs(l23) < ING_SIGN;
 	if (l23 / sb2 < 0.0) a2 = 2 * SXS_PI - a2;
 	x = -l31 / sb2;
-	flag |= fabs(x) > 1.0 - ING_EDGE;
+	flag |= near_one(x);
 	double g2 = acos(clamp1(x));
 	flag |= fabs(l32) < ING_SIGN;
 	if (l32 / sb2 < 0.0) g2 = 2 * SXS_PI - g2;
