@@ -289,6 +289,14 @@ int sxsg_plan_set_budget(sxsg_plan *plan, size_t bytes);
  * context as unusable). */
 enum { SXSG_ROT_CUDA = 0, SXSG_ROT_TC = 1 };
 int sxsg_plan_set_rotation(sxsg_plan *plan, int engine);
+/* Tile choices of a mixed-precision plan: slices of combos per block of the
+ * pipelined translation (1..64) and gamma pairs per thread of the rotation
+ * (2, 4, 6, 8, 12 or 16; values below what L + 1 needs are raised to it);
+ * 0 keeps the default, the entry of the library's autotuned table nearest
+ * to the plan's (L, Q) (sxsg_tiles_default).  Results do not depend on
+ * them. */
+int sxsg_plan_set_tiles(sxsg_plan *plan, int tr_slices, int rot_gamma);
+int sxsg_tiles_default(int L, int Q, int *tr_slices, int *rot_gamma);
 /* Run the GPU work for the current pose list (asynchronous until results). */
 int sxsg_plan_run(sxsg_plan *plan, int fit_mode);
 /* Copy results to the host.  Any pointer may be NULL.  chi/c1/c2/cell: [n];

@@ -194,6 +194,11 @@ class Plan:
         load().sxsg_plan_set_rotation.argtypes = [C.c_void_p, C.c_int]
         _check(load().sxsg_plan_set_rotation(self.h, int(engine)))
 
+    def set_tiles(self, tr_slices=0, rot_gamma=0):
+        """Tile choices (sxsg_plan_set_tiles); 0 keeps the tuned default."""
+        load().sxsg_plan_set_tiles.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        _check(load().sxsg_plan_set_tiles(self.h, int(tr_slices), int(rot_gamma)))
+
     def set_budget(self, nbytes):
         load().sxsg_plan_set_budget.argtypes = [C.c_void_p, C.c_size_t]
         _check(load().sxsg_plan_set_budget(self.h, int(nbytes)))
@@ -390,6 +395,14 @@ def poses_to_indices(rot, tr, zvals, L, ref_lig=(0.0, 0.0, 0.0), wrap=False):
     if k < 0:
         raise SxsError(last_error())
     return idx[keep.astype(bool)], keep.astype(bool)
+
+
+def tiles_default(L, Q):
+    """(slices per translation block, gamma pairs per rotation thread) of the
+    library's autotuned table for (L, Q) (sxsg_tiles_default)."""
+    sb, g = C.c_int(0), C.c_int(0)
+    _check(load().sxsg_tiles_default(C.c_int(L), C.c_int(Q), C.byref(sb), C.byref(g)))
+    return sb.value, g.value
 
 
 def poses_to_indices_gpu(rot, tr, zvals, L, ref_lig=(0.0, 0.0, 0.0), wrap=False, full=False):

@@ -84,7 +84,8 @@ int sxsk_const_int(const double *A, const double *B, int Q, int L, double *cst, 
 /* rotation table, m >= 0: out[(b,g)][pair][ch][q] = sum_{m1} tw[(m1' g) mod N] d^l_{m m1}(beta_b) C[ch][l,m1][q]
  * with C = spf_t, conjugated when conj != 0. */
 int sxsk_rotate(const void *spf_t, const void *dtab, const double2 *tw, int Q, int L, int conj, void *out,
-                int fp32, cudaStream_t s);   /* dtab in float when fp32 */
+                int fp32, int gsel, cudaStream_t s);   /* dtab in float when fp32; gsel: gamma pairs per
+                                                       * thread (0 = the fewest that cover L + 1) */
 
 /* The mixed path's rotation table on the tcgen05 tensor cores (3xTF32,
  * FP32 accumulation in tensor memory); same output as sxsk_rotate with
@@ -117,7 +118,8 @@ int sxsk_pose_scatter(const sxsk_pose *tmp, const int32_t *key, int64_t n, int32
 /* kernel launches one sxsk_translate call makes for this L */
 int sxsk_translate_launches(int L);
 int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, const int32_t *slices, int nslice,
-                   int cbase, int ncombo, int nzt, int Q, int L, void *R, int fp32, cudaStream_t s);
+                   int cbase, int ncombo, int nzt, int Q, int L, void *R, int fp32, int sb, cudaStream_t s);
+/* sb: slices per block of the pipelined FP32 kernel (0 = 8) */
 
 /* per-pose raw cross terms: cross[p][c][q] = cst[c][q] + 2 Re sum_m tw(m' a2) sum_l P R,
  * the m < 0 half folded in by symmetry; R holds the ncombo combos from combo_base.

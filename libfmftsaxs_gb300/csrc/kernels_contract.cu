@@ -503,7 +503,8 @@ __device__ __forceinline__ void cp_async16(void *sdst, const void *gsrc)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-/* slices per block of the pipelined column kernel */
+/* slices per block of the pipelined column kernel, unless a plan's tile
+ * choice (autotuned per L and Q) says otherwise */
 #define TP_SB 8
 
 /* shared bytes of k_translate_pipe<NB>: tau^m [8 q][NB NB + 4] and the U
@@ -511,7 +512,7 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 #define TP_SMEM(NB) (sizeof(float) * SXS_QT * ((NB) * (NB) + 4) + sizeof(float2) * SXS_SLICE * (NB) * 3 * SXS_QT)
 
 /* The FP32 column form with three channels per thread, pipelined over
- * slices: block = (tile, run of TP_SB consecutive slices, m); while the
+ * slices: block = (tile, run of sb consecutive slices, m); while the
  * threads apply tau^m to one slice's U columns (held in registers: 6 NB
  * floats), the U columns of the next slice stream into shared memory with
  * cp.async, so the global-load latency of the low occupancy that these
@@ -523,20 +524,20 @@ template <int NB>
 __global__ void __launch_bounds__(TCOL_THREADS(3), NB <= 8 ? 5 : (NB <= 12 ? 4 : (NB <= 20 ? 3 : (NB <= 28 ? 2 : 1))))
 k_translate_pipe(const float2 *__restrict__ U, const float *__restrict__ tau, const int32_t *__restrict__ combo_zbg,
                  const int32_t *__restrict__ slices, int nslice, int cbase, int ncombo, int L, int nzt, int m_lo,
-                 int nm, float2 *__restrict__ R)
+                 int nm, int sb, float2 *__restrict__ R)
 {
 	extern __shared__ __align__(16) unsigned char tps_raw[];
 	const int qstride = NB * NB + 4, rowf = 3 * SXS_QT;   /* float2 per pair of one combo */
 	float *ts = reinterpret_cast<float *>(tps_raw);
 	float2 *us = reinterpret_cast<float2 *>(tps_raw + sizeof(float) * SXS_QT * qstride);
 	int K = L + 1, N = 2 * L + 1, NP = K * (K + 1) / 2, nrow = K * N;
-	int ng = (nslice + TP_SB - 1) / TP_SB;
+	int ng = (nslice + sb - 1) / sb;
 	int bid = blockIdx.x;
 	int mi = bid % nm;
 	bid /= nm;
 	int gi = bid % ng, t = bid / ng;
 	int m = m_lo + mi, n = K - m, po = psym(m, K);
-	int s0 = gi * TP_SB, s1 = s0 + TP_SB < nslice ? s0 + TP_SB : nslice;
+	int s0 = gi * sb, s1 = s0 + sb < nslice ? s0 + sb : nslice;
 	int q = threadIdx.x % SXS_QT, cl = threadIdx.x / SXS_QT;
 	/* 16-byte chunks of one combo's n pairs: n x 3 x 8 float2 = 12 n; the
 	 * 8 threads of combo cl copy its chunks in 128-byte rows */
@@ -976,7 +977,7 @@ inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 template <typename S, int NB>
 static cudaError_t translate_col_launch(const void *U, const void *tau, const int32_t *combo_zbg,
                                         const int32_t *slices, int nslice, int cbase, int ncombo, int nzt, int NT,
-                                        int L, void *R, cudaStream_t s)
+                                        int L, void *R, int sb, cudaStream_t s)
 {
 	typedef typename Cx<S>::T V;
 	int K = L + 1;
@@ -988,7 +989,7 @@ static cudaError_t translate_col_launch(const void *U, const void *tau, const in
 	int nm = m_hi - m_lo + 1;
 	if constexpr (sizeof(S) == 4) {
 		/* FP32: three channels per thread, pipelined over runs of slices */
-		long nb = (long)NT * ((nslice + TP_SB - 1) / TP_SB) * nm;
+		long nb = (long)NT * ((nslice + sb - 1) / sb) * nm;
 		if (nb > 0x7fffffffL) return cudaErrorInvalidValue;
 		size_t smem = TP_SMEM(NB);
 		auto kern = k_translate_pipe<NB>;
@@ -1001,7 +1002,7 @@ static cudaError_t translate_col_launch(const void *U, const void *tau, const in
 		                                     (int)cudaSharedmemCarveoutMaxShared);
 		if (e != cudaSuccess) return e;
 		kern<<<(unsigned)nb, TCOL_THREADS(3), smem, s>>>((const float2 *)U, (const float *)tau, combo_zbg, slices,
-		                                                 nslice, cbase, ncombo, L, nzt, m_lo, nm, (float2 *)R);
+		                                                 nslice, cbase, ncombo, L, nzt, m_lo, nm, sb, (float2 *)R);
 		return cudaGetLastError();
 	} else {
 		/* FP64 (bound by its pipe): one channel per thread */
@@ -1021,18 +1022,18 @@ static cudaError_t translate_col_launch(const void *U, const void *tau, const in
 
 template <typename S>
 static cudaError_t translate_col_all(const void *U, const void *tau, const int32_t *combo_zbg, const int32_t *slices,
-                                     int nslice, int cbase, int ncombo, int nzt, int NT, int L, void *R,
+                                     int nslice, int cbase, int ncombo, int nzt, int NT, int L, void *R, int sb,
                                      cudaStream_t s)
 {
 	cudaError_t e = cudaSuccess;
-	if (!e) e = translate_col_launch<S, 4>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, s);
-	if (!e) e = translate_col_launch<S, 8>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, s);
-	if (!e) e = translate_col_launch<S, 12>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, s);
-	if (!e) e = translate_col_launch<S, 16>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, s);
-	if (!e) e = translate_col_launch<S, 20>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, s);
-	if (!e) e = translate_col_launch<S, 24>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, s);
-	if (!e) e = translate_col_launch<S, 28>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, s);
-	if (!e) e = translate_col_launch<S, 32>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, s);
+	if (!e) e = translate_col_launch<S, 4>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, sb, s);
+	if (!e) e = translate_col_launch<S, 8>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, sb, s);
+	if (!e) e = translate_col_launch<S, 12>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, sb, s);
+	if (!e) e = translate_col_launch<S, 16>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, sb, s);
+	if (!e) e = translate_col_launch<S, 20>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, sb, s);
+	if (!e) e = translate_col_launch<S, 24>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, sb, s);
+	if (!e) e = translate_col_launch<S, 28>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, sb, s);
+	if (!e) e = translate_col_launch<S, 32>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, sb, s);
 	return e;
 }
 
@@ -1093,10 +1094,13 @@ static int rotate_launch(const void *spf_t, const void *dtab, const double2 *tw,
 
 template <typename S>
 static int rotate_any(const void *spf_t, const void *dtab, const double2 *tw, int Q, int L, int conj, void *out,
-                      cudaStream_t s)
+                      int gsel, cudaStream_t s)
 {
-	/* gamma pairs per thread: the L + 1 pairs over ROT_GROUPS groups */
+	/* gamma pairs per thread: at least the L + 1 pairs over ROT_GROUPS
+	 * groups; a larger choice (gsel) leaves groups idle for fewer blocks'
+	 * worth of twiddle setup */
 	int need = (L + 1 + ROT_GROUPS - 1) / ROT_GROUPS;
+	if (gsel > need) need = gsel;
 	if (need <= 2) return rotate_launch<S, 2>(spf_t, dtab, tw, Q, L, conj, out, s);
 	if (need <= 4) return rotate_launch<S, 4>(spf_t, dtab, tw, Q, L, conj, out, s);
 	if (need <= 6) return rotate_launch<S, 6>(spf_t, dtab, tw, Q, L, conj, out, s);
@@ -1117,11 +1121,11 @@ int sxsk_spf_transpose(const double *flat, void *spf_t, int Q, int L, int fp32, 
 }
 
 int sxsk_rotate(const void *spf_t, const void *dtab, const double2 *tw, int Q, int L, int conj, void *out, int fp32,
-                cudaStream_t s)
+                int gsel, cudaStream_t s)
 {
 	if (L < 0 || L + 1 > SXS_LMAX_K || Q <= 0) return cudaErrorInvalidValue;
-	if (fp32) return rotate_any<float>(spf_t, dtab, tw, Q, L, conj, out, s);
-	return rotate_any<double>(spf_t, dtab, tw, Q, L, conj, out, s);
+	if (fp32) return rotate_any<float>(spf_t, dtab, tw, Q, L, conj, out, gsel, s);
+	return rotate_any<double>(spf_t, dtab, tw, Q, L, conj, out, gsel, s);
 }
 
 int sxsk_to_float(const double *a, float *b, long n, cudaStream_t s)
@@ -1167,14 +1171,15 @@ int sxsk_translate_launches(int L)
 }
 
 int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, const int32_t *slices, int nslice,
-                   int cbase, int ncombo, int nzt, int Q, int L, void *R, int fp32, cudaStream_t s)
+                   int cbase, int ncombo, int nzt, int Q, int L, void *R, int fp32, int sb, cudaStream_t s)
 {
 	if (nslice <= 0) return 0;
 	int NT = (Q + SXS_QT - 1) / SXS_QT;
+	if (sb < 1) sb = TP_SB;
 	if (L + 1 <= 32) {
 		if (fp32)
-			return translate_col_all<float>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, s);
-		return translate_col_all<double>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, s);
+			return translate_col_all<float>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, sb, s);
+		return translate_col_all<double>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, sb, s);
 	}
 	return translate_slices(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, Q, L, R, fp32, s);
 }

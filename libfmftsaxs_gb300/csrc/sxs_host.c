@@ -195,6 +195,7 @@ struct sxsg_plan {
 	void *d_P, *d_U;
 	int ext_tables;             /* P and U belong to the caller (serving cache) */
 	int rot_engine;             /* SXSG_ROT_*: rotation on CUDA cores or tensor cores */
+	int tr_slices, rot_gamma;   /* tile choices (sxsg_plan_set_tiles; 0 = the tuned table's) */
 	int tc_used;                /* the last run rotated on the tensor cores */
 	float *d_amat;              /* twiddle operand of the tensor-core rotation */
 	int *d_tcstat;              /* its status word (kernels.h, sxsk_rotate_tc) */
@@ -401,7 +402,39 @@ int sxs_plan_create_on(sxsg_plan **out, const double *A, const double *B, const 
 	size_t fr = 0, tot = 0;
 	cudaMemGetInfo(&fr, &tot);
 	p->r_budget = fr / 2;
+	sxsg_tiles_default(L, Q, &p->tr_slices, &p->rot_gamma);
 	*out = p;
+	return 0;
+}
+
+#include "tiles_table.h"
+
+int sxsg_tiles_default(int L, int Q, int *tr_slices, int *rot_gamma)
+{
+	int best = 0;
+	long bd = -1;
+	for (int i = 0; i < (int)(sizeof(sxs_tiles_table) / sizeof(sxs_tiles_table[0])); i++) {
+		long d = 100000L * labs((long)sxs_tiles_table[i].L - L) + labs((long)sxs_tiles_table[i].Q - Q);
+		if (bd < 0 || d < bd) {
+			bd = d;
+			best = i;
+		}
+	}
+	if (tr_slices) *tr_slices = sxs_tiles_table[best].tr_slices;
+	if (rot_gamma) *rot_gamma = sxs_tiles_table[best].rot_gamma;
+	return 0;
+}
+
+int sxsg_plan_set_tiles(sxsg_plan *p, int tr_slices, int rot_gamma)
+{
+	if (!p || tr_slices < 0 || tr_slices > 64 || (rot_gamma != 0 && rot_gamma != 2 && rot_gamma != 4 &&
+	                                              rot_gamma != 6 && rot_gamma != 8 && rot_gamma != 12 &&
+	                                              rot_gamma != 16))
+		return sxs_fail(-2, "sxsg_plan_set_tiles: bad tile choice");
+	int dsb = 0, dg = 0;
+	sxsg_tiles_default(p->L, p->Q, &dsb, &dg);
+	p->tr_slices = tr_slices ? tr_slices : dsb;
+	p->rot_gamma = rot_gamma ? rot_gamma : dg;
 	return 0;
 }
 
@@ -642,12 +675,12 @@ static int plan_rotations(sxsg_plan *p)
 		if (tc) SXS_CU(cudaMemsetAsync(p->d_tcstat, 0, sizeof(int), s));
 		if (!p->ext_tables || !p->P_valid) {
 			if (tc) SXS_K(sxsk_rotate_tc(p->d_At, p->lt->d_dtabf, p->d_tw, Q, L, 0, p->d_P, p->d_amat, p->d_tcstat, s));
-			else SXS_K(sxsk_rotate(p->d_At, dtab, p->d_tw, Q, L, 0, p->d_P, p->fp32, s));
+			else SXS_K(sxsk_rotate(p->d_At, dtab, p->d_tw, Q, L, 0, p->d_P, p->fp32, p->rot_gamma, s));
 			sxs_count_launches(tc ? 2 : 1);
 		}
 		if (!p->ext_tables || !p->U_valid) {
 			if (tc) SXS_K(sxsk_rotate_tc(p->d_Bt, p->lt->d_dtabf, p->d_tw, Q, L, 1, p->d_U, p->d_amat, p->d_tcstat, s));
-			else SXS_K(sxsk_rotate(p->d_Bt, dtab, p->d_tw, Q, L, 1, p->d_U, p->fp32, s));
+			else SXS_K(sxsk_rotate(p->d_Bt, dtab, p->d_tw, Q, L, 1, p->d_U, p->fp32, p->rot_gamma, s));
 			sxs_count_launches(tc ? 2 : 1);
 		}
 		p->tc_used = tc;
@@ -719,7 +752,7 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 		cudaEvent_t *e = p->cev + 3 * k;
 		SXS_CU(cudaEventRecord(e[0], s));
 		SXS_K(sxsk_translate(p->d_U, tau, p->d_combo + 3 * c0, p->d_slices + 2 * s0, (int)(s1 - s0), (int)c0,
-		                     (int)(c1 - c0), p->nzt, Q, L, p->d_R, p->fp32, s));
+		                     (int)(c1 - c0), p->nzt, Q, L, p->d_R, p->fp32, p->tr_slices, s));
 		SXS_CU(cudaEventRecord(e[1], s));
 		int64_t p0 = p->h_cstart[c0], p1 = p->h_cstart[c1];
 		SXS_K(sxsk_pose_cross(p->d_poses + p0, (int)(p1 - p0), (int)c0, (int)(c1 - c0), p->d_P, p->d_R, p->d_tw,

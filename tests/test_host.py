@@ -218,3 +218,12 @@ def test_pose_ingestion_wrap_option(lib):
     # sum of N (gamma2), N^2 (gamma1) and N^3 (alpha2)
     d = raw[diff] - wrapped[diff]
     assert np.all(d > 0) and np.all(d % N == 0)
+
+
+def test_tile_table_defaults(lib):
+    """The compiled-in tile table answers every (L, Q) with valid choices."""
+    for L in (5, 10, 15, 20, 25, 30, 40):
+        for Q in (8, 51, 101, 201, 400):
+            sb, g = lib.tiles_default(L, Q)
+            assert 1 <= sb <= 64
+            assert g in (0, 2, 4, 6, 8, 12, 16)
