@@ -321,6 +321,38 @@ int sxsg_plan_timings(sxsg_plan *plan, double *ms5);
 int sxsg_plan_chunks(const sxsg_plan *plan);
 void sxsg_plan_destroy(sxsg_plan *plan);
 
+/* ------------------------------------------------------------ batches
+ * Many dimers of uneven size (each its own L, q grid, experiment, pose list
+ * and fit grid) scored together: a batch captures, once, one CUDA graph of
+ * persistent kernels over all of them (the per-z tables per dimer; one
+ * launch per rotation group size; per phase one translation launch per
+ * column class and one per-pose launch; one fit launch), whose blocks take
+ * (dimer, tile, slice / pose block / pose group) work items largest first.
+ * A phase translates the chunks of several dimers into one shared device
+ * arena.  Plans: mixed precision, L <= 31, own rotation tables, pose lists
+ * set; each plan's results equal a sxsg_plan_run of it bit for bit and are
+ * read with sxsg_plan_results / sxsg_plan_topk after sxsg_batch_run.
+ * A batch holds the plans' device pointers: changing a plan's poses, tiles
+ * or budget, or destroying it, needs a new batch. */
+typedef struct sxsg_batch sxsg_batch;
+typedef struct {
+	int plans;          /* dimers */
+	int phases;         /* arena fills of the translated tables */
+	int launches;       /* kernel launches of one replay */
+	int64_t items;      /* work items of all persistent launches */
+	int64_t poses;      /* poses scored by one replay */
+	size_t arena_bytes; /* translated-table arena */
+	double ms[4];       /* last replay: [0] tables, [1] translation + per-pose, [2] fit, [3] whole graph */
+} sxsg_batch_stats;
+/* fit_mode: SXSG_FIT_GRID or SXSG_FIT_NONE; arena_bytes: upper bound on
+ * the translated-table arena (0 = what the dimers need, at most half the
+ * free device memory) */
+int sxsg_batch_create(sxsg_plan *const *plans, int nplan, int fit_mode, size_t arena_bytes, sxsg_batch **batch);
+/* one replay of the graph; returns when it has finished */
+int sxsg_batch_run(sxsg_batch *batch);
+int sxsg_batch_stats_get(const sxsg_batch *batch, sxsg_batch_stats *stats);
+void sxsg_batch_destroy(sxsg_batch *batch);
+
 /* ------------------------------------------------------------ serving
  * A persistent pool of workers that keeps the GPU busy with many scoring
  * jobs (the FFT-correlate work of sxs_compute_saxs_scores for one dimer

@@ -256,6 +256,51 @@ class Plan:
             pass
 
 
+class _BatchStats(C.Structure):
+    _fields_ = [("plans", C.c_int), ("phases", C.c_int), ("launches", C.c_int), ("items", C.c_int64),
+                ("poses", C.c_int64), ("arena_bytes", C.c_size_t), ("ms", C.c_double * 4)]
+
+
+class Batch:
+    """Many mixed-precision plans scored by one CUDA graph of persistent
+    kernels (sxsg_batch_*).  The plans keep their results: read them with
+    Plan.results / Plan.topk after run().  The batch holds the plans'
+    device pointers: keep the plans alive and unchanged while it exists."""
+
+    def __init__(self, plans, fit=FIT_GRID, arena_bytes=0):
+        lib = load()
+        lib.sxsg_batch_create.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_size_t, C.POINTER(C.c_void_p)]
+        lib.sxsg_batch_run.argtypes = [C.c_void_p]
+        lib.sxsg_batch_stats_get.argtypes = [C.c_void_p, C.POINTER(_BatchStats)]
+        lib.sxsg_batch_destroy.argtypes = [C.c_void_p]
+        lib.sxsg_batch_destroy.restype = None
+        self.plans = list(plans)
+        arr = (C.c_void_p * len(self.plans))(*[p.h.value for p in self.plans])
+        self.h = C.c_void_p()
+        _check(lib.sxsg_batch_create(arr, len(self.plans), int(fit), int(arena_bytes), C.byref(self.h)))
+
+    def run(self):
+        _check(load().sxsg_batch_run(self.h))
+
+    def stats(self):
+        st = _BatchStats()
+        _check(load().sxsg_batch_stats_get(self.h, C.byref(st)))
+        return dict(plans=st.plans, phases=st.phases, launches=st.launches, items=int(st.items),
+                    poses=int(st.poses), arena_bytes=int(st.arena_bytes), tables_ms=st.ms[0],
+                    phases_ms=st.ms[1], fit_ms=st.ms[2], total_ms=st.ms[3])
+
+    def close(self):
+        if self.h:
+            load().sxsg_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class _Request(C.Structure):
     _fields_ = [("A", C.c_void_p), ("B", C.c_void_p), ("keyA", C.c_uint64), ("keyB", C.c_uint64),
                 ("qvals", C.c_void_p), ("qnum", C.c_int), ("zvals", C.c_void_p), ("znum", C.c_int), ("L", C.c_int),

@@ -17,7 +17,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU = {"kernels_faithful.cu": ["-fmad=false"], "kernels_contract.cu": [], "kernels_lbfgsb.cu": ["-fmad=false"],
       "kernels_fitdf.cu": ["-fmad=false"], "kernels_tc.cu": [], "kernels_topk.cu": [],
       "kernels_ingest.cu": ["-fmad=false"]}
-C = ["sxs_host.c", "sxs_api.c", "sxs_tables.c", "sxs_serve.c", "sxs_exact.c"]
+C = ["sxs_host.c", "sxs_api.c", "sxs_tables.c", "sxs_serve.c", "sxs_exact.c", "sxs_batch.c"]
 
 
 def _cuda_home():

@@ -115,6 +115,11 @@ int sxsk_pose_decode(const int64_t *index, int64_t n, int N, int nb, int nz, sxs
                      int32_t *cnt, int32_t *zused, unsigned long long *err, cudaStream_t s);
 int sxsk_pose_scatter(const sxsk_pose *tmp, const int32_t *key, int64_t n, int32_t *pos, const int32_t *cid,
                       sxsk_pose *out, cudaStream_t s);
+/* gamma pairs per thread of the rotation for L and a tile choice gsel
+ * (0 = the fewest that cover L + 1): 2, 4, 6, 8, 12 or 16; 0 if none */
+int sxsk_rotate_group(int L, int gsel);
+/* slices per block of the pipelined FP32 translation when a plan sets none */
+#define SXSK_TP_SB 8
 /* kernel launches one sxsk_translate call makes for this L */
 int sxsk_translate_launches(int L);
 int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, const int32_t *slices, int nslice,
@@ -170,6 +175,71 @@ int sxsk_topk(const double *chi, const double *c1, const double *c2, long n, int
 int sxsk_pose_ingest(const double *rot, const double *tr, long n, const double *ref, const double *zvals, int znum,
                      int L, int wrap, long long *index, unsigned char *keep, unsigned int *nflag, long long *flagged,
                      cudaStream_t s);
+
+/* ------------------------------------------------------------------
+ * Batched persistent launches of the mixed path (many dimers at once).
+ * Each kernel runs a grid of (SMs x resident blocks) that take work items
+ * from an array in order through an atomic counter (*ctr, zeroed by the
+ * caller; a block takes the next item when it finishes one, so the array
+ * is ordered largest first).  An item is one block's work of the
+ * single-dimer kernel, on the job its first field names, and runs that
+ * kernel's own block code: results equal the single-dimer launches bit
+ * for bit.
+ */
+typedef struct {
+	const void *spf_t;      /* transposed coefficients (float) */
+	const void *dtab;       /* float Wigner-d table of L */
+	const double2 *tw;      /* twiddles [N] */
+	void *out;              /* rotation table (float) */
+	int Q, L, conj, pad;
+} sxsk_rot_job;
+/* items {job, q tile, beta b, m}; G = gamma pairs per thread (the
+ * single-dimer choice: 2, 4, 6, 8, 12 or 16); every job with N + (G-1) L
+ * <= tw_max twiddle pairs */
+int sxsk_rotate_batch(const sxsk_rot_job *jobs, const int4 *items, int nitems, int G, int tw_max, int *ctr,
+                      cudaStream_t s);
+
+typedef struct {
+	const void *U, *tau;              /* ligand rotation table, float tau of the job's z */
+	const int32_t *combo_zbg;         /* the chunk's combos (cbase = the first one's index) */
+	const int32_t *slices;            /* the chunk's slices */
+	void *R;                          /* the chunk's translated table */
+	int nslice, cbase, ncombo, L, nzt, sb;
+} sxsk_tr_job;
+/* items {job, q tile, slice group, m} for the m with L + 1 - m in
+ * (NB - 4, NB] (the pipelined FP32 kernel of that NB; L + 1 <= 32) */
+int sxsk_translate_batch(const sxsk_tr_job *jobs, const int4 *items, int nitems, int NB, int *ctr, cudaStream_t s);
+
+typedef struct {
+	const sxsk_pose *poses;           /* the chunk's poses */
+	const void *P, *R;                /* receptor rotation table, the chunk's translated table */
+	const double2 *tw;
+	const void *cst;                  /* double-float self terms */
+	void *cross;                      /* double-float cross terms of the dimer */
+	int npose, combo_base, ncombo, Q, L, pad;
+} sxsk_pc_job;
+/* items {job, q tile, block of 32 poses, 0} */
+int sxsk_pose_cross_batch(const sxsk_pc_job *jobs, const int4 *items, int nitems, int *ctr, cudaStream_t s);
+
+typedef struct {
+	const float2 *cross;
+	const sxsk_pose *order;
+	const double *fc;
+	const float2 *gdf;
+	const double *c1g, *c2g;
+	double *chi, *c1, *c2;
+	int32_t *cell;
+	double *grid;
+	double a0sum, peak;
+	int slot0, nslot, Q, n1, n2, tp, ppb, qc, gsm, pad;
+} sxsk_fit_job;
+/* the double-float grid fit's block shape for (Q, n1, n2): threads per pose
+ * tp, poses per block ppb, q per staged chunk qc, G staged in shared memory
+ * gsm, shared bytes; nonzero when no shape fits */
+int sxsk_fit_df_shape(int Q, int n1, int n2, int *tp, int *ppb, int *qc, int *gsm, size_t *smem);
+/* items {job, group of ppb poses}; smem = the largest shape's bytes */
+int sxsk_fit_grid_df_batch(const sxsk_fit_job *jobs, const int2 *items, int nitems, size_t smem, int *ctr,
+                           cudaStream_t s);
 
 #ifdef __cplusplus
 }

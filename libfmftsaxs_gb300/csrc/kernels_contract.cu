@@ -41,6 +41,16 @@ __device__ __forceinline__ void cfma(double2 &acc, double2 a, double2 b)
 }
 __device__ __forceinline__ float fma_s(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double fma_s(double a, double b, double c) { return fma(a, b, c); }
+/* Roundings written out: the rotation, translation and per-pose code leaves
+ * no multiply-add to the compiler to fuse or not, so every kernel that
+ * inlines it (the single-dimer and the batched launches) computes the same
+ * bits. */
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
 template <typename V> __device__ __forceinline__ V zero2() { V v; v.x = 0; v.y = 0; return v; }
 template <typename V> __device__ __forceinline__ V from2(double2 a) { V v; v.x = a.x; v.y = a.y; return v; }
 
@@ -167,13 +177,15 @@ __device__ __forceinline__ void rot_acc(double2 &A, double2 &B, const RotTw<doub
 /* X(gamma) = y0 + A + (h- part), X(N - gamma) = y0 + A - (h- part) */
 __device__ __forceinline__ void rot_out(float2 y0, float2 A, float2 B, float2 &xp, float2 &xm)
 {
-	xp = make_float2(y0.x + A.x - B.y, y0.y + A.y + B.x);
-	xm = make_float2(y0.x + A.x + B.y, y0.y + A.y - B.x);
+	float ax = add_rn(y0.x, A.x), ay = add_rn(y0.y, A.y);
+	xp = make_float2(sub_rn(ax, B.y), add_rn(ay, B.x));
+	xm = make_float2(add_rn(ax, B.y), sub_rn(ay, B.x));
 }
 __device__ __forceinline__ void rot_out(double2 y0, double2 A, double2 B, double2 &xp, double2 &xm)
 {
-	xp = make_double2(y0.x + A.x + B.x, y0.y + A.y + B.y);
-	xm = make_double2(y0.x + A.x - B.x, y0.y + A.y - B.y);
+	double ax = add_rn(y0.x, A.x), ay = add_rn(y0.y, A.y);
+	xp = make_double2(add_rn(ax, B.x), add_rn(ay, B.y));
+	xm = make_double2(sub_rn(ax, B.x), sub_rn(ay, B.y));
 }
 
 #define ROT_GROUPS 4
@@ -193,23 +205,22 @@ __device__ __forceinline__ void rot_out(double2 y0, double2 A, double2 B, double
  * channel and accumulates its G gamma pairs in registers; with CH = 3 one
  * twiddle load and index step serve the three channels.  The padding
  * q >= Q is written as zeros. */
+/* the extended twiddles hs[N + (G-1) L] of a rotation block (all threads) */
+template <typename S, int G>
+__device__ __forceinline__ void rotate_stage(const double2 *__restrict__ tw, int L, RotTw<S> *hs)
+{
+	int N = 2 * L + 1, ne = N + (G - 1) * L;
+	for (int k = threadIdx.x; k < ne; k += blockDim.x) hs[k] = rot_tw<S>(tw, k, N);
+}
+
+/* one block of k_rotate: (m, beta b, q tile t), twiddles staged in hs */
 template <typename S, int G, int CH>
-__global__ void __launch_bounds__(ROT_THREADS(CH))
-k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const S *__restrict__ dtab, const double2 *__restrict__ tw,
-         int Q, int L, int conj, typename Cx<S>::T *__restrict__ out)
+__device__ __forceinline__ void rotate_block(const typename Cx<S>::T *__restrict__ spf_t, const S *__restrict__ dtab,
+                                             const RotTw<S> *hs, int Q, int L, int conj,
+                                             typename Cx<S>::T *__restrict__ out, int t, int b, int m)
 {
 	typedef typename Cx<S>::T V;
-	extern __shared__ __align__(16) unsigned char rsm_raw[];
-	RotTw<S> *hs = reinterpret_cast<RotTw<S> *>(rsm_raw);   /* [N + (G-1) L] */
 	int K = L + 1, N = 2 * L + 1, K2 = K * K, NP = K * (K + 1) / 2, nrow = K * N;
-	int bid = blockIdx.x;
-	int m = bid % K;
-	bid /= K;
-	int b = bid % K;
-	int t = bid / K;
-	int ne = N + (G - 1) * L;
-	for (int k = threadIdx.x; k < ne; k += blockDim.x) hs[k] = rot_tw<S>(tw, k, N);
-	__syncthreads();
 	int qq = threadIdx.x % SXS_QT;
 	int ch0 = CH == 3 ? 0 : (threadIdx.x / SXS_QT) % 3;
 	int gg = threadIdx.x / ((3 / CH) * SXS_QT);
@@ -226,14 +237,14 @@ k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const S *__restrict__ dtab
 	for (int l = m; l <= L; l++) {
 		const S *dl = db + (size_t)l * N * N;
 		const V *Cl = C + (size_t)l * (l + 1) * Q;    /* lm of m1 = 0 */
-		S d0 = dl[0];
+		S d0 = dl[0], d0s = mul_rn(d0, sg);   /* the sign flips are exact */
 		V y0[CH];
 #pragma unroll
 		for (int c = 0; c < CH; c++) {
 			V c0 = zero2<V>();
 			if (qok) c0 = Cl[c * cstride];
-			y0[c].x = d0 * c0.x;
-			y0[c].y = d0 * c0.y * sg;
+			y0[c].x = mul_rn(d0, c0.x);
+			y0[c].y = mul_rn(d0s, c0.y);
 		}
 		V A[G][CH], B[G][CH];
 #pragma unroll
@@ -245,6 +256,7 @@ k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const S *__restrict__ dtab
 			base += g0;
 			if (base >= N) base -= N;
 			S dp = dl[m1], dm = dl[-m1];
+			S dps = mul_rn(dp, sg), dms = mul_rn(dm, sg);
 			V Sv[CH], Dv[CH];
 #pragma unroll
 			for (int c = 0; c < CH; c++) {
@@ -253,12 +265,11 @@ k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const S *__restrict__ dtab
 					cp = Cl[c * cstride + (size_t)m1 * Q];
 					cm = Cl[c * cstride - (ptrdiff_t)m1 * Q];
 				}
-				V yp;
-				yp.x = dp * cp.x;
-				yp.y = dp * cp.y * sg;
-				S mx = dm * cm.x, my = dm * cm.y * sg;
-				Sv[c].x = yp.x + mx; Sv[c].y = yp.y + my;
-				Dv[c].x = yp.x - mx; Dv[c].y = yp.y - my;
+				/* S = y(m1) + y(-m1), D = y(m1) - y(-m1): y(-m1) rounded, y(m1)
+				 * fused */
+				S mx = mul_rn(dm, cm.x), my = mul_rn(dms, cm.y);
+				Sv[c].x = fma_s(dp, cp.x, mx); Sv[c].y = fma_s(dps, cp.y, my);
+				Dv[c].x = fma_s(dp, cp.x, -mx); Dv[c].y = fma_s(dps, cp.y, -my);
 			}
 			int k = base;
 #pragma unroll
@@ -282,6 +293,61 @@ k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const S *__restrict__ dtab
 				if (g > 0) o[(size_t)(N - g) * gstride + c * SXS_QT] = xm;
 			}
 		}
+	}
+}
+
+template <typename S, int G, int CH>
+__global__ void __launch_bounds__(ROT_THREADS(CH))
+k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const S *__restrict__ dtab, const double2 *__restrict__ tw,
+         int Q, int L, int conj, typename Cx<S>::T *__restrict__ out)
+{
+	extern __shared__ __align__(16) unsigned char rsm_raw[];
+	RotTw<S> *hs = reinterpret_cast<RotTw<S> *>(rsm_raw);   /* [N + (G-1) L] */
+	int K = L + 1;
+	int bid = blockIdx.x;
+	int m = bid % K;
+	bid /= K;
+	int b = bid % K;
+	int t = bid / K;
+	rotate_stage<S, G>(tw, L, hs);
+	__syncthreads();
+	rotate_block<S, G, CH>(spf_t, dtab, hs, Q, L, conj, out, t, b, m);
+}
+
+/* next work item of a batched persistent kernel for the whole block (the
+ * leading barrier: every thread is done with the previous item) */
+__device__ __forceinline__ int next_item(int *ctr)
+{
+	__shared__ int s_it;
+	__syncthreads();
+	if (threadIdx.x == 0) s_it = atomicAdd(ctr, 1);
+	__syncthreads();
+	return s_it;
+}
+
+/* rotation blocks of many tables (mixed path); the twiddles are restaged
+ * when an item's table has other ones than the previous item's */
+template <int G, int CH>
+__global__ void __launch_bounds__(ROT_THREADS(CH))
+k_rotate_batch(const sxsk_rot_job *__restrict__ jobs, const int4 *__restrict__ items, int nitems, int *ctr)
+{
+	extern __shared__ __align__(16) unsigned char rsm_raw[];
+	RotTw<float> *hs = reinterpret_cast<RotTw<float> *>(rsm_raw);
+	const double2 *cur = nullptr;
+	int curL = -1;
+	for (;;) {
+		int it = next_item(ctr);
+		if (it >= nitems) break;
+		int4 w = items[it];
+		sxsk_rot_job j = jobs[w.x];
+		if (j.tw != cur || j.L != curL) {
+			rotate_stage<float, G>(j.tw, j.L, hs);
+			__syncthreads();
+			cur = j.tw;
+			curL = j.L;
+		}
+		rotate_block<float, G, CH>((const float2 *)j.spf_t, (const float *)j.dtab, hs, j.Q, j.L, j.conj,
+		                           (float2 *)j.out, w.y, w.z, w.w);
 	}
 }
 
@@ -408,11 +474,11 @@ __device__ __forceinline__ void tcol_row(const S *row, const V (&u)[CH][NB], V (
 #pragma unroll
 			for (int j = 0; j < CH; j++) {
 				if ((k & 1) == PAR) {
-					acc[j].x += tv[kk] * u[j][k].x;
-					acc[j].y += tv[kk] * u[j][k].y;
+					acc[j].x = fma_s(tv[kk], u[j][k].x, acc[j].x);
+					acc[j].y = fma_s(tv[kk], u[j][k].y, acc[j].y);
 				} else {
-					acc[j].x += tv[kk] * u[j][k].y;
-					acc[j].y -= tv[kk] * u[j][k].x;
+					acc[j].x = fma_s(tv[kk], u[j][k].y, acc[j].x);
+					acc[j].y = fma_s(-tv[kk], u[j][k].x, acc[j].y);
 				}
 			}
 		}
@@ -503,10 +569,6 @@ __device__ __forceinline__ void cp_async16(void *sdst, const void *gsrc)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-/* slices per block of the pipelined column kernel, unless a plan's tile
- * choice (autotuned per L and Q) says otherwise */
-#define TP_SB 8
-
 /* shared bytes of k_translate_pipe<NB>: tau^m [8 q][NB NB + 4] and the U
  * columns of one slice [SXS_SLICE combos][NB pairs][3 ch][8 q] */
 #define TP_SMEM(NB) (sizeof(float) * SXS_QT * ((NB) * (NB) + 4) + sizeof(float2) * SXS_SLICE * (NB) * 3 * SXS_QT)
@@ -520,23 +582,21 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
  * arithmetic.  tau^m(q z) is restaged only where z changes between slices
  * (slices are z-major).  The sums are those of k_translate_col with CH = 3:
  * rows in even/odd pairs, one tau load for three channels. */
+#define TP_MINB(NB) (NB <= 8 ? 5 : (NB <= 12 ? 4 : (NB <= 20 ? 3 : (NB <= 28 ? 2 : 1))))
+
+/* one block of k_translate_pipe: (tile t, slice group gi, m); raw = the
+ * block's TP_SMEM(NB) bytes of shared memory */
 template <int NB>
-__global__ void __launch_bounds__(TCOL_THREADS(3), NB <= 8 ? 5 : (NB <= 12 ? 4 : (NB <= 20 ? 3 : (NB <= 28 ? 2 : 1))))
-k_translate_pipe(const float2 *__restrict__ U, const float *__restrict__ tau, const int32_t *__restrict__ combo_zbg,
-                 const int32_t *__restrict__ slices, int nslice, int cbase, int ncombo, int L, int nzt, int m_lo,
-                 int nm, int sb, float2 *__restrict__ R)
+__device__ __forceinline__ void tpipe_block(const float2 *__restrict__ U, const float *__restrict__ tau,
+                                            const int32_t *__restrict__ combo_zbg, const int32_t *__restrict__ slices,
+                                            int nslice, int cbase, int ncombo, int L, int nzt, int t, int gi, int m,
+                                            int sb, float2 *__restrict__ R, unsigned char *raw)
 {
-	extern __shared__ __align__(16) unsigned char tps_raw[];
 	const int qstride = NB * NB + 4, rowf = 3 * SXS_QT;   /* float2 per pair of one combo */
-	float *ts = reinterpret_cast<float *>(tps_raw);
-	float2 *us = reinterpret_cast<float2 *>(tps_raw + sizeof(float) * SXS_QT * qstride);
+	float *ts = reinterpret_cast<float *>(raw);
+	float2 *us = reinterpret_cast<float2 *>(raw + sizeof(float) * SXS_QT * qstride);
 	int K = L + 1, N = 2 * L + 1, NP = K * (K + 1) / 2, nrow = K * N;
-	int ng = (nslice + sb - 1) / sb;
-	int bid = blockIdx.x;
-	int mi = bid % nm;
-	bid /= nm;
-	int gi = bid % ng, t = bid / ng;
-	int m = m_lo + mi, n = K - m, po = psym(m, K);
+	int n = K - m, po = psym(m, K);
 	int s0 = gi * sb, s1 = s0 + sb < nslice ? s0 + sb : nslice;
 	int q = threadIdx.x % SXS_QT, cl = threadIdx.x / SXS_QT;
 	/* 16-byte chunks of one combo's n pairs: n x 3 x 8 float2 = 12 n; the
@@ -602,6 +662,37 @@ k_translate_pipe(const float2 *__restrict__ U, const float *__restrict__ tau, co
 	}
 }
 
+template <int NB>
+__global__ void __launch_bounds__(TCOL_THREADS(3), TP_MINB(NB))
+k_translate_pipe(const float2 *__restrict__ U, const float *__restrict__ tau, const int32_t *__restrict__ combo_zbg,
+                 const int32_t *__restrict__ slices, int nslice, int cbase, int ncombo, int L, int nzt, int m_lo,
+                 int nm, int sb, float2 *__restrict__ R)
+{
+	extern __shared__ __align__(16) unsigned char tps_raw[];
+	int ng = (nslice + sb - 1) / sb;
+	int bid = blockIdx.x;
+	int mi = bid % nm;
+	bid /= nm;
+	int gi = bid % ng, t = bid / ng;
+	tpipe_block<NB>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, L, nzt, t, gi, m_lo + mi, sb, R, tps_raw);
+}
+
+/* pipelined translation blocks of many chunks (mixed path) */
+template <int NB>
+__global__ void __launch_bounds__(TCOL_THREADS(3), TP_MINB(NB))
+k_translate_batch(const sxsk_tr_job *__restrict__ jobs, const int4 *__restrict__ items, int nitems, int *ctr)
+{
+	extern __shared__ __align__(16) unsigned char tps_raw[];
+	for (;;) {
+		int it = next_item(ctr);
+		if (it >= nitems) break;
+		int4 w = items[it];
+		sxsk_tr_job j = jobs[w.x];
+		tpipe_block<NB>((const float2 *)j.U, (const float *)j.tau, j.combo_zbg, j.slices, j.nslice, j.cbase,
+		                j.ncombo, j.L, j.nzt, w.y, w.z, w.w, j.sb, (float2 *)j.R, tps_raw);
+	}
+}
+
 /* Storage of the per-pose cross terms: double on the FP64 path; on the FP32
  * path a double-float pair {hi, lo} = cst + 2 f formed with an error-free
  * sum (explicit round-to-nearest adds, never contracted), so that the fit
@@ -633,20 +724,16 @@ __device__ __forceinline__ void cross_store(float2 *o, const float2 *cst, size_t
  * with evict_first.  The pose's phase w_m = tw[(m a2) mod N] (doubled for m > 0)
  * is applied to R first, so each channel product needs only its real part:
  *   cross[src][c][q] = cst[c][q] + 2 sum_{m,l} Re(P_a[m,l] (w_m R_b[m,l])). */
+/* one block of k_pose_cross: (tile t, pose block pb), twiddles staged in tws */
 template <typename S, bool HINT>
-__global__ void __launch_bounds__(128)
-k_pose_cross(const sxsk_pose *__restrict__ poses, int npose, int combo_base, int ncombo,
-             const typename Cx<S>::T *__restrict__ P, const typename Cx<S>::T *__restrict__ R,
-             const double2 *__restrict__ tw, const typename CrossT<S>::T *__restrict__ cst, int Q, int L,
-             typename CrossT<S>::T *__restrict__ cross)
+__device__ __forceinline__ void pcross_block(const sxsk_pose *__restrict__ poses, int npose, int combo_base,
+                                             int ncombo, const typename Cx<S>::T *__restrict__ P,
+                                             const typename Cx<S>::T *__restrict__ R, const typename Cx<S>::T *tws,
+                                             const typename CrossT<S>::T *__restrict__ cst, int Q, int L,
+                                             typename CrossT<S>::T *__restrict__ cross, int t, int pb)
 {
 	typedef typename Cx<S>::T V;
-	__shared__ V tws[2 * SXS_LMAX_K - 1];
 	int K = L + 1, N = 2 * L + 1, NP = K * (K + 1) / 2, nrow = K * N;
-	for (int k = threadIdx.x; k < N; k += blockDim.x) tws[k] = from2<V>(tw[k]);
-	__syncthreads();
-	int bpt = (npose + PC_PPB - 1) / PC_PPB;
-	int t = blockIdx.x / bpt, pb = blockIdx.x % bpt;
 	int pi = pb * PC_PPB + threadIdx.x / SXS_QP, j2 = 2 * (threadIdx.x % SXS_QP);
 	if (pi >= npose) return;
 	int q0 = t * SXS_QT + j2;
@@ -702,9 +789,9 @@ k_pose_cross(const sxsk_pose *__restrict__ poses, int npose, int combo_base, int
 			V r0 = k ? cr[0].b : cr[0].a, r1 = k ? cr[1].b : cr[1].a, r2 = k ? cr[2].b : cr[2].a;
 			/* R' = w R */
 			V s0, s1, s2;
-			s0.x = wx * r0.x - wy * r0.y; s0.y = wx * r0.y + wy * r0.x;
-			s1.x = wx * r1.x - wy * r1.y; s1.y = wx * r1.y + wy * r1.x;
-			s2.x = wx * r2.x - wy * r2.y; s2.y = wx * r2.y + wy * r2.x;
+			s0.x = fma_s(wx, r0.x, mul_rn(-wy, r0.y)); s0.y = fma_s(wx, r0.y, mul_rn(wy, r0.x));
+			s1.x = fma_s(wx, r1.x, mul_rn(-wy, r1.y)); s1.y = fma_s(wx, r1.y, mul_rn(wy, r1.x));
+			s2.x = fma_s(wx, r2.x, mul_rn(-wy, r2.y)); s2.y = fma_s(wx, r2.y, mul_rn(wy, r2.x));
 			S *F = f[k];
 			if (sizeof(S) == 8) {
 				/* FP64 (bound by the FP64 pipe): the Re(a s) terms as FMA
@@ -722,12 +809,12 @@ k_pose_cross(const sxsk_pose *__restrict__ poses, int npose, int combo_base, int
 			} else {
 				/* FP32 (bound by the L1 data path): sums of products, whose
 				 * short dependence on F keeps more loads in flight */
-				F[0] += a0.x * s0.x - a0.y * s0.y;
-				F[1] += a0.x * s1.x - a0.y * s1.y + a1.x * s0.x - a1.y * s0.y;
-				F[2] += a0.x * s2.x - a0.y * s2.y + a2.x * s0.x - a2.y * s0.y;
-				F[3] += a1.x * s1.x - a1.y * s1.y;
-				F[4] += a1.x * s2.x - a1.y * s2.y + a2.x * s1.x - a2.y * s1.y;
-				F[5] += a2.x * s2.x - a2.y * s2.y;
+				F[0] = add_rn(F[0], fma_s(a0.x, s0.x, mul_rn(-a0.y, s0.y)));
+				F[1] = add_rn(F[1], fma_s(-a1.y, s0.y, fma_s(a1.x, s0.x, fma_s(a0.x, s1.x, mul_rn(-a0.y, s1.y)))));
+				F[2] = add_rn(F[2], fma_s(-a2.y, s0.y, fma_s(a2.x, s0.x, fma_s(a0.x, s2.x, mul_rn(-a0.y, s2.y)))));
+				F[3] = add_rn(F[3], fma_s(a1.x, s1.x, mul_rn(-a1.y, s1.y)));
+				F[4] = add_rn(F[4], fma_s(-a2.y, s1.y, fma_s(a2.x, s1.x, fma_s(a1.x, s2.x, mul_rn(-a1.y, s2.y)))));
+				F[5] = add_rn(F[5], fma_s(a2.x, s2.x, mul_rn(-a2.y, s2.y)));
 			}
 		}
 	}
@@ -739,6 +826,49 @@ k_pose_cross(const sxsk_pose *__restrict__ poses, int npose, int combo_base, int
 #pragma unroll
 			for (int c = 0; c < 6; c++) cross_store(o, cst, (size_t)c * Q + q, f[k][c]);
 		}
+	}
+}
+
+template <typename S, bool HINT>
+__global__ void __launch_bounds__(128)
+k_pose_cross(const sxsk_pose *__restrict__ poses, int npose, int combo_base, int ncombo,
+             const typename Cx<S>::T *__restrict__ P, const typename Cx<S>::T *__restrict__ R,
+             const double2 *__restrict__ tw, const typename CrossT<S>::T *__restrict__ cst, int Q, int L,
+             typename CrossT<S>::T *__restrict__ cross)
+{
+	typedef typename Cx<S>::T V;
+	__shared__ V tws[2 * SXS_LMAX_K - 1];
+	int N = 2 * L + 1;
+	for (int k = threadIdx.x; k < N; k += blockDim.x) tws[k] = from2<V>(tw[k]);
+	__syncthreads();
+	int bpt = (npose + PC_PPB - 1) / PC_PPB;
+	int t = blockIdx.x / bpt, pb = blockIdx.x % bpt;
+	pcross_block<S, HINT>(poses, npose, combo_base, ncombo, P, R, tws, cst, Q, L, cross, t, pb);
+}
+
+/* per-pose blocks of many chunks (mixed path); the twiddles are restaged
+ * when an item's job has other ones than the previous item's */
+__global__ void __launch_bounds__(128)
+k_pose_cross_batch(const sxsk_pc_job *__restrict__ jobs, const int4 *__restrict__ items, int nitems, int *ctr)
+{
+	__shared__ float2 tws[2 * SXS_LMAX_K - 1];
+	const double2 *cur = nullptr;
+	int curL = -1;
+	for (;;) {
+		int it = next_item(ctr);
+		if (it >= nitems) break;
+		int4 w = items[it];
+		sxsk_pc_job j = jobs[w.x];
+		if (j.tw != cur || j.L != curL) {
+			int N = 2 * j.L + 1;
+			for (int k = threadIdx.x; k < N; k += blockDim.x) tws[k] = from2<float2>(j.tw[k]);
+			__syncthreads();
+			cur = j.tw;
+			curL = j.L;
+		}
+		pcross_block<float, true>(j.poses, j.npose, j.combo_base, j.ncombo, (const float2 *)j.P,
+		                          (const float2 *)j.R, tws, (const float2 *)j.cst, j.Q, j.L, (float2 *)j.cross, w.y,
+		                          w.z);
 	}
 }
 
@@ -1092,6 +1222,16 @@ static int rotate_launch(const void *spf_t, const void *dtab, const double2 *tw,
 	return cudaGetLastError();
 }
 
+extern "C" int sxsk_rotate_group(int L, int gsel)
+{
+	int need = (L + 1 + ROT_GROUPS - 1) / ROT_GROUPS;
+	if (gsel > need) need = gsel;
+	static const int gs[6] = {2, 4, 6, 8, 12, 16};
+	for (int i = 0; i < 6; i++)
+		if (need <= gs[i]) return gs[i];
+	return 0;
+}
+
 template <typename S>
 static int rotate_any(const void *spf_t, const void *dtab, const double2 *tw, int Q, int L, int conj, void *out,
                       int gsel, cudaStream_t s)
@@ -1099,15 +1239,64 @@ static int rotate_any(const void *spf_t, const void *dtab, const double2 *tw, in
 	/* gamma pairs per thread: at least the L + 1 pairs over ROT_GROUPS
 	 * groups; a larger choice (gsel) leaves groups idle for fewer blocks'
 	 * worth of twiddle setup */
-	int need = (L + 1 + ROT_GROUPS - 1) / ROT_GROUPS;
-	if (gsel > need) need = gsel;
-	if (need <= 2) return rotate_launch<S, 2>(spf_t, dtab, tw, Q, L, conj, out, s);
-	if (need <= 4) return rotate_launch<S, 4>(spf_t, dtab, tw, Q, L, conj, out, s);
-	if (need <= 6) return rotate_launch<S, 6>(spf_t, dtab, tw, Q, L, conj, out, s);
-	if (need <= 8) return rotate_launch<S, 8>(spf_t, dtab, tw, Q, L, conj, out, s);
-	if (need <= 12) return rotate_launch<S, 12>(spf_t, dtab, tw, Q, L, conj, out, s);
-	if (need <= 16) return rotate_launch<S, 16>(spf_t, dtab, tw, Q, L, conj, out, s);
-	return cudaErrorInvalidValue;
+	switch (sxsk_rotate_group(L, gsel)) {
+	case 2: return rotate_launch<S, 2>(spf_t, dtab, tw, Q, L, conj, out, s);
+	case 4: return rotate_launch<S, 4>(spf_t, dtab, tw, Q, L, conj, out, s);
+	case 6: return rotate_launch<S, 6>(spf_t, dtab, tw, Q, L, conj, out, s);
+	case 8: return rotate_launch<S, 8>(spf_t, dtab, tw, Q, L, conj, out, s);
+	case 12: return rotate_launch<S, 12>(spf_t, dtab, tw, Q, L, conj, out, s);
+	case 16: return rotate_launch<S, 16>(spf_t, dtab, tw, Q, L, conj, out, s);
+	default: return cudaErrorInvalidValue;
+	}
+}
+
+/* grid of a batched persistent launch: every resident block of the kernel
+ * on every SM, at most one block per item */
+template <typename F>
+static cudaError_t persistent_grid(F kern, int threads, size_t smem, int nitems, int *grid)
+{
+	int dev = 0, nsm = 0, per = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (!e) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+	if (!e) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, threads, smem);
+	if (e) return e;
+	if (per < 1) return cudaErrorInvalidConfiguration;
+	long g = (long)nsm * per;
+	*grid = (int)(g < nitems ? g : nitems);
+	return cudaSuccess;
+}
+
+template <int G>
+static int rotate_batch_launch(const sxsk_rot_job *jobs, const int4 *items, int nitems, int tw_max, int *ctr,
+                               cudaStream_t s)
+{
+	constexpr int CH = G <= 6 ? 3 : 1;   /* the FP32 choice of rotate_launch */
+	size_t smem = sizeof(RotTw<float>) * (size_t)tw_max;
+	auto kern = k_rotate_batch<G, CH>;
+	cudaError_t e = cudaSuccess;
+	if (smem > 48 * 1024) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	int grid = 0;
+	if (!e) e = persistent_grid(kern, ROT_THREADS(CH), smem, nitems, &grid);
+	if (e) return e;
+	kern<<<grid, ROT_THREADS(CH), smem, s>>>(jobs, items, nitems, ctr);
+	return cudaGetLastError();
+}
+
+template <int NB>
+static int translate_batch_launch(const sxsk_tr_job *jobs, const int4 *items, int nitems, int *ctr, cudaStream_t s)
+{
+	size_t smem = TP_SMEM(NB);
+	auto kern = k_translate_batch<NB>;
+	cudaError_t e = cudaSuccess;
+	if (smem > 48 * 1024) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	if (!e)
+		e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+		                         (int)cudaSharedmemCarveoutMaxShared);
+	int grid = 0;
+	if (!e) e = persistent_grid(kern, TCOL_THREADS(3), smem, nitems, &grid);
+	if (e) return e;
+	kern<<<grid, TCOL_THREADS(3), smem, s>>>(jobs, items, nitems, ctr);
+	return cudaGetLastError();
 }
 
 extern "C" {
@@ -1175,7 +1364,7 @@ int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, con
 {
 	if (nslice <= 0) return 0;
 	int NT = (Q + SXS_QT - 1) / SXS_QT;
-	if (sb < 1) sb = TP_SB;
+	if (sb < 1) sb = SXSK_TP_SB;
 	if (L + 1 <= 32) {
 		if (fp32)
 			return translate_col_all<float>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, sb, s);
@@ -1199,6 +1388,47 @@ int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, int ncomb
 		k_pose_cross<double, false><<<(unsigned)nb, 128, 0, s>>>(poses, npose, combo_base, ncombo, (const double2 *)P,
 		                                                   (const double2 *)R, tw, (const double *)cst, Q, L,
 		                                                   (double *)cross);
+	return cudaGetLastError();
+}
+
+int sxsk_rotate_batch(const sxsk_rot_job *jobs, const int4 *items, int nitems, int G, int tw_max, int *ctr,
+                      cudaStream_t s)
+{
+	if (nitems <= 0) return 0;
+	switch (G) {
+	case 2: return rotate_batch_launch<2>(jobs, items, nitems, tw_max, ctr, s);
+	case 4: return rotate_batch_launch<4>(jobs, items, nitems, tw_max, ctr, s);
+	case 6: return rotate_batch_launch<6>(jobs, items, nitems, tw_max, ctr, s);
+	case 8: return rotate_batch_launch<8>(jobs, items, nitems, tw_max, ctr, s);
+	case 12: return rotate_batch_launch<12>(jobs, items, nitems, tw_max, ctr, s);
+	case 16: return rotate_batch_launch<16>(jobs, items, nitems, tw_max, ctr, s);
+	default: return cudaErrorInvalidValue;
+	}
+}
+
+int sxsk_translate_batch(const sxsk_tr_job *jobs, const int4 *items, int nitems, int NB, int *ctr, cudaStream_t s)
+{
+	if (nitems <= 0) return 0;
+	switch (NB) {
+	case 4: return translate_batch_launch<4>(jobs, items, nitems, ctr, s);
+	case 8: return translate_batch_launch<8>(jobs, items, nitems, ctr, s);
+	case 12: return translate_batch_launch<12>(jobs, items, nitems, ctr, s);
+	case 16: return translate_batch_launch<16>(jobs, items, nitems, ctr, s);
+	case 20: return translate_batch_launch<20>(jobs, items, nitems, ctr, s);
+	case 24: return translate_batch_launch<24>(jobs, items, nitems, ctr, s);
+	case 28: return translate_batch_launch<28>(jobs, items, nitems, ctr, s);
+	case 32: return translate_batch_launch<32>(jobs, items, nitems, ctr, s);
+	default: return cudaErrorInvalidValue;
+	}
+}
+
+int sxsk_pose_cross_batch(const sxsk_pc_job *jobs, const int4 *items, int nitems, int *ctr, cudaStream_t s)
+{
+	if (nitems <= 0) return 0;
+	int grid = 0;
+	cudaError_t e = persistent_grid(k_pose_cross_batch, 128, 0, nitems, &grid);
+	if (e) return e;
+	k_pose_cross_batch<<<grid, 128, 0, s>>>(jobs, items, nitems, ctr);
 	return cudaGetLastError();
 }
 

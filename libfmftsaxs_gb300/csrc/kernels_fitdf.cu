@@ -20,6 +20,8 @@
 #include "kernels.h"
 #include "fitdf_core.h"
 
+#include <string.h>
+
 namespace {
 
 #define FITD_THREADS 128
@@ -30,53 +32,80 @@ namespace {
 /* G(c1, q) is staged in shared memory up to this size, else read from global */
 #define FITD_GSMEM (64 * 1024)
 
+/* shared-memory carve-up of a fit block (sizes from the job's shape) */
+struct FitSm {
+	dfl *cs;      /* [ppb][8][qc + 1]: VV VD VW DD DW WW F3G P4 */
+	dfl *fs;      /* [FITD_NFC][Q] */
+	dfl *c2s;     /* [n2] */
+	dfl *gs;      /* [n1][Q] G(c1, q) when gsm */
+	double *red;  /* [ppb*tp][2] */
+	int *redc;    /* [ppb*tp] */
+	dfl *sf;      /* [ppb]: 1/norm */
+	dfl *sfd;     /* [ppb][2]: U2, D4 */
+	int *srcs;    /* [ppb] */
+};
+
+__device__ __forceinline__ FitSm fit_sm(const sxsk_fit_job &J, double *sm)
+{
+	FitSm r;
+	int ld = J.qc + 1, nthr = J.ppb * J.tp;
+	r.cs = reinterpret_cast<dfl *>(sm);
+	r.fs = r.cs + (size_t)J.ppb * 8 * ld;
+	r.c2s = r.fs + (size_t)FITD_NFC * J.Q;
+	r.gs = r.c2s + J.n2;
+	r.red = reinterpret_cast<double *>(r.gs + (J.gsm ? (size_t)J.n1 * J.Q : 0));
+	r.redc = (int *)(r.red + 2 * nthr);
+	r.sf = reinterpret_cast<dfl *>(r.redc + ((nthr + 1) & ~1));
+	r.sfd = r.sf + J.ppb;
+	r.srcs = (int *)(r.sfd + 2 * J.ppb);
+	return r;
+}
+
+/* per-job constants of a fit block: the scaled fit constants, the c2 grid
+ * and (gsm) G(c1, q) */
+__device__ __forceinline__ void fit_stage(const sxsk_fit_job &J, const FitSm &m)
+{
+	int tid = threadIdx.x, Q = J.Q;
+	double pk2 = J.peak * J.peak;
+	for (int k = tid; k < FITD_NFC * Q; k += blockDim.x) {
+		int c = k / Q, i = k % Q;
+		m.fs[k] = df_from(J.fc[i * FITD_NFC + c] * (c < 3 ? pk2 : J.peak));
+	}
+	for (int k = tid; k < J.n2; k += blockDim.x) m.c2s[k] = df_from(J.c2g[k]);
+	if (J.gsm)
+		for (int k = tid; k < J.n1 * Q; k += blockDim.x) {
+			float2 v = J.gdf[k];
+			m.gs[k] = df_mk(v.x, v.y);
+		}
+}
+
 /* Block = ppb poses x tp threads; thread (pose, c1 row lt, lt + tp, ...).
  * Per group of poses the q range runs in chunks of qc: the block stages the
  * chunk's normalised channel rows (plus the q before it), fills F3G and P4,
  * and every thread advances the running sums of its (pose, c1) over the
  * chunk.  After the last chunk a thread has the polynomial coefficients of
- * its row and scans the c2 cells. */
-__global__ void __launch_bounds__(FITD_THREADS, 5)
-k_fit_grid_df(const float2 *__restrict__ cross, const sxsk_pose *__restrict__ order, int slot0, int nslot, int Q,
-              const double *__restrict__ fc, double a0sum, double peak, const float2 *__restrict__ gdf,
-              const double *__restrict__ c1g, int n1, const double *__restrict__ c2g, int n2, int tp, int ppb,
-              int qc, int gsm, double *__restrict__ chi, double *__restrict__ c1o, double *__restrict__ c2o,
-              int32_t *__restrict__ cello, double *__restrict__ grid)
+ * its row and scans the c2 cells.  One call = one group grp (block-wide,
+ * after fit_stage). */
+__device__ __forceinline__ void fit_group(const sxsk_fit_job &J, const FitSm &m, int grp)
 {
-	extern __shared__ double sm[];
+	const float2 *__restrict__ cross = J.cross;
+	int Q = J.Q, n1 = J.n1, n2 = J.n2, tp = J.tp, ppb = J.ppb, qc = J.qc;
+	double a0sum = J.a0sum;
 	int ld = qc + 1;                                   /* staged q per row: the previous q + the chunk */
-	dfl *cs = reinterpret_cast<dfl *>(sm);             /* [ppb][8][ld]: VV VD VW DD DW WW F3G P4 */
-	dfl *fs = cs + (size_t)ppb * 8 * ld;               /* [FITD_NFC][Q] */
-	dfl *c2s = fs + (size_t)FITD_NFC * Q;              /* [n2] */
-	dfl *gs = c2s + n2;                                /* [n1][Q] G(c1, q) when gsm */
-	double *red = reinterpret_cast<double *>(gs + (gsm ? (size_t)n1 * Q : 0)); /* [ppb*tp][2] */
-	int *redc = (int *)(red + 2 * ppb * tp);           /* [ppb*tp] */
-	dfl *sf = reinterpret_cast<dfl *>(redc + ((ppb * tp + 1) & ~1)); /* [ppb]: 1/norm */
-	dfl *sfd = sf + ppb;                               /* [ppb][2]: U2, D4 */
-	int *srcs = (int *)(sfd + 2 * ppb);                /* [ppb] */
+	dfl *cs = m.cs, *fs = m.fs, *c2s = m.c2s, *sf = m.sf, *sfd = m.sfd;
+	double *red = m.red;
+	int *redc = m.redc, *srcs = m.srcs;
 	int tid = threadIdx.x;
 	int nthr = ppb * tp;
 	int lp = tid / tp, lt = tid % tp;
-	double pk2 = peak * peak;
-	for (int k = tid; k < FITD_NFC * Q; k += blockDim.x) {
-		int c = k / Q, i = k % Q;
-		fs[k] = df_from(fc[i * FITD_NFC + c] * (c < 3 ? pk2 : peak));
-	}
-	for (int k = tid; k < n2; k += blockDim.x) c2s[k] = df_from(c2g[k]);
-	if (gsm)
-		for (int k = tid; k < n1 * Q; k += blockDim.x) {
-			float2 v = gdf[k];
-			gs[k] = df_mk(v.x, v.y);
-		}
-	const dfl *gtab = gsm ? gs : reinterpret_cast<const dfl *>(gdf);
-	int ngroup = (nslot + ppb - 1) / ppb;
+	const dfl *gtab = J.gsm ? m.gs : reinterpret_cast<const dfl *>(J.gdf);
 	int nround = (n1 + tp - 1) / tp;
-	for (int grp = blockIdx.x; grp < ngroup; grp += gridDim.x) {
+	{
 		int s0 = grp * ppb;
-		int nhere = min(ppb, nslot - s0);
+		int nhere = min(ppb, J.nslot - s0);
 		bool live = tid < nthr && lp < nhere;
 		__syncthreads();
-		if (tid < nhere) srcs[tid] = order ? order[slot0 + s0 + tid].src : slot0 + s0 + tid;
+		if (tid < nhere) srcs[tid] = J.order ? J.order[J.slot0 + s0 + tid].src : J.slot0 + s0 + tid;
 		__syncthreads();
 		if (tid < nhere) {
 			/* norm = VV + DD + WW + VW - VD - DW at q_0 (the model at q_0 with
@@ -138,11 +167,11 @@ k_fit_grid_df(const float2 *__restrict__ cross, const sxsk_pose *__restrict__ or
 				dfl U2 = sfd[2 * lp], D4 = sfd[2 * lp + 1];
 				dfl u[2], d[4];
 				df_row_finish(&st, u, d);
-				if (grid) {
+				if (J.grid) {
 					for (int i2 = 0; i2 < n2; i2++) {
 						double uu = df_to(df_up(u, U2, c2s[i2])), dd = df_to(df_down(d, D4, c2s[i2]));
 						double k = uu / dd;
-						grid[((size_t)pid * n1 + j) * n2 + i2] = a0sum + k * (-2.0 * uu + k * dd);
+						J.grid[((size_t)pid * n1 + j) * n2 + i2] = a0sum + k * (-2.0 * uu + k * dd);
 					}
 				}
 				dfl bu, bd;
@@ -174,27 +203,58 @@ k_fit_grid_df(const float2 *__restrict__ cross, const sxsk_pose *__restrict__ or
 				}
 			}
 			if (bcell >= 0) {
-				chi[pid] = sqrt(bscore);
-				c1o[pid] = c1g[bcell / n2];
-				c2o[pid] = c2g[bcell % n2];
+				J.chi[pid] = sqrt(bscore);
+				J.c1[pid] = J.c1g[bcell / n2];
+				J.c2[pid] = J.c2g[bcell % n2];
 			} else {
-				chi[pid] = __longlong_as_double(0x7ff8000000000000LL);
-				c1o[pid] = __longlong_as_double(0x7ff8000000000000LL);
-				c2o[pid] = __longlong_as_double(0x7ff8000000000000LL);
+				J.chi[pid] = __longlong_as_double(0x7ff8000000000000LL);
+				J.c1[pid] = __longlong_as_double(0x7ff8000000000000LL);
+				J.c2[pid] = __longlong_as_double(0x7ff8000000000000LL);
 			}
-			if (cello) cello[pid] = bcell;
+			if (J.cell) J.cell[pid] = bcell;
 		}
+	}
+}
+
+__global__ void __launch_bounds__(FITD_THREADS, 5) k_fit_grid_df(sxsk_fit_job J)
+{
+	extern __shared__ double sm[];
+	FitSm m = fit_sm(J, sm);
+	fit_stage(J, m);
+	int ngroup = (J.nslot + J.ppb - 1) / J.ppb;
+	for (int grp = blockIdx.x; grp < ngroup; grp += gridDim.x) fit_group(J, m, grp);
+}
+
+/* fit groups of many dimers: items {job, group}; a block restages the
+ * per-job constants when an item's job differs from the previous item's */
+__global__ void __launch_bounds__(FITD_THREADS, 5)
+k_fit_grid_df_batch(const sxsk_fit_job *__restrict__ jobs, const int2 *__restrict__ items, int nitems, int *ctr)
+{
+	extern __shared__ double sm[];
+	__shared__ int s_it;
+	int cur = -1;
+	for (;;) {
+		__syncthreads();
+		if (threadIdx.x == 0) s_it = atomicAdd(ctr, 1);
+		__syncthreads();
+		int it = s_it;
+		if (it >= nitems) break;
+		int2 w = items[it];
+		sxsk_fit_job J = jobs[w.x];
+		FitSm m = fit_sm(J, sm);
+		if (w.x != cur) {
+			fit_stage(J, m);
+			cur = w.x;
+		}
+		fit_group(J, m, w.y);   /* starts with a barrier: the staged constants are visible */
 	}
 }
 
 } // namespace
 
-extern "C" int sxsk_fit_grid_df(const float2 *cross, const sxsk_pose *order, int slot0, int nslot, int Q,
-                                const double *fc, double a0sum, double peak, const float2 *gdf, const double *c1g,
-                                int n1, const double *c2g, int n2, int max_blocks, double *chi, double *c1,
-                                double *c2, int32_t *cell, double *grid, cudaStream_t s)
+extern "C" int sxsk_fit_df_shape(int Q, int n1, int n2, int *tp_out, int *ppb_out, int *qc_out, int *gsm_out,
+                                 size_t *smem_out)
 {
-	if (nslot <= 0) return 0;
 	if (n1 <= 0 || n2 <= 0 || Q <= 0) return cudaErrorInvalidValue;
 	int tp = n1 < FITD_THREADS ? n1 : FITD_THREADS;
 	int ppb = FITD_THREADS / tp;
@@ -211,14 +271,54 @@ extern "C" int sxsk_fit_grid_df(const float2 *cross, const sxsk_pose *order, int
 		ppb = (ppb + 1) / 2;
 	}
 	if (smem > 227 * 1024) return cudaErrorInvalidValue;
+	*tp_out = tp;
+	*ppb_out = ppb;
+	*qc_out = qc;
+	*gsm_out = gsm;
+	*smem_out = smem;
+	return 0;
+}
+
+extern "C" int sxsk_fit_grid_df(const float2 *cross, const sxsk_pose *order, int slot0, int nslot, int Q,
+                                const double *fc, double a0sum, double peak, const float2 *gdf, const double *c1g,
+                                int n1, const double *c2g, int n2, int max_blocks, double *chi, double *c1,
+                                double *c2, int32_t *cell, double *grid, cudaStream_t s)
+{
+	if (nslot <= 0) return 0;
+	sxsk_fit_job J;
+	memset(&J, 0, sizeof(J));
+	size_t smem = 0;
+	int rc = sxsk_fit_df_shape(Q, n1, n2, &J.tp, &J.ppb, &J.qc, &J.gsm, &smem);
+	if (rc) return rc;
+	J.cross = cross; J.order = order; J.fc = fc; J.gdf = gdf; J.c1g = c1g; J.c2g = c2g;
+	J.chi = chi; J.c1 = c1; J.c2 = c2; J.cell = cell; J.grid = grid;
+	J.a0sum = a0sum; J.peak = peak; J.slot0 = slot0; J.nslot = nslot; J.Q = Q; J.n1 = n1; J.n2 = n2;
 	if (smem > 48 * 1024) {
 		cudaError_t e = cudaFuncSetAttribute(k_fit_grid_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 		if (e != cudaSuccess) return e;
 	}
-	long ngroup = (nslot + ppb - 1) / ppb;
+	long ngroup = (nslot + J.ppb - 1) / J.ppb;
 	int grid_n = (int)(ngroup < (long)max_blocks || max_blocks <= 0 ? ngroup : max_blocks);
-	k_fit_grid_df<<<grid_n, FITD_THREADS, smem, s>>>(cross, order, slot0, nslot, Q, fc, a0sum, peak, gdf, c1g, n1,
-	                                                  c2g, n2, tp, ppb, qc, gsm, chi, c1, c2, cell, grid);
+	k_fit_grid_df<<<grid_n, FITD_THREADS, smem, s>>>(J);
+	return cudaGetLastError();
+}
+
+extern "C" int sxsk_fit_grid_df_batch(const sxsk_fit_job *jobs, const int2 *items, int nitems, size_t smem, int *ctr,
+                                      cudaStream_t s)
+{
+	if (nitems <= 0) return 0;
+	cudaError_t e = cudaSuccess;
+	if (smem > 48 * 1024)
+		e = cudaFuncSetAttribute(k_fit_grid_df_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	int dev = 0, nsm = 0, per = 0;
+	if (!e) e = cudaGetDevice(&dev);
+	if (!e) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+	if (!e) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fit_grid_df_batch, FITD_THREADS, smem);
+	if (e) return e;
+	if (per < 1) return cudaErrorInvalidConfiguration;
+	long g = (long)nsm * per;
+	int grid = (int)(g < nitems ? g : nitems);
+	k_fit_grid_df_batch<<<grid, FITD_THREADS, smem, s>>>(jobs, items, nitems, ctr);
 	return cudaGetLastError();
 }
 

@@ -1,0 +1,672 @@
+/*
+ * Batches of dimers: many mixed-precision plans (each one dimer with its own
+ * L, q grid, experiment, pose list and fit grid) scored by one CUDA graph of
+ * persistent kernels.
+ *
+ * Work items.  Every stage of a plan run is a grid of independent blocks:
+ * rotation blocks (table, q tile, beta, m), translation blocks (chunk, q
+ * tile, slice group, m) per column class NB, per-pose blocks (chunk, q tile,
+ * 32 poses) and fit groups (dimer, group of poses).  The batch lists those
+ * blocks of all dimers as (job, ...) items, ordered by estimated cost,
+ * largest first, and runs each list with one persistent launch of (SMs x
+ * resident blocks) blocks that take items through an atomic counter.  An
+ * item runs the single-dimer kernel's own block code, so every output equals
+ * a sxsg_plan_run of its plan bit for bit.
+ *
+ * Phases.  The translated table of a dimer is cut into chunks of whole
+ * slices (as a plan run does); chunks of all dimers are packed first-fit,
+ * largest first, into phases whose chunks fit one shared device arena.  A
+ * phase is the translation launches of its chunks (one per column class,
+ * on parallel branches of the graph) followed by one per-pose launch.
+ *
+ * Graph.  Zeroing the item counters, the per-z tables of every dimer (two
+ * branches), the rotation launches (one per gamma group size), the phases
+ * and the fit launch are captured once at sxsg_batch_create; a run is one
+ * cudaGraphLaunch.  Stage times come from event nodes in the graph.
+ */
+#include <stdlib.h>
+#include <string.h>
+
+#include "sxs_internal.h"
+
+#define SXSB_BR 8        /* branch streams of the capture */
+#define SXSB_ALIGN 256
+
+typedef struct {
+	double cost;
+	int64_t seq;
+	int4 w;
+} bitem;
+
+typedef struct {
+	int plan;
+	int64_t s0, s1;          /* slices */
+	int64_t c0, c1;          /* combos */
+	size_t bytes;
+	int phase;
+	size_t off;              /* in the arena */
+} bpiece;
+
+typedef struct {
+	int kind;                /* 0 rotation, 1 translation, 2 per-pose, 3 fit */
+	int arg;                 /* G or NB */
+	int phase;
+	int nitems;
+	size_t jobs_off, items_off;
+	int ctr;                 /* counter slot */
+} blaunch;
+
+struct sxsg_batch {
+	int n, fit_mode;
+	sxsg_plan **plans;
+	sxs_plan_view *v;
+	cudaStream_t s, br[SXSB_BR];
+	cudaEvent_t fork, join[SXSB_BR];
+	cudaEvent_t ev[4];       /* graph event nodes: start, tables done, phases done, end */
+	cudaGraph_t graph;
+	cudaGraphExec_t exec;
+	void *d_buf, *d_arena;
+	size_t arena;
+	size_t fit_smem;
+	int nphase, nlaunch, nkern;
+	int64_t nitems, nposes;
+	double ms[4];
+};
+
+static int cmp_item(const void *a, const void *b)
+{
+	const bitem *x = a, *y = b;
+	if (x->cost != y->cost) return x->cost > y->cost ? -1 : 1;
+	return x->seq < y->seq ? -1 : (x->seq > y->seq);
+}
+
+static int cmp_piece(const void *a, const void *b)
+{
+	const bpiece *x = a, *y = b;
+	if (x->bytes != y->bytes) return x->bytes > y->bytes ? -1 : 1;
+	if (x->plan != y->plan) return x->plan < y->plan ? -1 : 1;
+	return x->s0 < y->s0 ? -1 : (x->s0 > y->s0);
+}
+
+/* growable host arrays */
+typedef struct {
+	void *p;
+	size_t n, cap, elem;
+} bvec;
+
+static void *bv_push(bvec *v)
+{
+	if (v->n == v->cap) {
+		size_t nc = v->cap ? 2 * v->cap : 256;
+		void *q = realloc(v->p, nc * v->elem);
+		if (!q) return NULL;
+		v->p = q;
+		v->cap = nc;
+	}
+	return (char *)v->p + v->elem * v->n++;
+}
+
+static size_t al(size_t x) { return (x + SXSB_ALIGN - 1) & ~(size_t)(SXSB_ALIGN - 1); }
+
+/* bytes of one combo's translated rows */
+static size_t combo_bytes(const sxs_plan_view *v) { return (size_t)v->NP * 3 * SXS_QT * v->NT * sizeof(float2); }
+
+void sxsg_batch_destroy(sxsg_batch *b)
+{
+	if (!b) return;
+	if (b->s) cudaStreamSynchronize(b->s);
+	if (b->exec) cudaGraphExecDestroy(b->exec);
+	if (b->graph) cudaGraphDestroy(b->graph);
+	if (b->d_buf) cudaFree(b->d_buf);
+	if (b->d_arena) cudaFree(b->d_arena);
+	for (int i = 0; i < SXSB_BR; i++) {
+		if (b->br[i]) cudaStreamDestroy(b->br[i]);
+		if (b->join[i]) cudaEventDestroy(b->join[i]);
+	}
+	for (int i = 0; i < 4; i++)
+		if (b->ev[i]) cudaEventDestroy(b->ev[i]);
+	if (b->fork) cudaEventDestroy(b->fork);
+	if (b->s) cudaStreamDestroy(b->s);
+	free(b->plans);
+	free(b->v);
+	free(b);
+}
+
+/* Host side of the work lists: jobs and items of every launch in one
+ * staging buffer (offsets into the device copy), launches in graph order. */
+typedef struct {
+	char *h;
+	size_t used, cap;
+	bvec launches;
+} bstage;
+
+static size_t st_put(bstage *st, const void *src, size_t bytes)
+{
+	size_t off = al(st->used);
+	if (off + bytes > st->cap) {
+		size_t nc = st->cap ? st->cap : 1 << 20;
+		while (nc < off + bytes) nc *= 2;
+		char *q = realloc(st->h, nc);
+		if (!q) return (size_t)-1;
+		st->h = q;
+		st->cap = nc;
+	}
+	if (bytes) memcpy(st->h + off, src, bytes);
+	st->used = off + bytes;
+	return off;
+}
+
+/* sorts items (largest cost first), stores the jobs and items, appends the
+ * launch */
+static int st_launch(bstage *st, int kind, int arg, int phase, const void *jobs, size_t jbytes, bvec *items,
+                     int pair)
+{
+	if (items->n == 0) return 0;
+	if (items->n > INT32_MAX) return sxs_fail(-2, "sxsg_batch_create: too many work items in one launch");
+	qsort(items->p, items->n, sizeof(bitem), cmp_item);
+	size_t ib = items->n * (pair ? sizeof(int2) : sizeof(int4));
+	char *tmp = malloc(ib);
+	if (!tmp) return sxs_fail(-5, "out of host memory");
+	const bitem *it = items->p;
+	for (size_t i = 0; i < items->n; i++) {
+		if (pair) {
+			int2 w = {it[i].w.x, it[i].w.y};
+			memcpy(tmp + i * sizeof(int2), &w, sizeof(w));
+		} else {
+			memcpy(tmp + i * sizeof(int4), &it[i].w, sizeof(int4));
+		}
+	}
+	blaunch *L = bv_push(&st->launches);
+	if (!L) {
+		free(tmp);
+		return sxs_fail(-5, "out of host memory");
+	}
+	L->kind = kind;
+	L->arg = arg;
+	L->phase = phase;
+	L->nitems = (int)items->n;
+	L->jobs_off = st_put(st, jobs, jbytes);
+	L->items_off = st_put(st, tmp, ib);
+	L->ctr = (int)st->launches.n - 1;
+	free(tmp);
+	items->n = 0;
+	if (L->jobs_off == (size_t)-1 || L->items_off == (size_t)-1) return sxs_fail(-5, "out of host memory");
+	return 0;
+}
+
+static int add_item(bvec *items, double cost, int x, int y, int z, int w)
+{
+	bitem *it = bv_push(items);
+	if (!it) return sxs_fail(-5, "out of host memory");
+	it->cost = cost;
+	it->seq = (int64_t)items->n;
+	it->w.x = x;
+	it->w.y = y;
+	it->w.z = z;
+	it->w.w = w;
+	return 0;
+}
+
+/* rotation launches: one per gamma group size, items (table, t, b, m) */
+static int build_rotations(sxsg_batch *b, bstage *st)
+{
+	static const int gs[6] = {2, 4, 6, 8, 12, 16};
+	bvec items = {NULL, 0, 0, sizeof(bitem)};
+	int rc = 0;
+	sxsk_rot_job *jobs = malloc(sizeof(sxsk_rot_job) * 2 * (size_t)b->n);
+	if (!jobs) return sxs_fail(-5, "out of host memory");
+	for (int gi = 0; gi < 6 && !rc; gi++) {
+		int G = gs[gi], nj = 0, twmax = 0;
+		for (int i = 0; i < b->n && !rc; i++) {
+			const sxs_plan_view *v = &b->v[i];
+			if (sxsk_rotate_group(v->L, v->rot_gamma) != G) continue;
+			int K = v->L + 1, N = 2 * v->L + 1;
+			int tw = N + (G - 1) * v->L;
+			if (tw > twmax) twmax = tw;
+			for (int tab = 0; tab < 2; tab++) {
+				sxsk_rot_job *j = &jobs[nj];
+				memset(j, 0, sizeof(*j));
+				j->spf_t = tab ? v->Bt : v->At;
+				j->dtab = v->dtabf;
+				j->tw = v->tw;
+				j->out = tab ? v->U : v->P;
+				j->Q = v->Q;
+				j->L = v->L;
+				j->conj = tab;
+				for (int t = 0; t < v->NT && !rc; t++)
+					for (int bb = 0; bb < K && !rc; bb++)
+						for (int m = 0; m < K && !rc; m++) {
+							/* multiply-adds of the block: sum over l >= m of l */
+							double cost = 0.5 * ((double)v->L * (v->L + 1) - (double)m * (m - 1)) + (K - m);
+							rc = add_item(&items, cost, nj, t, bb, m);
+						}
+				nj++;
+			}
+		}
+		if (!rc) rc = st_launch(st, 0, G | (twmax << 8), -1, jobs, sizeof(sxsk_rot_job) * nj, &items, 0);
+	}
+	free(jobs);
+	free(items.p);
+	return rc;
+}
+
+/* chunks of every dimer's translated table, packed into phases */
+static int build_phases(sxsg_batch *b, bstage *st, size_t arena_req)
+{
+	bvec pieces = {NULL, 0, 0, sizeof(bpiece)};
+	int rc = 0;
+	size_t total = 0, largest_slice = 0;
+	for (int i = 0; i < b->n; i++) {
+		const sxs_plan_view *v = &b->v[i];
+		if (v->nslice > 0) {
+			size_t sl = combo_bytes(v) * SXS_SLICE;
+			if (sl > largest_slice) largest_slice = sl;
+			total += al(combo_bytes(v) * (size_t)v->ncombo);
+		}
+	}
+	size_t fr = 0, tot = 0;
+	cudaMemGetInfo(&fr, &tot);
+	size_t arena = arena_req ? arena_req : fr / 2;
+	if (arena > total) arena = total;
+	if (total > 0 && arena < al(largest_slice)) {
+		if (arena_req) return sxs_fail(-2, "sxsg_batch_create: arena of %zu bytes below one slice (%zu)", arena_req,
+		                               al(largest_slice));
+		return sxs_fail(-5, "sxsg_batch_create: free device memory below one slice of a translated table");
+	}
+	for (int i = 0; i < b->n && !rc; i++) {
+		const sxs_plan_view *v = &b->v[i];
+		if (v->nslice <= 0) continue;
+		size_t pc = combo_bytes(v);
+		int64_t chunk = (int64_t)(arena / (pc * SXS_SLICE));
+		if (chunk < 1) chunk = 1;
+		int64_t s0 = 0;
+		while (s0 < v->nslice && !rc) {
+			int64_t s1 = s0 + chunk < v->nslice ? s0 + chunk : v->nslice;
+			/* whole slices may overshoot by combos of a partial slice: shrink */
+			for (;;) {
+				int64_t c0 = v->h_slices[2 * s0], c1 = v->h_slices[2 * (s1 - 1)] + v->h_slices[2 * (s1 - 1) + 1];
+				if (al(pc * (size_t)(c1 - c0)) <= arena || s1 == s0 + 1) break;
+				s1--;
+			}
+			bpiece *p = bv_push(&pieces);
+			if (!p) {
+				rc = sxs_fail(-5, "out of host memory");
+				break;
+			}
+			p->plan = i;
+			p->s0 = s0;
+			p->s1 = s1;
+			p->c0 = v->h_slices[2 * s0];
+			p->c1 = v->h_slices[2 * (s1 - 1)] + v->h_slices[2 * (s1 - 1) + 1];
+			p->bytes = al(pc * (size_t)(p->c1 - p->c0));
+			p->phase = -1;
+			s0 = s1;
+		}
+	}
+	if (rc) {
+		free(pieces.p);
+		return rc;
+	}
+	bpiece *pc = pieces.p;
+	size_t np = pieces.n;
+	qsort(pc, np, sizeof(bpiece), cmp_piece);
+	/* first fit, largest first */
+	size_t *fill = calloc(np > 0 ? np : 1, sizeof(size_t));
+	int nphase = 0;
+	for (size_t k = 0; k < np; k++) {
+		int ph = 0;
+		while (ph < nphase && fill[ph] + pc[k].bytes > arena) ph++;
+		if (ph == nphase) nphase++;
+		pc[k].phase = ph;
+		pc[k].off = fill[ph];
+		fill[ph] += pc[k].bytes;
+	}
+	size_t used = 0;
+	for (int ph = 0; ph < nphase; ph++) used = fill[ph] > used ? fill[ph] : used;
+	free(fill);
+	b->nphase = nphase;
+	b->arena = used;
+	if (used > 0) {
+		cudaError_t e = cudaMalloc(&b->d_arena, used);
+		if (e) {
+			free(pieces.p);
+			return sxs_cuda_fail(e, "sxsg_batch_create arena");
+		}
+	}
+	/* per phase: translation launches per column class, then one per-pose launch */
+	bvec items = {NULL, 0, 0, sizeof(bitem)};
+	sxsk_tr_job *tj = malloc(sizeof(sxsk_tr_job) * (np > 0 ? np : 1));
+	sxsk_pc_job *pj = malloc(sizeof(sxsk_pc_job) * (np > 0 ? np : 1));
+	int *jmap = malloc(sizeof(int) * (np > 0 ? np : 1));
+	if (!tj || !pj || !jmap) rc = sxs_fail(-5, "out of host memory");
+	for (int ph = 0; ph < nphase && !rc; ph++) {
+		int nj = 0;
+		for (size_t k = 0; k < np; k++) {
+			if (pc[k].phase != ph) continue;
+			const bpiece *p = &pc[k];
+			const sxs_plan_view *v = &b->v[p->plan];
+			void *R = (char *)b->d_arena + p->off;
+			sxsk_tr_job *t = &tj[nj];
+			memset(t, 0, sizeof(*t));
+			t->U = v->U;
+			t->tau = v->tauf;
+			t->combo_zbg = v->combo + 3 * p->c0;
+			t->slices = v->slices + 2 * p->s0;
+			t->R = R;
+			t->nslice = (int)(p->s1 - p->s0);
+			t->cbase = (int)p->c0;
+			t->ncombo = (int)(p->c1 - p->c0);
+			t->L = v->L;
+			t->nzt = v->nzt;
+			t->sb = v->tr_slices >= 1 ? v->tr_slices : SXSK_TP_SB;
+			sxsk_pc_job *q = &pj[nj];
+			memset(q, 0, sizeof(*q));
+			int64_t p0 = v->h_cstart[p->c0], p1 = v->h_cstart[p->c1];
+			q->poses = v->poses + p0;
+			q->P = v->P;
+			q->R = R;
+			q->tw = v->tw;
+			q->cst = v->cst;
+			q->cross = v->cross;
+			q->npose = (int)(p1 - p0);
+			q->combo_base = (int)p->c0;
+			q->ncombo = (int)(p->c1 - p->c0);
+			q->Q = v->Q;
+			q->L = v->L;
+			jmap[nj] = (int)k;
+			nj++;
+		}
+		for (int NB = 4; NB <= 32 && !rc; NB += 4) {
+			for (int j = 0; j < nj && !rc; j++) {
+				const sxsk_tr_job *t = &tj[j];
+				const sxs_plan_view *v = &b->v[pc[jmap[j]].plan];
+				int K = t->L + 1;
+				int m_hi = K - (NB - 3), m_lo = K - NB;
+				if (m_hi > t->L) m_hi = t->L;
+				if (m_lo < 0) m_lo = 0;
+				int ng = (t->nslice + t->sb - 1) / t->sb;
+				const int32_t *hs = v->h_slices + 2 * pc[jmap[j]].s0;
+				for (int g = 0; g < ng && !rc; g++) {
+					/* combos of the slice group x n^2 multiply-adds each */
+					int sa = g * t->sb, sz = sa + t->sb < t->nslice ? sa + t->sb : t->nslice;
+					double nc = (double)(hs[2 * (sz - 1)] + hs[2 * (sz - 1) + 1] - hs[2 * sa]);
+					for (int tt = 0; tt < v->NT && !rc; tt++)
+						for (int m = m_lo; m <= m_hi && !rc; m++) {
+							int n = K - m;
+							rc = add_item(&items, nc * n * n, j, tt, g, m);
+						}
+				}
+			}
+			if (!rc) rc = st_launch(st, 1, NB, ph, tj, sizeof(sxsk_tr_job) * nj, &items, 0);
+		}
+		for (int j = 0; j < nj && !rc; j++) {
+			const sxsk_pc_job *q = &pj[j];
+			const sxs_plan_view *v = &b->v[pc[jmap[j]].plan];
+			int bpt = (q->npose + 31) / 32;
+			for (int tt = 0; tt < v->NT && !rc; tt++)
+				for (int pb = 0; pb < bpt && !rc; pb++) rc = add_item(&items, (double)v->NP, j, tt, pb, 0);
+		}
+		if (!rc) rc = st_launch(st, 2, 0, ph, pj, sizeof(sxsk_pc_job) * nj, &items, 0);
+	}
+	free(items.p);
+	free(tj);
+	free(pj);
+	free(jmap);
+	free(pieces.p);
+	return rc;
+}
+
+/* fit launch: items (dimer, group of poses) */
+static int build_fit(sxsg_batch *b, bstage *st)
+{
+	bvec items = {NULL, 0, 0, sizeof(bitem)};
+	sxsk_fit_job *jobs = calloc((size_t)b->n, sizeof(sxsk_fit_job));
+	int rc = jobs ? 0 : sxs_fail(-5, "out of host memory"), nj = 0;
+	b->fit_smem = 0;
+	for (int i = 0; i < b->n && !rc; i++) {
+		const sxs_plan_view *v = &b->v[i];
+		if (v->npose <= 0) continue;
+		sxsk_fit_job *J = &jobs[nj];
+		size_t smem = 0;
+		int e = sxsk_fit_df_shape(v->Q, v->n1, v->n2, &J->tp, &J->ppb, &J->qc, &J->gsm, &smem);
+		if (e) {
+			rc = sxs_fail(-2, "sxsg_batch_create: plan %d: no block shape fits its fit grid", i);
+			break;
+		}
+		if (smem > b->fit_smem) b->fit_smem = smem;
+		J->cross = (const float2 *)v->cross;
+		J->order = NULL;
+		J->fc = v->fc;
+		J->gdf = v->gdf;
+		J->c1g = v->c1g;
+		J->c2g = v->c2g;
+		J->chi = v->chi;
+		J->c1 = v->c1;
+		J->c2 = v->c2;
+		J->cell = v->cell;
+		J->grid = NULL;
+		J->a0sum = v->a0sum;
+		J->peak = v->peak;
+		J->slot0 = 0;
+		J->nslot = (int)v->npose;
+		J->Q = v->Q;
+		J->n1 = v->n1;
+		J->n2 = v->n2;
+		int ngroup = (J->nslot + J->ppb - 1) / J->ppb;
+		double cost = (double)v->Q * ((v->n1 + J->tp - 1) / J->tp) * v->n2;
+		for (int g = 0; g < ngroup && !rc; g++) rc = add_item(&items, cost, nj, g, 0, 0);
+		nj++;
+	}
+	if (!rc) rc = st_launch(st, 3, 0, -1, jobs, sizeof(sxsk_fit_job) * nj, &items, 1);
+	free(jobs);
+	free(items.p);
+	return rc;
+}
+
+static int launch_one(sxsg_batch *b, const blaunch *L, int *ctr, cudaStream_t s)
+{
+	char *base = b->d_buf;
+	const void *jobs = base + L->jobs_off, *items = base + L->items_off;
+	int *c = ctr + L->ctr;
+	switch (L->kind) {
+	case 0: return sxsk_rotate_batch(jobs, items, L->nitems, L->arg & 0xff, L->arg >> 8, c, s);
+	case 1: return sxsk_translate_batch(jobs, items, L->nitems, L->arg, c, s);
+	case 2: return sxsk_pose_cross_batch(jobs, items, L->nitems, c, s);
+	default: return sxsk_fit_grid_df_batch(jobs, items, L->nitems, b->fit_smem, c, s);
+	}
+}
+
+/* The graph, captured from b->s: counters zeroed; the per-z tables on two
+ * branches beside the rotation launches; per phase the translation launches
+ * on parallel branches, joined before the per-pose launch; the fit. */
+static int capture(sxsg_batch *b, const blaunch *ls, int nl, int *ctr)
+{
+	cudaStream_t s = b->s;
+	int rc = 0, nk = 0;
+	SXS_CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+	cudaError_t e = cudaMemsetAsync(ctr, 0, sizeof(int) * (size_t)(nl > 0 ? nl : 1), s);
+	if (!e) e = cudaEventRecordWithFlags(b->ev[0], s, cudaEventRecordExternal);
+	/* per-z tables of every dimer on two branches */
+	if (!e) e = cudaEventRecord(b->fork, s);
+	for (int k = 0; k < 2 && !e; k++) e = cudaStreamWaitEvent(b->br[k], b->fork, 0);
+	for (int i = 0; i < b->n && !e && !rc; i++) {
+		if (b->v[i].nzt <= 0) continue;
+		rc = sxs_plan_ztables_on(b->plans[i], b->br[i & 1]);
+		nk += 3;
+	}
+	int li = 0;
+	while (li < nl && ls[li].kind == 0 && !e && !rc) {
+		rc = launch_one(b, &ls[li], ctr, s);
+		nk++;
+		li++;
+	}
+	for (int k = 0; k < 2 && !e; k++) {
+		e = cudaEventRecord(b->join[k], b->br[k]);
+		if (!e) e = cudaStreamWaitEvent(s, b->join[k], 0);
+	}
+	if (!e) e = cudaEventRecordWithFlags(b->ev[1], s, cudaEventRecordExternal);
+	/* phases */
+	for (int ph = 0; ph < b->nphase && !e && !rc; ph++) {
+		int nb = 0;
+		if (!e) e = cudaEventRecord(b->fork, s);
+		while (li < nl && ls[li].kind == 1 && ls[li].phase == ph && !e && !rc) {
+			cudaStream_t bs = b->br[nb % SXSB_BR];
+			if (nb < SXSB_BR) e = cudaStreamWaitEvent(bs, b->fork, 0);
+			if (!e) rc = launch_one(b, &ls[li], ctr, bs);
+			nk++;
+			nb++;
+			li++;
+		}
+		for (int k = 0; k < nb && k < SXSB_BR && !e; k++) {
+			e = cudaEventRecord(b->join[k], b->br[k]);
+			if (!e) e = cudaStreamWaitEvent(s, b->join[k], 0);
+		}
+		if (li < nl && ls[li].kind == 2 && ls[li].phase == ph && !e && !rc) {
+			rc = launch_one(b, &ls[li], ctr, s);
+			nk++;
+			li++;
+		}
+	}
+	if (!e) e = cudaEventRecordWithFlags(b->ev[2], s, cudaEventRecordExternal);
+	if (li < nl && ls[li].kind == 3 && !e && !rc) {
+		rc = launch_one(b, &ls[li], ctr, s);
+		nk++;
+		li++;
+	}
+	if (!e) e = cudaEventRecordWithFlags(b->ev[3], s, cudaEventRecordExternal);
+	cudaGraph_t g = NULL;
+	cudaError_t e2 = cudaStreamEndCapture(s, &g);
+	if (!e) e = e2;
+	if (rc || e) {
+		if (g) cudaGraphDestroy(g);
+		return rc ? rc : sxs_cuda_fail(e, "sxsg_batch_create capture");
+	}
+	if (li != nl) {
+		cudaGraphDestroy(g);
+		return sxs_fail(-2, "sxsg_batch_create: launch list out of order");
+	}
+	b->graph = g;
+	e = cudaGraphInstantiate(&b->exec, g, 0);
+	if (e) return sxs_cuda_fail(e, "sxsg_batch_create instantiate");
+	b->nkern = nk;
+	return 0;
+}
+
+int sxsg_batch_create(sxsg_plan *const *plans, int nplan, int fit_mode, size_t arena_bytes, sxsg_batch **out)
+{
+	if (!plans || nplan <= 0 || !out) return sxs_fail(-2, "sxsg_batch_create: bad arguments");
+	if (fit_mode != SXSG_FIT_GRID && fit_mode != SXSG_FIT_NONE)
+		return sxs_fail(-2, "sxsg_batch_create: fit mode must be SXSG_FIT_GRID or SXSG_FIT_NONE");
+	*out = NULL;
+	int rc = sxs_ensure_init();
+	if (rc) return rc;
+	sxsg_batch *b = calloc(1, sizeof(*b));
+	if (!b) return sxs_fail(-5, "out of host memory");
+	b->n = nplan;
+	b->fit_mode = fit_mode;
+	b->plans = malloc(sizeof(sxsg_plan *) * (size_t)nplan);
+	b->v = calloc((size_t)nplan, sizeof(sxs_plan_view));
+	if (!b->plans || !b->v) {
+		sxsg_batch_destroy(b);
+		return sxs_fail(-5, "out of host memory");
+	}
+	for (int i = 0; i < nplan && !rc; i++) {
+		b->plans[i] = plans[i];
+		if (!plans[i]) {
+			rc = sxs_fail(-2, "sxsg_batch_create: plan %d is NULL", i);
+			break;
+		}
+		for (int k = 0; k < i; k++)
+			if (plans[k] == plans[i]) rc = sxs_fail(-2, "sxsg_batch_create: plan %d listed twice", i);
+		if (!rc) rc = sxs_plan_batch_view(plans[i], &b->v[i]);
+		const sxs_plan_view *v = &b->v[i];
+		if (!rc && !v->fp32) rc = sxs_fail(-2, "sxsg_batch_create: plan %d is not mixed precision", i);
+		if (!rc && v->L + 1 > 32) rc = sxs_fail(-2, "sxsg_batch_create: plan %d has L = %d > 31", i, v->L);
+		if (!rc && v->ext_tables) rc = sxs_fail(-2, "sxsg_batch_create: plan %d uses caller rotation tables", i);
+		if (!rc && fit_mode == SXSG_FIT_GRID && (v->n1 <= 0 || v->n2 <= 0))
+			rc = sxs_fail(-2, "sxsg_batch_create: plan %d has no (c1, c2) grid", i);
+		if (!rc && sxsk_rotate_group(v->L, v->rot_gamma) == 0)
+			rc = sxs_fail(-2, "sxsg_batch_create: plan %d: no rotation group for its tile choice", i);
+		b->nposes += v->npose;
+	}
+	cudaError_t e = cudaSuccess;
+	if (!rc) e = cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking);
+	for (int k = 0; k < SXSB_BR && !e && !rc; k++) {
+		e = cudaStreamCreateWithFlags(&b->br[k], cudaStreamNonBlocking);
+		if (!e) e = cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming);
+	}
+	if (!e && !rc) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+	for (int k = 0; k < 4 && !e && !rc; k++) e = cudaEventCreate(&b->ev[k]);
+	if (e && !rc) rc = sxs_cuda_fail(e, "sxsg_batch_create streams");
+	bstage st = {NULL, 0, 0, {NULL, 0, 0, sizeof(blaunch)}};
+	if (!rc) rc = build_rotations(b, &st);
+	if (!rc) rc = build_phases(b, &st, arena_bytes);
+	if (!rc && fit_mode == SXSG_FIT_GRID) rc = build_fit(b, &st);
+	int nl = (int)st.launches.n;
+	size_t ctr_off = al(st.used);
+	if (!rc) {
+		e = cudaMalloc(&b->d_buf, ctr_off + sizeof(int) * (size_t)(nl > 0 ? nl : 1));
+		if (!e && st.used) e = cudaMemcpy(b->d_buf, st.h, st.used, cudaMemcpyHostToDevice);
+		if (e) rc = sxs_cuda_fail(e, "sxsg_batch_create work lists");
+	}
+	if (!rc) {
+		const blaunch *ls = st.launches.p;
+		for (int k = 0; k < nl; k++) b->nitems += ls[k].nitems;
+		b->nlaunch = nl;
+		rc = capture(b, ls, nl, (int *)((char *)b->d_buf + ctr_off));
+	}
+	free(st.h);
+	free(st.launches.p);
+	if (rc) {
+		sxsg_batch_destroy(b);
+		return rc;
+	}
+	*out = b;
+	return 0;
+}
+
+int sxsg_batch_run(sxsg_batch *b)
+{
+	if (!b || !b->exec) return sxs_fail(-2, "sxsg_batch_run: no batch");
+	cudaEvent_t a, z;
+	SXS_CU(cudaEventCreate(&a));
+	cudaError_t e = cudaEventCreate(&z);
+	if (e) {
+		cudaEventDestroy(a);
+		return sxs_cuda_fail(e, "sxsg_batch_run events");
+	}
+	e = cudaEventRecord(a, b->s);
+	if (!e) e = cudaGraphLaunch(b->exec, b->s);
+	if (!e) e = cudaEventRecord(z, b->s);
+	if (!e) e = cudaEventSynchronize(z);
+	if (!e) e = cudaGetLastError();
+	float t[4] = {0, 0, 0, 0};
+	if (!e) {
+		cudaEventElapsedTime(&t[0], b->ev[0], b->ev[1]);
+		cudaEventElapsedTime(&t[1], b->ev[1], b->ev[2]);
+		cudaEventElapsedTime(&t[2], b->ev[2], b->ev[3]);
+		cudaEventElapsedTime(&t[3], a, z);
+	}
+	cudaEventDestroy(a);
+	cudaEventDestroy(z);
+	if (e) return sxs_cuda_fail(e, "sxsg_batch_run");
+	for (int k = 0; k < 4; k++) b->ms[k] = t[k];
+	float pms[5] = {t[0], t[1], 0.0f, t[2], t[3]};
+	for (int i = 0; i < b->n; i++) sxs_plan_mark_run(b->plans[i], b->fit_mode, pms);
+	sxs_count_launches(b->nkern);
+	return 0;
+}
+
+int sxsg_batch_stats_get(const sxsg_batch *b, sxsg_batch_stats *st)
+{
+	if (!b || !st) return sxs_fail(-2, "sxsg_batch_stats_get: bad arguments");
+	memset(st, 0, sizeof(*st));
+	st->plans = b->n;
+	st->phases = b->nphase;
+	st->launches = b->nkern;
+	st->items = b->nitems;
+	st->poses = b->nposes;
+	st->arena_bytes = b->arena;
+	for (int k = 0; k < 4; k++) st->ms[k] = b->ms[k];
+	return 0;
+}

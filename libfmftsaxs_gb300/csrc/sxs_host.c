@@ -201,6 +201,8 @@ struct sxsg_plan {
 	int *d_tcstat;              /* its status word (kernels.h, sxsk_rotate_tc) */
 	int P_valid, U_valid;       /* caller tables already hold this run's rows */
 	int tw_variant; /* -1 none, 0 simple_ft, 1 exact */
+	double *h_tw;               /* host copy of the twiddles (lives with the plan) */
+	int64_t run_chunk, run_nch; /* slices per chunk and chunks of the prepared run */
 	/* poses */
 	int64_t npose;
 	int skip;
@@ -276,6 +278,7 @@ void sxsg_plan_destroy(sxsg_plan *p)
 	for (int i = 0; i < p->ncev; i++) cudaEventDestroy(p->cev[i]);
 	free(p->cev);
 	free(p->h_z);
+	free(p->h_tw);
 	free(p);
 }
 
@@ -660,18 +663,9 @@ static int plan_rotations(sxsg_plan *p)
 	cudaStream_t s = p->s;
 	/* every run rebuilds the rotation tables: a run is the whole per-call
 	 * work of the reference's sxs_compute_saxs_scores */
-	int variant = p->skip == 1 ? 0 : 1;
 	{
-		double *tw = malloc(sizeof(double) * 2 * N);
-		sxs_twiddles_host(N, variant, tw);
-		cudaError_t e = cudaMemcpyAsync(p->d_tw, tw, sizeof(double2) * N, cudaMemcpyHostToDevice, p->s);
-		free(tw);
-		if (e) return sxs_cuda_fail(e, "twiddle upload");
 		const void *dtab = p->fp32 ? (const void *)p->lt->d_dtabf : (const void *)p->lt->d_dtab;
 		int tc = p->fp32 && p->rot_engine == SXSG_ROT_TC && 2 * N <= 128;
-		if (tc && !p->d_amat)
-			SXS_CU(cudaMallocAsync((void **)&p->d_amat, sizeof(float) * sxsk_rotate_tc_scratch(L), s));
-		if (tc && !p->d_tcstat) SXS_CU(cudaMallocAsync((void **)&p->d_tcstat, sizeof(int), s));
 		if (tc) SXS_CU(cudaMemsetAsync(p->d_tcstat, 0, sizeof(int), s));
 		if (!p->ext_tables || !p->P_valid) {
 			if (tc) SXS_K(sxsk_rotate_tc(p->d_At, p->lt->d_dtabf, p->d_tw, Q, L, 0, p->d_P, p->d_amat, p->d_tcstat, s));
@@ -685,7 +679,6 @@ static int plan_rotations(sxsg_plan *p)
 		}
 		p->tc_used = tc;
 		if (p->ext_tables) p->P_valid = p->U_valid = 1;
-		p->tw_variant = variant;
 	}
 	return 0;
 }
@@ -716,25 +709,76 @@ static int plan_events(sxsg_plan *p, int need)
 	return 0;
 }
 
-int sxsg_plan_run(sxsg_plan *p, int fit_mode)
+int sxs_plan_batch_view(sxsg_plan *p, sxs_plan_view *v)
 {
-	if (!p) return sxs_fail(-2, "sxsg_plan_run: null plan");
+	int variant = p->skip == 1 ? 0 : 1;
+	if (!p->h_tw) {
+		p->h_tw = malloc(sizeof(double) * 2 * p->N);
+		if (!p->h_tw) return sxs_fail(-5, "out of host memory");
+	}
+	if (p->tw_variant != variant) {
+		sxs_twiddles_host(p->N, variant, p->h_tw);
+		SXS_CU(cudaMemcpyAsync(p->d_tw, p->h_tw, sizeof(double2) * p->N, cudaMemcpyHostToDevice, p->s));
+		p->tw_variant = variant;
+	}
+	SXS_CU(cudaStreamSynchronize(p->s));
+	memset(v, 0, sizeof(*v));
+	v->L = p->L; v->Q = p->Q; v->NT = p->NT; v->NP = p->NP; v->n1 = p->n1; v->n2 = p->n2; v->fp32 = p->fp32;
+	v->ext_tables = p->ext_tables; v->nzt = p->nzt; v->ncombo = p->ncombo; v->nslice = p->nslice;
+	v->tr_slices = p->tr_slices; v->rot_gamma = p->rot_gamma; v->npose = p->npose;
+	v->At = p->d_At; v->Bt = p->d_Bt; v->dtabf = p->lt->d_dtabf; v->tw = p->d_tw; v->P = p->d_P; v->U = p->d_U;
+	v->tauf = p->d_tauf; v->combo = p->d_combo; v->slices = p->d_slices; v->h_slices = p->h_slices;
+	v->h_cstart = p->h_cstart; v->poses = p->d_poses; v->cst = p->d_cstf; v->cross = p->d_cross;
+	v->fc = p->d_fc; v->c1g = p->d_c1g; v->c2g = p->d_c2g; v->gdf = p->d_gdf; v->a0sum = p->a0sum; v->peak = p->peak;
+	v->chi = p->d_chi; v->c1 = p->d_c1; v->c2 = p->d_c2; v->cell = p->d_cell;
+	return 0;
+}
+
+int sxs_plan_ztables_on(sxsg_plan *p, cudaStream_t s)
+{
+	return p->nzt > 0 ? plan_ztables(p, s) : 0;
+}
+
+void sxs_plan_mark_run(sxsg_plan *p, int fit_mode, const float *ms)
+{
+	p->last_fit = fit_mode;
+	p->grid_valid = 0;
+	p->tc_used = 0;
+	for (int i = 0; i < 5; i++) p->ms[i] = ms ? ms[i] : 0.0;
+}
+
+/* Host work before a run's launches: the twiddles (host copy kept with the
+ * plan, so the upload needs no wait), the tensor-core scratch, the
+ * translated table's chunking, its buffer and the timing events, the
+ * L-BFGS-B workspace.  After it, sxs_plan_enqueue issues only stream work
+ * that a CUDA graph can capture. */
+int sxs_plan_prepare(sxsg_plan *p, int fit_mode)
+{
 	if (fit_mode == SXSG_FIT_GRID && (p->n1 <= 0 || p->n2 <= 0))
 		return sxs_fail(-2, "sxsg_plan_run: grid fit needs a (c1, c2) grid");
 	if (fit_mode < 0 || fit_mode > 2) return sxs_fail(-2, "sxsg_plan_run: unknown fit mode %d", fit_mode);
-	int rc;
 	cudaStream_t s = p->s;
-	int Q = p->Q, L = p->L;
-	SXS_CU(cudaEventRecord(p->ev[0], s));
-	if ((rc = plan_tables(p))) return rc;
-	SXS_CU(cudaEventRecord(p->ev[1], s));
+	int N = p->N, rc;
+	int variant = p->skip == 1 ? 0 : 1;
+	if (!p->h_tw) {
+		p->h_tw = malloc(sizeof(double) * 2 * N);
+		if (!p->h_tw) return sxs_fail(-5, "out of host memory");
+	}
+	if (p->tw_variant != variant) {
+		sxs_twiddles_host(N, variant, p->h_tw);
+		SXS_CU(cudaMemcpyAsync(p->d_tw, p->h_tw, sizeof(double2) * N, cudaMemcpyHostToDevice, s));
+		p->tw_variant = variant;
+	}
+	int tc = p->fp32 && p->rot_engine == SXSG_ROT_TC && 2 * N <= 128;
+	if (tc && !p->d_amat)
+		SXS_CU(cudaMallocAsync((void **)&p->d_amat, sizeof(float) * sxsk_rotate_tc_scratch(p->L), s));
+	if (tc && !p->d_tcstat) SXS_CU(cudaMallocAsync((void **)&p->d_tcstat, sizeof(int), s));
 	/* translated table in chunks of whole slices that fit the budget */
 	size_t per_combo = (size_t)p->NP * 3 * SXS_QT * p->NT * p->celem;
 	int64_t chunk = (int64_t)(p->r_budget / (per_combo * SXS_SLICE));   /* slices per chunk */
 	if (chunk < 1) chunk = 1;
 	if (chunk > p->nslice) chunk = p->nslice;
 	int64_t nch = chunk > 0 ? (p->nslice + chunk - 1) / chunk : 0;
-	p->last_chunks = (int)(nch < INT32_MAX ? nch : INT32_MAX);
 	if (nch > INT32_MAX / 3) return sxs_fail(-2, "sxsg_plan_run: too many chunks");
 	if ((rc = plan_events(p, (int)(3 * nch)))) return rc;
 	int64_t rcap = chunk * SXS_SLICE;
@@ -742,33 +786,52 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 	if (rcap > 0 && p->R_combos < rcap) {
 		pfree(p, p->d_R);
 		p->d_R = NULL;
-		SXS_CU(cudaMallocAsync(&p->d_R, per_combo * rcap, p->s));
+		SXS_CU(cudaMallocAsync(&p->d_R, per_combo * rcap, s));
 		p->R_combos = rcap;
 	}
+	if (fit_mode == SXSG_FIT_LBFGSB && !p->d_scaled && p->npose > 0)
+		SXS_CU(cudaMallocAsync((void **)&p->d_scaled, sizeof(double) * (size_t)p->npose * 6 * p->Q, s));
+	p->run_chunk = chunk;
+	p->run_nch = nch;
+	p->last_chunks = (int)(nch < INT32_MAX ? nch : INT32_MAX);
+	return 0;
+}
+
+/* The launches of a prepared run on the plan's stream (its side stream
+ * forks from and joins it): tables, the chunks of translation and per-pose
+ * contraction, and the fit unless fit_mode is SXSG_FIT_NONE.  timed: record
+ * the stage events that sxsg_plan_timings reads. */
+int sxs_plan_enqueue(sxsg_plan *p, int fit_mode, int timed)
+{
+	int rc;
+	cudaStream_t s = p->s;
+	int Q = p->Q, L = p->L;
+	int64_t chunk = p->run_chunk, nch = p->run_nch;
+	if (timed) SXS_CU(cudaEventRecord(p->ev[0], s));
+	if ((rc = plan_tables(p))) return rc;
+	if (timed) SXS_CU(cudaEventRecord(p->ev[1], s));
 	const void *tau = p->fp32 ? (const void *)p->d_tauf : (const void *)p->d_tau;
 	for (int64_t k = 0; k < nch; k++) {
 		int64_t s0 = k * chunk, s1 = s0 + chunk < p->nslice ? s0 + chunk : p->nslice;
 		int64_t c0 = p->h_slices[2 * s0], c1 = p->h_slices[2 * (s1 - 1)] + p->h_slices[2 * (s1 - 1) + 1];
 		cudaEvent_t *e = p->cev + 3 * k;
-		SXS_CU(cudaEventRecord(e[0], s));
+		if (timed) SXS_CU(cudaEventRecord(e[0], s));
 		SXS_K(sxsk_translate(p->d_U, tau, p->d_combo + 3 * c0, p->d_slices + 2 * s0, (int)(s1 - s0), (int)c0,
 		                     (int)(c1 - c0), p->nzt, Q, L, p->d_R, p->fp32, p->tr_slices, s));
-		SXS_CU(cudaEventRecord(e[1], s));
+		if (timed) SXS_CU(cudaEventRecord(e[1], s));
 		int64_t p0 = p->h_cstart[c0], p1 = p->h_cstart[c1];
 		SXS_K(sxsk_pose_cross(p->d_poses + p0, (int)(p1 - p0), (int)c0, (int)(c1 - c0), p->d_P, p->d_R, p->d_tw,
 		                      p->fp32 ? (const void *)p->d_cstf : (const void *)p->d_cst, Q, L,
 		                      p->d_cross, p->fp32, s));
-		SXS_CU(cudaEventRecord(e[2], s));
+		if (timed) SXS_CU(cudaEventRecord(e[2], s));
 		sxs_count_launches(sxsk_translate_launches(L) + 1);
 	}
-	SXS_CU(cudaEventRecord(p->ev[5], s));
+	if (timed) SXS_CU(cudaEventRecord(p->ev[5], s));
 	int n = (int)p->npose;
 	if (fit_mode == SXSG_FIT_GRID) {
 		SXS_K(plan_fit_grid(p, n, p->d_chi, p->d_c1, p->d_c2, p->d_cell, NULL, s));
 		sxs_count_launches(n > 0 ? 1 : 0);
 	} else if (fit_mode == SXSG_FIT_LBFGSB) {
-		if (!p->d_scaled && n > 0)
-			SXS_CU(cudaMallocAsync((void **)&p->d_scaled, sizeof(double) * (size_t)n * 6 * Q, s));
 		SXS_K(sxs_fit_lbfgsb_launch(p->d_cross, p->fp32, p->d_scaled, n, Q, p->d_q, p->d_a, p->mult, p->peak, 1, p->d_chi,
 		                            p->d_c1, p->d_c2, p->d_scale, p->d_iters, s));
 		sxs_count_launches(n > 0 ? 2 : 0);
@@ -776,6 +839,17 @@ int sxsg_plan_run(sxsg_plan *p, int fit_mode)
 	}
 	p->last_fit = fit_mode;
 	p->grid_valid = 0;
+	return 0;
+}
+
+int sxsg_plan_run(sxsg_plan *p, int fit_mode)
+{
+	if (!p) return sxs_fail(-2, "sxsg_plan_run: null plan");
+	int rc = sxs_plan_prepare(p, fit_mode);
+	if (!rc) rc = sxs_plan_enqueue(p, fit_mode, 1);
+	if (rc) return rc;
+	cudaStream_t s = p->s;
+	int64_t nch = p->run_nch;
 	cudaEvent_t end;
 	SXS_CU(cudaEventCreate(&end));
 	SXS_CU(cudaEventRecord(end, s));

@@ -75,6 +75,36 @@ size_t sxs_plan_table_bytes(int L, int Q, int precision);
 size_t sxs_plan_base_bytes(int L, int Q, int nzt, int64_t npose, int n1, int precision, int fit_mode);
 size_t sxs_plan_combo_bytes(int L, int Q, int precision);
 
+/* What a batch of plans (sxs_batch.c) reads of one plan: its sizes, the
+ * device tables its kernels use and its outputs. */
+typedef struct {
+	int L, Q, NT, NP, n1, n2, fp32, ext_tables, nzt, ncombo, nslice, tr_slices, rot_gamma;
+	int64_t npose;
+	const void *At, *Bt;            /* transposed coefficients */
+	const float *dtabf;             /* float Wigner-d table of L */
+	const double2 *tw;              /* twiddles (uploaded) */
+	void *P, *U;                    /* rotation tables */
+	const float *tauf;              /* float per-z translation tables */
+	const int32_t *combo, *slices;  /* device combos [ncombo][3], slices [nslice][2] */
+	const int32_t *h_slices;        /* host copy of the slices */
+	const int64_t *h_cstart;        /* first sorted pose of each combo [ncombo + 1] */
+	const sxsk_pose *poses;         /* sorted by combo */
+	const void *cst;                /* double-float self terms */
+	void *cross;                    /* double-float cross terms [npose][6][Q] */
+	const double *fc, *c1g, *c2g;
+	const float2 *gdf;
+	double a0sum, peak;
+	double *chi, *c1, *c2;
+	int32_t *cell;
+} sxs_plan_view;
+/* fills v after uploading the twiddles of the plan's pose list (waits for
+ * the plan's stream) */
+int sxs_plan_batch_view(sxsg_plan *p, sxs_plan_view *v);
+/* the per-z tables of the plan's touched z on stream s */
+int sxs_plan_ztables_on(sxsg_plan *p, cudaStream_t s);
+/* a batch filled the plan's outputs with this fit */
+void sxs_plan_mark_run(sxsg_plan *p, int fit_mode, const float *ms);
+
 /* per-q constants of the grid fit: fc[Q][5] */
 void sxs_fit_constants(const double *q, const double *a, int Q, double *fc);
 
