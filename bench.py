@@ -402,6 +402,149 @@ def run_serving(g, args):
     return out
 
 
+def run_batch(g, args):
+    """Many uneven dimers (workload.batch_specs, mixed precision, grid fit)
+    scored three ways:
+      graph    the resident plans of a wave of dimers that fit in device
+               memory scored by one CUDA graph of persistent kernels
+               (sxsg_batch_run); checked bit for bit against the plan runs
+      plans    the same resident plans run one after another (sxsg_plan_run)
+      serving  the same dimers submitted at once to the serving loop, which
+               sets up each job (uploads, pose decode, tables) itself
+    Times are host wall clock around synchronous calls; the graph's device
+    time per stage comes from event nodes in the graph."""
+    from libfmftsaxs_gb300 import workload as wl
+    specs, rpool, lpool = wl.batch_specs(args.batch_dimers, seed=args.seed + 3, max_poses=args.batch_max_poses)
+    t0 = time.perf_counter()
+    recs = wl.pool_molecules(rpool, workers=min(16, os.cpu_count() or 1))
+    ligs = wl.pool_molecules(lpool, workers=min(16, os.cpu_count() or 1))
+    dims = [wl.build_dimer(sp, recs[sp["rec"]], ligs[sp["lig"]], g) for sp in specs]
+    t_build = time.perf_counter() - t0
+    poses = sum(len(d.index) for d in dims)
+    free, total = g.device_memory()
+    budget = int(0.7 * free)
+    waves, cur, used = [], [], 0
+    for i, d in enumerate(dims):
+        nb = wl.plan_bytes(d.L, d.Q, len(d.index), len(d.z))
+        if cur and used + nb > budget:
+            waves.append(cur)
+            cur, used = [], 0
+        cur.append(i)
+        used += nb
+    if cur:
+        waves.append(cur)
+    graph_s, plans_s, same = 0.0, 0.0, True
+    forms, seq_stage = {}, np.zeros(4)
+    ref_chi = {}
+
+    def first_chi(plans, wv):
+        # chi of the first launch form run on this wave, the reference of the others
+        if wv[0] not in ref_chi:
+            ref_chi[wv[0]] = [p.results()["chi"] for p in plans]
+        return ref_chi[wv[0]]
+    dev = np.zeros(3)
+    phases = launches = items = 0
+    create_s = 0.0
+    for wv in waves:
+        plans = []
+        for i in wv:
+            d = dims[i]
+            p = g.Plan(d.A, d.B, d.q, d.z, d.L, d.a, d.mult, d.peak, d.c1g, d.c2g, precision=g.MIXED)
+            p.set_poses(d.index, skip=1)
+            plans.append(p)
+        # the other launch forms, briefly (each checked bit for bit below)
+        for fl in (0, g.BATCH_PERSISTENT, g.BATCH_OVERLAP, g.BATCH_PERSISTENT | g.BATCH_OVERLAP):
+            if fl == g.BATCH_DEFAULT:
+                continue
+            bb = g.Batch(plans, fit=g.FIT_GRID, flags=fl)
+            bb.run()
+            t0 = time.perf_counter()
+            bb.run()
+            f = forms.setdefault(fl, np.zeros(4))
+            f[0] += time.perf_counter() - t0
+            sf = bb.stats()
+            f[1:] += (sf["tables_ms"], sf["phases_ms"], sf["fit_ms"])
+            bb.close()
+            same &= all(np.array_equal(p.results()["chi"], q) for p, q in zip(plans, first_chi(plans, wv)))
+        t0 = time.perf_counter()
+        b = g.Batch(plans, fit=g.FIT_GRID)
+        create_s += time.perf_counter() - t0
+        for _ in range(args.warmup):
+            b.run()
+        ts, ds = [], []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            b.run()
+            ts.append(time.perf_counter() - t0)
+            st = b.stats()
+            ds.append((st["tables_ms"], st["phases_ms"], st["fit_ms"]))
+        graph_s += float(np.median(ts))
+        dev += np.median(np.array(ds), axis=0)
+        phases += st["phases"]
+        launches += st["launches"]
+        items += st["items"]
+        got = [p.results() for p in plans]
+        arena = st["arena_bytes"]
+        b.close()
+
+        def seq():
+            # each plan with the batch's arena as its translated-table bound,
+            # released after its run so that the next plan has the room
+            st4 = np.zeros(4)
+            for p in plans:
+                p.set_budget(arena)
+                p.run(g.FIT_GRID)
+                tm = p.timings()
+                st4 += (tm["tables"], tm["translate"], tm["pose"], tm["fit"])
+                p.set_budget(1)
+            return st4
+        seq()
+        t0 = time.perf_counter()
+        seq_stage += seq()
+        plans_s += time.perf_counter() - t0
+        for p, r in zip(plans, got):
+            a = p.results()
+            same &= all(np.array_equal(a[k], r[k]) for k in ("chi", "c1", "c2", "cell"))
+            p.close()
+    srv_s = None
+    if not args.skip_batch_serve:
+        for rep in range(2):
+            srv = g.Server(max_active=args.serve_active)
+            t0 = time.perf_counter()
+            tickets = [srv.submit(A=d.A, B=d.B, qvals=d.q, zvals=d.z, L=d.L, a=d.a, mult=d.mult, peak=d.peak,
+                                  index=d.index, c1grid=d.c1g, c2grid=d.c2g, precision=g.MIXED) for d in dims]
+            for t in tickets:
+                srv.wait(t)
+            srv_s = time.perf_counter() - t0
+            srv.close()
+    hist = {}
+    for d in dims:
+        hist["L%d" % d.L] = hist.get("L%d" % d.L, 0) + 1
+    out = {"dimers": len(dims), "poses": int(poses), "waves": len(waves), "phases": int(phases),
+           "graph_kernel_launches": int(launches), "work_items": int(items),
+           "graph": {"ms_per_step": graph_s * 1e3, "poses_per_s": poses / graph_s,
+                     "device_ms": {"tables": dev[0], "translate_and_pose": dev[1], "fit": dev[2]}},
+           "graph_forms_ms": {{0: "one_block_per_item", 1: "persistent", 2: "one_block_per_item+overlap",
+                               3: "persistent+overlap"}[k]: {"total": v[0] * 1e3, "tables": v[1], "phases": v[2],
+                                                             "fit": v[3]} for k, v in forms.items()},
+           "graph_default_form": "persistent",
+           "plans_sequential": {"ms_per_step": plans_s * 1e3, "poses_per_s": poses / plans_s,
+                                "device_ms": dict(zip(("tables", "translate", "pose", "fit"), seq_stage.tolist()))},
+           "serving": ({"ms_per_step": srv_s * 1e3, "poses_per_s": poses / srv_s,
+                        "note": "per-job plan set-up, uploads and pose decode included; %d jobs on the device"
+                                % args.serve_active} if srv_s else None),
+           "bitwise_equal_to_plan_runs": bool(same),
+           "setup_s": {"dimers": t_build, "batch_create": create_s},
+           "scenario": "%d dimers from pools of %d receptors (%d-%d atoms) and %d ligands (%d-%d atoms); L %s; "
+                       "Q in {51, 101, 201}; %d-%d poses log-uniform (|t| in [25, 45] A), %d in all; grid fit 11x41; "
+                       "steps: median of %d graph replays after %d"
+                       % (len(dims), len(rpool), min(r[0] for r in rpool), max(r[0] for r in rpool), len(lpool),
+                          min(r[0] for r in lpool), max(r[0] for r in lpool), json.dumps(hist),
+                          min(len(d.index) for d in dims), max(len(d.index) for d in dims), poses, args.steps,
+                          args.warmup)}
+    return out
+
+
 def run_ours(args):
     import libfmftsaxs_gb300 as g
     from libfmftsaxs_gb300 import build as libbuild
@@ -524,6 +667,8 @@ def run_ours(args):
     out["expansion"] = expansion_timing(g, w, fp64_peak)
     if not args.skip_serve:
         out["serving"] = run_serving(g, args)
+    if not args.skip_batch:
+        out["batch"] = run_batch(g, args)
     print(json.dumps(out))
 
 
@@ -590,6 +735,10 @@ def main():
     ap.add_argument("--serve-active", type=int, default=4, help="serving: jobs on the device at once")
     ap.add_argument("--serve-cap-gb", type=float, default=150.0, help="serving: HBM cap")
     ap.add_argument("--serve-fp64", action="store_true", help="serving: also run the FP64 path")
+    ap.add_argument("--skip-batch", action="store_true", help="no batched-dimers scenario")
+    ap.add_argument("--skip-batch-serve", action="store_true", help="batched dimers: no serving comparison")
+    ap.add_argument("--batch-dimers", type=int, default=64)
+    ap.add_argument("--batch-max-poses", type=int, default=200000)
     args = ap.parse_args()
     if args.gpus > 1 and int(os.environ.get("RANK", "0")) != 0:
         return  # the path does not shard: one GPU runs, other ranks idle

@@ -164,6 +164,8 @@ const char *sxsg_last_error(void);
 int sxsg_init(int device);
 /* Number of kernel launches issued by this library since load. */
 long long sxsg_launch_count(void);
+/* Free and total memory of the library's device (cudaMemGetInfo). */
+int sxsg_device_memory(size_t *free_bytes, size_t *total_bytes);
 
 /* Form-factor constants of one type name of the reference's mapping file
  * ("C", "N", "O", "S", "CH2", ...; src/form_factor_table.c:8-49, 76-107):
@@ -277,7 +279,8 @@ int sxsg_plan_create(sxsg_plan **plan, const double *A, const double *B, const d
 int sxsg_plan_set_poses(sxsg_plan *plan, const int64_t *index, int64_t n, int skip);
 /* Upper bound on the device memory of the per-chunk translated table (the
  * default is half the free memory at plan creation); touched (z, b2, g2)
- * combos are processed in chunks that fit. */
+ * combos are processed in chunks that fit.  A bound below the plan's
+ * current buffer releases that buffer (after the plan's queued work). */
 int sxsg_plan_set_budget(sxsg_plan *plan, size_t bytes);
 /* Rotation engine of a mixed-precision plan: SXSG_ROT_CUDA (CUDA cores,
  * the default) or SXSG_ROT_TC (tcgen05 tensor cores, 3xTF32 with FP32
@@ -344,10 +347,18 @@ typedef struct {
 	size_t arena_bytes; /* translated-table arena */
 	double ms[4];       /* last replay: [0] tables, [1] translation + per-pose, [2] fit, [3] whole graph */
 } sxsg_batch_stats;
+/* Launch forms of a batch (flags):
+ *   SXSG_BATCH_PERSISTENT  persistent kernels (SMs x resident blocks taking
+ *                          items through an atomic counter); without it one
+ *                          block per item, in order
+ *   SXSG_BATCH_OVERLAP     two arena halves: the translations of phase
+ *                          k + 1 run beside the per-pose work of phase k */
+enum { SXSG_BATCH_PERSISTENT = 1, SXSG_BATCH_OVERLAP = 2 };
 /* fit_mode: SXSG_FIT_GRID or SXSG_FIT_NONE; arena_bytes: upper bound on
  * the translated-table arena (0 = what the dimers need, at most half the
  * free device memory) */
-int sxsg_batch_create(sxsg_plan *const *plans, int nplan, int fit_mode, size_t arena_bytes, sxsg_batch **batch);
+int sxsg_batch_create(sxsg_plan *const *plans, int nplan, int fit_mode, size_t arena_bytes, int flags,
+                      sxsg_batch **batch);
 /* one replay of the graph; returns when it has finished */
 int sxsg_batch_run(sxsg_batch *batch);
 int sxsg_batch_stats_get(const sxsg_batch *batch, sxsg_batch_stats *stats);

@@ -16,6 +16,8 @@ FIT_NONE, FIT_GRID, FIT_LBFGSB = 0, 1, 2
 FP64 = 0
 MIXED = 1
 ROT_CUDA, ROT_TC = 0, 1
+BATCH_PERSISTENT, BATCH_OVERLAP = 1, 2
+BATCH_DEFAULT = BATCH_PERSISTENT
 
 _lib = None
 
@@ -70,6 +72,13 @@ def last_error():
 
 def launch_count():
     return int(load().sxsg_launch_count())
+
+
+def device_memory():
+    """(free, total) bytes of the library's device."""
+    f, t = C.c_size_t(), C.c_size_t()
+    _check(load().sxsg_device_memory(C.byref(f), C.byref(t)))
+    return int(f.value), int(t.value)
 
 
 def init(device=0):
@@ -267,9 +276,11 @@ class Batch:
     Plan.results / Plan.topk after run().  The batch holds the plans'
     device pointers: keep the plans alive and unchanged while it exists."""
 
-    def __init__(self, plans, fit=FIT_GRID, arena_bytes=0):
+    def __init__(self, plans, fit=FIT_GRID, arena_bytes=0, flags=None):
         lib = load()
-        lib.sxsg_batch_create.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_size_t, C.POINTER(C.c_void_p)]
+        lib.sxsg_batch_create.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_size_t, C.c_int, C.POINTER(C.c_void_p)]
+        if flags is None:
+            flags = BATCH_DEFAULT
         lib.sxsg_batch_run.argtypes = [C.c_void_p]
         lib.sxsg_batch_stats_get.argtypes = [C.c_void_p, C.POINTER(_BatchStats)]
         lib.sxsg_batch_destroy.argtypes = [C.c_void_p]
@@ -277,7 +288,7 @@ class Batch:
         self.plans = list(plans)
         arr = (C.c_void_p * len(self.plans))(*[p.h.value for p in self.plans])
         self.h = C.c_void_p()
-        _check(lib.sxsg_batch_create(arr, len(self.plans), int(fit), int(arena_bytes), C.byref(self.h)))
+        _check(lib.sxsg_batch_create(arr, len(self.plans), int(fit), int(arena_bytes), int(flags), C.byref(self.h)))
 
     def run(self):
         _check(load().sxsg_batch_run(self.h))

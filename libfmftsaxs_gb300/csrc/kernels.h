@@ -177,11 +177,12 @@ int sxsk_pose_ingest(const double *rot, const double *tr, long n, const double *
                      cudaStream_t s);
 
 /* ------------------------------------------------------------------
- * Batched persistent launches of the mixed path (many dimers at once).
- * Each kernel runs a grid of (SMs x resident blocks) that take work items
- * from an array in order through an atomic counter (*ctr, zeroed by the
- * caller; a block takes the next item when it finishes one, so the array
- * is ordered largest first).  An item is one block's work of the
+ * Batched launches of the mixed path (many dimers at once).  With a
+ * counter (*ctr, zeroed by the caller) a kernel runs persistently: a grid
+ * of (SMs x resident blocks) that take work items from an array in order
+ * through the counter (a block takes the next item when it finishes one,
+ * so the array is ordered largest first).  With ctr = NULL it runs one
+ * block per item, in array order.  An item is one block's work of the
  * single-dimer kernel, on the job its first field names, and runs that
  * kernel's own block code: results equal the single-dimer launches bit
  * for bit.

@@ -314,10 +314,13 @@ k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const S *__restrict__ dtab
 	rotate_block<S, G, CH>(spf_t, dtab, hs, Q, L, conj, out, t, b, m);
 }
 
-/* next work item of a batched persistent kernel for the whole block (the
- * leading barrier: every thread is done with the previous item) */
-__device__ __forceinline__ int next_item(int *ctr)
+/* Work item k (from 0) of a block of a batched kernel.  Persistent launch
+ * (ctr != NULL): the next unclaimed item, for the whole block (the leading
+ * barrier: every thread is done with the previous item).  One block per
+ * item (ctr == NULL): item blockIdx.x, then none. */
+__device__ __forceinline__ int next_item(int *ctr, int k, int nitems)
 {
+	if (!ctr) return k == 0 ? (int)blockIdx.x : nitems;
 	__shared__ int s_it;
 	__syncthreads();
 	if (threadIdx.x == 0) s_it = atomicAdd(ctr, 1);
@@ -335,8 +338,8 @@ k_rotate_batch(const sxsk_rot_job *__restrict__ jobs, const int4 *__restrict__ i
 	RotTw<float> *hs = reinterpret_cast<RotTw<float> *>(rsm_raw);
 	const double2 *cur = nullptr;
 	int curL = -1;
-	for (;;) {
-		int it = next_item(ctr);
+	for (int k = 0;; k++) {
+		int it = next_item(ctr, k, nitems);
 		if (it >= nitems) break;
 		int4 w = items[it];
 		sxsk_rot_job j = jobs[w.x];
@@ -683,8 +686,8 @@ __global__ void __launch_bounds__(TCOL_THREADS(3), TP_MINB(NB))
 k_translate_batch(const sxsk_tr_job *__restrict__ jobs, const int4 *__restrict__ items, int nitems, int *ctr)
 {
 	extern __shared__ __align__(16) unsigned char tps_raw[];
-	for (;;) {
-		int it = next_item(ctr);
+	for (int k = 0;; k++) {
+		int it = next_item(ctr, k, nitems);
 		if (it >= nitems) break;
 		int4 w = items[it];
 		sxsk_tr_job j = jobs[w.x];
@@ -854,8 +857,8 @@ k_pose_cross_batch(const sxsk_pc_job *__restrict__ jobs, const int4 *__restrict_
 	__shared__ float2 tws[2 * SXS_LMAX_K - 1];
 	const double2 *cur = nullptr;
 	int curL = -1;
-	for (;;) {
-		int it = next_item(ctr);
+	for (int k = 0;; k++) {
+		int it = next_item(ctr, k, nitems);
 		if (it >= nitems) break;
 		int4 w = items[it];
 		sxsk_pc_job j = jobs[w.x];
@@ -1250,11 +1253,16 @@ static int rotate_any(const void *spf_t, const void *dtab, const double2 *tw, in
 	}
 }
 
-/* grid of a batched persistent launch: every resident block of the kernel
- * on every SM, at most one block per item */
+/* grid of a batched launch: persistent (ctr != NULL), every resident block
+ * of the kernel on every SM, at most one block per item; else one block
+ * per item */
 template <typename F>
-static cudaError_t persistent_grid(F kern, int threads, size_t smem, int nitems, int *grid)
+static cudaError_t persistent_grid(F kern, int threads, size_t smem, int nitems, const int *ctr, int *grid)
 {
+	if (!ctr) {
+		*grid = nitems;
+		return cudaSuccess;
+	}
 	int dev = 0, nsm = 0, per = 0;
 	cudaError_t e = cudaGetDevice(&dev);
 	if (!e) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -1276,7 +1284,7 @@ static int rotate_batch_launch(const sxsk_rot_job *jobs, const int4 *items, int 
 	cudaError_t e = cudaSuccess;
 	if (smem > 48 * 1024) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	int grid = 0;
-	if (!e) e = persistent_grid(kern, ROT_THREADS(CH), smem, nitems, &grid);
+	if (!e) e = persistent_grid(kern, ROT_THREADS(CH), smem, nitems, ctr, &grid);
 	if (e) return e;
 	kern<<<grid, ROT_THREADS(CH), smem, s>>>(jobs, items, nitems, ctr);
 	return cudaGetLastError();
@@ -1293,7 +1301,7 @@ static int translate_batch_launch(const sxsk_tr_job *jobs, const int4 *items, in
 		e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
 		                         (int)cudaSharedmemCarveoutMaxShared);
 	int grid = 0;
-	if (!e) e = persistent_grid(kern, TCOL_THREADS(3), smem, nitems, &grid);
+	if (!e) e = persistent_grid(kern, TCOL_THREADS(3), smem, nitems, ctr, &grid);
 	if (e) return e;
 	kern<<<grid, TCOL_THREADS(3), smem, s>>>(jobs, items, nitems, ctr);
 	return cudaGetLastError();
@@ -1426,7 +1434,7 @@ int sxsk_pose_cross_batch(const sxsk_pc_job *jobs, const int4 *items, int nitems
 {
 	if (nitems <= 0) return 0;
 	int grid = 0;
-	cudaError_t e = persistent_grid(k_pose_cross_batch, 128, 0, nitems, &grid);
+	cudaError_t e = persistent_grid(k_pose_cross_batch, 128, 0, nitems, ctr, &grid);
 	if (e) return e;
 	k_pose_cross_batch<<<grid, 128, 0, s>>>(jobs, items, nitems, ctr);
 	return cudaGetLastError();

@@ -233,11 +233,17 @@ k_fit_grid_df_batch(const sxsk_fit_job *__restrict__ jobs, const int2 *__restric
 	extern __shared__ double sm[];
 	__shared__ int s_it;
 	int cur = -1;
-	for (;;) {
-		__syncthreads();
-		if (threadIdx.x == 0) s_it = atomicAdd(ctr, 1);
-		__syncthreads();
-		int it = s_it;
+	for (int k = 0;; k++) {
+		int it;
+		if (ctr) {
+			/* persistent: the next unclaimed item */
+			__syncthreads();
+			if (threadIdx.x == 0) s_it = atomicAdd(ctr, 1);
+			__syncthreads();
+			it = s_it;
+		} else {
+			it = k == 0 ? (int)blockIdx.x : nitems;   /* one block per item */
+		}
 		if (it >= nitems) break;
 		int2 w = items[it];
 		sxsk_fit_job J = jobs[w.x];
@@ -310,14 +316,14 @@ extern "C" int sxsk_fit_grid_df_batch(const sxsk_fit_job *jobs, const int2 *item
 	cudaError_t e = cudaSuccess;
 	if (smem > 48 * 1024)
 		e = cudaFuncSetAttribute(k_fit_grid_df_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-	int dev = 0, nsm = 0, per = 0;
+	int dev = 0, nsm = 0, per = 1;
 	if (!e) e = cudaGetDevice(&dev);
 	if (!e) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-	if (!e) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fit_grid_df_batch, FITD_THREADS, smem);
+	if (!e && ctr) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fit_grid_df_batch, FITD_THREADS, smem);
 	if (e) return e;
 	if (per < 1) return cudaErrorInvalidConfiguration;
 	long g = (long)nsm * per;
-	int grid = (int)(g < nitems ? g : nitems);
+	int grid = ctr ? (int)(g < nitems ? g : nitems) : nitems;   /* persistent, or one block per item */
 	k_fit_grid_df_batch<<<grid, FITD_THREADS, smem, s>>>(jobs, items, nitems, ctr);
 	return cudaGetLastError();
 }

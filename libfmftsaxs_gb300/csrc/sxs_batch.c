@@ -7,11 +7,13 @@
  * rotation blocks (table, q tile, beta, m), translation blocks (chunk, q
  * tile, slice group, m) per column class NB, per-pose blocks (chunk, q tile,
  * 32 poses) and fit groups (dimer, group of poses).  The batch lists those
- * blocks of all dimers as (job, ...) items, ordered by estimated cost,
- * largest first, and runs each list with one persistent launch of (SMs x
- * resident blocks) blocks that take items through an atomic counter.  An
- * item runs the single-dimer kernel's own block code, so every output equals
- * a sxsg_plan_run of its plan bit for bit.
+ * blocks of all dimers as (job, ...) items: jobs by estimated cost, largest
+ * first, the items of a job in the single-dimer kernel's block order (its
+ * L2 reuse between neighbouring blocks).  Each list runs as one launch:
+ * persistent (SMs x resident blocks taking items through an atomic counter,
+ * SXSG_BATCH_PERSISTENT) or one block per item.  An item runs the
+ * single-dimer kernel's own block code, so every output equals a
+ * sxsg_plan_run of its plan bit for bit.
  *
  * Phases.  The translated table of a dimer is cut into chunks of whole
  * slices (as a plan run does); chunks of all dimers are packed first-fit,
@@ -20,8 +22,9 @@
  * on parallel branches of the graph) followed by one per-pose launch.
  *
  * Graph.  Zeroing the item counters, the per-z tables of every dimer (two
- * branches), the rotation launches (one per gamma group size), the phases
- * and the fit launch are captured once at sxsg_batch_create; a run is one
+ * high-priority branches, so that their FP64 blocks run beside the rotation
+ * blocks), the rotation launches (one per gamma group size), the phases and
+ * the fit launch are captured once at sxsg_batch_create; a run is one
  * cudaGraphLaunch.  Stage times come from event nodes in the graph.
  */
 #include <stdlib.h>
@@ -60,8 +63,9 @@ struct sxsg_batch {
 	int n, fit_mode;
 	sxsg_plan **plans;
 	sxs_plan_view *v;
-	cudaStream_t s, br[SXSB_BR];
-	cudaEvent_t fork, join[SXSB_BR];
+	int flags;
+	cudaStream_t s, ps, br[SXSB_BR];   /* origin (tables, fit), pose lane, translation lanes */
+	cudaEvent_t fork, join[SXSB_BR], evpose[2];
 	cudaEvent_t ev[4];       /* graph event nodes: start, tables done, phases done, end */
 	cudaGraph_t graph;
 	cudaGraphExec_t exec;
@@ -125,7 +129,10 @@ void sxsg_batch_destroy(sxsg_batch *b)
 	}
 	for (int i = 0; i < 4; i++)
 		if (b->ev[i]) cudaEventDestroy(b->ev[i]);
+	for (int i = 0; i < 2; i++)
+		if (b->evpose[i]) cudaEventDestroy(b->evpose[i]);
 	if (b->fork) cudaEventDestroy(b->fork);
+	if (b->ps) cudaStreamDestroy(b->ps);
 	if (b->s) cudaStreamDestroy(b->s);
 	free(b->plans);
 	free(b->v);
@@ -207,6 +214,18 @@ static int add_item(bvec *items, double cost, int x, int y, int z, int w)
 	return 0;
 }
 
+/* Items [i0, n) are one job's, added in the single-dimer kernel's block
+ * order; they all get the job's total cost, so that a launch takes the jobs
+ * largest first and the blocks of each job in that order (neighbouring
+ * blocks share table rows in L2 as in the single-dimer launch). */
+static void job_cost(bvec *items, size_t i0)
+{
+	bitem *it = items->p;
+	double tot = 0;
+	for (size_t i = i0; i < items->n; i++) tot += it[i].cost;
+	for (size_t i = i0; i < items->n; i++) it[i].cost = tot;
+}
+
 /* rotation launches: one per gamma group size, items (table, t, b, m) */
 static int build_rotations(sxsg_batch *b, bstage *st)
 {
@@ -233,6 +252,7 @@ static int build_rotations(sxsg_batch *b, bstage *st)
 				j->Q = v->Q;
 				j->L = v->L;
 				j->conj = tab;
+				size_t i0 = items.n;
 				for (int t = 0; t < v->NT && !rc; t++)
 					for (int bb = 0; bb < K && !rc; bb++)
 						for (int m = 0; m < K && !rc; m++) {
@@ -240,6 +260,7 @@ static int build_rotations(sxsg_batch *b, bstage *st)
 							double cost = 0.5 * ((double)v->L * (v->L + 1) - (double)m * (m - 1)) + (K - m);
 							rc = add_item(&items, cost, nj, t, bb, m);
 						}
+				job_cost(&items, i0);
 				nj++;
 			}
 		}
@@ -266,8 +287,10 @@ static int build_phases(sxsg_batch *b, bstage *st, size_t arena_req)
 	}
 	size_t fr = 0, tot = 0;
 	cudaMemGetInfo(&fr, &tot);
+	int halves = (b->flags & SXSG_BATCH_OVERLAP) ? 2 : 1;
 	size_t arena = arena_req ? arena_req : fr / 2;
-	if (arena > total) arena = total;
+	if (arena > total * halves) arena = total * halves;
+	arena = arena / halves & ~(size_t)(SXSB_ALIGN - 1);   /* one phase's share */
 	if (total > 0 && arena < al(largest_slice)) {
 		if (arena_req) return sxs_fail(-2, "sxsg_batch_create: arena of %zu bytes below one slice (%zu)", arena_req,
 		                               al(largest_slice));
@@ -324,6 +347,10 @@ static int build_phases(sxsg_batch *b, bstage *st, size_t arena_req)
 	size_t used = 0;
 	for (int ph = 0; ph < nphase; ph++) used = fill[ph] > used ? fill[ph] : used;
 	free(fill);
+	/* phase k uses arena half k mod halves */
+	for (size_t k = 0; k < np; k++) pc[k].off += (size_t)(pc[k].phase % halves) * used;
+	if (nphase < 2) halves = 1;
+	used *= (size_t)halves;
 	b->nphase = nphase;
 	b->arena = used;
 	if (used > 0) {
@@ -386,16 +413,18 @@ static int build_phases(sxsg_batch *b, bstage *st, size_t arena_req)
 				if (m_lo < 0) m_lo = 0;
 				int ng = (t->nslice + t->sb - 1) / t->sb;
 				const int32_t *hs = v->h_slices + 2 * pc[jmap[j]].s0;
-				for (int g = 0; g < ng && !rc; g++) {
-					/* combos of the slice group x n^2 multiply-adds each */
-					int sa = g * t->sb, sz = sa + t->sb < t->nslice ? sa + t->sb : t->nslice;
-					double nc = (double)(hs[2 * (sz - 1)] + hs[2 * (sz - 1) + 1] - hs[2 * sa]);
-					for (int tt = 0; tt < v->NT && !rc; tt++)
+				size_t i0 = items.n;
+				for (int tt = 0; tt < v->NT && !rc; tt++)
+					for (int g = 0; g < ng && !rc; g++) {
+						/* combos of the slice group x n^2 multiply-adds each */
+						int sa = g * t->sb, sz = sa + t->sb < t->nslice ? sa + t->sb : t->nslice;
+						double nc = (double)(hs[2 * (sz - 1)] + hs[2 * (sz - 1) + 1] - hs[2 * sa]);
 						for (int m = m_lo; m <= m_hi && !rc; m++) {
 							int n = K - m;
 							rc = add_item(&items, nc * n * n, j, tt, g, m);
 						}
-				}
+					}
+				job_cost(&items, i0);
 			}
 			if (!rc) rc = st_launch(st, 1, NB, ph, tj, sizeof(sxsk_tr_job) * nj, &items, 0);
 		}
@@ -403,8 +432,10 @@ static int build_phases(sxsg_batch *b, bstage *st, size_t arena_req)
 			const sxsk_pc_job *q = &pj[j];
 			const sxs_plan_view *v = &b->v[pc[jmap[j]].plan];
 			int bpt = (q->npose + 31) / 32;
+			size_t i0 = items.n;
 			for (int tt = 0; tt < v->NT && !rc; tt++)
 				for (int pb = 0; pb < bpt && !rc; pb++) rc = add_item(&items, (double)v->NP, j, tt, pb, 0);
+			job_cost(&items, i0);
 		}
 		if (!rc) rc = st_launch(st, 2, 0, ph, pj, sizeof(sxsk_pc_job) * nj, &items, 0);
 	}
@@ -454,7 +485,9 @@ static int build_fit(sxsg_batch *b, bstage *st)
 		J->n2 = v->n2;
 		int ngroup = (J->nslot + J->ppb - 1) / J->ppb;
 		double cost = (double)v->Q * ((v->n1 + J->tp - 1) / J->tp) * v->n2;
+		size_t i0 = items.n;
 		for (int g = 0; g < ngroup && !rc; g++) rc = add_item(&items, cost, nj, g, 0, 0);
+		job_cost(&items, i0);
 		nj++;
 	}
 	if (!rc) rc = st_launch(st, 3, 0, -1, jobs, sizeof(sxsk_fit_job) * nj, &items, 1);
@@ -467,7 +500,7 @@ static int launch_one(sxsg_batch *b, const blaunch *L, int *ctr, cudaStream_t s)
 {
 	char *base = b->d_buf;
 	const void *jobs = base + L->jobs_off, *items = base + L->items_off;
-	int *c = ctr + L->ctr;
+	int *c = ctr ? ctr + L->ctr : NULL;   /* NULL: one block per item */
 	switch (L->kind) {
 	case 0: return sxsk_rotate_batch(jobs, items, L->nitems, L->arg & 0xff, L->arg >> 8, c, s);
 	case 1: return sxsk_translate_batch(jobs, items, L->nitems, L->arg, c, s);
@@ -477,12 +510,19 @@ static int launch_one(sxsg_batch *b, const blaunch *L, int *ctr, cudaStream_t s)
 }
 
 /* The graph, captured from b->s: counters zeroed; the per-z tables on two
- * branches beside the rotation launches; per phase the translation launches
- * on parallel branches, joined before the per-pose launch; the fit. */
+ * branches beside the rotation launches; then the phases on two lanes:
+ * the translation launches of a phase on one stream per column class (the
+ * classes of a phase run side by side, each class's phases in order), the
+ * per-pose launch of a phase on the pose lane once its translations are
+ * done.  A phase's translations wait for the per-pose launch of the last
+ * phase that used the same arena half: with SXSG_BATCH_OVERLAP (two
+ * halves) the translations of phase k + 1 run beside the per-pose work of
+ * phase k.  The fit follows the last per-pose launch. */
 static int capture(sxsg_batch *b, const blaunch *ls, int nl, int *ctr)
 {
-	cudaStream_t s = b->s;
+	cudaStream_t s = b->s, ps = b->ps;
 	int rc = 0, nk = 0;
+	int *c = (b->flags & SXSG_BATCH_PERSISTENT) ? ctr : NULL;
 	SXS_CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
 	cudaError_t e = cudaMemsetAsync(ctr, 0, sizeof(int) * (size_t)(nl > 0 ? nl : 1), s);
 	if (!e) e = cudaEventRecordWithFlags(b->ev[0], s, cudaEventRecordExternal);
@@ -496,7 +536,7 @@ static int capture(sxsg_batch *b, const blaunch *ls, int nl, int *ctr)
 	}
 	int li = 0;
 	while (li < nl && ls[li].kind == 0 && !e && !rc) {
-		rc = launch_one(b, &ls[li], ctr, s);
+		rc = launch_one(b, &ls[li], c, s);
 		nk++;
 		li++;
 	}
@@ -506,30 +546,39 @@ static int capture(sxsg_batch *b, const blaunch *ls, int nl, int *ctr)
 	}
 	if (!e) e = cudaEventRecordWithFlags(b->ev[1], s, cudaEventRecordExternal);
 	/* phases */
+	if (!e) e = cudaEventRecord(b->fork, s);
+	for (int k = 0; k < SXSB_BR && !e; k++) e = cudaStreamWaitEvent(b->br[k], b->fork, 0);
+	if (!e) e = cudaStreamWaitEvent(ps, b->fork, 0);
+	int halves = (b->flags & SXSG_BATCH_OVERLAP) ? 2 : 1;
 	for (int ph = 0; ph < b->nphase && !e && !rc; ph++) {
-		int nb = 0;
-		if (!e) e = cudaEventRecord(b->fork, s);
+		int h = ph % halves;
 		while (li < nl && ls[li].kind == 1 && ls[li].phase == ph && !e && !rc) {
-			cudaStream_t bs = b->br[nb % SXSB_BR];
-			if (nb < SXSB_BR) e = cudaStreamWaitEvent(bs, b->fork, 0);
-			if (!e) rc = launch_one(b, &ls[li], ctr, bs);
+			int cls = ls[li].arg / 4 - 1;
+			cudaStream_t bs = b->br[cls];
+			if (ph >= halves) e = cudaStreamWaitEvent(bs, b->evpose[h], 0);
+			if (!e) rc = launch_one(b, &ls[li], c, bs);
+			if (!e && !rc) e = cudaEventRecord(b->join[cls], bs);
+			if (!e) e = cudaStreamWaitEvent(ps, b->join[cls], 0);
 			nk++;
-			nb++;
 			li++;
-		}
-		for (int k = 0; k < nb && k < SXSB_BR && !e; k++) {
-			e = cudaEventRecord(b->join[k], b->br[k]);
-			if (!e) e = cudaStreamWaitEvent(s, b->join[k], 0);
 		}
 		if (li < nl && ls[li].kind == 2 && ls[li].phase == ph && !e && !rc) {
-			rc = launch_one(b, &ls[li], ctr, s);
+			rc = launch_one(b, &ls[li], c, ps);
 			nk++;
 			li++;
 		}
+		if (!e && !rc) e = cudaEventRecord(b->evpose[h], ps);
 	}
+	/* every lane back into the origin stream */
+	for (int k = 0; k < SXSB_BR && !e; k++) {
+		e = cudaEventRecord(b->join[k], b->br[k]);
+		if (!e) e = cudaStreamWaitEvent(s, b->join[k], 0);
+	}
+	if (!e) e = cudaEventRecord(b->evpose[0], ps);
+	if (!e) e = cudaStreamWaitEvent(s, b->evpose[0], 0);
 	if (!e) e = cudaEventRecordWithFlags(b->ev[2], s, cudaEventRecordExternal);
 	if (li < nl && ls[li].kind == 3 && !e && !rc) {
-		rc = launch_one(b, &ls[li], ctr, s);
+		rc = launch_one(b, &ls[li], c, s);
 		nk++;
 		li++;
 	}
@@ -552,9 +601,12 @@ static int capture(sxsg_batch *b, const blaunch *ls, int nl, int *ctr)
 	return 0;
 }
 
-int sxsg_batch_create(sxsg_plan *const *plans, int nplan, int fit_mode, size_t arena_bytes, sxsg_batch **out)
+int sxsg_batch_create(sxsg_plan *const *plans, int nplan, int fit_mode, size_t arena_bytes, int flags,
+                      sxsg_batch **out)
 {
 	if (!plans || nplan <= 0 || !out) return sxs_fail(-2, "sxsg_batch_create: bad arguments");
+	if (flags & ~(SXSG_BATCH_PERSISTENT | SXSG_BATCH_OVERLAP))
+		return sxs_fail(-2, "sxsg_batch_create: unknown flags 0x%x", flags);
 	if (fit_mode != SXSG_FIT_GRID && fit_mode != SXSG_FIT_NONE)
 		return sxs_fail(-2, "sxsg_batch_create: fit mode must be SXSG_FIT_GRID or SXSG_FIT_NONE");
 	*out = NULL;
@@ -564,6 +616,7 @@ int sxsg_batch_create(sxsg_plan *const *plans, int nplan, int fit_mode, size_t a
 	if (!b) return sxs_fail(-5, "out of host memory");
 	b->n = nplan;
 	b->fit_mode = fit_mode;
+	b->flags = flags;
 	b->plans = malloc(sizeof(sxsg_plan *) * (size_t)nplan);
 	b->v = calloc((size_t)nplan, sizeof(sxs_plan_view));
 	if (!b->plans || !b->v) {
@@ -591,8 +644,16 @@ int sxsg_batch_create(sxsg_plan *const *plans, int nplan, int fit_mode, size_t a
 	}
 	cudaError_t e = cudaSuccess;
 	if (!rc) e = cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking);
+	if (!e && !rc) e = cudaStreamCreateWithFlags(&b->ps, cudaStreamNonBlocking);
+	for (int k = 0; k < 2 && !e && !rc; k++) e = cudaEventCreateWithFlags(&b->evpose[k], cudaEventDisableTiming);
+	int plo = 0, phi = 0;
+	if (!e && !rc) e = cudaDeviceGetStreamPriorityRange(&plo, &phi);
 	for (int k = 0; k < SXSB_BR && !e && !rc; k++) {
-		e = cudaStreamCreateWithFlags(&b->br[k], cudaStreamNonBlocking);
+		/* the per-z tables (branches 0 and 1: FP64 pipe) at the highest
+		 * priority: their blocks take SM slots as they free up beside the
+		 * rotation blocks (FP32 pipe) instead of waiting for the rotation
+		 * grids to be dispatched */
+		e = cudaStreamCreateWithPriority(&b->br[k], cudaStreamNonBlocking, k < 2 ? phi : plo);
 		if (!e) e = cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming);
 	}
 	if (!e && !rc) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);

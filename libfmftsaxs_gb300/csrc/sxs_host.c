@@ -56,6 +56,17 @@ static long long g_launches = 0;
 void sxs_count_launches(int n) { __atomic_add_fetch(&g_launches, n, __ATOMIC_RELAXED); }
 long long sxsg_launch_count(void) { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
 
+int sxsg_device_memory(size_t *free_bytes, size_t *total_bytes)
+{
+	int rc = sxs_ensure_init();
+	if (rc) return rc;
+	size_t f = 0, t = 0;
+	SXS_CU(cudaMemGetInfo(&f, &t));
+	if (free_bytes) *free_bytes = f;
+	if (total_bytes) *total_bytes = t;
+	return 0;
+}
+
 int sxsg_init(int device)
 {
 	pthread_mutex_lock(&g_init_lock);
@@ -453,6 +464,13 @@ int sxsg_plan_set_budget(sxsg_plan *p, size_t bytes)
 {
 	if (!p) return sxs_fail(-2, "sxsg_plan_set_budget: null plan");
 	p->r_budget = bytes;
+	size_t per_combo = (size_t)p->NP * 3 * SXS_QT * p->NT * p->celem;
+	if (p->d_R && (size_t)p->R_combos * per_combo > bytes) {
+		/* stream-ordered: runs already queued keep their buffer */
+		pfree(p, p->d_R);
+		p->d_R = NULL;
+		p->R_combos = 0;
+	}
 	return 0;
 }
 

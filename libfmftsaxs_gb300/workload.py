@@ -145,3 +145,95 @@ def triple_counts(index, L):
     key = (z * nb + b1) * nb + b2
     u, c = np.unique(key, return_counts=True)
     return u, c
+
+
+def batch_specs(n=64, seed=2026, min_poses=1000, max_poses=200000, pool=16):
+    """Sizes of the batched workload of many uneven dimers.  A pool of
+    `pool` receptors (atoms log-uniform in [500, 8000]) and `pool` ligands
+    (in [300, 5000]), Rg of a compact protein of na / 8 residues, is drawn
+    first; each dimer pairs one of each with L uniform in {10, 15, 20, 25,
+    30}, Q in {51, 101, 201} on [0, 0.5], a pose count log-uniform in
+    [min_poses, max_poses] with |t| in [25, 45] A, and the (c1, c2) of its
+    experiment uniform in [0.97, 1.03] x [0, 3].  Returns (dimers, receptor
+    pool, ligand pool); a pool entry is (atoms, Rg, seed)."""
+    rng = np.random.default_rng(seed)
+
+    def mol(lo, hi, k):
+        na = int(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        return (na, 2.2 * (na / 8.0) ** 0.38, seed + 7919 * (k + 1))
+    recs = [mol(500, 8000, k) for k in range(pool)]
+    ligs = [mol(300, 5000, pool + k) for k in range(pool)]
+    out = []
+    for i in range(n):
+        out.append(dict(rec=int(rng.integers(pool)), lig=int(rng.integers(pool)),
+                        L=int(rng.choice((10, 15, 20, 25, 30))), Q=int(rng.choice((51, 101, 201))), qmax=0.5,
+                        npose=int(np.exp(rng.uniform(np.log(min_poses), np.log(max_poses)))), t=(25.0, 45.0),
+                        c1=float(rng.uniform(0.97, 1.03)), c2=float(rng.uniform(0.0, 3.0)), seed=seed + 1000 * (i + 1)))
+    return out, recs, ligs
+
+
+def _pool_molecule(entry):
+    na, rg, seed = entry
+    m = synth.make_molecule(na, rg, seed)
+    return m.xyz, m.elements
+
+
+def pool_molecules(entries, workers=1):
+    """The molecules of pool entries (atoms, Rg, seed), built in `workers`
+    spawned processes (the random walks are the slow part)."""
+    if workers <= 1 or len(entries) <= 1:
+        res = [_pool_molecule(e) for e in entries]
+    else:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(min(workers, len(entries))) as pool:
+            res = pool.map(_pool_molecule, entries)
+    return [synth.Molecule(x, el) for x, el in res]
+
+
+def build_dimer(spec, rec, lig, lib=None):
+    """One dimer of batch_specs from its pool molecules: accessible
+    fractions and expansions on the GPU, the noisy profile of a seeded native
+    pose at the spec's (c1, c2), poses ingested on the GPU."""
+    if lib is None:
+        import importlib
+        lib = importlib.import_module(__package__)
+    cfg = dict(spec, lists=(spec["npose"],))
+    L, Q, seed = spec["L"], spec["Q"], spec["seed"]
+    w = Workload()
+    w.L, w.Q = L, Q
+    w.q = lib.mkarray(0.0, cfg["qmax"], Q)
+    rec = rec.translated(-rec.center_of_extrema())
+    lig = lig.translated(-lig.centroid())
+    rec.sasa = lib.sasa(rec.xyz, rec.radius)
+    lig.sasa = lib.sasa(lig.xyz, lig.radius)
+    water = lib.ff_water()
+    w.A = lib.expand(rec.xyz, *form_factors(lib, rec), rec.sasa, water, w.q, L)
+    w.B = lib.expand(lig.xyz, *form_factors(lib, lig), lig.sasa, water, w.q, L)
+    r = np.random.default_rng(seed + 7)
+    Rn = synth.random_rotations(1, r)[0]
+    Tn = synth.random_translations(1, cfg["t"][0], cfg["t"][1], r)[0]
+    native = synth.join(rec, synth.Molecule(lig.xyz @ Rn.T + Tn, lig.elements))
+    native = native.translated(-native.centroid())
+    native.sasa = lib.sasa(native.xyz, native.radius)
+    C = lib.expand(native.xyz, *form_factors(lib, native), native.sasa, water, w.q, L)
+    rm = float(np.mean(native.radius))
+    I, _ = lib.profile_from_spf(C, L, w.q, rm, spec["c1"], spec["c2"])
+    w.exp = synth.noisy_experiment(w.q, I, 0.01, r)
+    w.a, w.mult, w.peak = lib.bin_experiment(w.exp[0], w.exp[1], w.exp[2], w.q, rm)
+    w.z = zvals(cfg)
+    w.index = pose_lists(cfg, seed, lambda R, T, z, L: lib.poses_to_indices_gpu(R, T, z, L)[:2], w.z, L)
+    w.c1g, w.c2g = synth.C1_GRID, synth.C2_GRID
+    w.natoms = (rec.natoms, lig.natoms)
+    return w
+
+
+def plan_bytes(L, Q, npose, nz):
+    """Device bytes of a mixed-precision plan of this size with its pose list
+    set (rotation tables, per-z tables, outputs), for packing dimers into
+    device memory."""
+    K, N, NT = L + 1, 2 * L + 1, (Q + 7) // 8
+    NP = K * (K + 1) // 2
+    rot = 2 * NT * K * N * NP * 3 * 8 * 8
+    tau = NT * nz * K ** 3 * 8 * 12 + nz * Q * N * 8
+    out = npose * (6 * Q * 8 + 4 * 8 + 8 + 32 + 8)
+    return rot + tau + out + 64 * Q * K * K

@@ -1,7 +1,8 @@
-"""Batches of dimers (sxsg_batch_*): one CUDA graph of persistent kernels
-over many mixed-precision plans of different L, q grids and pose counts
-gives every plan bit for bit the results of its own sxsg_plan_run, with one
-phase or many (a small arena), on every replay, with or without the fit."""
+"""Batches of dimers (sxsg_batch_*): one CUDA graph over many
+mixed-precision plans of different L, q grids and pose counts gives every
+plan bit for bit the results of its own sxsg_plan_run, in every launch form
+(persistent or one block per item, one arena or two halves), with one phase
+or many (a small arena), on every replay, with or without the fit."""
 import numpy as np
 import pytest
 
@@ -54,8 +55,8 @@ def _alone(plans, fit, cross=True):
     return out
 
 
-def _batched(gpu, plans, fit, arena=0, reps=1, cross=True):
-    b = gpu.Batch(plans, fit=fit, arena_bytes=arena)
+def _batched(gpu, plans, fit, arena=0, reps=1, cross=True, flags=None):
+    b = gpu.Batch(plans, fit=fit, arena_bytes=arena, flags=flags)
     runs = []
     for _ in range(reps):
         b.run()
@@ -70,8 +71,9 @@ def _same(x, y):
         np.testing.assert_array_equal(x[k], y[k], err_msg=k)
 
 
-def test_batch_equals_plan_runs(gpu, plans):
-    runs, st = _batched(gpu, plans, gpu.FIT_GRID, reps=2)
+@pytest.mark.parametrize("flags", [0, 1, 2, 3])
+def test_batch_equals_plan_runs(gpu, plans, flags):
+    runs, st = _batched(gpu, plans, gpu.FIT_GRID, reps=2, flags=flags)
     alone = _alone(plans, gpu.FIT_GRID)
     assert st["plans"] == len(plans) and st["poses"] == sum(p.n for p in plans)
     assert st["total_ms"] > 0 and st["launches"] > 0
@@ -81,10 +83,12 @@ def test_batch_equals_plan_runs(gpu, plans):
     assert all(np.isfinite(a["chi"]).all() for a in alone)
 
 
-def test_batch_many_phases(gpu, plans):
-    # an arena of 64 MB holds a few slices of the largest tables: many chunks and phases
-    runs, st = _batched(gpu, plans, gpu.FIT_GRID, arena=64 << 20)
-    assert st["phases"] > 4 and st["arena_bytes"] <= 64 << 20
+@pytest.mark.parametrize("flags", [1, 3])
+def test_batch_many_phases(gpu, plans, flags):
+    # an arena of 96 MB holds a few slices of the largest tables (40 MB per
+    # slice at L = 30, Q = 201): many chunks and phases
+    runs, st = _batched(gpu, plans, gpu.FIT_GRID, arena=96 << 20, flags=flags)
+    assert st["phases"] > 4 and st["arena_bytes"] <= 96 << 20
     alone = _alone(plans, gpu.FIT_GRID)
     for a, b in zip(alone, runs[0]):
         _same(a, b)
