@@ -414,10 +414,15 @@ def run_batch(g, args):
     Times are host wall clock around synchronous calls; the graph's device
     time per stage comes from event nodes in the graph."""
     from libfmftsaxs_gb300 import workload as wl
-    specs, rpool, lpool = wl.batch_specs(args.batch_dimers, seed=args.seed + 3, max_poses=args.batch_max_poses)
+    specs, rpool, lpool = wl.batch_specs(args.batch_dimers * (1 if args.batch_lmax >= 30 else 4), seed=args.seed + 3,
+                                         max_poses=args.batch_max_poses)
+    specs = [sp for sp in specs if sp["L"] <= args.batch_lmax][:args.batch_dimers]   # profiling cases
     t0 = time.perf_counter()
-    recs = wl.pool_molecules(rpool, workers=min(16, os.cpu_count() or 1))
-    ligs = wl.pool_molecules(lpool, workers=min(16, os.cpu_count() or 1))
+    ur = sorted({sp["rec"] for sp in specs})
+    ul = sorted({sp["lig"] for sp in specs})
+    nw = min(16, os.cpu_count() or 1)
+    recs = dict(zip(ur, wl.pool_molecules([rpool[i] for i in ur], workers=nw)))
+    ligs = dict(zip(ul, wl.pool_molecules([lpool[i] for i in ul], workers=nw)))
     dims = [wl.build_dimer(sp, recs[sp["rec"]], ligs[sp["lig"]], g) for sp in specs]
     t_build = time.perf_counter() - t0
     poses = sum(len(d.index) for d in dims)
@@ -435,13 +440,6 @@ def run_batch(g, args):
         waves.append(cur)
     graph_s, plans_s, same = 0.0, 0.0, True
     forms, seq_stage = {}, np.zeros(4)
-    ref_chi = {}
-
-    def first_chi(plans, wv):
-        # chi of the first launch form run on this wave, the reference of the others
-        if wv[0] not in ref_chi:
-            ref_chi[wv[0]] = [p.results()["chi"] for p in plans]
-        return ref_chi[wv[0]]
     dev = np.zeros(3)
     phases = launches = items = 0
     create_s = 0.0
@@ -452,20 +450,6 @@ def run_batch(g, args):
             p = g.Plan(d.A, d.B, d.q, d.z, d.L, d.a, d.mult, d.peak, d.c1g, d.c2g, precision=g.MIXED)
             p.set_poses(d.index, skip=1)
             plans.append(p)
-        # the other launch forms, briefly (each checked bit for bit below)
-        for fl in (0, g.BATCH_PERSISTENT, g.BATCH_OVERLAP, g.BATCH_PERSISTENT | g.BATCH_OVERLAP):
-            if fl == g.BATCH_DEFAULT:
-                continue
-            bb = g.Batch(plans, fit=g.FIT_GRID, flags=fl)
-            bb.run()
-            t0 = time.perf_counter()
-            bb.run()
-            f = forms.setdefault(fl, np.zeros(4))
-            f[0] += time.perf_counter() - t0
-            sf = bb.stats()
-            f[1:] += (sf["tables_ms"], sf["phases_ms"], sf["fit_ms"])
-            bb.close()
-            same &= all(np.array_equal(p.results()["chi"], q) for p, q in zip(plans, first_chi(plans, wv)))
         t0 = time.perf_counter()
         b = g.Batch(plans, fit=g.FIT_GRID)
         create_s += time.perf_counter() - t0
@@ -486,6 +470,20 @@ def run_batch(g, args):
         got = [p.results() for p in plans]
         arena = st["arena_bytes"]
         b.close()
+        # the other launch forms, briefly (each checked bit for bit below)
+        for fl in (0, g.BATCH_PERSISTENT, g.BATCH_OVERLAP, g.BATCH_PERSISTENT | g.BATCH_OVERLAP):
+            if fl == g.BATCH_DEFAULT:
+                continue
+            bb = g.Batch(plans, fit=g.FIT_GRID, flags=fl)
+            bb.run()
+            t0 = time.perf_counter()
+            bb.run()
+            f = forms.setdefault(fl, np.zeros(4))
+            f[0] += time.perf_counter() - t0
+            sf = bb.stats()
+            f[1:] += (sf["tables_ms"], sf["phases_ms"], sf["fit_ms"])
+            bb.close()
+            same &= all(np.array_equal(p.results()["chi"], r["chi"]) for p, r in zip(plans, got))
 
         def seq():
             # each plan with the batch's arena as its translated-table bound,
@@ -538,8 +536,8 @@ def run_batch(g, args):
            "scenario": "%d dimers from pools of %d receptors (%d-%d atoms) and %d ligands (%d-%d atoms); L %s; "
                        "Q in {51, 101, 201}; %d-%d poses log-uniform (|t| in [25, 45] A), %d in all; grid fit 11x41; "
                        "steps: median of %d graph replays after %d"
-                       % (len(dims), len(rpool), min(r[0] for r in rpool), max(r[0] for r in rpool), len(lpool),
-                          min(r[0] for r in lpool), max(r[0] for r in lpool), json.dumps(hist),
+                       % (len(dims), len(ur), min(rpool[i][0] for i in ur), max(rpool[i][0] for i in ur), len(ul),
+                          min(lpool[i][0] for i in ul), max(lpool[i][0] for i in ul), json.dumps(hist),
                           min(len(d.index) for d in dims), max(len(d.index) for d in dims), poses, args.steps,
                           args.warmup)}
     return out
@@ -739,6 +737,7 @@ def main():
     ap.add_argument("--skip-batch-serve", action="store_true", help="batched dimers: no serving comparison")
     ap.add_argument("--batch-dimers", type=int, default=64)
     ap.add_argument("--batch-max-poses", type=int, default=200000)
+    ap.add_argument("--batch-lmax", type=int, default=30, help="batched dimers: only those with L up to this")
     args = ap.parse_args()
     if args.gpus > 1 and int(os.environ.get("RANK", "0")) != 0:
         return  # the path does not shard: one GPU runs, other ranks idle
