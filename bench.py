@@ -326,10 +326,13 @@ def expansion_timing(g, w, fp64_peak):
 def run_serving(g, args):
     """Serving scenario: Poisson arrivals of scoring requests (each one dimer
     with its own lmax, q grid, experiment and pose list) into the serving
-    loop; latency = submit to results on the host."""
+    loop; latency = submit to results on the host.  Requests draw their pose
+    lists as windows of one seeded list per L (generated once and ingested on
+    the GPU), so that long windows need no per-request pose generation; a
+    waiter thread collects results while requests keep arriving."""
+    import threading
     from libfmftsaxs_gb300 import synth, workload as wl
     rng = np.random.default_rng(args.seed + 77)
-    nreq = max(1, int(round(args.serve_rate * args.serve_window)))
     Ls, Qs = (10, 15, 20, 25, 30), (51, 101, 201)
     nrec, nlig = 4, 4
     def mol(lo, hi, seed):
@@ -350,8 +353,21 @@ def run_serving(g, args):
             expd[key] = g.expand(m.xyz, v, d, m.sasa, g.ff_water(), q, L)
         return expd[key]
 
-    reqs, used_rec = [], []
-    for k in range(nreq):
+    z = np.arange(25.0, 46.0)
+    pool_n = args.serve_max_poses
+    pools = {}
+    for L in Ls:
+        r = np.random.default_rng(args.seed + 500 + L)
+        idx = []
+        while sum(len(x) for x in idx) < pool_n:
+            m = min(1 << 20, 2 * pool_n)
+            R = synth.random_rotations(m, r)
+            T = synth.random_translations(m, 25.0, 45.0, r)
+            idx.append(g.poses_to_indices_gpu(R, T, z, L)[0])
+        pools[L] = np.concatenate(idx)[:pool_n]
+    profiles = {}
+
+    def request(k, used_rec):
         if used_rec and rng.random() < 0.3:
             ri, L, Q = used_rec[rng.integers(len(used_rec))]
         else:
@@ -360,43 +376,66 @@ def run_serving(g, args):
         li = int(rng.integers(nlig))
         q = g.mkarray(0.0, 0.5, Q)
         A, B = expansion("r", ri, L, Q), expansion("l", li, L, Q)
-        I, _ = g.profile_from_spf(A, L, q, 1.7, 1.0, 1.0)
-        exp = synth.noisy_experiment(q, I, 0.01, rng)
+        if (ri, L, Q) not in profiles:
+            profiles[(ri, L, Q)] = g.profile_from_spf(A, L, q, 1.7, 1.0, 1.0)[0]
+        exp = synth.noisy_experiment(q, profiles[(ri, L, Q)], 0.01, rng)
         a, mult, peak = g.bin_experiment(exp[0], exp[1], exp[2], q, 1.7)
         npose = int(np.exp(rng.uniform(np.log(args.serve_min_poses), np.log(args.serve_max_poses))))
-        z = np.arange(25.0, 46.0)
-        R = synth.random_rotations(npose, rng)
-        T = synth.random_translations(npose, 25.0, 45.0, rng)
-        idx, _ = g.poses_to_indices(R, T, z, L)
-        reqs.append(dict(A=A, B=B, qvals=q, zvals=z, L=L, a=a, mult=mult, peak=peak, index=idx,
-                         c1grid=synth.C1_GRID, c2grid=synth.C2_GRID, keyA=1000 * ri + 1, keyB=2000 * li + 2))
-    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, size=nreq))
+        off = int(rng.integers(0, pool_n - npose + 1))
+        return dict(A=A, B=B, qvals=q, zvals=z, L=L, a=a, mult=mult, peak=peak, index=pools[L][off:off + npose],
+                    c1grid=synth.C1_GRID, c2grid=synth.C2_GRID, keyA=1000 * ri + 1, keyB=2000 * li + 2)
+
     out = {}
     for prec, name in ((g.MIXED, "mixed"), (g.FP64, "fp64")):
         if name == "fp64" and not args.serve_fp64:
             continue
+        window = args.serve_window if name == "mixed" else (args.serve_fp64_window or args.serve_window)
+        nreq = max(1, int(round(args.serve_rate * window)))
+        arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, size=nreq))
+        used_rec = []
+        reqs = [request(k, used_rec) for k in range(nreq)]
         srv = g.Server(hbm_cap=int(args.serve_cap_gb * 2 ** 30), max_active=args.serve_active)
+        tickets, lat = [], []
+        cv = threading.Condition()
+
+        def waiter():
+            k = 0
+            while k < nreq:
+                with cv:
+                    while k >= len(tickets):
+                        cv.wait()
+                    t = tickets[k]
+                lat.append(srv.wait(t)["latency_ms"])
+                k += 1
+        th = threading.Thread(target=waiter)
+        th.start()
         t0 = time.perf_counter()
-        tickets = []
         for r, ta in zip(reqs, arrivals):
             dt = ta - (time.perf_counter() - t0)
             if dt > 0:
                 time.sleep(dt)
-            tickets.append(srv.submit(precision=prec, **r))
-        lat = np.array([srv.wait(t)["latency_ms"] for t in tickets])
+            t = srv.submit(precision=prec, **r)
+            with cv:
+                tickets.append(t)
+                cv.notify()
+        t_sub = time.perf_counter() - t0
+        th.join()
         wall = time.perf_counter() - t0
         st = srv.stats()
         srv.close()
+        lat = np.array(lat)
         poses = sum(len(r["index"]) for r in reqs)
-        out[name] = {"p50_ms": float(np.percentile(lat, 50)), "p95_ms": float(np.percentile(lat, 95)),
-                     "p99_ms": float(np.percentile(lat, 99)), "poses_per_s": poses / wall,
-                     "requests_per_s": nreq / wall, "cache_hits": st["cache_hits"],
-                     "cache_misses": st["cache_misses"]}
-    out["scenario"] = ("%d requests, Poisson arrivals at %.0f/s; each one dimer: receptor %d-%d atoms, ligand %d-%d "
+        out[name] = {"requests": nreq, "window_s": window, "p50_ms": float(np.percentile(lat, 50)),
+                     "p95_ms": float(np.percentile(lat, 95)), "p99_ms": float(np.percentile(lat, 99)),
+                     "max_ms": float(lat.max()), "poses": int(poses), "poses_per_s": poses / wall,
+                     "offered_poses_per_s": poses / t_sub, "requests_per_s": nreq / wall, "drain_s": wall - t_sub,
+                     "cache_hits": st["cache_hits"], "cache_misses": st["cache_misses"]}
+    out["scenario"] = ("Poisson arrivals at %.0f/s; each request one dimer: receptor %d-%d atoms, ligand %d-%d "
                        "(pools of %d and %d molecules, 30%% of requests reuse a served receptor), L in %s, Q in %s, "
-                       "%d-%d poses log-uniform, |t| in [25,45] A, grid fit 11x41; up to %d jobs on the device "
-                       "under a %.0f GB cap"
-                       % (nreq, args.serve_rate, min(r.natoms for r in recs), max(r.natoms for r in recs),
+                       "%d-%d poses log-uniform (windows of one seeded list per L), |t| in [25,45] A, grid fit "
+                       "11x41; up to %d jobs on the device under a %.0f GB cap; poses_per_s = all poses over "
+                       "first arrival to last result"
+                       % (args.serve_rate, min(r.natoms for r in recs), max(r.natoms for r in recs),
                           min(m.natoms for m in ligs), max(m.natoms for m in ligs), nrec, nlig, list(Ls), list(Qs),
                           args.serve_min_poses, args.serve_max_poses, args.serve_active, args.serve_cap_gb))
     return out
@@ -733,6 +772,8 @@ def main():
     ap.add_argument("--serve-active", type=int, default=4, help="serving: jobs on the device at once")
     ap.add_argument("--serve-cap-gb", type=float, default=150.0, help="serving: HBM cap")
     ap.add_argument("--serve-fp64", action="store_true", help="serving: also run the FP64 path")
+    ap.add_argument("--serve-fp64-window", type=float, default=0.0,
+                    help="serving: seconds of arrivals for the FP64 arm (0 = --serve-window)")
     ap.add_argument("--skip-batch", action="store_true", help="no batched-dimers scenario")
     ap.add_argument("--skip-batch-serve", action="store_true", help="batched dimers: no serving comparison")
     ap.add_argument("--batch-dimers", type=int, default=64)
