@@ -300,6 +300,18 @@ int sxsg_plan_set_rotation(sxsg_plan *plan, int engine);
  * them. */
 int sxsg_plan_set_tiles(sxsg_plan *plan, int tr_slices, int rot_gamma);
 int sxsg_tiles_default(int L, int Q, int *tr_slices, int *rot_gamma);
+/* Translation fused with the per-pose contraction (mixed precision,
+ * L <= 31): the translated rows of a chunk's combos are contracted with
+ * their poses' receptor rows as they are formed, never stored; per pose and
+ * m the six channel sums are kept and added over m.  It saves the round
+ * trip of the translated rows through device memory (2.5 MB per row at
+ * L = 30, Q = 201, for ~1-3 poses each in sparse lists) but gathers the
+ * receptor rows at the translation's low occupancy, and measured slower on
+ * GB300 at every density tried, so SXSG_FUSE_AUTO (default) keeps the
+ * stored rows; SXSG_FUSE_ON selects it.  Results differ from the stored-row
+ * path only by FP32 rounding (another summation order). */
+enum { SXSG_FUSE_AUTO = 0, SXSG_FUSE_ON = 1, SXSG_FUSE_OFF = 2 };
+int sxsg_plan_set_fused(sxsg_plan *plan, int mode);
 /* Run the GPU work for the current pose list (asynchronous until results). */
 int sxsg_plan_run(sxsg_plan *plan, int fit_mode);
 /* Copy results to the host.  Any pointer may be NULL.  chi/c1/c2/cell: [n];

@@ -17,6 +17,7 @@ FP64 = 0
 MIXED = 1
 ROT_CUDA, ROT_TC = 0, 1
 BATCH_PERSISTENT, BATCH_OVERLAP = 1, 2
+FUSE_AUTO, FUSE_ON, FUSE_OFF = 0, 1, 2
 BATCH_DEFAULT = BATCH_PERSISTENT
 
 _lib = None
@@ -187,6 +188,8 @@ class Plan:
         self.c1g = f64(c1grid if c1grid is not None else np.zeros(0))
         self.c2g = f64(c2grid if c2grid is not None else np.zeros(0))
         self.L, self.Q = L, len(self.q)
+        self.mult, self.peak = float(mult), float(peak)
+        self.index = np.zeros(0, dtype=np.int64)
         self.h = C.c_void_p()
         _check(lib.sxsg_plan_create(C.byref(self.h), self.A.ctypes.data, self.B.ctypes.data, self.q.ctypes.data,
                                     self.Q, self.z.ctypes.data, len(self.z), L, self.a.ctypes.data, mult, peak,
@@ -198,6 +201,7 @@ class Plan:
         idx = np.ascontiguousarray(index, dtype=np.int64)
         self.n = len(idx)
         _check(load().sxsg_plan_set_poses(self.h, idx.ctypes.data, self.n, int(skip)))
+        self.index = idx
 
     def set_rotation(self, engine):
         load().sxsg_plan_set_rotation.argtypes = [C.c_void_p, C.c_int]
@@ -207,6 +211,12 @@ class Plan:
         """Tile choices (sxsg_plan_set_tiles); 0 keeps the tuned default."""
         load().sxsg_plan_set_tiles.argtypes = [C.c_void_p, C.c_int, C.c_int]
         _check(load().sxsg_plan_set_tiles(self.h, int(tr_slices), int(rot_gamma)))
+
+    def set_fused(self, mode):
+        """Translation fused with the per-pose contraction (sxsg_plan_set_fused):
+        FUSE_AUTO, FUSE_ON or FUSE_OFF."""
+        load().sxsg_plan_set_fused.argtypes = [C.c_void_p, C.c_int]
+        _check(load().sxsg_plan_set_fused(self.h, int(mode)))
 
     def set_budget(self, nbytes):
         load().sxsg_plan_set_budget.argtypes = [C.c_void_p, C.c_size_t]

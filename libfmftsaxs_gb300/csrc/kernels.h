@@ -133,6 +133,20 @@ int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, con
  * fit that reads the terms touches the FP64 pipe. */
 int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, int ncombo, const void *P, const void *R,
                     const double2 *tw, const void *cst, int Q, int L, void *cross, int fp32, cudaStream_t s);
+/* The mixed path's translation fused with the per-pose contraction, for
+ * sparse pose lists (few poses per translated row): the translated rows of
+ * the chunk's combos are never stored; per pose and m the six channel sums
+ * go to part[pose - pose_base][m][6][NT 8] (sxsk_fused_part_floats floats
+ * per pose), and sxsk_fused_reduce adds them over m (ascending) into the
+ * double-float cross terms.  poses: the plan's sorted poses; cstart[c]: the
+ * first sorted pose of global combo c; L + 1 <= 32. */
+size_t sxsk_fused_part_floats(int L, int Q);
+int sxsk_translate_fused(const void *U, const void *tau, const int32_t *combo_zbg, const int32_t *slices, int nslice,
+                         int cbase, int nzt, int Q, int L, int sb, const sxsk_pose *poses, const int32_t *cstart,
+                         int pose_base, const void *P, const double2 *tw, float *part, cudaStream_t s);
+/* cross of the npose poses from `poses` (their part rows from 0) */
+int sxsk_fused_reduce(const sxsk_pose *poses, int npose, const float *part, int Q, int L, const void *cst,
+                      void *cross, cudaStream_t s);
 /* double -> double-float pairs {hi, lo} */
 int sxsk_to_df(const double *a, float2 *b, long n, cudaStream_t s);
 /* double-float pairs -> double (hi + lo), in place allowed */
@@ -221,6 +235,32 @@ typedef struct {
 } sxsk_pc_job;
 /* items {job, q tile, block of 32 poses, 0} */
 int sxsk_pose_cross_batch(const sxsk_pc_job *jobs, const int4 *items, int nitems, int *ctr, cudaStream_t s);
+
+typedef struct {
+	const void *U, *tau;              /* ligand rotation table, float tau of the job's z */
+	const int32_t *combo_zbg;         /* the chunk's combos (cbase = the first one's index) */
+	const int32_t *slices;            /* the chunk's slices */
+	const sxsk_pose *poses;           /* the plan's sorted poses */
+	const int32_t *cstart;            /* first sorted pose of each combo of the plan */
+	const void *P;                    /* receptor rotation table */
+	const double2 *tw;
+	float *part;                      /* the chunk's per-pose sums */
+	int nslice, cbase, L, nzt, sb, pose_base, Q, pad;
+} sxsk_tf_job;
+/* fused translation (sxsk_translate_fused) of many chunks: items {job, q
+ * tile, slice group, m} for the m of column class NB */
+int sxsk_translate_fused_batch(const sxsk_tf_job *jobs, const int4 *items, int nitems, int NB, int *ctr,
+                               cudaStream_t s);
+
+typedef struct {
+	const sxsk_pose *poses;           /* the chunk's poses */
+	const float *part;                /* their per-pose sums */
+	const void *cst;                  /* double-float self terms */
+	void *cross;                      /* double-float cross terms of the dimer */
+	int npose, Q, L, pad;
+} sxsk_fr_job;
+/* sxsk_fused_reduce of many chunks: items {job, block of 128 (pose, q), 0, 0} */
+int sxsk_fused_reduce_batch(const sxsk_fr_job *jobs, const int4 *items, int nitems, int *ctr, cudaStream_t s);
 
 typedef struct {
 	const float2 *cross;

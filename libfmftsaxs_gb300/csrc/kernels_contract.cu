@@ -665,6 +665,186 @@ __device__ __forceinline__ void tpipe_block(const float2 *__restrict__ U, const 
 	}
 }
 
+/* poses per pass of a thread of the fused kernel: the per-pose sums
+ * (6 floats each) share the registers with the U columns (6 NB floats) */
+#define TF_KMAX(NB) ((NB) <= 16 ? 4 : ((NB) <= 24 ? 2 : 1))
+/* resident blocks per SM the fused kernel is compiled for (registers of
+ * the per-pose sums beside the U columns, without spills) */
+#define TF_MINB(NB) ((NB) <= 12 ? 3 : ((NB) <= 20 ? 2 : 1))
+
+/* F += the six channel products of one pair: Re(P_a (w R_b)) summed over
+ * (a, b) and (b, a) as in k_pose_cross */
+__device__ __forceinline__ void fused_acc(float *F, const float2 *__restrict__ pp, float wx, float wy, const float2 *a)
+{
+	float2 p0 = pp[0], p1 = pp[SXS_QT], p2 = pp[2 * SXS_QT];
+	float2 s0, s1, s2;
+	s0.x = fmaf(wx, a[0].x, __fmul_rn(-wy, a[0].y)); s0.y = fmaf(wx, a[0].y, __fmul_rn(wy, a[0].x));
+	s1.x = fmaf(wx, a[1].x, __fmul_rn(-wy, a[1].y)); s1.y = fmaf(wx, a[1].y, __fmul_rn(wy, a[1].x));
+	s2.x = fmaf(wx, a[2].x, __fmul_rn(-wy, a[2].y)); s2.y = fmaf(wx, a[2].y, __fmul_rn(wy, a[2].x));
+	F[0] = __fadd_rn(F[0], fmaf(p0.x, s0.x, __fmul_rn(-p0.y, s0.y)));
+	F[1] = __fadd_rn(F[1], fmaf(-p1.y, s0.y, fmaf(p1.x, s0.x, fmaf(p0.x, s1.x, __fmul_rn(-p0.y, s1.y)))));
+	F[2] = __fadd_rn(F[2], fmaf(-p2.y, s0.y, fmaf(p2.x, s0.x, fmaf(p0.x, s2.x, __fmul_rn(-p0.y, s2.y)))));
+	F[3] = __fadd_rn(F[3], fmaf(p1.x, s1.x, __fmul_rn(-p1.y, s1.y)));
+	F[4] = __fadd_rn(F[4], fmaf(-p2.y, s1.y, fmaf(p2.x, s1.x, fmaf(p1.x, s2.x, __fmul_rn(-p1.y, s2.y)))));
+	F[5] = __fadd_rn(F[5], fmaf(p2.x, s2.x, __fmul_rn(-p2.y, s2.y)));
+}
+
+/* shared bytes of the fused kernel: those of k_translate_pipe<NB> plus the
+ * twiddles */
+#define TF_SMEM(NB) (TP_SMEM(NB) + sizeof(float2) * (2 * SXS_LMAX_K))
+
+/* One block of the fused translation for sparse pose lists: the block of
+ * k_translate_pipe (tile t, slice group gi, m), whose translated rows are
+ * contracted at once with the receptor rows of their combos' poses instead
+ * of being stored: thread (combo, q) computes the rows R[m, m + i], i < n,
+ * from its U columns in registers, up to TF_KMAX(NB) poses of the combo per
+ * pass (a combo with more poses recomputes its rows per pass), and writes
+ * per pose and m the six sums
+ *   part[pose - pose_base][m][ch][t 8 + q] = sum_i Re(P_a(b1, g1)[m, m + i] w_m R_b[m, m + i])
+ * (a, b as in k_pose_cross; w_m = tw[(m a2) mod N], doubled for m > 0).
+ * cstart[c] = the first sorted pose of global combo c (cstart[ncombo] = the
+ * pose count); raw = the block's TF_SMEM(NB) bytes. */
+template <int NB>
+__device__ __forceinline__ void tfused_block(const float2 *__restrict__ U, const float *__restrict__ tau,
+                                             const int32_t *__restrict__ combo_zbg,
+                                             const int32_t *__restrict__ slices, int nslice, int cbase, int L,
+                                             int nzt, int t, int gi, int m, int sb,
+                                             const sxsk_pose *__restrict__ poses, const int32_t *__restrict__ cstart,
+                                             int pose_base, const float2 *__restrict__ P,
+                                             const double2 *__restrict__ tw, float *__restrict__ part, int QP,
+                                             unsigned char *raw)
+{
+	constexpr int KMAX = TF_KMAX(NB);
+	const int qstride = NB * NB + 4, rowf = 3 * SXS_QT;
+	float *ts = reinterpret_cast<float *>(raw);
+	float2 *us = reinterpret_cast<float2 *>(raw + sizeof(float) * SXS_QT * qstride);
+	float2 *tws = reinterpret_cast<float2 *>(raw + TP_SMEM(NB));
+	int K = L + 1, N = 2 * L + 1, NP = K * (K + 1) / 2, nrow = K * N;
+	int n = K - m, po = psym(m, K);
+	int s0 = gi * sb, s1 = s0 + sb < nslice ? s0 + sb : nslice;
+	int q = threadIdx.x % SXS_QT, cl = threadIdx.x / SXS_QT;
+	for (int k = threadIdx.x; k < N; k += blockDim.x) tws[k] = from2<float2>(tw[k]);
+	const int per = n * rowf / 2;
+	auto issue = [&](int s) {
+		int cf = slices[2 * s] - cbase, nc = slices[2 * s + 1];
+		if (cl < nc) {
+			int cc = cf + cl;
+			int b2 = combo_zbg[3 * cc + 1], g2 = combo_zbg[3 * cc + 2];
+			const float2 *src = U + (((size_t)t * nrow + b2 * N + g2) * NP + po) * rowf;
+			float2 *dst = us + (size_t)cl * NB * rowf;
+			for (int r = q; r < per; r += SXS_QT) cp_async16(dst + 2 * r, src + 2 * r);
+		}
+		cp_async_commit();
+	};
+	int zcur = -1;
+	if (s0 < s1) issue(s0);
+	for (int s = s0; s < s1; s++) {
+		int cf = slices[2 * s] - cbase, nc = slices[2 * s + 1];
+		int zi = combo_zbg[3 * cf];
+		if (zi != zcur) {
+			__syncthreads();   /* no thread still reads the previous tau */
+			const float *tz = tau + ((((size_t)t * nzt + zi) * K + m) * K) * K * SXS_QT;
+			for (int k = threadIdx.x; k < SXS_QT * NB * NB; k += blockDim.x) {
+				int qq = k % SXS_QT, r = k / SXS_QT;
+				int i = r / NB, kk = r % NB;
+				float v = 0;
+				if (i < n && kk < n) v = tz[((size_t)(m + i) * K + m + kk) * SXS_QT + qq];
+				ts[qq * qstride + i * NB + kk] = v;
+			}
+			zcur = zi;
+		}
+		cp_async_wait_all();
+		__syncthreads();   /* this slice's U columns, tau and the twiddles visible to all */
+		bool act = cl < nc;
+		float2 u[3][NB];
+		if (act) {
+			const float2 *uc = us + (size_t)cl * NB * rowf + q;
+#pragma unroll
+			for (int j = 0; j < 3; j++)
+#pragma unroll
+				for (int k = 0; k < NB; k++) u[j][k] = k < n ? uc[k * rowf + j * SXS_QT] : zero2<float2>();
+		}
+		__syncthreads();   /* the buffer is free for the next slice */
+		if (s + 1 < s1) issue(s + 1);
+		if (act) {
+			int c = cbase + cf + cl;
+			const float *tq = ts + q * qstride;
+			int p1 = cstart[c + 1];
+			for (int pb = cstart[c]; pb < p1; pb += KMAX) {
+				const float2 *Pp[KMAX];
+				float wx[KMAX], wy[KMAX], F[KMAX][6];
+#pragma unroll
+				for (int kb = 0; kb < KMAX; kb++) {
+					int pi = pb + kb < p1 ? pb + kb : pb;   /* a spare slot repeats the first pose */
+					sxsk_pose ps = poses[pi];
+					Pp[kb] = P + (((size_t)t * nrow + ps.b1 * N + ps.g1) * NP + po) * rowf + q;
+					int e = (m * ps.a2) % N;
+					float2 w = tws[e];
+					float f = m > 0 ? 2.0f : 1.0f;
+					wx[kb] = f * w.x;
+					wy[kb] = f * w.y;
+#pragma unroll
+					for (int ch = 0; ch < 6; ch++) F[kb][ch] = 0.0f;
+				}
+				for (int i = 0; i < n; i += 2) {
+					float2 a[3];
+					tcol_row<0, 3, float, float2, NB>(tq + i * NB, u, a);
+#pragma unroll
+					for (int kb = 0; kb < KMAX; kb++) fused_acc(F[kb], Pp[kb] + (size_t)i * rowf, wx[kb], wy[kb], a);
+					if (i + 1 < n) {
+						tcol_row<1, 3, float, float2, NB>(tq + (i + 1) * NB, u, a);
+#pragma unroll
+						for (int kb = 0; kb < KMAX; kb++)
+							fused_acc(F[kb], Pp[kb] + (size_t)(i + 1) * rowf, wx[kb], wy[kb], a);
+					}
+				}
+#pragma unroll
+				for (int kb = 0; kb < KMAX; kb++) {
+					if (pb + kb < p1) {
+						float *o = part + (((size_t)(pb + kb - pose_base) * K + m) * 6) * QP + t * SXS_QT + q;
+#pragma unroll
+						for (int ch = 0; ch < 6; ch++) o[(size_t)ch * QP] = F[kb][ch];
+					}
+				}
+			}
+		}
+	}
+}
+
+template <int NB>
+__global__ void __launch_bounds__(TCOL_THREADS(3), TF_MINB(NB))
+k_translate_fused(const float2 *__restrict__ U, const float *__restrict__ tau, const int32_t *__restrict__ combo_zbg,
+                  const int32_t *__restrict__ slices, int nslice, int cbase, int L, int nzt, int m_lo, int nm, int sb,
+                  const sxsk_pose *__restrict__ poses, const int32_t *__restrict__ cstart, int pose_base,
+                  const float2 *__restrict__ P, const double2 *__restrict__ tw, float *__restrict__ part, int QP)
+{
+	extern __shared__ __align__(16) unsigned char tps_raw[];
+	int ng = (nslice + sb - 1) / sb;
+	int bid = blockIdx.x;
+	int mi = bid % nm;
+	bid /= nm;
+	int gi = bid % ng, t = bid / ng;
+	tfused_block<NB>(U, tau, combo_zbg, slices, nslice, cbase, L, nzt, t, gi, m_lo + mi, sb, poses, cstart, pose_base,
+	                 P, tw, part, QP, tps_raw);
+}
+
+/* fused translation blocks of many chunks */
+template <int NB>
+__global__ void __launch_bounds__(TCOL_THREADS(3), TF_MINB(NB))
+k_translate_fused_batch(const sxsk_tf_job *__restrict__ jobs, const int4 *__restrict__ items, int nitems, int *ctr)
+{
+	extern __shared__ __align__(16) unsigned char tps_raw[];
+	for (int k = 0;; k++) {
+		int it = next_item(ctr, k, nitems);
+		if (it >= nitems) break;
+		int4 w = items[it];
+		sxsk_tf_job j = jobs[w.x];
+		tfused_block<NB>((const float2 *)j.U, (const float *)j.tau, j.combo_zbg, j.slices, j.nslice, j.cbase, j.L,
+		                 j.nzt, w.y, w.z, w.w, j.sb, j.poses, j.cstart, j.pose_base, (const float2 *)j.P, j.tw, j.part,
+		                 ((j.Q + SXS_QT - 1) / SXS_QT) * SXS_QT, tps_raw);
+	}
+}
+
 template <int NB>
 __global__ void __launch_bounds__(TCOL_THREADS(3), TP_MINB(NB))
 k_translate_pipe(const float2 *__restrict__ U, const float *__restrict__ tau, const int32_t *__restrict__ combo_zbg,
@@ -717,6 +897,46 @@ __device__ __forceinline__ void cross_store(float2 *o, const float2 *cst, size_t
 	e = __fadd_rn(e, c.y);
 	float h = __fadd_rn(s, e);
 	o[i] = make_float2(h, __fsub_rn(e, __fsub_rn(h, s)));
+}
+
+/* cross[src][c][q] = cst[c][q] + 2 sum_m part[p][m][c][q] (m ascending, FP32)
+ * as double-float pairs; thread = (pose, q) */
+__device__ __forceinline__ void fused_reduce_at(const sxsk_pose *__restrict__ poses, int npose,
+                                                const float *__restrict__ part, int K, int Q, int QP,
+                                                const float2 *__restrict__ cst, float2 *__restrict__ cross, long i)
+{
+	if (i >= (long)npose * Q) return;
+	int p = (int)(i / Q), q = (int)(i % Q);
+	const float *src = part + (size_t)p * K * 6 * QP + q;
+	float2 *o = cross + (size_t)poses[p].src * 6 * Q;
+#pragma unroll
+	for (int c = 0; c < 6; c++) {
+		float f = 0.0f;
+		for (int m = 0; m < K; m++) f = __fadd_rn(f, src[((size_t)m * 6 + c) * QP]);
+		cross_store(o, cst, (size_t)c * Q + q, f);
+	}
+}
+
+__global__ void __launch_bounds__(128)
+k_fused_reduce(const sxsk_pose *__restrict__ poses, int npose, const float *__restrict__ part, int K, int Q, int QP,
+               const float2 *__restrict__ cst, float2 *__restrict__ cross)
+{
+	fused_reduce_at(poses, npose, part, K, Q, QP, cst, cross, (long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+/* the sums over m of many chunks: items {job, block of 128 (pose, q)} */
+__global__ void __launch_bounds__(128)
+k_fused_reduce_batch(const sxsk_fr_job *__restrict__ jobs, const int4 *__restrict__ items, int nitems, int *ctr)
+{
+	for (int k = 0;; k++) {
+		int it = next_item(ctr, k, nitems);
+		if (it >= nitems) break;
+		int4 w = items[it];
+		sxsk_fr_job j = jobs[w.x];
+		int QP = ((j.Q + SXS_QT - 1) / SXS_QT) * SXS_QT;
+		fused_reduce_at(j.poses, j.npose, j.part, j.L + 1, j.Q, QP, (const float2 *)j.cst, (float2 *)j.cross,
+		                (long)w.y * blockDim.x + threadIdx.x);
+	}
 }
 
 /* Per-pose cross terms of one chunk, all q tiles.  Thread = (pose, 2
@@ -1307,6 +1527,51 @@ static int translate_batch_launch(const sxsk_tr_job *jobs, const int4 *items, in
 	return cudaGetLastError();
 }
 
+template <int NB>
+static cudaError_t translate_fused_launch(const float2 *U, const float *tau, const int32_t *combo_zbg,
+                                          const int32_t *slices, int nslice, int cbase, int nzt, int NT, int L, int sb,
+                                          const sxsk_pose *poses, const int32_t *cstart, int pose_base,
+                                          const float2 *P, const double2 *tw, float *part, cudaStream_t s)
+{
+	int K = L + 1;
+	int m_hi = K - (NB - 3), m_lo = K - NB;
+	if (m_hi > L) m_hi = L;
+	if (m_lo < 0) m_lo = 0;
+	if (m_hi < m_lo) return cudaSuccess;
+	int nm = m_hi - m_lo + 1;
+	long nb = (long)NT * ((nslice + sb - 1) / sb) * nm;
+	if (nb > 0x7fffffffL) return cudaErrorInvalidValue;
+	size_t smem = TF_SMEM(NB);
+	auto kern = k_translate_fused<NB>;
+	cudaError_t e = cudaSuccess;
+	if (smem > 48 * 1024) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	if (!e)
+		e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+		                         (int)cudaSharedmemCarveoutMaxShared);
+	if (e) return e;
+	kern<<<(unsigned)nb, TCOL_THREADS(3), smem, s>>>(U, tau, combo_zbg, slices, nslice, cbase, L, nzt, m_lo, nm, sb,
+	                                                 poses, cstart, pose_base, P, tw, part, NT * SXS_QT);
+	return cudaGetLastError();
+}
+
+template <int NB>
+static int translate_fused_batch_launch(const sxsk_tf_job *jobs, const int4 *items, int nitems, int *ctr,
+                                        cudaStream_t s)
+{
+	size_t smem = TF_SMEM(NB);
+	auto kern = k_translate_fused_batch<NB>;
+	cudaError_t e = cudaSuccess;
+	if (smem > 48 * 1024) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	if (!e)
+		e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+		                         (int)cudaSharedmemCarveoutMaxShared);
+	int grid = 0;
+	if (!e) e = persistent_grid(kern, TCOL_THREADS(3), smem, nitems, ctr, &grid);
+	if (e) return e;
+	kern<<<grid, TCOL_THREADS(3), smem, s>>>(jobs, items, nitems, ctr);
+	return cudaGetLastError();
+}
+
 extern "C" {
 
 int sxsk_spf_transpose(const double *flat, void *spf_t, int Q, int L, int fp32, cudaStream_t s)
@@ -1381,6 +1646,41 @@ int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, con
 	return translate_slices(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, Q, L, R, fp32, s);
 }
 
+size_t sxsk_fused_part_floats(int L, int Q)
+{
+	return (size_t)(L + 1) * 6 * ((Q + SXS_QT - 1) / SXS_QT) * SXS_QT;
+}
+
+int sxsk_translate_fused(const void *U, const void *tau, const int32_t *combo_zbg, const int32_t *slices, int nslice,
+                         int cbase, int nzt, int Q, int L, int sb, const sxsk_pose *poses, const int32_t *cstart,
+                         int pose_base, const void *P, const double2 *tw, float *part, cudaStream_t s)
+{
+	if (nslice <= 0) return 0;
+	if (L + 1 > 32) return cudaErrorInvalidValue;
+	int NT = (Q + SXS_QT - 1) / SXS_QT;
+	if (sb < 1) sb = SXSK_TP_SB;
+	const float2 *u = (const float2 *)U, *p = (const float2 *)P;
+	const float *ta = (const float *)tau;
+	cudaError_t e = cudaSuccess;
+#define TFL(NB)                                                                                                     \
+	if (!e) e = translate_fused_launch<NB>(u, ta, combo_zbg, slices, nslice, cbase, nzt, NT, L, sb, poses, cstart, \
+	                                       pose_base, p, tw, part, s);
+	TFL(4) TFL(8) TFL(12) TFL(16) TFL(20) TFL(24) TFL(28) TFL(32)
+#undef TFL
+	return e;
+}
+
+int sxsk_fused_reduce(const sxsk_pose *poses, int npose, const float *part, int Q, int L, const void *cst,
+                      void *cross, cudaStream_t s)
+{
+	if (npose <= 0) return 0;
+	int QP = ((Q + SXS_QT - 1) / SXS_QT) * SXS_QT;
+	long n = (long)npose * Q;
+	k_fused_reduce<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(poses, npose, part, L + 1, Q, QP, (const float2 *)cst,
+	                                                            (float2 *)cross);
+	return cudaGetLastError();
+}
+
 int sxsk_pose_cross(const sxsk_pose *poses, int npose, int combo_base, int ncombo, const void *P, const void *R,
                     const double2 *tw, const void *cst, int Q, int L, void *cross, int fp32, cudaStream_t s)
 {
@@ -1412,6 +1712,33 @@ int sxsk_rotate_batch(const sxsk_rot_job *jobs, const int4 *items, int nitems, i
 	case 16: return rotate_batch_launch<16>(jobs, items, nitems, tw_max, ctr, s);
 	default: return cudaErrorInvalidValue;
 	}
+}
+
+int sxsk_translate_fused_batch(const sxsk_tf_job *jobs, const int4 *items, int nitems, int NB, int *ctr,
+                               cudaStream_t s)
+{
+	if (nitems <= 0) return 0;
+	switch (NB) {
+	case 4: return translate_fused_batch_launch<4>(jobs, items, nitems, ctr, s);
+	case 8: return translate_fused_batch_launch<8>(jobs, items, nitems, ctr, s);
+	case 12: return translate_fused_batch_launch<12>(jobs, items, nitems, ctr, s);
+	case 16: return translate_fused_batch_launch<16>(jobs, items, nitems, ctr, s);
+	case 20: return translate_fused_batch_launch<20>(jobs, items, nitems, ctr, s);
+	case 24: return translate_fused_batch_launch<24>(jobs, items, nitems, ctr, s);
+	case 28: return translate_fused_batch_launch<28>(jobs, items, nitems, ctr, s);
+	case 32: return translate_fused_batch_launch<32>(jobs, items, nitems, ctr, s);
+	default: return cudaErrorInvalidValue;
+	}
+}
+
+int sxsk_fused_reduce_batch(const sxsk_fr_job *jobs, const int4 *items, int nitems, int *ctr, cudaStream_t s)
+{
+	if (nitems <= 0) return 0;
+	int grid = 0;
+	cudaError_t e = persistent_grid(k_fused_reduce_batch, 128, 0, nitems, ctr, &grid);
+	if (e) return e;
+	k_fused_reduce_batch<<<grid, 128, 0, s>>>(jobs, items, nitems, ctr);
+	return cudaGetLastError();
 }
 
 int sxsk_translate_batch(const sxsk_tr_job *jobs, const int4 *items, int nitems, int NB, int *ctr, cudaStream_t s)

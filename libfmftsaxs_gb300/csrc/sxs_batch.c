@@ -51,7 +51,8 @@ typedef struct {
 } bpiece;
 
 typedef struct {
-	int kind;                /* 0 rotation, 1 translation, 2 per-pose, 3 fit */
+	int kind;                /* 0 rotation, 1 translation, 2 per-pose, 3 fit, 4 fused translation,
+	                          * 5 sums over m of the fused path */
 	int arg;                 /* G or NB */
 	int phase;
 	int nitems;
@@ -272,6 +273,35 @@ static int build_rotations(sxsg_batch *b, bstage *st)
 }
 
 /* chunks of every dimer's translated table, packed into phases */
+/* device bytes of a piece's slices [s0, s1): its translated rows, or on the
+ * fused path its poses' per-m sums */
+static size_t piece_bytes(const sxs_plan_view *v, int64_t s0, int64_t s1)
+{
+	int64_t c0 = v->h_slices[2 * s0], c1 = v->h_slices[2 * (s1 - 1)] + v->h_slices[2 * (s1 - 1) + 1];
+	if (v->fused) return al(sizeof(float) * sxsk_fused_part_floats(v->L, v->Q) * (size_t)(v->h_cstart[c1] - v->h_cstart[c0]));
+	return al(combo_bytes(v) * (size_t)(c1 - c0));
+}
+
+/* translation items of one job for column class NB: (job, t, slice group, m)
+ * in the single-dimer block order, costed by combos x n^2 */
+static int tr_items(bvec *items, int j, const sxs_plan_view *v, const int32_t *hs, int nslice, int sb, int NB)
+{
+	int K = v->L + 1, rc = 0;
+	int m_hi = K - (NB - 3), m_lo = K - NB;
+	if (m_hi > v->L) m_hi = v->L;
+	if (m_lo < 0) m_lo = 0;
+	int ng = (nslice + sb - 1) / sb;
+	size_t i0 = items->n;
+	for (int tt = 0; tt < v->NT && !rc; tt++)
+		for (int g = 0; g < ng && !rc; g++) {
+			int sa = g * sb, sz = sa + sb < nslice ? sa + sb : nslice;
+			double nc = (double)(hs[2 * (sz - 1)] + hs[2 * (sz - 1) + 1] - hs[2 * sa]);
+			for (int m = m_lo; m <= m_hi && !rc; m++) rc = add_item(items, nc * (K - m) * (K - m), j, tt, g, m);
+		}
+	job_cost(items, i0);
+	return rc;
+}
+
 static int build_phases(sxsg_batch *b, bstage *st, size_t arena_req)
 {
 	bvec pieces = {NULL, 0, 0, sizeof(bpiece)};
@@ -279,11 +309,12 @@ static int build_phases(sxsg_batch *b, bstage *st, size_t arena_req)
 	size_t total = 0, largest_slice = 0;
 	for (int i = 0; i < b->n; i++) {
 		const sxs_plan_view *v = &b->v[i];
-		if (v->nslice > 0) {
-			size_t sl = combo_bytes(v) * SXS_SLICE;
+		if (v->nslice <= 0) continue;
+		for (int64_t k = 0; k < v->nslice; k++) {
+			size_t sl = piece_bytes(v, k, k + 1);
 			if (sl > largest_slice) largest_slice = sl;
-			total += al(combo_bytes(v) * (size_t)v->ncombo);
 		}
+		total += piece_bytes(v, 0, v->nslice);
 	}
 	size_t fr = 0, tot = 0;
 	cudaMemGetInfo(&fr, &tot);
@@ -291,26 +322,18 @@ static int build_phases(sxsg_batch *b, bstage *st, size_t arena_req)
 	size_t arena = arena_req ? arena_req : fr / 2;
 	if (arena > total * halves) arena = total * halves;
 	arena = arena / halves & ~(size_t)(SXSB_ALIGN - 1);   /* one phase's share */
-	if (total > 0 && arena < al(largest_slice)) {
+	if (total > 0 && arena < largest_slice) {
 		if (arena_req) return sxs_fail(-2, "sxsg_batch_create: arena of %zu bytes below one slice (%zu)", arena_req,
-		                               al(largest_slice));
+		                               largest_slice);
 		return sxs_fail(-5, "sxsg_batch_create: free device memory below one slice of a translated table");
 	}
+	/* pieces: runs of whole slices that fit the arena share */
 	for (int i = 0; i < b->n && !rc; i++) {
 		const sxs_plan_view *v = &b->v[i];
-		if (v->nslice <= 0) continue;
-		size_t pc = combo_bytes(v);
-		int64_t chunk = (int64_t)(arena / (pc * SXS_SLICE));
-		if (chunk < 1) chunk = 1;
 		int64_t s0 = 0;
 		while (s0 < v->nslice && !rc) {
-			int64_t s1 = s0 + chunk < v->nslice ? s0 + chunk : v->nslice;
-			/* whole slices may overshoot by combos of a partial slice: shrink */
-			for (;;) {
-				int64_t c0 = v->h_slices[2 * s0], c1 = v->h_slices[2 * (s1 - 1)] + v->h_slices[2 * (s1 - 1) + 1];
-				if (al(pc * (size_t)(c1 - c0)) <= arena || s1 == s0 + 1) break;
-				s1--;
-			}
+			int64_t s1 = s0 + 1;
+			while (s1 < v->nslice && piece_bytes(v, s0, s1 + 1) <= arena) s1++;
 			bpiece *p = bv_push(&pieces);
 			if (!p) {
 				rc = sxs_fail(-5, "out of host memory");
@@ -321,7 +344,7 @@ static int build_phases(sxsg_batch *b, bstage *st, size_t arena_req)
 			p->s1 = s1;
 			p->c0 = v->h_slices[2 * s0];
 			p->c1 = v->h_slices[2 * (s1 - 1)] + v->h_slices[2 * (s1 - 1) + 1];
-			p->bytes = al(pc * (size_t)(p->c1 - p->c0));
+			p->bytes = piece_bytes(v, s0, s1);
 			p->phase = -1;
 			s0 = s1;
 		}
@@ -360,19 +383,56 @@ static int build_phases(sxsg_batch *b, bstage *st, size_t arena_req)
 			return sxs_cuda_fail(e, "sxsg_batch_create arena");
 		}
 	}
-	/* per phase: translation launches per column class, then one per-pose launch */
+	/* per phase: translation launches per column class (stored rows, fused),
+	 * then the per-pose launches (contraction of stored rows, sums over m) */
 	bvec items = {NULL, 0, 0, sizeof(bitem)};
-	sxsk_tr_job *tj = malloc(sizeof(sxsk_tr_job) * (np > 0 ? np : 1));
-	sxsk_pc_job *pj = malloc(sizeof(sxsk_pc_job) * (np > 0 ? np : 1));
-	int *jmap = malloc(sizeof(int) * (np > 0 ? np : 1));
-	if (!tj || !pj || !jmap) rc = sxs_fail(-5, "out of host memory");
+	size_t nn = np > 0 ? np : 1;
+	sxsk_tr_job *tj = malloc(sizeof(sxsk_tr_job) * nn);
+	sxsk_pc_job *pj = malloc(sizeof(sxsk_pc_job) * nn);
+	sxsk_tf_job *fj = malloc(sizeof(sxsk_tf_job) * nn);
+	sxsk_fr_job *rj = malloc(sizeof(sxsk_fr_job) * nn);
+	int *jmap = malloc(sizeof(int) * nn), *fmap = malloc(sizeof(int) * nn);
+	if (!tj || !pj || !fj || !rj || !jmap || !fmap) rc = sxs_fail(-5, "out of host memory");
 	for (int ph = 0; ph < nphase && !rc; ph++) {
-		int nj = 0;
+		int nj = 0, nf = 0;
 		for (size_t k = 0; k < np; k++) {
 			if (pc[k].phase != ph) continue;
 			const bpiece *p = &pc[k];
 			const sxs_plan_view *v = &b->v[p->plan];
 			void *R = (char *)b->d_arena + p->off;
+			int64_t p0 = v->h_cstart[p->c0], p1 = v->h_cstart[p->c1];
+			int sb = v->tr_slices >= 1 ? v->tr_slices : SXSK_TP_SB;
+			if (v->fused) {
+				sxsk_tf_job *t = &fj[nf];
+				memset(t, 0, sizeof(*t));
+				t->U = v->U;
+				t->tau = v->tauf;
+				t->combo_zbg = v->combo + 3 * p->c0;
+				t->slices = v->slices + 2 * p->s0;
+				t->poses = v->poses;
+				t->cstart = v->cstart;
+				t->P = v->P;
+				t->tw = v->tw;
+				t->part = R;
+				t->nslice = (int)(p->s1 - p->s0);
+				t->cbase = (int)p->c0;
+				t->L = v->L;
+				t->nzt = v->nzt;
+				t->sb = sb;
+				t->pose_base = (int)p0;
+				t->Q = v->Q;
+				sxsk_fr_job *r = &rj[nf];
+				memset(r, 0, sizeof(*r));
+				r->poses = v->poses + p0;
+				r->part = R;
+				r->cst = v->cst;
+				r->cross = v->cross;
+				r->npose = (int)(p1 - p0);
+				r->Q = v->Q;
+				r->L = v->L;
+				fmap[nf++] = (int)k;
+				continue;
+			}
 			sxsk_tr_job *t = &tj[nj];
 			memset(t, 0, sizeof(*t));
 			t->U = v->U;
@@ -385,10 +445,9 @@ static int build_phases(sxsg_batch *b, bstage *st, size_t arena_req)
 			t->ncombo = (int)(p->c1 - p->c0);
 			t->L = v->L;
 			t->nzt = v->nzt;
-			t->sb = v->tr_slices >= 1 ? v->tr_slices : SXSK_TP_SB;
+			t->sb = sb;
 			sxsk_pc_job *q = &pj[nj];
 			memset(q, 0, sizeof(*q));
-			int64_t p0 = v->h_cstart[p->c0], p1 = v->h_cstart[p->c1];
 			q->poses = v->poses + p0;
 			q->P = v->P;
 			q->R = R;
@@ -400,33 +459,21 @@ static int build_phases(sxsg_batch *b, bstage *st, size_t arena_req)
 			q->ncombo = (int)(p->c1 - p->c0);
 			q->Q = v->Q;
 			q->L = v->L;
-			jmap[nj] = (int)k;
-			nj++;
+			jmap[nj++] = (int)k;
 		}
 		for (int NB = 4; NB <= 32 && !rc; NB += 4) {
 			for (int j = 0; j < nj && !rc; j++) {
-				const sxsk_tr_job *t = &tj[j];
-				const sxs_plan_view *v = &b->v[pc[jmap[j]].plan];
-				int K = t->L + 1;
-				int m_hi = K - (NB - 3), m_lo = K - NB;
-				if (m_hi > t->L) m_hi = t->L;
-				if (m_lo < 0) m_lo = 0;
-				int ng = (t->nslice + t->sb - 1) / t->sb;
-				const int32_t *hs = v->h_slices + 2 * pc[jmap[j]].s0;
-				size_t i0 = items.n;
-				for (int tt = 0; tt < v->NT && !rc; tt++)
-					for (int g = 0; g < ng && !rc; g++) {
-						/* combos of the slice group x n^2 multiply-adds each */
-						int sa = g * t->sb, sz = sa + t->sb < t->nslice ? sa + t->sb : t->nslice;
-						double nc = (double)(hs[2 * (sz - 1)] + hs[2 * (sz - 1) + 1] - hs[2 * sa]);
-						for (int m = m_lo; m <= m_hi && !rc; m++) {
-							int n = K - m;
-							rc = add_item(&items, nc * n * n, j, tt, g, m);
-						}
-					}
-				job_cost(&items, i0);
+				const bpiece *p = &pc[jmap[j]];
+				const sxs_plan_view *v = &b->v[p->plan];
+				rc = tr_items(&items, j, v, v->h_slices + 2 * p->s0, tj[j].nslice, tj[j].sb, NB);
 			}
 			if (!rc) rc = st_launch(st, 1, NB, ph, tj, sizeof(sxsk_tr_job) * nj, &items, 0);
+			for (int j = 0; j < nf && !rc; j++) {
+				const bpiece *p = &pc[fmap[j]];
+				const sxs_plan_view *v = &b->v[p->plan];
+				rc = tr_items(&items, j, v, v->h_slices + 2 * p->s0, fj[j].nslice, fj[j].sb, NB);
+			}
+			if (!rc) rc = st_launch(st, 4, NB, ph, fj, sizeof(sxsk_tf_job) * nf, &items, 0);
 		}
 		for (int j = 0; j < nj && !rc; j++) {
 			const sxsk_pc_job *q = &pj[j];
@@ -438,11 +485,21 @@ static int build_phases(sxsg_batch *b, bstage *st, size_t arena_req)
 			job_cost(&items, i0);
 		}
 		if (!rc) rc = st_launch(st, 2, 0, ph, pj, sizeof(sxsk_pc_job) * nj, &items, 0);
+		for (int j = 0; j < nf && !rc; j++) {
+			long nblk = ((long)rj[j].npose * rj[j].Q + 127) / 128;
+			size_t i0 = items.n;
+			for (long k = 0; k < nblk && !rc; k++) rc = add_item(&items, (double)(rj[j].L + 1), j, (int)k, 0, 0);
+			job_cost(&items, i0);
+		}
+		if (!rc) rc = st_launch(st, 5, 0, ph, rj, sizeof(sxsk_fr_job) * nf, &items, 0);
 	}
 	free(items.p);
 	free(tj);
 	free(pj);
+	free(fj);
+	free(rj);
 	free(jmap);
+	free(fmap);
 	free(pieces.p);
 	return rc;
 }
@@ -505,6 +562,8 @@ static int launch_one(sxsg_batch *b, const blaunch *L, int *ctr, cudaStream_t s)
 	case 0: return sxsk_rotate_batch(jobs, items, L->nitems, L->arg & 0xff, L->arg >> 8, c, s);
 	case 1: return sxsk_translate_batch(jobs, items, L->nitems, L->arg, c, s);
 	case 2: return sxsk_pose_cross_batch(jobs, items, L->nitems, c, s);
+	case 4: return sxsk_translate_fused_batch(jobs, items, L->nitems, L->arg, c, s);
+	case 5: return sxsk_fused_reduce_batch(jobs, items, L->nitems, c, s);
 	default: return sxsk_fit_grid_df_batch(jobs, items, L->nitems, b->fit_smem, c, s);
 	}
 }
@@ -552,7 +611,7 @@ static int capture(sxsg_batch *b, const blaunch *ls, int nl, int *ctr)
 	int halves = (b->flags & SXSG_BATCH_OVERLAP) ? 2 : 1;
 	for (int ph = 0; ph < b->nphase && !e && !rc; ph++) {
 		int h = ph % halves;
-		while (li < nl && ls[li].kind == 1 && ls[li].phase == ph && !e && !rc) {
+		while (li < nl && (ls[li].kind == 1 || ls[li].kind == 4) && ls[li].phase == ph && !e && !rc) {
 			int cls = ls[li].arg / 4 - 1;
 			cudaStream_t bs = b->br[cls];
 			if (ph >= halves) e = cudaStreamWaitEvent(bs, b->evpose[h], 0);
@@ -562,7 +621,7 @@ static int capture(sxsg_batch *b, const blaunch *ls, int nl, int *ctr)
 			nk++;
 			li++;
 		}
-		if (li < nl && ls[li].kind == 2 && ls[li].phase == ph && !e && !rc) {
+		while (li < nl && (ls[li].kind == 2 || ls[li].kind == 5) && ls[li].phase == ph && !e && !rc) {
 			rc = launch_one(b, &ls[li], c, ps);
 			nk++;
 			li++;

@@ -213,7 +213,13 @@ struct sxsg_plan {
 	int P_valid, U_valid;       /* caller tables already hold this run's rows */
 	int tw_variant; /* -1 none, 0 simple_ft, 1 exact */
 	double *h_tw;               /* host copy of the twiddles (lives with the plan) */
-	int64_t run_chunk, run_nch; /* slices per chunk and chunks of the prepared run */
+	int64_t run_nch;            /* chunks of the prepared run */
+	int64_t *h_chunk;           /* [run_nch + 1] first slice of each chunk */
+	int fuse_mode;              /* SXSG_FUSE_*: translation fused with the per-pose contraction */
+	int run_fused;              /* the prepared run uses the fused path */
+	int32_t *d_cstart;          /* [ncombo + 1] first sorted pose of each combo (fused path) */
+	float *d_part;              /* per-pose, per-m sums of the fused path */
+	size_t part_cap;            /* floats in d_part */
 	/* poses */
 	int64_t npose;
 	int skip;
@@ -264,7 +270,8 @@ static void plan_free_poses(sxsg_plan *p)
 	pfree(p, p->d_slices);
 	p->h_slices = NULL; p->d_slices = NULL; p->nslice = 0;
 	pfree(p, p->d_poses); pfree(p, p->d_combo); pfree(p, p->d_zt); pfree(p, p->d_bes); pfree(p, p->d_tau);
-	pfree(p, p->d_tauf);
+	pfree(p, p->d_tauf); pfree(p, p->d_cstart);
+	p->d_cstart = NULL;
 	p->h_combo = NULL; p->h_cstart = NULL; p->h_zt = NULL;
 	p->d_poses = NULL; p->d_combo = NULL; p->d_zt = NULL; p->d_bes = NULL; p->d_tau = NULL; p->d_tauf = NULL;
 }
@@ -277,7 +284,7 @@ void sxsg_plan_destroy(sxsg_plan *p)
 	plan_free_poses(p);
 	pfree(p, p->d_A); pfree(p, p->d_B); pfree(p, p->d_q); pfree(p, p->d_fc); pfree(p, p->d_a); pfree(p, p->d_gtab); pfree(p, p->d_gdf);
 	pfree(p, p->d_c1g); pfree(p, p->d_c2g); pfree(p, p->d_cst); pfree(p, p->d_cstf); pfree(p, p->d_At); pfree(p, p->d_Bt);
-	pfree(p, p->d_tw); pfree(p, p->d_R); pfree(p, p->d_amat); pfree(p, p->d_tcstat);
+	pfree(p, p->d_tw); pfree(p, p->d_R); pfree(p, p->d_amat); pfree(p, p->d_tcstat); pfree(p, p->d_part);
 	if (!p->ext_tables) {
 		pfree(p, p->d_P);
 		pfree(p, p->d_U);
@@ -290,6 +297,7 @@ void sxsg_plan_destroy(sxsg_plan *p)
 	free(p->cev);
 	free(p->h_z);
 	free(p->h_tw);
+	free(p->h_chunk);
 	free(p);
 }
 
@@ -616,6 +624,16 @@ int sxsg_plan_set_poses(sxsg_plan *p, const int64_t *index, int64_t n, int skip)
 	if (!e && p->nslice > 0)
 		e = cudaMemcpyAsync(p->d_slices, p->h_slices, sizeof(int32_t) * 2 * p->nslice, cudaMemcpyHostToDevice, p->s);
 	if (!e && nzt > 0) e = cudaMemcpyAsync(p->d_zt, p->h_zt, sizeof(double) * nzt, cudaMemcpyHostToDevice, p->s);
+	if (!e) {
+		/* combo starts for the fused path (pose counts fit int32) */
+		int32_t *cs = malloc(sizeof(int32_t) * (ncombo + 1));
+		if (!cs) return sxs_fail(-5, "out of host memory");
+		for (int k = 0; k <= ncombo; k++) cs[k] = (int32_t)p->h_cstart[k];
+		e = cudaMallocAsync((void **)&p->d_cstart, sizeof(int32_t) * (ncombo + 1), p->s);
+		if (!e) e = cudaMemcpyAsync(p->d_cstart, cs, sizeof(int32_t) * (ncombo + 1), cudaMemcpyHostToDevice, p->s);
+		if (!e) e = cudaStreamSynchronize(p->s);
+		free(cs);
+	}
 	if (e) return sxs_cuda_fail(e, "sxsg_plan_set_poses upload");
 	size_t need = (size_t)nn;
 	if ((rc = grow(p, (void **)&p->d_cross, &p->out_cap, need * 6 * p->Q, sizeof(double)))) return rc;
@@ -727,6 +745,25 @@ static int plan_events(sxsg_plan *p, int need)
 	return 0;
 }
 
+/* SXSG_FUSE_AUTO keeps the stored rows: on GB300 the fused form measured
+ * slower at every density tried (1.1-12 poses per translated row, L 10-30):
+ * its receptor-row gathers run at the translation's occupancy (1-2 blocks of
+ * 4 warps per SM), where the per-pose kernel streams them at 6 blocks */
+int sxs_plan_uses_fused(const sxsg_plan *p)
+{
+	return p->fp32 && p->L + 1 <= 32 && p->ncombo > 0 && p->fuse_mode == SXSG_FUSE_ON;
+}
+
+int sxsg_plan_set_fused(sxsg_plan *p, int mode)
+{
+	if (!p) return sxs_fail(-2, "sxsg_plan_set_fused: null plan");
+	if (mode < SXSG_FUSE_AUTO || mode > SXSG_FUSE_OFF) return sxs_fail(-2, "sxsg_plan_set_fused: unknown mode %d", mode);
+	if (mode == SXSG_FUSE_ON && (!p->fp32 || p->L + 1 > 32))
+		return sxs_fail(-2, "sxsg_plan_set_fused: the fused path needs a mixed-precision plan with L <= 31");
+	p->fuse_mode = mode;
+	return 0;
+}
+
 int sxs_plan_batch_view(sxsg_plan *p, sxs_plan_view *v)
 {
 	int variant = p->skip == 1 ? 0 : 1;
@@ -744,6 +781,7 @@ int sxs_plan_batch_view(sxsg_plan *p, sxs_plan_view *v)
 	v->L = p->L; v->Q = p->Q; v->NT = p->NT; v->NP = p->NP; v->n1 = p->n1; v->n2 = p->n2; v->fp32 = p->fp32;
 	v->ext_tables = p->ext_tables; v->nzt = p->nzt; v->ncombo = p->ncombo; v->nslice = p->nslice;
 	v->tr_slices = p->tr_slices; v->rot_gamma = p->rot_gamma; v->npose = p->npose;
+	v->fused = sxs_plan_uses_fused(p); v->cstart = p->d_cstart;
 	v->At = p->d_At; v->Bt = p->d_Bt; v->dtabf = p->lt->d_dtabf; v->tw = p->d_tw; v->P = p->d_P; v->U = p->d_U;
 	v->tauf = p->d_tauf; v->combo = p->d_combo; v->slices = p->d_slices; v->h_slices = p->h_slices;
 	v->h_cstart = p->h_cstart; v->poses = p->d_poses; v->cst = p->d_cstf; v->cross = p->d_cross;
@@ -791,25 +829,53 @@ int sxs_plan_prepare(sxsg_plan *p, int fit_mode)
 	if (tc && !p->d_amat)
 		SXS_CU(cudaMallocAsync((void **)&p->d_amat, sizeof(float) * sxsk_rotate_tc_scratch(p->L), s));
 	if (tc && !p->d_tcstat) SXS_CU(cudaMallocAsync((void **)&p->d_tcstat, sizeof(int), s));
-	/* translated table in chunks of whole slices that fit the budget */
-	size_t per_combo = (size_t)p->NP * 3 * SXS_QT * p->NT * p->celem;
-	int64_t chunk = (int64_t)(p->r_budget / (per_combo * SXS_SLICE));   /* slices per chunk */
-	if (chunk < 1) chunk = 1;
-	if (chunk > p->nslice) chunk = p->nslice;
-	int64_t nch = chunk > 0 ? (p->nslice + chunk - 1) / chunk : 0;
+	p->run_fused = sxs_plan_uses_fused(p);
+	free(p->h_chunk);
+	p->h_chunk = malloc(sizeof(int64_t) * (size_t)(p->nslice + 1));
+	if (!p->h_chunk) return sxs_fail(-5, "out of host memory");
+	int64_t nch = 0;
+	if (p->run_fused) {
+		/* chunks of whole slices whose poses' sums fit the budget */
+		size_t per_pose = sizeof(float) * sxsk_fused_part_floats(p->L, p->Q);
+		int64_t cap = (int64_t)(p->r_budget / per_pose), most = 0;
+		int64_t s0 = 0;
+		while (s0 < p->nslice) {
+			int64_t s1 = s0 + 1;
+			int64_t base = p->h_cstart[p->h_slices[2 * s0]];
+			while (s1 < p->nslice && p->h_cstart[p->h_slices[2 * s1] + p->h_slices[2 * s1 + 1]] - base <= cap) s1++;
+			int64_t np = p->h_cstart[p->h_slices[2 * (s1 - 1)] + p->h_slices[2 * (s1 - 1) + 1]] - base;
+			if (np > most) most = np;
+			p->h_chunk[nch++] = s0;
+			s0 = s1;
+		}
+		size_t need = (size_t)most * sxsk_fused_part_floats(p->L, p->Q);
+		if (need > p->part_cap) {
+			pfree(p, p->d_part);
+			p->d_part = NULL;
+			SXS_CU(cudaMallocAsync((void **)&p->d_part, sizeof(float) * need, s));
+			p->part_cap = need;
+		}
+	} else {
+		/* translated table in chunks of whole slices that fit the budget */
+		size_t per_combo = (size_t)p->NP * 3 * SXS_QT * p->NT * p->celem;
+		int64_t chunk = (int64_t)(p->r_budget / (per_combo * SXS_SLICE));   /* slices per chunk */
+		if (chunk < 1) chunk = 1;
+		if (chunk > p->nslice) chunk = p->nslice;
+		for (int64_t s0 = 0; s0 < p->nslice; s0 += chunk) p->h_chunk[nch++] = s0;
+		int64_t rcap = chunk * SXS_SLICE;
+		if (rcap > p->ncombo) rcap = p->ncombo;
+		if (rcap > 0 && p->R_combos < rcap) {
+			pfree(p, p->d_R);
+			p->d_R = NULL;
+			SXS_CU(cudaMallocAsync(&p->d_R, per_combo * rcap, s));
+			p->R_combos = rcap;
+		}
+	}
+	p->h_chunk[nch] = p->nslice;
 	if (nch > INT32_MAX / 3) return sxs_fail(-2, "sxsg_plan_run: too many chunks");
 	if ((rc = plan_events(p, (int)(3 * nch)))) return rc;
-	int64_t rcap = chunk * SXS_SLICE;
-	if (rcap > p->ncombo) rcap = p->ncombo;
-	if (rcap > 0 && p->R_combos < rcap) {
-		pfree(p, p->d_R);
-		p->d_R = NULL;
-		SXS_CU(cudaMallocAsync(&p->d_R, per_combo * rcap, s));
-		p->R_combos = rcap;
-	}
 	if (fit_mode == SXSG_FIT_LBFGSB && !p->d_scaled && p->npose > 0)
 		SXS_CU(cudaMallocAsync((void **)&p->d_scaled, sizeof(double) * (size_t)p->npose * 6 * p->Q, s));
-	p->run_chunk = chunk;
 	p->run_nch = nch;
 	p->last_chunks = (int)(nch < INT32_MAX ? nch : INT32_MAX);
 	return 0;
@@ -824,23 +890,32 @@ int sxs_plan_enqueue(sxsg_plan *p, int fit_mode, int timed)
 	int rc;
 	cudaStream_t s = p->s;
 	int Q = p->Q, L = p->L;
-	int64_t chunk = p->run_chunk, nch = p->run_nch;
+	int64_t nch = p->run_nch;
 	if (timed) SXS_CU(cudaEventRecord(p->ev[0], s));
 	if ((rc = plan_tables(p))) return rc;
 	if (timed) SXS_CU(cudaEventRecord(p->ev[1], s));
 	const void *tau = p->fp32 ? (const void *)p->d_tauf : (const void *)p->d_tau;
 	for (int64_t k = 0; k < nch; k++) {
-		int64_t s0 = k * chunk, s1 = s0 + chunk < p->nslice ? s0 + chunk : p->nslice;
+		int64_t s0 = p->h_chunk[k], s1 = p->h_chunk[k + 1];
 		int64_t c0 = p->h_slices[2 * s0], c1 = p->h_slices[2 * (s1 - 1)] + p->h_slices[2 * (s1 - 1) + 1];
+		int64_t p0 = p->h_cstart[c0], p1 = p->h_cstart[c1];
 		cudaEvent_t *e = p->cev + 3 * k;
 		if (timed) SXS_CU(cudaEventRecord(e[0], s));
-		SXS_K(sxsk_translate(p->d_U, tau, p->d_combo + 3 * c0, p->d_slices + 2 * s0, (int)(s1 - s0), (int)c0,
-		                     (int)(c1 - c0), p->nzt, Q, L, p->d_R, p->fp32, p->tr_slices, s));
-		if (timed) SXS_CU(cudaEventRecord(e[1], s));
-		int64_t p0 = p->h_cstart[c0], p1 = p->h_cstart[c1];
-		SXS_K(sxsk_pose_cross(p->d_poses + p0, (int)(p1 - p0), (int)c0, (int)(c1 - c0), p->d_P, p->d_R, p->d_tw,
-		                      p->fp32 ? (const void *)p->d_cstf : (const void *)p->d_cst, Q, L,
-		                      p->d_cross, p->fp32, s));
+		if (p->run_fused) {
+			/* translation and per-pose sums in one pass, then the sum over m */
+			SXS_K(sxsk_translate_fused(p->d_U, tau, p->d_combo + 3 * c0, p->d_slices + 2 * s0, (int)(s1 - s0),
+			                           (int)c0, p->nzt, Q, L, p->tr_slices, p->d_poses, p->d_cstart, (int)p0, p->d_P,
+			                           p->d_tw, p->d_part, s));
+			if (timed) SXS_CU(cudaEventRecord(e[1], s));
+			SXS_K(sxsk_fused_reduce(p->d_poses + p0, (int)(p1 - p0), p->d_part, Q, L, p->d_cstf, p->d_cross, s));
+		} else {
+			SXS_K(sxsk_translate(p->d_U, tau, p->d_combo + 3 * c0, p->d_slices + 2 * s0, (int)(s1 - s0), (int)c0,
+			                     (int)(c1 - c0), p->nzt, Q, L, p->d_R, p->fp32, p->tr_slices, s));
+			if (timed) SXS_CU(cudaEventRecord(e[1], s));
+			SXS_K(sxsk_pose_cross(p->d_poses + p0, (int)(p1 - p0), (int)c0, (int)(c1 - c0), p->d_P, p->d_R, p->d_tw,
+			                      p->fp32 ? (const void *)p->d_cstf : (const void *)p->d_cst, Q, L,
+			                      p->d_cross, p->fp32, s));
+		}
 		if (timed) SXS_CU(cudaEventRecord(e[2], s));
 		sxs_count_launches(sxsk_translate_launches(L) + 1);
 	}

@@ -79,6 +79,8 @@ size_t sxs_plan_combo_bytes(int L, int Q, int precision);
  * device tables its kernels use and its outputs. */
 typedef struct {
 	int L, Q, NT, NP, n1, n2, fp32, ext_tables, nzt, ncombo, nslice, tr_slices, rot_gamma;
+	int fused;                      /* the plan's runs fuse translation and per-pose contraction */
+	const int32_t *cstart;          /* device first sorted pose of each combo */
 	int64_t npose;
 	const void *At, *Bt;            /* transposed coefficients */
 	const float *dtabf;             /* float Wigner-d table of L */
@@ -97,6 +99,9 @@ typedef struct {
 	double *chi, *c1, *c2;
 	int32_t *cell;
 } sxs_plan_view;
+/* the next run of the plan fuses the translation with the per-pose
+ * contraction (mode and pose density) */
+int sxs_plan_uses_fused(const sxsg_plan *p);
 /* fills v after uploading the twiddles of the plan's pose list (waits for
  * the plan's stream) */
 int sxs_plan_batch_view(sxsg_plan *p, sxs_plan_view *v);

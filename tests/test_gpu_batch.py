@@ -1,6 +1,8 @@
 """Batches of dimers (sxsg_batch_*): one CUDA graph over many
-mixed-precision plans of different L, q grids and pose counts gives every
-plan bit for bit the results of its own sxsg_plan_run, in every launch form
+mixed-precision plans of different L, q grids and pose counts (sparse and
+dense lists; stored translated rows, and the fused translation on every
+third plan) gives every plan bit
+for bit the results of its own sxsg_plan_run, in every launch form
 (persistent or one block per item, one arena or two halves), with one phase
 or many (a small arena), on every replay, with or without the fit."""
 import numpy as np
@@ -8,15 +10,16 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-# (L, Q, receptor atoms, ligand atoms, poses): every translation column class
-# (L + 1 up to 32), q tiles with and without padding, pose counts from a few
-# blocks to many chunks
+# (L, Q, receptor atoms, ligand atoms, poses[, |t| range]): every translation
+# column class (L + 1 up to 32), q tiles with and without padding, pose
+# counts from a few blocks to many chunks; sparse lists and two dense ones
+# (|t| within 2 A: tens of poses per translated row)
 SPECS = [(4, 9, 120, 80, 300), (10, 51, 400, 250, 3000), (15, 101, 600, 300, 8000), (20, 51, 500, 300, 2500),
          (20, 101, 900, 500, 20000), (25, 37, 700, 400, 6000), (30, 201, 800, 450, 1500), (31, 12, 300, 200, 4000),
-         (10, 201, 300, 200, 500)]
+         (10, 201, 300, 200, 500), (12, 24, 300, 200, 20000, (25.0, 26.0)), (20, 51, 400, 300, 30000, (30.0, 31.5))]
 
 
-def _dimer(g, L, Q, nrec, nlig, npose, seed):
+def _dimer(g, L, Q, nrec, nlig, npose, trange=(25.0, 40.0), seed=0):
     from libfmftsaxs_gb300 import synth, workload as wl
     rng = np.random.default_rng(seed)
     rec = synth.make_molecule(nrec, 2.2 * (nrec / 8.0) ** 0.38, seed).with_sasa()
@@ -30,9 +33,9 @@ def _dimer(g, L, Q, nrec, nlig, npose, seed):
     I, _ = g.profile_from_spf(A, L, q, 1.7, c1, c2)
     eq, ei, ee = synth.noisy_experiment(q, I, 0.01, rng)
     a, mult, peak = g.bin_experiment(eq, ei, ee, q, 1.7)
-    z = np.arange(25.0, 41.0)
+    z = np.arange(np.floor(trange[0]), np.ceil(trange[1]) + 1.0)
     R = synth.random_rotations(npose, rng)
-    T = synth.random_translations(npose, 25.0, 40.0, rng)
+    T = synth.random_translations(npose, trange[0], trange[1], rng)
     idx, _ = g.poses_to_indices(R, T, z, L)
     p = g.Plan(A, B, q, z, L, a, mult, peak, synth.C1_GRID, synth.C2_GRID, precision=g.MIXED)
     p.set_poses(idx, skip=1)
@@ -42,6 +45,8 @@ def _dimer(g, L, Q, nrec, nlig, npose, seed):
 @pytest.fixture(scope="module")
 def plans(gpu):
     ps = [_dimer(gpu, *s, seed=700 + 13 * i) for i, s in enumerate(SPECS)]
+    for p in ps[1::3]:
+        p.set_fused(gpu.FUSE_ON)   # some dimers on the fused translation
     yield ps
     for p in ps:
         p.close()
