@@ -314,18 +314,29 @@ k_rotate(const typename Cx<S>::T *__restrict__ spf_t, const S *__restrict__ dtab
 	rotate_block<S, G, CH>(spf_t, dtab, hs, Q, L, conj, out, t, b, m);
 }
 
-/* Work item k (from 0) of a block of a batched kernel.  Persistent launch
- * (ctr != NULL): the next unclaimed item, for the whole block (the leading
- * barrier: every thread is done with the previous item).  One block per
- * item (ctr == NULL): item blockIdx.x, then none. */
-__device__ __forceinline__ int next_item(int *ctr, int k, int nitems)
+/* The work items of a block of a batched kernel:
+ *   for (it = item_begin(..); it < nitems; it = item_advance(..)) {
+ *           nxt = item_claim(ctr); ...work on item it... }
+ * Persistent launch (ctr != NULL): unclaimed items in order; thread 0
+ * claims the next one through the counter when the block starts on the
+ * current one, so the atomic's round trip overlaps the work, and publishes
+ * it after a barrier (every thread is done with the current item).  One
+ * block per item (ctr == NULL): item blockIdx.x, then none. */
+__device__ __forceinline__ int item_begin(int *ctr, int *s_it)
 {
-	if (!ctr) return k == 0 ? (int)blockIdx.x : nitems;
-	__shared__ int s_it;
+	if (!ctr) return (int)blockIdx.x;
+	if (threadIdx.x == 0) *s_it = atomicAdd(ctr, 1);
 	__syncthreads();
-	if (threadIdx.x == 0) s_it = atomicAdd(ctr, 1);
+	return *s_it;
+}
+__device__ __forceinline__ int item_claim(int *ctr) { return ctr && threadIdx.x == 0 ? atomicAdd(ctr, 1) : 0; }
+__device__ __forceinline__ int item_advance(int *ctr, int *s_it, int nxt, int nitems)
+{
+	if (!ctr) return nitems;
 	__syncthreads();
-	return s_it;
+	if (threadIdx.x == 0) *s_it = nxt;
+	__syncthreads();
+	return *s_it;
 }
 
 /* rotation blocks of many tables (mixed path); the twiddles are restaged
@@ -338,9 +349,10 @@ k_rotate_batch(const sxsk_rot_job *__restrict__ jobs, const int4 *__restrict__ i
 	RotTw<float> *hs = reinterpret_cast<RotTw<float> *>(rsm_raw);
 	const double2 *cur = nullptr;
 	int curL = -1;
-	for (int k = 0;; k++) {
-		int it = next_item(ctr, k, nitems);
-		if (it >= nitems) break;
+	__shared__ int s_it;
+	int nxt = 0;
+	for (int it = item_begin(ctr, &s_it); it < nitems; it = item_advance(ctr, &s_it, nxt, nitems)) {
+		nxt = item_claim(ctr);
 		int4 w = items[it];
 		sxsk_rot_job j = jobs[w.x];
 		if (j.tw != cur || j.L != curL) {
@@ -834,9 +846,10 @@ __global__ void __launch_bounds__(TCOL_THREADS(3), TF_MINB(NB))
 k_translate_fused_batch(const sxsk_tf_job *__restrict__ jobs, const int4 *__restrict__ items, int nitems, int *ctr)
 {
 	extern __shared__ __align__(16) unsigned char tps_raw[];
-	for (int k = 0;; k++) {
-		int it = next_item(ctr, k, nitems);
-		if (it >= nitems) break;
+	__shared__ int s_it;
+	int nxt = 0;
+	for (int it = item_begin(ctr, &s_it); it < nitems; it = item_advance(ctr, &s_it, nxt, nitems)) {
+		nxt = item_claim(ctr);
 		int4 w = items[it];
 		sxsk_tf_job j = jobs[w.x];
 		tfused_block<NB>((const float2 *)j.U, (const float *)j.tau, j.combo_zbg, j.slices, j.nslice, j.cbase, j.L,
@@ -866,9 +879,10 @@ __global__ void __launch_bounds__(TCOL_THREADS(3), TP_MINB(NB))
 k_translate_batch(const sxsk_tr_job *__restrict__ jobs, const int4 *__restrict__ items, int nitems, int *ctr)
 {
 	extern __shared__ __align__(16) unsigned char tps_raw[];
-	for (int k = 0;; k++) {
-		int it = next_item(ctr, k, nitems);
-		if (it >= nitems) break;
+	__shared__ int s_it;
+	int nxt = 0;
+	for (int it = item_begin(ctr, &s_it); it < nitems; it = item_advance(ctr, &s_it, nxt, nitems)) {
+		nxt = item_claim(ctr);
 		int4 w = items[it];
 		sxsk_tr_job j = jobs[w.x];
 		tpipe_block<NB>((const float2 *)j.U, (const float *)j.tau, j.combo_zbg, j.slices, j.nslice, j.cbase,
@@ -928,9 +942,10 @@ k_fused_reduce(const sxsk_pose *__restrict__ poses, int npose, const float *__re
 __global__ void __launch_bounds__(128)
 k_fused_reduce_batch(const sxsk_fr_job *__restrict__ jobs, const int4 *__restrict__ items, int nitems, int *ctr)
 {
-	for (int k = 0;; k++) {
-		int it = next_item(ctr, k, nitems);
-		if (it >= nitems) break;
+	__shared__ int s_it;
+	int nxt = 0;
+	for (int it = item_begin(ctr, &s_it); it < nitems; it = item_advance(ctr, &s_it, nxt, nitems)) {
+		nxt = item_claim(ctr);
 		int4 w = items[it];
 		sxsk_fr_job j = jobs[w.x];
 		int QP = ((j.Q + SXS_QT - 1) / SXS_QT) * SXS_QT;
@@ -1077,9 +1092,10 @@ k_pose_cross_batch(const sxsk_pc_job *__restrict__ jobs, const int4 *__restrict_
 	__shared__ float2 tws[2 * SXS_LMAX_K - 1];
 	const double2 *cur = nullptr;
 	int curL = -1;
-	for (int k = 0;; k++) {
-		int it = next_item(ctr, k, nitems);
-		if (it >= nitems) break;
+	__shared__ int s_it;
+	int nxt = 0;
+	for (int it = item_begin(ctr, &s_it); it < nitems; it = item_advance(ctr, &s_it, nxt, nitems)) {
+		nxt = item_claim(ctr);
 		int4 w = items[it];
 		sxsk_pc_job j = jobs[w.x];
 		if (j.tw != cur || j.L != curL) {

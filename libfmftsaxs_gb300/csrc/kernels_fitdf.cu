@@ -233,18 +233,17 @@ k_fit_grid_df_batch(const sxsk_fit_job *__restrict__ jobs, const int2 *__restric
 	extern __shared__ double sm[];
 	__shared__ int s_it;
 	int cur = -1;
-	for (int k = 0;; k++) {
-		int it;
-		if (ctr) {
-			/* persistent: the next unclaimed item */
-			__syncthreads();
-			if (threadIdx.x == 0) s_it = atomicAdd(ctr, 1);
-			__syncthreads();
-			it = s_it;
-		} else {
-			it = k == 0 ? (int)blockIdx.x : nitems;   /* one block per item */
-		}
-		if (it >= nitems) break;
+	/* items as in the batched contraction kernels: persistent (ctr), the
+	 * next item claimed while the block works on the current one, or one
+	 * block per item */
+	int it = (int)blockIdx.x;
+	if (ctr) {
+		if (threadIdx.x == 0) s_it = atomicAdd(ctr, 1);
+		__syncthreads();
+		it = s_it;
+	}
+	for (; it < nitems;) {
+		int nxt = ctr && threadIdx.x == 0 ? atomicAdd(ctr, 1) : 0;
 		int2 w = items[it];
 		sxsk_fit_job J = jobs[w.x];
 		FitSm m = fit_sm(J, sm);
@@ -253,6 +252,11 @@ k_fit_grid_df_batch(const sxsk_fit_job *__restrict__ jobs, const int2 *__restric
 			cur = w.x;
 		}
 		fit_group(J, m, w.y);   /* starts with a barrier: the staged constants are visible */
+		if (!ctr) break;
+		__syncthreads();
+		if (threadIdx.x == 0) s_it = nxt;
+		__syncthreads();
+		it = s_it;
 	}
 }
 
