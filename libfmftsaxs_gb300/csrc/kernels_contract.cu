@@ -237,12 +237,12 @@ __device__ __forceinline__ void rotate_block(const typename Cx<S>::T *__restrict
 	for (int l = m; l <= L; l++) {
 		const S *dl = db + (size_t)l * N * N;
 		const V *Cl = C + (size_t)l * (l + 1) * Q;    /* lm of m1 = 0 */
-		S d0 = dl[0], d0s = mul_rn(d0, sg);   /* the sign flips are exact */
+		S d0 = __ldg(dl), d0s = mul_rn(d0, sg);   /* the sign flips are exact */
 		V y0[CH];
 #pragma unroll
 		for (int c = 0; c < CH; c++) {
 			V c0 = zero2<V>();
-			if (qok) c0 = Cl[c * cstride];
+			if (qok) c0 = __ldg(Cl + c * cstride);
 			y0[c].x = mul_rn(d0, c0.x);
 			y0[c].y = mul_rn(d0s, c0.y);
 		}
@@ -255,15 +255,15 @@ __device__ __forceinline__ void rotate_block(const typename Cx<S>::T *__restrict
 		for (int m1 = 1; m1 <= l; m1++) {
 			base += g0;
 			if (base >= N) base -= N;
-			S dp = dl[m1], dm = dl[-m1];
+			S dp = __ldg(dl + m1), dm = __ldg(dl - m1);
 			S dps = mul_rn(dp, sg), dms = mul_rn(dm, sg);
 			V Sv[CH], Dv[CH];
 #pragma unroll
 			for (int c = 0; c < CH; c++) {
 				V cp = zero2<V>(), cm = zero2<V>();
 				if (qok) {
-					cp = Cl[c * cstride + (size_t)m1 * Q];
-					cm = Cl[c * cstride - (ptrdiff_t)m1 * Q];
+					cp = __ldg(Cl + c * cstride + (size_t)m1 * Q);
+					cm = __ldg(Cl + c * cstride - (ptrdiff_t)m1 * Q);
 				}
 				/* S = y(m1) + y(-m1), D = y(m1) - y(-m1): y(-m1) rounded, y(m1)
 				 * fused */
@@ -640,7 +640,7 @@ __device__ __forceinline__ void tpipe_block(const float2 *__restrict__ U, const 
 				int qq = k % SXS_QT, r = k / SXS_QT;
 				int i = r / NB, kk = r % NB;
 				float v = 0;
-				if (i < n && kk < n) v = tz[((size_t)(m + i) * K + m + kk) * SXS_QT + qq];
+				if (i < n && kk < n) v = __ldg(tz + ((size_t)(m + i) * K + m + kk) * SXS_QT + qq);
 				ts[qq * qstride + i * NB + kk] = v;
 			}
 			zcur = zi;
@@ -760,7 +760,7 @@ __device__ __forceinline__ void tfused_block(const float2 *__restrict__ U, const
 				int qq = k % SXS_QT, r = k / SXS_QT;
 				int i = r / NB, kk = r % NB;
 				float v = 0;
-				if (i < n && kk < n) v = tz[((size_t)(m + i) * K + m + kk) * SXS_QT + qq];
+				if (i < n && kk < n) v = __ldg(tz + ((size_t)(m + i) * K + m + kk) * SXS_QT + qq);
 				ts[qq * qstride + i * NB + kk] = v;
 			}
 			zcur = zi;
