@@ -123,7 +123,10 @@ void sxsg_batch_destroy(sxsg_batch *b)
 	if (b->exec) cudaGraphExecDestroy(b->exec);
 	if (b->graph) cudaGraphDestroy(b->graph);
 	if (b->d_buf) cudaFree(b->d_buf);
-	if (b->d_arena) cudaFree(b->d_arena);
+	if (b->d_arena) {
+		cudaFreeAsync(b->d_arena, b->s);
+		cudaStreamSynchronize(b->s);
+	}
 	for (int i = 0; i < SXSB_BR; i++) {
 		if (b->br[i]) cudaStreamDestroy(b->br[i]);
 		if (b->join[i]) cudaEventDestroy(b->join[i]);
@@ -377,7 +380,9 @@ static int build_phases(sxsg_batch *b, bstage *st, size_t arena_req)
 	b->nphase = nphase;
 	b->arena = used;
 	if (used > 0) {
-		cudaError_t e = cudaMalloc(&b->d_arena, used);
+		/* from the stream-ordered pool, as a plan's translated table */
+		cudaError_t e = cudaMallocAsync(&b->d_arena, used, b->s);
+		if (!e) e = cudaStreamSynchronize(b->s);
 		if (e) {
 			free(pieces.p);
 			return sxs_cuda_fail(e, "sxsg_batch_create arena");
