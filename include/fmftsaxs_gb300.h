@@ -348,7 +348,10 @@ void sxsg_plan_destroy(sxsg_plan *plan);
  * set; each plan's results equal a sxsg_plan_run of it bit for bit and are
  * read with sxsg_plan_results / sxsg_plan_topk after sxsg_batch_run.
  * A batch holds the plans' device pointers: changing a plan's poses, tiles
- * or budget, or destroying it, needs a new batch. */
+ * or budget, or destroying it, needs a new batch; the batches (and plan
+ * runs) of one plan must not run at the same time, as they write its
+ * outputs.  After a run each plan's sxsg_plan_timings reports the batch's
+ * stages ([0] tables, [1] translation + per-pose, [3] fit, [4] graph). */
 typedef struct sxsg_batch sxsg_batch;
 typedef struct {
 	int plans;          /* dimers */
