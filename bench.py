@@ -510,7 +510,8 @@ def run_batch(g, args):
         arena = st["arena_bytes"]
         b.close()
         # the other launch forms, briefly (each checked bit for bit below)
-        for fl in (0, g.BATCH_PERSISTENT, g.BATCH_OVERLAP, g.BATCH_PERSISTENT | g.BATCH_OVERLAP):
+        for fl in (0, g.BATCH_PERSISTENT, g.BATCH_OVERLAP | g.BATCH_PERSISTENT, g.BATCH_ITEMS,
+                   g.BATCH_ITEMS | g.BATCH_PERSISTENT, g.BATCH_ITEMS | g.BATCH_PERSISTENT | g.BATCH_OVERLAP):
             if fl == g.BATCH_DEFAULT:
                 continue
             bb = g.Batch(plans, fit=g.FIT_GRID, flags=fl)
@@ -561,10 +562,12 @@ def run_batch(g, args):
            "graph_kernel_launches": int(launches), "work_items": int(items),
            "graph": {"ms_per_step": graph_s * 1e3, "poses_per_s": poses / graph_s,
                      "device_ms": {"tables": dev[0], "translate_and_pose": dev[1], "fit": dev[2]}},
-           "graph_forms_ms": {{0: "one_block_per_item", 1: "persistent", 2: "one_block_per_item+overlap",
-                               3: "persistent+overlap"}[k]: {"total": v[0] * 1e3, "tables": v[1], "phases": v[2],
-                                                             "fit": v[3]} for k, v in forms.items()},
-           "graph_default_form": "persistent",
+           "graph_forms_ms": {{0: "chunk_launches", 1: "chunk_launches+persistent", 3: "chunk_launches+persistent+overlap",
+                               4: "items", 5: "items+persistent", 7: "items+persistent+overlap"}[k]:
+                              {"total": v[0] * 1e3, "tables": v[1], "phases": v[2], "fit": v[3]}
+                              for k, v in forms.items()},
+           "graph_default_form": "chunk_launches+persistent (translation and per-pose work as single-dimer launches "
+                                 "per chunk; rotations and fit as persistent work-item launches)",
            "plans_sequential": {"ms_per_step": plans_s * 1e3, "poses_per_s": poses / plans_s,
                                 "device_ms": dict(zip(("tables", "translate", "pose", "fit"), seq_stage.tolist()))},
            "serving": ({"ms_per_step": srv_s * 1e3, "poses_per_s": poses / srv_s,

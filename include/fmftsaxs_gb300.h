@@ -363,12 +363,19 @@ typedef struct {
 	double ms[4];       /* last replay: [0] tables, [1] translation + per-pose, [2] fit, [3] whole graph */
 } sxsg_batch_stats;
 /* Launch forms of a batch (flags):
- *   SXSG_BATCH_PERSISTENT  persistent kernels (SMs x resident blocks taking
- *                          items through an atomic counter); without it one
- *                          block per item, in order
+ *   SXSG_BATCH_PERSISTENT  work-item launches run persistently (SMs x
+ *                          resident blocks taking items through an atomic
+ *                          counter); without it one block per item, in order
+ *   SXSG_BATCH_ITEMS       the translation and per-pose work of a phase as
+ *                          work-item launches over all its chunks too;
+ *                          without it (faster on GB300) each chunk's
+ *                          translation and per-pose work are the single-dimer
+ *                          launches, inside the same graph and phases; the
+ *                          rotations and the fit are work-item launches in
+ *                          every form
  *   SXSG_BATCH_OVERLAP     two arena halves: the translations of phase
  *                          k + 1 run beside the per-pose work of phase k */
-enum { SXSG_BATCH_PERSISTENT = 1, SXSG_BATCH_OVERLAP = 2 };
+enum { SXSG_BATCH_PERSISTENT = 1, SXSG_BATCH_OVERLAP = 2, SXSG_BATCH_ITEMS = 4 };
 /* fit_mode: SXSG_FIT_GRID or SXSG_FIT_NONE; arena_bytes: upper bound on
  * the translated-table arena (0 = what the dimers need, at most half the
  * free device memory) */

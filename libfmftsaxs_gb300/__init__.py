@@ -16,7 +16,7 @@ FIT_NONE, FIT_GRID, FIT_LBFGSB = 0, 1, 2
 FP64 = 0
 MIXED = 1
 ROT_CUDA, ROT_TC = 0, 1
-BATCH_PERSISTENT, BATCH_OVERLAP = 1, 2
+BATCH_PERSISTENT, BATCH_OVERLAP, BATCH_ITEMS = 1, 2, 4
 FUSE_AUTO, FUSE_ON, FUSE_OFF = 0, 1, 2
 BATCH_DEFAULT = BATCH_PERSISTENT
 

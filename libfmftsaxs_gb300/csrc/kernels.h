@@ -120,6 +120,10 @@ int sxsk_pose_scatter(const sxsk_pose *tmp, const int32_t *key, int64_t n, int32
 int sxsk_rotate_group(int L, int gsel);
 /* slices per block of the pipelined FP32 translation when a plan sets none */
 #define SXSK_TP_SB 8
+/* the launch of sxsk_translate (FP32) for column class NB alone (the m with
+ * L + 1 - m in (NB - 4, NB]); nothing when the class has no m for L */
+int sxsk_translate_class(const void *U, const void *tau, const int32_t *combo_zbg, const int32_t *slices, int nslice,
+                         int cbase, int ncombo, int nzt, int Q, int L, void *R, int sb, int NB, cudaStream_t s);
 /* kernel launches one sxsk_translate call makes for this L */
 int sxsk_translate_launches(int L);
 int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, const int32_t *slices, int nslice,
@@ -144,6 +148,11 @@ size_t sxsk_fused_part_floats(int L, int Q);
 int sxsk_translate_fused(const void *U, const void *tau, const int32_t *combo_zbg, const int32_t *slices, int nslice,
                          int cbase, int nzt, int Q, int L, int sb, const sxsk_pose *poses, const int32_t *cstart,
                          int pose_base, const void *P, const double2 *tw, float *part, cudaStream_t s);
+/* sxsk_translate_fused for column class NB alone */
+int sxsk_translate_fused_class(const void *U, const void *tau, const int32_t *combo_zbg, const int32_t *slices,
+                               int nslice, int cbase, int nzt, int Q, int L, int sb, const sxsk_pose *poses,
+                               const int32_t *cstart, int pose_base, const void *P, const double2 *tw, float *part,
+                               int NB, cudaStream_t s);
 /* cross of the npose poses from `poses` (their part rows from 0) */
 int sxsk_fused_reduce(const sxsk_pose *poses, int npose, const float *part, int Q, int L, const void *cst,
                       void *cross, cudaStream_t s);
@@ -219,7 +228,7 @@ typedef struct {
 	const int32_t *combo_zbg;         /* the chunk's combos (cbase = the first one's index) */
 	const int32_t *slices;            /* the chunk's slices */
 	void *R;                          /* the chunk's translated table */
-	int nslice, cbase, ncombo, L, nzt, sb;
+	int nslice, cbase, ncombo, L, nzt, sb, Q, pad;
 } sxsk_tr_job;
 /* items {job, q tile, slice group, m} for the m with L + 1 - m in
  * (NB - 4, NB] (the pipelined FP32 kernel of that NB; L + 1 <= 32) */

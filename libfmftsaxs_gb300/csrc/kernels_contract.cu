@@ -1633,6 +1633,22 @@ int sxsk_pose_scatter(const sxsk_pose *tmp, const int32_t *key, int64_t n, int32
 	return cudaGetLastError();
 }
 
+int sxsk_translate_class(const void *U, const void *tau, const int32_t *combo_zbg, const int32_t *slices, int nslice,
+                         int cbase, int ncombo, int nzt, int Q, int L, void *R, int sb, int NB, cudaStream_t s)
+{
+	if (nslice <= 0) return 0;
+	if (L + 1 > 32) return cudaErrorInvalidValue;
+	int NT = (Q + SXS_QT - 1) / SXS_QT;
+	if (sb < 1) sb = SXSK_TP_SB;
+#define TCL(C)                                                                                                     \
+	case C: return translate_col_launch<float, C>(U, tau, combo_zbg, slices, nslice, cbase, ncombo, nzt, NT, L, R, sb, s);
+	switch (NB) {
+		TCL(4) TCL(8) TCL(12) TCL(16) TCL(20) TCL(24) TCL(28) TCL(32)
+	default: return cudaErrorInvalidValue;
+	}
+#undef TCL
+}
+
 int sxsk_translate_launches(int L)
 {
 	int K = L + 1;
@@ -1684,6 +1700,28 @@ int sxsk_translate_fused(const void *U, const void *tau, const int32_t *combo_zb
 	TFL(4) TFL(8) TFL(12) TFL(16) TFL(20) TFL(24) TFL(28) TFL(32)
 #undef TFL
 	return e;
+}
+
+int sxsk_translate_fused_class(const void *U, const void *tau, const int32_t *combo_zbg, const int32_t *slices,
+                               int nslice, int cbase, int nzt, int Q, int L, int sb, const sxsk_pose *poses,
+                               const int32_t *cstart, int pose_base, const void *P, const double2 *tw, float *part,
+                               int NB, cudaStream_t s)
+{
+	if (nslice <= 0) return 0;
+	if (L + 1 > 32) return cudaErrorInvalidValue;
+	int NT = (Q + SXS_QT - 1) / SXS_QT;
+	if (sb < 1) sb = SXSK_TP_SB;
+	const float2 *u = (const float2 *)U, *p = (const float2 *)P;
+	const float *ta = (const float *)tau;
+#define TFC(C)                                                                                                     \
+	case C:                                                                                                        \
+		return translate_fused_launch<C>(u, ta, combo_zbg, slices, nslice, cbase, nzt, NT, L, sb, poses, cstart,   \
+		                                 pose_base, p, tw, part, s);
+	switch (NB) {
+		TFC(4) TFC(8) TFC(12) TFC(16) TFC(20) TFC(24) TFC(28) TFC(32)
+	default: return cudaErrorInvalidValue;
+	}
+#undef TFC
 }
 
 int sxsk_fused_reduce(const sxsk_pose *poses, int npose, const float *part, int Q, int L, const void *cst,

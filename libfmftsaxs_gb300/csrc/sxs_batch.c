@@ -55,7 +55,7 @@ typedef struct {
 	                          * 5 sums over m of the fused path */
 	int arg;                 /* G or NB */
 	int phase;
-	int nitems;
+	int nitems, njobs;
 	size_t jobs_off, items_off;
 	int ctr;                 /* counter slot */
 } blaunch;
@@ -169,14 +169,15 @@ static size_t st_put(bstage *st, const void *src, size_t bytes)
 
 /* sorts items (largest cost first), stores the jobs and items, appends the
  * launch */
-static int st_launch(bstage *st, int kind, int arg, int phase, const void *jobs, size_t jbytes, bvec *items,
-                     int pair)
+static int st_launch(bstage *st, int kind, int arg, int phase, const void *jobs, size_t jbytes, int njobs,
+                     bvec *items, int pair)
 {
-	if (items->n == 0) return 0;
+	/* a launch over work items, or (no items) one launch per job */
+	if (njobs == 0 || (items->n == 0 && kind != 1 && kind != 2 && kind != 4 && kind != 5)) return 0;
 	if (items->n > INT32_MAX) return sxs_fail(-2, "sxsg_batch_create: too many work items in one launch");
 	qsort(items->p, items->n, sizeof(bitem), cmp_item);
 	size_t ib = items->n * (pair ? sizeof(int2) : sizeof(int4));
-	char *tmp = malloc(ib);
+	char *tmp = malloc(ib > 0 ? ib : 1);
 	if (!tmp) return sxs_fail(-5, "out of host memory");
 	const bitem *it = items->p;
 	for (size_t i = 0; i < items->n; i++) {
@@ -196,6 +197,7 @@ static int st_launch(bstage *st, int kind, int arg, int phase, const void *jobs,
 	L->arg = arg;
 	L->phase = phase;
 	L->nitems = (int)items->n;
+	L->njobs = njobs;
 	L->jobs_off = st_put(st, jobs, jbytes);
 	L->items_off = st_put(st, tmp, ib);
 	L->ctr = (int)st->launches.n - 1;
@@ -268,7 +270,7 @@ static int build_rotations(sxsg_batch *b, bstage *st)
 				nj++;
 			}
 		}
-		if (!rc) rc = st_launch(st, 0, G | (twmax << 8), -1, jobs, sizeof(sxsk_rot_job) * nj, &items, 0);
+		if (!rc) rc = st_launch(st, 0, G | (twmax << 8), -1, jobs, sizeof(sxsk_rot_job) * nj, nj, &items, 0);
 	}
 	free(jobs);
 	free(items.p);
@@ -451,6 +453,7 @@ static int build_phases(sxsg_batch *b, bstage *st, size_t arena_req)
 			t->L = v->L;
 			t->nzt = v->nzt;
 			t->sb = sb;
+			t->Q = v->Q;
 			sxsk_pc_job *q = &pj[nj];
 			memset(q, 0, sizeof(*q));
 			q->poses = v->poses + p0;
@@ -466,21 +469,22 @@ static int build_phases(sxsg_batch *b, bstage *st, size_t arena_req)
 			q->L = v->L;
 			jmap[nj++] = (int)k;
 		}
+		int it_mode = b->flags & SXSG_BATCH_ITEMS;
 		for (int NB = 4; NB <= 32 && !rc; NB += 4) {
-			for (int j = 0; j < nj && !rc; j++) {
+			for (int j = 0; j < nj && !rc && it_mode; j++) {
 				const bpiece *p = &pc[jmap[j]];
 				const sxs_plan_view *v = &b->v[p->plan];
 				rc = tr_items(&items, j, v, v->h_slices + 2 * p->s0, tj[j].nslice, tj[j].sb, NB);
 			}
-			if (!rc) rc = st_launch(st, 1, NB, ph, tj, sizeof(sxsk_tr_job) * nj, &items, 0);
-			for (int j = 0; j < nf && !rc; j++) {
+			if (!rc) rc = st_launch(st, 1, NB, ph, tj, sizeof(sxsk_tr_job) * nj, nj, &items, 0);
+			for (int j = 0; j < nf && !rc && it_mode; j++) {
 				const bpiece *p = &pc[fmap[j]];
 				const sxs_plan_view *v = &b->v[p->plan];
 				rc = tr_items(&items, j, v, v->h_slices + 2 * p->s0, fj[j].nslice, fj[j].sb, NB);
 			}
-			if (!rc) rc = st_launch(st, 4, NB, ph, fj, sizeof(sxsk_tf_job) * nf, &items, 0);
+			if (!rc) rc = st_launch(st, 4, NB, ph, fj, sizeof(sxsk_tf_job) * nf, nf, &items, 0);
 		}
-		for (int j = 0; j < nj && !rc; j++) {
+		for (int j = 0; j < nj && !rc && it_mode; j++) {
 			const sxsk_pc_job *q = &pj[j];
 			const sxs_plan_view *v = &b->v[pc[jmap[j]].plan];
 			int bpt = (q->npose + 31) / 32;
@@ -489,14 +493,14 @@ static int build_phases(sxsg_batch *b, bstage *st, size_t arena_req)
 				for (int pb = 0; pb < bpt && !rc; pb++) rc = add_item(&items, (double)v->NP, j, tt, pb, 0);
 			job_cost(&items, i0);
 		}
-		if (!rc) rc = st_launch(st, 2, 0, ph, pj, sizeof(sxsk_pc_job) * nj, &items, 0);
-		for (int j = 0; j < nf && !rc; j++) {
+		if (!rc) rc = st_launch(st, 2, 0, ph, pj, sizeof(sxsk_pc_job) * nj, nj, &items, 0);
+		for (int j = 0; j < nf && !rc && it_mode; j++) {
 			long nblk = ((long)rj[j].npose * rj[j].Q + 127) / 128;
 			size_t i0 = items.n;
 			for (long k = 0; k < nblk && !rc; k++) rc = add_item(&items, (double)(rj[j].L + 1), j, (int)k, 0, 0);
 			job_cost(&items, i0);
 		}
-		if (!rc) rc = st_launch(st, 5, 0, ph, rj, sizeof(sxsk_fr_job) * nf, &items, 0);
+		if (!rc) rc = st_launch(st, 5, 0, ph, rj, sizeof(sxsk_fr_job) * nf, nf, &items, 0);
 	}
 	free(items.p);
 	free(tj);
@@ -552,18 +556,62 @@ static int build_fit(sxsg_batch *b, bstage *st)
 		job_cost(&items, i0);
 		nj++;
 	}
-	if (!rc) rc = st_launch(st, 3, 0, -1, jobs, sizeof(sxsk_fit_job) * nj, &items, 1);
+	if (!rc) rc = st_launch(st, 3, 0, -1, jobs, sizeof(sxsk_fit_job) * nj, nj, &items, 1);
 	free(jobs);
 	free(items.p);
 	return rc;
 }
 
-static int launch_one(sxsg_batch *b, const blaunch *L, int *ctr, cudaStream_t s)
+/* does column class NB hold an m for L (translate_col_launch's range) */
+static int class_used(int L, int NB)
+{
+	int K = L + 1, m_hi = K - (NB - 3), m_lo = K - NB;
+	if (m_hi > L) m_hi = L;
+	if (m_lo < 0) m_lo = 0;
+	return m_hi >= m_lo;
+}
+
+/* The translation and per-pose launches of a phase without work items: the
+ * single-dimer kernels, one launch per piece (and column class), read from
+ * the host copy of the jobs.  *nk += the kernels launched. */
+static int launch_pieces(const blaunch *L, const char *hbase, int *nk, cudaStream_t s)
+{
+	const char *hj = hbase + L->jobs_off;
+	int rc = 0;
+	for (int j = 0; j < L->njobs && !rc; j++) {
+		if (L->kind == 1) {
+			const sxsk_tr_job *t = (const sxsk_tr_job *)hj + j;
+			if (!class_used(t->L, L->arg)) continue;
+			rc = sxsk_translate_class(t->U, t->tau, t->combo_zbg, t->slices, t->nslice, t->cbase, t->ncombo, t->nzt,
+			                          t->Q, t->L, t->R, t->sb, L->arg, s);
+		} else if (L->kind == 4) {
+			const sxsk_tf_job *t = (const sxsk_tf_job *)hj + j;
+			if (!class_used(t->L, L->arg)) continue;
+			rc = sxsk_translate_fused_class(t->U, t->tau, t->combo_zbg, t->slices, t->nslice, t->cbase, t->nzt, t->Q,
+			                                t->L, t->sb, t->poses, t->cstart, t->pose_base, t->P, t->tw, t->part,
+			                                L->arg, s);
+		} else if (L->kind == 2) {
+			const sxsk_pc_job *q = (const sxsk_pc_job *)hj + j;
+			rc = sxsk_pose_cross(q->poses, q->npose, q->combo_base, q->ncombo, q->P, q->R, q->tw, q->cst, q->Q, q->L,
+			                     q->cross, 1, s);
+		} else {
+			const sxsk_fr_job *r = (const sxsk_fr_job *)hj + j;
+			rc = sxsk_fused_reduce(r->poses, r->npose, r->part, r->Q, r->L, r->cst, r->cross, s);
+		}
+		(*nk)++;
+	}
+	return rc;
+}
+
+static int launch_one(sxsg_batch *b, const blaunch *L, int *ctr, const char *hbase, int *nk, cudaStream_t s)
 {
 	char *base = b->d_buf;
 	const void *jobs = base + L->jobs_off, *items = base + L->items_off;
 	int *c = ctr ? ctr + L->ctr : NULL;   /* NULL: one block per item */
-	switch (L->kind) {
+	int k = L->kind;
+	if (!(b->flags & SXSG_BATCH_ITEMS) && (k == 1 || k == 2 || k == 4 || k == 5)) return launch_pieces(L, hbase, nk, s);
+	if (L->nitems > 0) (*nk)++;
+	switch (k) {
 	case 0: return sxsk_rotate_batch(jobs, items, L->nitems, L->arg & 0xff, L->arg >> 8, c, s);
 	case 1: return sxsk_translate_batch(jobs, items, L->nitems, L->arg, c, s);
 	case 2: return sxsk_pose_cross_batch(jobs, items, L->nitems, c, s);
@@ -582,7 +630,7 @@ static int launch_one(sxsg_batch *b, const blaunch *L, int *ctr, cudaStream_t s)
  * phase that used the same arena half: with SXSG_BATCH_OVERLAP (two
  * halves) the translations of phase k + 1 run beside the per-pose work of
  * phase k.  The fit follows the last per-pose launch. */
-static int capture(sxsg_batch *b, const blaunch *ls, int nl, int *ctr)
+static int capture(sxsg_batch *b, const blaunch *ls, int nl, int *ctr, const char *hbase)
 {
 	cudaStream_t s = b->s, ps = b->ps;
 	int rc = 0, nk = 0;
@@ -600,8 +648,7 @@ static int capture(sxsg_batch *b, const blaunch *ls, int nl, int *ctr)
 	}
 	int li = 0;
 	while (li < nl && ls[li].kind == 0 && !e && !rc) {
-		rc = launch_one(b, &ls[li], c, s);
-		nk++;
+		rc = launch_one(b, &ls[li], c, hbase, &nk, s);
 		li++;
 	}
 	for (int k = 0; k < 2 && !e; k++) {
@@ -620,15 +667,13 @@ static int capture(sxsg_batch *b, const blaunch *ls, int nl, int *ctr)
 			int cls = ls[li].arg / 4 - 1;
 			cudaStream_t bs = b->br[cls];
 			if (ph >= halves) e = cudaStreamWaitEvent(bs, b->evpose[h], 0);
-			if (!e) rc = launch_one(b, &ls[li], c, bs);
+			if (!e) rc = launch_one(b, &ls[li], c, hbase, &nk, bs);
 			if (!e && !rc) e = cudaEventRecord(b->join[cls], bs);
 			if (!e) e = cudaStreamWaitEvent(ps, b->join[cls], 0);
-			nk++;
 			li++;
 		}
 		while (li < nl && (ls[li].kind == 2 || ls[li].kind == 5) && ls[li].phase == ph && !e && !rc) {
-			rc = launch_one(b, &ls[li], c, ps);
-			nk++;
+			rc = launch_one(b, &ls[li], c, hbase, &nk, ps);
 			li++;
 		}
 		if (!e && !rc) e = cudaEventRecord(b->evpose[h], ps);
@@ -642,8 +687,7 @@ static int capture(sxsg_batch *b, const blaunch *ls, int nl, int *ctr)
 	if (!e) e = cudaStreamWaitEvent(s, b->evpose[0], 0);
 	if (!e) e = cudaEventRecordWithFlags(b->ev[2], s, cudaEventRecordExternal);
 	if (li < nl && ls[li].kind == 3 && !e && !rc) {
-		rc = launch_one(b, &ls[li], c, s);
-		nk++;
+		rc = launch_one(b, &ls[li], c, hbase, &nk, s);
 		li++;
 	}
 	if (!e) e = cudaEventRecordWithFlags(b->ev[3], s, cudaEventRecordExternal);
@@ -669,7 +713,7 @@ int sxsg_batch_create(sxsg_plan *const *plans, int nplan, int fit_mode, size_t a
                       sxsg_batch **out)
 {
 	if (!plans || nplan <= 0 || !out) return sxs_fail(-2, "sxsg_batch_create: bad arguments");
-	if (flags & ~(SXSG_BATCH_PERSISTENT | SXSG_BATCH_OVERLAP))
+	if (flags & ~(SXSG_BATCH_PERSISTENT | SXSG_BATCH_OVERLAP | SXSG_BATCH_ITEMS))
 		return sxs_fail(-2, "sxsg_batch_create: unknown flags 0x%x", flags);
 	if (fit_mode != SXSG_FIT_GRID && fit_mode != SXSG_FIT_NONE)
 		return sxs_fail(-2, "sxsg_batch_create: fit mode must be SXSG_FIT_GRID or SXSG_FIT_NONE");
@@ -738,7 +782,7 @@ int sxsg_batch_create(sxsg_plan *const *plans, int nplan, int fit_mode, size_t a
 		const blaunch *ls = st.launches.p;
 		for (int k = 0; k < nl; k++) b->nitems += ls[k].nitems;
 		b->nlaunch = nl;
-		rc = capture(b, ls, nl, (int *)((char *)b->d_buf + ctr_off));
+		rc = capture(b, ls, nl, (int *)((char *)b->d_buf + ctr_off), st.h);
 	}
 	free(st.h);
 	free(st.launches.p);

@@ -76,7 +76,7 @@ def _same(x, y):
         np.testing.assert_array_equal(x[k], y[k], err_msg=k)
 
 
-@pytest.mark.parametrize("flags", [0, 1, 2, 3])
+@pytest.mark.parametrize("flags", [0, 1, 2, 3, 5, 7])
 def test_batch_equals_plan_runs(gpu, plans, flags):
     runs, st = _batched(gpu, plans, gpu.FIT_GRID, reps=2, flags=flags)
     alone = _alone(plans, gpu.FIT_GRID)
@@ -88,7 +88,7 @@ def test_batch_equals_plan_runs(gpu, plans, flags):
     assert all(np.isfinite(a["chi"]).all() for a in alone)
 
 
-@pytest.mark.parametrize("flags", [1, 3])
+@pytest.mark.parametrize("flags", [1, 3, 5])
 def test_batch_many_phases(gpu, plans, flags):
     # an arena of 96 MB holds a few slices of the largest tables (40 MB per
     # slice at L = 30, Q = 201): many chunks and phases
