@@ -338,13 +338,14 @@ void sxsg_plan_destroy(sxsg_plan *plan);
 
 /* ------------------------------------------------------------ batches
  * Many dimers of uneven size (each its own L, q grid, experiment, pose list
- * and fit grid) scored together: a batch captures, once, one CUDA graph of
- * persistent kernels over all of them (the per-z tables per dimer; one
- * launch per rotation group size; per phase one translation launch per
- * column class and one per-pose launch; one fit launch), whose blocks take
- * (dimer, tile, slice / pose block / pose group) work items largest first.
- * A phase translates the chunks of several dimers into one shared device
- * arena.  Plans: mixed precision, L <= 31, own rotation tables, pose lists
+ * and fit grid) scored together: a batch captures, once, one CUDA graph
+ * over all of them: the per-z tables per dimer; one persistent launch per
+ * rotation group size whose blocks take (table, tile, beta, m) work items,
+ * largest dimers first; phases, each translating the chunks of several
+ * dimers into one shared device arena and then contracting them with their
+ * poses (single-dimer launches per chunk, or work-item launches with
+ * SXSG_BATCH_ITEMS); one persistent fit launch over (dimer, pose group)
+ * items.  Plans: mixed precision, L <= 31, own rotation tables, pose lists
  * set; each plan's results equal a sxsg_plan_run of it bit for bit and are
  * read with sxsg_plan_results / sxsg_plan_topk after sxsg_batch_run.
  * A batch holds the plans' device pointers: changing a plan's poses, tiles

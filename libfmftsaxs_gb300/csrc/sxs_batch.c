@@ -1,7 +1,6 @@
 /*
  * Batches of dimers: many mixed-precision plans (each one dimer with its own
- * L, q grid, experiment, pose list and fit grid) scored by one CUDA graph of
- * persistent kernels.
+ * L, q grid, experiment, pose list and fit grid) scored by one CUDA graph.
  *
  * Work items.  Every stage of a plan run is a grid of independent blocks:
  * rotation blocks (table, q tile, beta, m), translation blocks (chunk, q
@@ -18,8 +17,12 @@
  * Phases.  The translated table of a dimer is cut into chunks of whole
  * slices (as a plan run does); chunks of all dimers are packed first-fit,
  * largest first, into phases whose chunks fit one shared device arena.  A
- * phase is the translation launches of its chunks (one per column class,
- * on parallel branches of the graph) followed by one per-pose launch.
+ * phase is the translation of its chunks (a stream per column class, the
+ * classes on parallel branches of the graph) followed by their per-pose
+ * work.  By default those are the single-dimer launches of each chunk (they
+ * measured faster than work-item launches of the same blocks); with
+ * SXSG_BATCH_ITEMS they are work-item launches over all the phase's chunks.
+ * The rotations and the fit are always work-item launches.
  *
  * Graph.  Zeroing the item counters, the per-z tables of every dimer (two
  * high-priority branches, so that their FP64 blocks run beside the rotation
