@@ -281,6 +281,30 @@ static int build_rotations(sxsg_batch *b, bstage *st)
 }
 
 /* chunks of every dimer's translated table, packed into phases */
+/* First fit: item k (of bytes[k] <= cap, in the given order) goes to the
+ * first phase with room, at offset off[k] there; returns the number of
+ * phases and in *used the fullest phase's bytes.  The batch passes its
+ * chunks largest first. */
+int sxs_pack_first_fit(const size_t *bytes, size_t n, size_t cap, int *phase, size_t *off, size_t *used)
+{
+	size_t *fill = calloc(n > 0 ? n : 1, sizeof(size_t));
+	int nphase = 0;
+	if (!fill) return -1;
+	for (size_t k = 0; k < n; k++) {
+		int ph = 0;
+		while (ph < nphase && fill[ph] + bytes[k] > cap) ph++;
+		if (ph == nphase) nphase++;
+		phase[k] = ph;
+		off[k] = fill[ph];
+		fill[ph] += bytes[k];
+	}
+	size_t u = 0;
+	for (int ph = 0; ph < nphase; ph++) u = fill[ph] > u ? fill[ph] : u;
+	free(fill);
+	*used = u;
+	return nphase;
+}
+
 /* device bytes of a piece's slices [s0, s1): its translated rows, or on the
  * fused path its poses' per-m sums */
 static size_t piece_bytes(const sxs_plan_view *v, int64_t s0, int64_t s1)
@@ -365,19 +389,24 @@ static int build_phases(sxsg_batch *b, bstage *st, size_t arena_req)
 	size_t np = pieces.n;
 	qsort(pc, np, sizeof(bpiece), cmp_piece);
 	/* first fit, largest first */
-	size_t *fill = calloc(np > 0 ? np : 1, sizeof(size_t));
-	int nphase = 0;
-	for (size_t k = 0; k < np; k++) {
-		int ph = 0;
-		while (ph < nphase && fill[ph] + pc[k].bytes > arena) ph++;
-		if (ph == nphase) nphase++;
-		pc[k].phase = ph;
-		pc[k].off = fill[ph];
-		fill[ph] += pc[k].bytes;
+	size_t *pb = malloc(sizeof(size_t) * (np > 0 ? np : 1)), *po = malloc(sizeof(size_t) * (np > 0 ? np : 1));
+	int *pp = malloc(sizeof(int) * (np > 0 ? np : 1));
+	if (!pb || !po || !pp) {
+		free(pb); free(po); free(pp); free(pieces.p);
+		return sxs_fail(-5, "out of host memory");
 	}
+	for (size_t k = 0; k < np; k++) pb[k] = pc[k].bytes;
 	size_t used = 0;
-	for (int ph = 0; ph < nphase; ph++) used = fill[ph] > used ? fill[ph] : used;
-	free(fill);
+	int nphase = sxs_pack_first_fit(pb, np, arena, pp, po, &used);
+	if (nphase < 0) {
+		free(pb); free(po); free(pp); free(pieces.p);
+		return sxs_fail(-5, "out of host memory");
+	}
+	for (size_t k = 0; k < np; k++) {
+		pc[k].phase = pp[k];
+		pc[k].off = po[k];
+	}
+	free(pb); free(po); free(pp);
 	/* phase k uses arena half k mod halves */
 	for (size_t k = 0; k < np; k++) pc[k].off += (size_t)(pc[k].phase % halves) * used;
 	if (nphase < 2) halves = 1;

@@ -110,6 +110,9 @@ int sxs_plan_ztables_on(sxsg_plan *p, cudaStream_t s);
 /* a batch filled the plan's outputs with this fit */
 void sxs_plan_mark_run(sxsg_plan *p, int fit_mode, const float *ms);
 
+/* first-fit packing of the batch's chunks into arena phases (sxs_batch.c) */
+int sxs_pack_first_fit(const size_t *bytes, size_t n, size_t cap, int *phase, size_t *off, size_t *used);
+
 /* per-q constants of the grid fit: fc[Q][5] */
 void sxs_fit_constants(const double *q, const double *a, int Q, double *fc);
 

@@ -227,3 +227,39 @@ def test_tile_table_defaults(lib):
             sb, g = lib.tiles_default(L, Q)
             assert 1 <= sb <= 64
             assert g in (0, 2, 4, 6, 8, 12, 16)
+
+
+def test_batch_first_fit_packing():
+    """The batch's first-fit packing of translated-table chunks into arena
+    phases (sxs_pack_first_fit): every chunk in one phase, within the arena,
+    no two chunks of a phase overlapping, a new phase only when no earlier
+    one has room."""
+    import ctypes as C
+    import numpy as np
+    from libfmftsaxs_gb300 import load
+    lib = load()
+    f = lib.sxs_pack_first_fit
+    f.argtypes = [C.c_void_p, C.c_size_t, C.c_size_t, C.c_void_p, C.c_void_p, C.POINTER(C.c_size_t)]
+    f.restype = C.c_int
+    rng = np.random.default_rng(5)
+    for trial in range(50):
+        n = int(rng.integers(1, 300))
+        cap = int(rng.integers(1000, 100000))
+        sizes = np.sort(rng.integers(1, cap + 1, size=n).astype(np.uint64))[::-1].copy()
+        phase = np.zeros(n, dtype=np.int32)
+        off = np.zeros(n, dtype=np.uint64)
+        used = C.c_size_t()
+        nph = f(sizes.ctypes.data, n, cap, phase.ctypes.data, off.ctypes.data, C.byref(used))
+        assert 1 <= nph <= n and phase.min() >= 0 and phase.max() == nph - 1
+        fill = np.zeros(nph, dtype=np.uint64)
+        for ph in range(nph):
+            sel = np.where(phase == ph)[0]
+            iv = sorted((int(off[k]), int(off[k] + sizes[k])) for k in sel)
+            assert iv[-1][1] <= cap
+            assert all(a[1] <= b[0] for a, b in zip(iv, iv[1:]))
+            fill[ph] = sizes[sel].sum()
+        assert int(used.value) == int(fill.max())
+        for k in range(n):   # no earlier phase had room when chunk k was placed
+            for ph in range(phase[k]):
+                placed = sizes[(phase == ph) & (np.arange(n) < k)].sum()
+                assert placed + sizes[k] > cap
