@@ -100,11 +100,6 @@ size_t sxsk_rotate_tc_scratch(int L);
  * did not finish in either bounded wait: output invalid, its tensor memory
  * was not freed and the context must be considered unusable). */
 
-/* translated ligand table for the combos of a run of slices, m >= 0, all q tiles:
- * R[t][c][pair(m,l)][ch][q] = sum_{l1>=m} conj(T[t][zi][m][l][l1][q]) U[t][(b2,g2)][pair(m,l1)][ch][q].
- * combo_zbg = the combos of the chunk (cbase = the first one's index),
- * slices[nslice][2] = {first combo, count} runs of <= 16 combos sharing z;
- * R holds ncombo combos; tau is float when fp32; nzt = z count of tau */
 /* Pose list on the device (src/index.c:3-29 packing, most significant
  * first: z slot, beta1, beta2, alpha2, gamma1, gamma2).  decode: one thread
  * per pose writes the decoded pose and its combo key (zi nb + b2) N + g2,
@@ -126,6 +121,11 @@ int sxsk_translate_class(const void *U, const void *tau, const int32_t *combo_zb
                          int cbase, int ncombo, int nzt, int Q, int L, void *R, int sb, int NB, cudaStream_t s);
 /* kernel launches one sxsk_translate call makes for this L */
 int sxsk_translate_launches(int L);
+/* translated ligand table for the combos of a run of slices, m >= 0, all q tiles:
+ * R[t][c][pair(m,l)][ch][q] = sum_{l1>=m} conj(T[t][zi][m][l][l1][q]) U[t][(b2,g2)][pair(m,l1)][ch][q].
+ * combo_zbg = the combos of the chunk (cbase = the first one's index),
+ * slices[nslice][2] = {first combo, count} runs of <= 16 combos sharing z;
+ * R holds ncombo combos; tau is float when fp32; nzt = z count of tau */
 int sxsk_translate(const void *U, const void *tau, const int32_t *combo_zbg, const int32_t *slices, int nslice,
                    int cbase, int ncombo, int nzt, int Q, int L, void *R, int fp32, int sb, cudaStream_t s);
 /* sb: slices per block of the pipelined FP32 kernel (0 = 8) */
