@@ -322,6 +322,7 @@ int sxs_plan_create_on(sxsg_plan **out, const double *A, const double *B, const 
 	int rc = sxs_ltables_get(L, &lt);
 	if (rc) return rc;
 	sxsg_plan *p = calloc(1, sizeof(*p));
+	if (!p) return sxs_fail(-5, "out of host memory");
 	p->L = L; p->K = L + 1; p->N = 2 * L + 1; p->K2 = p->K * p->K; p->Q = Q; p->nz = nz;
 	p->n1 = n1; p->n2 = n2; p->precision = precision; p->lt = lt; p->s = stream ? stream : g_stream;
 	p->ext_tables = ext_tables;
@@ -334,6 +335,10 @@ int sxs_plan_create_on(sxsg_plan **out, const double *A, const double *B, const 
 	for (int i = 0; i < Q; i++) s0 += a[6 * i];
 	p->a0sum = s0;
 	p->h_z = malloc(sizeof(double) * nz);
+	if (!p->h_z) {
+		free(p);
+		return sxs_fail(-5, "out of host memory");
+	}
 	memcpy(p->h_z, z, sizeof(double) * nz);
 	size_t spf_n = (size_t)3 * Q * p->K2 * 2;
 	cudaError_t e = cudaSuccess;
@@ -375,15 +380,24 @@ int sxs_plan_create_on(sxsg_plan **out, const double *A, const double *B, const 
 	if (!e) e = cudaMemcpyAsync(p->d_q, q, sizeof(double) * Q, cudaMemcpyHostToDevice, s);
 	if (!e) {
 		double *fc = malloc(sizeof(double) * 5 * Q);
-		sxs_fit_constants(q, a, Q, fc);
-		e = cudaMemcpyAsync(p->d_fc, fc, sizeof(double) * 5 * Q, cudaMemcpyHostToDevice, p->s);
-		free(fc);
+		if (!fc) {
+			e = cudaErrorMemoryAllocation;
+		} else {
+			sxs_fit_constants(q, a, Q, fc);
+			e = cudaMemcpyAsync(p->d_fc, fc, sizeof(double) * 5 * Q, cudaMemcpyHostToDevice, p->s);
+			/* pageable source: the copy has taken it when the call returns */
+			free(fc);
+		}
 	}
 	if (!e) e = cudaMemcpyAsync(p->d_a, a, sizeof(double) * 6 * Q, cudaMemcpyHostToDevice, s);
 	if (!e && n1 > 0) {
 		/* G(c1, q) = c1^3 exp(-mult (c1^2 - 1) q^2) exactly as point_score
 		 * evaluates it (src/min_saxs.c:404-423) */
 		double *g = malloc(sizeof(double) * n1 * Q);
+		if (!g) {
+			sxsg_plan_destroy(p);
+			return sxs_fail(-5, "out of host memory");
+		}
 		for (int i = 0; i < n1; i++) {
 			double c1 = c1g[i];
 			double corr = -mult * (c1 * c1 - 1.0);
@@ -393,6 +407,11 @@ int sxs_plan_create_on(sxsg_plan **out, const double *A, const double *B, const 
 		e = cudaMemcpyAsync(p->d_gtab, g, sizeof(double) * n1 * Q, cudaMemcpyHostToDevice, p->s);
 		if (!e && p->fp32) {
 			float *gd = malloc(sizeof(float) * 2 * n1 * Q);
+			if (!gd) {
+				free(g);
+				sxsg_plan_destroy(p);
+				return sxs_fail(-5, "out of host memory");
+			}
 			for (size_t k = 0; k < (size_t)n1 * Q; k++) {
 				float h = (float)g[k];
 				gd[2 * k] = h;
@@ -552,13 +571,17 @@ int sxsg_plan_set_poses(sxsg_plan *p, const int64_t *index, int64_t n, int skip)
 		/* touched z -> slot */
 		for (int i = 0; i < nz; i++) zslot[i] = h_zu[i] ? nzt++ : -1;
 		p->nzt = nzt;
-		p->h_zt = malloc(sizeof(double) * (nzt > 0 ? nzt : 1));
-		for (int i = 0; i < nz; i++) if (zslot[i] >= 0) p->h_zt[zslot[i]] = p->h_z[i];
-		/* combos in key order; h_cnt becomes the first slot of each key */
 		for (int64_t k = 0; k < nkey; k++) if (h_cnt[k]) ncombo++;
 		p->ncombo = ncombo;
+		p->h_zt = malloc(sizeof(double) * (nzt > 0 ? nzt : 1));
 		p->h_combo = malloc(sizeof(int32_t) * 3 * (ncombo > 0 ? ncombo : 1));
 		p->h_cstart = malloc(sizeof(int64_t) * (ncombo + 1));
+		p->h_slices = malloc(sizeof(int32_t) * 2 * (ncombo > 0 ? ncombo : 1));
+		if (!p->h_zt || !p->h_combo || !p->h_cstart || !p->h_slices) rc = sxs_fail(-5, "out of host memory");
+	}
+	if (!e && !rc) {
+		for (int i = 0; i < nz; i++) if (zslot[i] >= 0) p->h_zt[zslot[i]] = p->h_z[i];
+		/* combos in key order; h_cnt becomes the first slot of each key */
 		int c = 0;
 		int32_t run = 0;
 		for (int64_t k = 0; k < nkey; k++) {
@@ -579,7 +602,6 @@ int sxsg_plan_set_poses(sxsg_plan *p, const int64_t *index, int64_t n, int skip)
 		}
 		p->h_cstart[ncombo] = n;
 		/* slices for the translation kernel */
-		p->h_slices = malloc(sizeof(int32_t) * 2 * (ncombo > 0 ? ncombo : 1));
 		p->nslice = 0;
 		for (int k = 0; k < ncombo; k++) {
 			int ns = p->nslice;

@@ -318,6 +318,7 @@ int sxsg_server_create(sxsg_server **out, size_t hbm_cap, int max_active)
 	int rc = sxs_ensure_init();
 	if (rc) return rc;
 	sxsg_server *s = calloc(1, sizeof(*s));
+	if (!s) return sxs_fail(-5, "out of host memory");
 	pthread_mutex_init(&s->mu, NULL);
 	pthread_cond_init(&s->cv_work, NULL);
 	pthread_cond_init(&s->cv_done, NULL);
@@ -330,6 +331,10 @@ int sxsg_server_create(sxsg_server **out, size_t hbm_cap, int max_active)
 	s->nworkers = max_active;
 	s->th = calloc(max_active, sizeof(pthread_t));
 	s->streams = calloc(max_active, sizeof(cudaStream_t));
+	if (!s->th || !s->streams) {
+		free(s->th); free(s->streams); free(s);
+		return sxs_fail(-5, "out of host memory");
+	}
 	for (int i = 0; i < max_active; i++) {
 		cudaError_t e = cudaStreamCreateWithFlags(&s->streams[i], cudaStreamNonBlocking);
 		if (e) {
@@ -340,9 +345,19 @@ int sxsg_server_create(sxsg_server **out, size_t hbm_cap, int max_active)
 	}
 	for (int i = 0; i < max_active; i++) {
 		sxs_winfo *w = malloc(sizeof(*w));
-		w->s = s;
-		w->id = i;
-		pthread_create(&s->th[i], NULL, worker, w);
+		if (w) {
+			w->s = s;
+			w->id = i;
+		}
+		if (!w || pthread_create(&s->th[i], NULL, worker, w)) {
+			/* stop and join the workers already started, then release */
+			free(w);
+			int started = i;
+			for (int k = started; k < max_active; k++) cudaStreamDestroy(s->streams[k]);
+			s->nworkers = started;
+			sxsg_server_destroy(s);
+			return sxs_fail(-5, "sxsg_server_create: cannot start worker %d", i);
+		}
 	}
 	*out = s;
 	return 0;
@@ -354,6 +369,13 @@ static void *dup_arr(const void *p, size_t n)
 	void *d = malloc(n);
 	memcpy(d, p, n);
 	return d;
+}
+
+static void job_free(sxs_job *j)
+{
+	if (!j) return;
+	free(j->A); free(j->B); free(j->q); free(j->z); free(j->a); free(j->c1g); free(j->c2g); free(j->index);
+	free(j->chi); free(j->c1); free(j->c2); free(j);
 }
 
 int64_t sxsg_server_submit(sxsg_server *s, const sxsg_request *r)
@@ -368,6 +390,7 @@ int64_t sxsg_server_submit(sxsg_server *s, const sxsg_request *r)
 	int L = r->L, Q = r->qnum, K = L + 1, N = 2 * L + 1;
 	size_t spf = sizeof(double) * 3 * Q * K * K * 2;
 	sxs_job *j = calloc(1, sizeof(*j));
+	if (!j) return sxs_fail(-5, "out of host memory");
 	j->A = dup_arr(r->A, spf);
 	j->B = dup_arr(r->B, spf);
 	j->q = dup_arr(r->qvals, sizeof(double) * Q);
@@ -388,6 +411,12 @@ int64_t sxsg_server_submit(sxsg_server *s, const sxsg_request *r)
 	j->c2 = malloc(sizeof(double) * n);
 	/* touched z and the combo bound for the footprint */
 	char *zu = calloc(r->znum, 1);
+	if (!j->A || !j->B || !j->q || !j->z || !j->a || (r->c1grid && r->n1 > 0 && !j->c1g) ||
+	    (r->c2grid && r->n2 > 0 && !j->c2g) || (r->n > 0 && !j->index) || !j->chi || !j->c1 || !j->c2 || !zu) {
+		free(zu);
+		job_free(j);
+		return sxs_fail(-5, "out of host memory");
+	}
 	int64_t per_z = (int64_t)K * K * N * N * N;
 	int nzt = 0;
 	for (int64_t i = 0; i < r->n; i++) {
@@ -413,13 +442,19 @@ int64_t sxsg_server_submit(sxsg_server *s, const sxsg_request *r)
 	pthread_mutex_lock(&s->mu);
 	if (s->stop) {
 		pthread_mutex_unlock(&s->mu);
-		free(j->A); free(j->B); free(j->q); free(j->z); free(j->a); free(j->c1g); free(j->c2g); free(j->index);
-		free(j->chi); free(j->c1); free(j->c2); free(j);
+		job_free(j);
 		return sxs_fail(-2, "sxsg_server_submit: server is shutting down");
 	}
 	if (s->njobs == s->capjobs) {
-		s->capjobs = s->capjobs ? 2 * s->capjobs : 64;
-		s->jobs = realloc(s->jobs, sizeof(sxs_job *) * s->capjobs);
+		int64_t cap = s->capjobs ? 2 * s->capjobs : 64;
+		sxs_job **nj = realloc(s->jobs, sizeof(sxs_job *) * cap);
+		if (!nj) {
+			pthread_mutex_unlock(&s->mu);
+			job_free(j);
+			return sxs_fail(-5, "out of host memory");
+		}
+		s->jobs = nj;
+		s->capjobs = cap;
 	}
 	j->ticket = s->njobs;
 	s->jobs[s->njobs++] = j;
