@@ -16,12 +16,22 @@
 #define DIE(msg) sxs_die(__func__, (msg))
 #define NEED(ptr) do { if ((ptr) == NULL) DIE("Null pointer"); } while (0)
 
+/* Zeroed allocation for the drop-in functions, which exit on error like
+ * the reference (n or size 0 still returns a distinct pointer). */
+static void *xcalloc(const char *func, size_t n, size_t size)
+{
+	void *p = calloc(n ? n : 1, size ? size : 1);
+	if (!p) sxs_die(func, "out of memory");
+	return p;
+}
+#define XCALLOC(n, size) xcalloc(__func__, (n), (size))
+
 /* ======================================================== containers */
 
 /* src/pdb2spf.c:178-207 */
 struct sxs_spf_sing *sxs_spf_sing_create(int L)
 {
-	struct sxs_spf_sing *s = calloc(1, sizeof(*s));
+	struct sxs_spf_sing *s = XCALLOC(1, sizeof(*s));
 	sxs_spf_sing_init(s, L);
 	return s;
 }
@@ -30,8 +40,8 @@ void sxs_spf_sing_init(struct sxs_spf_sing *s, int L)
 {
 	if (!s) return;
 	s->L = L;
-	s->re = calloc((size_t)(L + 1) * (L + 1), sizeof(double));
-	s->im = calloc((size_t)(L + 1) * (L + 1), sizeof(double));
+	s->re = XCALLOC((size_t)(L + 1) * (L + 1), sizeof(double));
+	s->im = XCALLOC((size_t)(L + 1) * (L + 1), sizeof(double));
 }
 
 void sxs_spf_sing_destroy(struct sxs_spf_sing *s)
@@ -52,7 +62,7 @@ void sxs_spf_sing_free(struct sxs_spf_sing *s)
  * arrays, which the reference leaks (pdb2spf.c:241-250). */
 struct sxs_spf_full *sxs_spf_full_create(int L, int qnum)
 {
-	struct sxs_spf_full *s = malloc(sizeof(*s));
+	struct sxs_spf_full *s = XCALLOC(1, sizeof(*s));
 	sxs_spf_full_init(s, L, qnum);
 	return s;
 }
@@ -63,9 +73,9 @@ void sxs_spf_full_init(struct sxs_spf_full *s, int L, int qnum)
 	s->L = L;
 	s->qnum = qnum;
 	s->rm = 0.0;
-	s->V = calloc(qnum, sizeof(*s->V));
-	s->D = calloc(qnum, sizeof(*s->D));
-	s->W = calloc(qnum, sizeof(*s->W));
+	s->V = XCALLOC(qnum, sizeof(*s->V));
+	s->D = XCALLOC(qnum, sizeof(*s->D));
+	s->W = XCALLOC(qnum, sizeof(*s->W));
 	for (int i = 0; i < qnum; i++) {
 		s->V[i] = sxs_spf_sing_create(L);
 		s->D[i] = sxs_spf_sing_create(L);
@@ -183,7 +193,7 @@ int sxsg_spf_from_flat(struct sxs_spf_full *s, const double *flat)
  * without freeing it. */
 struct sxs_profile *sxs_profile_create(double *qvals, int qnum, int cross_terms_flag)
 {
-	struct sxs_profile *p = calloc(1, sizeof(*p));
+	struct sxs_profile *p = XCALLOC(1, sizeof(*p));
 	sxs_profile_init(p, qvals, qnum, cross_terms_flag);
 	return p;
 }
@@ -194,8 +204,8 @@ void sxs_profile_init(struct sxs_profile *p, double *qvals, int qnum, int cross_
 	p->qnum = qnum;
 	p->rerr = SXS_REL_ERR;
 	p->qvals = qvals;
-	p->in = calloc(qnum, sizeof(double));
-	p->err = calloc(qnum, sizeof(double));
+	p->in = XCALLOC(qnum, sizeof(double));
+	p->err = XCALLOC(qnum, sizeof(double));
 	p->score = INFINITY;
 	p->c1 = SXS_C1_DEFAULT;
 	p->c2 = SXS_C2_DEFAULT;
@@ -206,12 +216,12 @@ void sxs_profile_init(struct sxs_profile *p, double *qvals, int qnum, int cross_
 
 void sxs_profile_alloc_cross_terms(struct sxs_profile *p, int qnum)
 {
-	p->VV = calloc(qnum, sizeof(double));
-	p->VD = calloc(qnum, sizeof(double));
-	p->VW = calloc(qnum, sizeof(double));
-	p->DD = calloc(qnum, sizeof(double));
-	p->DW = calloc(qnum, sizeof(double));
-	p->WW = calloc(qnum, sizeof(double));
+	p->VV = XCALLOC(qnum, sizeof(double));
+	p->VD = XCALLOC(qnum, sizeof(double));
+	p->VW = XCALLOC(qnum, sizeof(double));
+	p->DD = XCALLOC(qnum, sizeof(double));
+	p->DW = XCALLOC(qnum, sizeof(double));
+	p->WW = XCALLOC(qnum, sizeof(double));
 }
 
 void sxs_profile_destroy(struct sxs_profile *p)
@@ -256,7 +266,7 @@ struct sxs_profile *sxs_profile_fread(FILE *f)
 		n++;
 	}
 	rewind(f);
-	double *qv = calloc(n, sizeof(double));
+	double *qv = XCALLOC(n, sizeof(double));
 	struct sxs_profile *p = sxs_profile_create(qv, n, 0);
 	for (int i = 0; i < n; i++)
 		if (fscanf(f, "%lf %lf %lf\n", &qv[i], &p->in[i], &p->err[i]) != 3) DIE("Wrong input file format.");
@@ -310,7 +320,7 @@ void sxs_profile_from_spf(struct sxs_profile *p, struct sxs_spf_full *s, double 
  * bounded by exp->qnum. */
 double *scoring_helper(struct sxs_profile *e, int qnum, double *qvals)
 {
-	double *a = calloc((size_t)6 * qnum, sizeof(double));
+	double *a = XCALLOC((size_t)6 * qnum, sizeof(double));
 	int j = 0;
 	for (int i = 0; i < qnum; i++) {
 		double lo = i > 0 ? qvals[i - 1] : qvals[0], hi = qvals[i];
@@ -332,7 +342,7 @@ double *scoring_helper(struct sxs_profile *e, int qnum, double *qvals)
 /* src/min_saxs.c:108-150 */
 struct sxs_opt_params *sxs_opt_params_create(struct sxs_profile *e, double *qvals, int qnum, double rm)
 {
-	struct sxs_opt_params *p = calloc(1, sizeof(*p));
+	struct sxs_opt_params *p = XCALLOC(1, sizeof(*p));
 	sxs_opt_params_init(p, e, qvals, qnum, rm);
 	return p;
 }
@@ -476,7 +486,11 @@ static int fit_profiles_gpu(struct sxs_profile **profiles, const int *sel, int n
 	if (rc) return rc;
 	int Q = profiles[sel[0]]->qnum;
 	cudaStream_t s = sxs_default_stream();
-	double *h_c = malloc(sizeof(double) * (size_t)n * 6 * Q);
+	double *h_c = malloc(sizeof(double) * (size_t)n * 6 * Q), *h_o = malloc(sizeof(double) * 4 * n);
+	if (!h_c || !h_o) {
+		free(h_c); free(h_o);
+		return sxs_fail(-5, "out of host memory");
+	}
 	for (int k = 0; k < n; k++) {
 		struct sxs_profile *p = profiles[sel[k]];
 		double *dst = h_c + (size_t)k * 6 * Q;
@@ -505,7 +519,6 @@ static int fit_profiles_gpu(struct sxs_profile **profiles, const int *sel, int n
 		                                       d_o + 2 * n, d_o + 3 * n, d_it, s);
 		sxs_count_launches(2);
 	}
-	double *h_o = malloc(sizeof(double) * 4 * n);
 	if (!e) e = cudaMemcpyAsync(h_o, d_o, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, s);
 	if (!e) e = cudaStreamSynchronize(s);
 	cudaFree(d_c); cudaFree(d_t); cudaFree(d_q); cudaFree(d_a); cudaFree(d_o); cudaFree(d_it);
@@ -534,7 +547,7 @@ void sxs_fit_params(struct sxs_profile **profiles, struct sxs_opt_params *params
 	NEED(profiles);
 	NEED(params);
 	NEED(mask);
-	int *sel = malloc(sizeof(int) * (n > 0 ? n : 1));
+	int *sel = XCALLOC(n > 0 ? n : 1, sizeof(int));
 	int k = 0;
 	for (int i = 0; i < n; i++) if (mask[i] == 1) sel[k++] = i;
 	if (k > 0 && fit_profiles_gpu(profiles, sel, k, params, 1)) DIE(sxsg_last_error());
@@ -567,7 +580,7 @@ double *sxs_mkarray(double begin, double end, int qnum)
 		exit(EXIT_FAILURE);
 	}
 	double step = (end - begin) / (qnum - 1);
-	double *q = calloc(qnum, sizeof(double));
+	double *q = XCALLOC(qnum, sizeof(double));
 	q[0] = begin;
 	for (int i = 1; i < qnum; i++) q[i] = q[i - 1] + step;
 	return q;
@@ -898,10 +911,10 @@ void sxs_compute_saxs_scores(double *scores, double *c1, double *c2, int *index_
 	NEED(scores); NEED(c1); NEED(c2); NEED(index_list);
 	if (A->L != L || B->L != L || A->qnum != qnum || B->qnum != qnum) DIE("expansions do not match L / qnum");
 	size_t spf_n = (size_t)3 * qnum * (L + 1) * (L + 1) * 2;
-	double *fa = malloc(sizeof(double) * spf_n), *fb = malloc(sizeof(double) * spf_n);
+	double *fa = XCALLOC(spf_n, sizeof(double)), *fb = XCALLOC(spf_n, sizeof(double));
 	sxsg_spf_to_flat(A, fa);
 	sxsg_spf_to_flat(B, fb);
-	int64_t *idx = malloc(sizeof(int64_t) * nout);
+	int64_t *idx = XCALLOC(nout > 0 ? nout : 1, sizeof(int64_t));
 	for (int i = 0; i < nout; i++) idx[i] = index_list[i];
 	sxsg_plan *p = NULL;
 	int rc = sxsg_plan_create(&p, fa, fb, qvals, qnum, zvals, znum, L, params->a, params->mult, params->peak, NULL, 0,
