@@ -80,6 +80,10 @@ int sxsg_score_exact(const double *rec_xyz, int nrec, const double *lig_xyz, int
 	size_t spf_n = (size_t)3 * Q * K * K * 2;
 	double *h_xyz = malloc(sizeof(double) * 3 * na * (size_t)B);
 	double *wf = calloc(na, sizeof(double));
+	if (!h_xyz || !wf) {
+		free(h_xyz); free(wf);
+		return sxs_fail(-5, "out of host memory");
+	}
 	if (water_w) memcpy(wf, water_w, sizeof(double) * na);
 	double *d_xyz = NULL, *d_vac = NULL, *d_dum = NULL, *d_wf = NULL, *d_q = NULL, *d_a = NULL, *d_rad = NULL;
 	double *d_spf = NULL, *d_cross = NULL, *d_ct = NULL, *d_chi = NULL, *d_c1 = NULL, *d_c2 = NULL;
@@ -148,6 +152,7 @@ int sxsg_sasa(const double *xyz, const double *radius, int natoms, double probe,
 	double *h_sph = NULL;
 	if (!sph) {
 		h_sph = malloc(sizeof(double) * 3 * npts);
+		if (!h_sph) return sxs_fail(-5, "out of host memory");
 		for (int k = 0; k < npts; k++) {
 			double kk = k + 0.5;
 			double phi = acos(1.0 - 2.0 * kk / npts);

@@ -129,6 +129,7 @@ int sxsg_expand(const double *xyz, const double *vac, const double *dum, const d
 	int K = L + 1;
 	size_t spf_n = (size_t)3 * Q * K * K * 2;
 	double *wf = malloc(sizeof(double) * (natoms > 0 ? natoms : 1));
+	if (!wf) return sxs_fail(-5, "out of host memory");
 	for (int i = 0; i < natoms; i++) wf[i] = sasa ? water_ff * sasa[i] : 0.0;
 	double *d_xyz = NULL, *d_vac = NULL, *d_dum = NULL, *d_wf = NULL, *d_q = NULL, *d_rad = NULL, *d_out = NULL;
 	double2 *d_ylm = NULL;

@@ -236,17 +236,23 @@ static double *dsymb_build(int L)
 	size_t n = (size_t)K * K * K * N;
 	double *ds = calloc(n, sizeof(double));
 	quad_t_ *f = malloc(sizeof(quad_t_) * (4 * L + 2));
+	if (!ds || !f) {
+		free(ds); free(f);
+		return NULL;
+	}
 	f[0] = 1;
 	for (int i = 1; i <= 4 * L + 1; i++) f[i] = f[i - 1] * (quad_t_)i;
 	enum { NT = 8 };
 	pthread_t th[NT];
 	dsymb_job jobs[NT];
 	int nt = K < NT ? K : NT;
+	int started[NT] = {0};
 	for (int t = 0; t < nt; t++) {
 		jobs[t] = (dsymb_job){L, t, nt, f, ds};
-		pthread_create(&th[t], NULL, dsymb_worker, &jobs[t]);
+		started[t] = pthread_create(&th[t], NULL, dsymb_worker, &jobs[t]) == 0;
+		if (!started[t]) dsymb_worker(&jobs[t]);   /* no thread: this share on the caller's */
 	}
-	for (int t = 0; t < nt; t++) pthread_join(th[t], NULL);
+	for (int t = 0; t < nt; t++) if (started[t]) pthread_join(th[t], NULL);
 	free(f);
 	return ds;
 }
@@ -281,16 +287,22 @@ int sxs_ltables_get(int L, const sxs_ltables **out)
 	}
 	int K = L + 1, N = 2 * L + 1;
 	sxs_ltables *t = calloc(1, sizeof(*t));
-	t->L = L;
 	size_t dsz = (size_t)K * N * N;
 	double *h_dt = malloc(sizeof(double) * dsz * K);
-	double step = (SXS_PI - 0.0) / (K - 1);
-	for (int b = 0; b < K; b++) sxs_wigner_d_host(L, 0.0 + b * step, h_dt + b * dsz);
 	const double *h_ds = sxs_dsymb_cached(L);
 	double *h_yn = malloc(sizeof(double) * K * N);
-	sxs_ynorm_host(L, h_yn);
 	int nll = K * (K + 1) / 2;
 	int2 *h_ll = malloc(sizeof(int2) * nll);
+	float *h_df = malloc(sizeof(float) * dsz * K);
+	if (!t || !h_dt || !h_ds || !h_yn || !h_ll || !h_df) {
+		free(t); free(h_dt); free(h_yn); free(h_ll); free(h_df);
+		pthread_mutex_unlock(&g_lt_lock);
+		return sxs_fail(-5, "out of host memory (per-L tables, L=%d)", L);
+	}
+	t->L = L;
+	double step = (SXS_PI - 0.0) / (K - 1);
+	for (int b = 0; b < K; b++) sxs_wigner_d_host(L, 0.0 + b * step, h_dt + b * dsz);
+	sxs_ynorm_host(L, h_yn);
 	int k = 0;
 	for (int l = 0; l <= L; l++)
 		for (int l1 = l; l1 <= L; l1++) { h_ll[k].x = l; h_ll[k].y = l1; k++; }
@@ -303,15 +315,13 @@ int sxs_ltables_get(int L, const sxs_ltables **out)
 	if (e == cudaSuccess) e = cudaMalloc((void **)&t->d_ll1, sizeof(int2) * nll);
 	if (e == cudaSuccess) e = cudaMemcpy(t->d_dtab, h_dt, sizeof(double) * dsz * K, cudaMemcpyHostToDevice);
 	if (e == cudaSuccess) {
-		float *h_df = malloc(sizeof(float) * dsz * K);
 		for (size_t i = 0; i < dsz * K; i++) h_df[i] = (float)h_dt[i];
 		e = cudaMemcpy(t->d_dtabf, h_df, sizeof(float) * dsz * K, cudaMemcpyHostToDevice);
-		free(h_df);
 	}
 	if (e == cudaSuccess) e = cudaMemcpy(t->d_dsymb, h_ds, sizeof(double) * (size_t)K * K * K * N, cudaMemcpyHostToDevice);
 	if (e == cudaSuccess) e = cudaMemcpy(t->d_ynorm, h_yn, sizeof(double) * K * N, cudaMemcpyHostToDevice);
 	if (e == cudaSuccess) e = cudaMemcpy(t->d_ll1, h_ll, sizeof(int2) * nll, cudaMemcpyHostToDevice);
-	free(h_dt); free(h_yn); free(h_ll);
+	free(h_dt); free(h_yn); free(h_ll); free(h_df);
 	if (e != cudaSuccess) {
 		cudaFree(t->d_dtab); cudaFree(t->d_dtabf); cudaFree(t->d_dsymb); cudaFree(t->d_ynorm); cudaFree(t->d_ll1);
 		free(t);
